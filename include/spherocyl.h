@@ -1,0 +1,144 @@
+/*
+ * spherocyl.h -- C ABI of libspherocyl, the GB300 (sm_103a) implementation of the
+ * overdamped-dynamics hot path of tmarschall/spherocyls: 2D bidisperse
+ * spherocylinder packings under Lees-Edwards simple shear and affine box resize,
+ * plus energy minimisation.
+ *
+ * The reference has no library API; its callers are the CLI drivers, which build
+ * one box object and call one run method (src/cpp/main.cpp:63-196,
+ * src/cpp/main_resize.cpp:63-193, src/cpp/main_relax.cpp:63-181).  Each entry
+ * point below names the reference routine it replaces.  One handle holds one or
+ * more independent periodic boxes ("systems") that advance together; with one
+ * system a handle is a drop-in for SpherocylBox (src/cpp/spherocyl_box.h:26-122).
+ *
+ * Conventions
+ *  - Every function returns an int status (SC_OK == 0) and never exits or aborts;
+ *    sc_last_error() gives a one-line description of the last failure.
+ *  - Arrays are plain host pointers, copied on entry; the library owns all device
+ *    memory and never keeps a caller pointer.
+ *  - Per-particle arrays concatenate the systems in order, each in the reference's
+ *    particle order.  "sys" arguments take a system index or -1 for all systems.
+ *  - A handle is used by one host thread at a time; its work runs on its own CUDA
+ *    stream (or the stream given to sc_set_stream).
+ */
+#ifndef SPHEROCYL_H
+#define SPHEROCYL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (the reference's exit(1)/assert/checkCudaError paths,
+ *      src/cuda/cudaErr.cpp:11-19, become these) ---- */
+#define SC_OK 0
+#define SC_E_ARG 1      /* invalid argument */
+#define SC_E_IO 2       /* file could not be read or written */
+#define SC_E_NAN 3      /* a position or angle became non-finite */
+#define SC_E_OVERFLOW 4 /* neighbour list or cell capacity exceeded */
+#define SC_E_NOCONV 5   /* minimiser stopped at its iteration cap */
+#define SC_E_TIMEOUT 6  /* a bounded device wait gave up */
+#define SC_E_CUDA 7     /* CUDA runtime error */
+#define SC_E_STATE 8    /* call not valid in the handle's current state */
+#define SC_E_NOMEM 9    /* host or device allocation failed */
+
+#define SC_PREC_FP64 0  /* plain FP64: the reference's arithmetic, step for step */
+#define SC_PREC_MIXED 1 /* FP32 pair geometry, FP64 state and accumulators */
+
+#define SC_STRESS_COMPAT 0 /* stress exactly as src/cpp accumulates it (with its slips) */
+#define SC_STRESS_VIRIAL 1 /* the intended contact virial */
+
+#define SC_FMT_SP 0 /* src/cpp position file: "N L phi gamma gamma_tot rate dt" */
+#define SC_FMT_SD 1 /* src/cuda position file: "N Lx Ly phi gamma gamma_tot rate dt" */
+
+typedef struct sc_handle sc_handle;
+
+typedef struct sc_options {
+  int precision;   /* SC_PREC_* */
+  int stress_mode; /* SC_STRESS_* */
+  int device;      /* CUDA device ordinal */
+  int max_nbrs;    /* FP64 neighbour-list capacity per particle, 0 = default (64) */
+  int use_graphs;  /* capture step chunks in CUDA graphs (1) or launch eagerly (0) */
+  int block;       /* threads per block of the mixed force pass, 0 = autotune */
+  int profile;     /* record per-pass CUDA events inside run calls (sc_get_pass_times) */
+} sc_options;
+
+const char *sc_version(void);
+const char *sc_status_string(int status);
+void sc_default_options(sc_options *opt);
+
+/* Create a handle holding n_sys periodic square boxes of side L[s] and padding
+ * pad[s] (0 = automatic, as configure_cells, src/cpp/spherocyl_box.cpp:240-241).
+ * Replaces SpherocylBox(L, N, x, y, phi, A*, R*, pad), src/cpp/spherocyl_box.cpp:152-173:
+ * positions and angles are wrapped, MOI and rotation coefficients derived
+ * (set_particle :188-221), cells configured (:223-268) and lists built (:320-355). */
+int sc_create(const sc_options *opt, int n_sys, const int *n_per_sys, const double *L,
+              const double *pad, const double *x, const double *y, const double *phi,
+              const double *R, const double *A, sc_handle **out);
+int sc_destroy(sc_handle *h);
+const char *sc_last_error(const sc_handle *h);
+int sc_set_stream(sc_handle *h, void *cuda_stream);
+int sc_synchronize(sc_handle *h);
+
+/* Setters, src/cpp/spherocyl_box.h:112-119 (set_strain_rate, set_resize_rate,
+ * set_step, set_cell_padding, set_gamma, set_total_gamma). */
+int sc_set_strain_rate(sc_handle *h, int sys, double v);
+int sc_set_resize_rate(sc_handle *h, int sys, double v);
+int sc_set_step(sc_handle *h, int sys, double v);
+int sc_set_gamma(sc_handle *h, int sys, double v);
+int sc_set_total_gamma(sc_handle *h, int sys, double v);
+
+/* find_neighbors, src/cpp/spherocyl_box.cpp:320-355 (forced rebuild). */
+int sc_find_neighbors(sc_handle *h);
+/* calc_forces, src/cpp/strain_dynamics.cpp:137-153. */
+int sc_calc_forces(sc_handle *h);
+/* calc_se, src/cpp/spherocyl_box.cpp:502-522: forces plus per-system
+ * E, Pxx, Pyy, Pxy, Pyx written to se_out[5*s + k] (se_out may be NULL). */
+int sc_calc_se(sc_handle *h, double *se_out);
+
+/* nsteps Heun steps under Lees-Edwards shear: strain_step followed by
+ * calc_forces, or calc_se every se_every steps (run_strain's inner loop,
+ * src/cpp/strain_dynamics.cpp:179-235 and :285-296).  When se_every > 0 and
+ * se_out != NULL, se_out receives (nsteps/se_every) records of 5*n_sys values. */
+int sc_strain_steps(sc_handle *h, int nsteps, int se_every, double *se_out);
+/* nsteps Heun steps with affine resize by (1-rate)^dt per step (shrink != 0) or its
+ * inverse (resize_step + calc_forces, src/cpp/resize_dynamics.cpp:164-243, :297-307). */
+int sc_resize_steps(sc_handle *h, int nsteps, int shrink, int se_every, double *se_out);
+/* Fixed-step gradient descent (gradient_descent_minimize's loop,
+ * src/cpp/relaxation_dynamics.cpp:11-85): calc_se, stop when every system's
+ * E <= e_min, else x += dt F.  *steps_taken receives the iterations done. */
+int sc_gd_minimize(sc_handle *h, int max_steps, double e_min, int *steps_taken,
+                   double *e_final);
+
+/* State readers, original particle order, systems concatenated. */
+int sc_get_state(sc_handle *h, double *x, double *y, double *phi);
+int sc_get_forces(sc_handle *h, double *fx, double *fy, double *tau);
+/* Per-system scalars: out[0..9] = Lx Ly gamma gamma_total pad W H packing rows cols. */
+int sc_get_box(sc_handle *h, int sys, double *out);
+/* Half neighbour list of one system as (p, q) pairs with p < q, sorted; with
+ * pairs == NULL only *n_pairs is written.  (The reference's m_pvNeighbors.) */
+int sc_get_pairs(sc_handle *h, int sys, int *pairs, long cap, long *n_pairs);
+/* Counters: out[0] steps, out[1] neighbour rebuilds, out[2] device status bits. */
+int sc_get_counters(sc_handle *h, long long *out);
+/* Mean device time per force pass of the last run call with profiling on:
+ * out[0] corrector passes (ms), out[1] predictor passes (ms), out[2] rebuild
+ * chains (ms), out[3..5] the number of each. */
+int sc_get_pass_times(sc_handle *h, double *out);
+
+/* Seeded crossing-free random packing: species alternate by index (R = r_small
+ * for even, r_small*r_ratio for odd indices), A = a_over_r * R, L from the packing
+ * fraction sum(pi R^2 + 4 A R)/L^2, centres uniform, angles uniform in [0, pi),
+ * a placement rejected while its spine comes closer than min_sep * (R_i + R_j) to
+ * an earlier spine.  Replaces random_configuration's rand()/time(0) placement
+ * (src/cpp/spherocyl_box.cpp:694-790) with a reproducible one. */
+int sc_generate_packing(int n, double packing, double a_over_r, double r_small, double r_ratio,
+                        uint64_t seed, double min_sep, double *x, double *y, double *phi,
+                        double *R, double *A, double *L);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPHEROCYL_H */

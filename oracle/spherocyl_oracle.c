@@ -1,0 +1,638 @@
+/*
+ * spherocyl_oracle.c -- TEST INFRASTRUCTURE ONLY (the oracle).
+ *
+ * A plain-C restatement of the single-threaded CPU path of tmarschall/spherocyls
+ * (src/cpp).  The tests, the smoke check and the CPU-baseline leg of the benchmark
+ * use it as the checker for the CUDA library.  It is never linked into, or called
+ * by, the product library.
+ *
+ * Every routine follows one reference routine and cites it.  Arithmetic is written
+ * so that the floating-point operations and their order are the reference's
+ * (compiled with -ffp-contract=off), which makes the restatement bit-identical to
+ * the compiled reference on the same machine; tests/test_oracle_pin.py checks that
+ * against fixtures produced by the reference itself (tests/golden/).
+ *
+ * State is one box: SoA arrays in the reference's particle order.  The half
+ * neighbour list is a growable array per particle, filled in the reference's
+ * traversal order (own cell, then the 8 neighbour cells in table order).
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "spherocyl_oracle.h"
+
+/* The reference's truncated pi (src/cpp/spherocyl_box.cpp:12).  Its value enters
+ * the moment of inertia, the rotation coefficient and the angle wrap, so the
+ * oracle uses the same constant to stay bit-identical. */
+static const double REF_PI = 3.14159265358979;
+
+typedef struct {
+  int *data;
+  int len, cap;
+} ivec;
+
+static int ivec_push(ivec *v, int x) {
+  if (v->len == v->cap) {
+    int nc = v->cap ? 2 * v->cap : 8;
+    int *nd = (int *)realloc(v->data, (size_t)nc * sizeof(int));
+    if (!nd) return -1;
+    v->data = nd;
+    v->cap = nc;
+  }
+  v->data[v->len++] = x;
+  return 0;
+}
+
+static void ivec_free_array(ivec *v, int n) {
+  if (!v) return;
+  for (int i = 0; i < n; i++) free(v[i].data);
+  free(v);
+}
+
+struct orc_box {
+  int n;
+  double Lx, Ly;
+  double gamma, gamma_total, strain_rate, resize_rate, step, pad;
+  double Rmax, Amax, packing;
+  int rows, cols, ncells;
+  double W, H;
+  /* particles (the reference's Spherocyl struct, src/cpp/spherocyl_box.h:10-24) */
+  double *x, *y, *phi, *R, *A, *I, *RC, *fx, *fy, *tau, *xm, *ym;
+  int *cell;
+  /* the copy used by the Heun predictor (m_psTempParticles) */
+  double *tx, *ty, *tphi, *tfx, *tfy, *ttau;
+  ivec *cells;     /* per-cell particle lists, ncells of them */
+  int *cell_nbrs;  /* 8 neighbour cells per cell */
+  ivec *nbrs;      /* per-particle half lists */
+  double E, Pxx, Pyy, Pxy, Pyx;
+  long n_rebuilds;
+  int err;
+};
+
+/* ---- per-particle constants and wrap: set_particle, spherocyl_box.cpp:188-221 ---- */
+static void wrap_particle(orc_box *b, int p) {
+  /* the wrap loops of set_particle :204-215, repeated in find_cells :279-290 */
+  while (b->x[p] > b->Lx) b->x[p] -= b->Lx;
+  while (b->x[p] < 0.0) b->x[p] += b->Lx;
+  while (b->y[p] > b->Ly) b->y[p] -= b->Ly;
+  while (b->y[p] < 0.0) b->y[p] += b->Ly;
+  while (b->phi[p] > REF_PI) b->phi[p] -= 2 * REF_PI;
+  while (b->phi[p] < -REF_PI) b->phi[p] += 2 * REF_PI;
+}
+
+static void set_particle(orc_box *b, int p, double x, double y, double phi, double A, double R) {
+  b->x[p] = x;
+  b->y[p] = y;
+  b->phi[p] = phi;
+  b->A[p] = A;
+  b->R[p] = R;
+  double al = A / R;
+  double C = (3 * REF_PI + 24 * al + 6 * REF_PI * al * al + 8 * al * al * al);
+  double area = R * (REF_PI * R + 4 * A);
+  b->I[p] = R * R * R * R * C / (6 * area);
+  b->RC[p] = (8 * al + 6 * REF_PI * al * al + 8 * al * al * al) / C;
+  wrap_particle(b, p);
+  if (b->A[p] > b->Amax) b->Amax = b->A[p];
+  if (b->R[p] > b->Rmax) b->Rmax = b->R[p];
+}
+
+/* calculate_packing_fraction, spherocyl_box.cpp:357-366 */
+static double packing_fraction(const orc_box *b) {
+  double filled = 0.0;
+  for (int p = 0; p < b->n; p++) filled += (REF_PI * b->R[p] + 4.0 * b->A[p]) * b->R[p];
+  return filled / (b->Lx * b->Ly);
+}
+
+/* ---- cell grid: configure_cells, spherocyl_box.cpp:223-268 ---- */
+static int configure_cells(orc_box *b) {
+  double wmin = 2.24 * (b->Rmax + b->Amax) + b->pad;
+  double hmin = 2 * (b->Rmax + b->Amax) + b->pad;
+  int rows = (int)(b->Ly / hmin);
+  int cols = (int)(b->Lx / wmin);
+  ivec_free_array(b->cells, b->ncells);
+  free(b->cell_nbrs);
+  b->rows = rows > 1 ? rows : 1;
+  b->cols = cols > 1 ? cols : 1;
+  b->ncells = b->rows * b->cols;
+  b->W = b->Lx / b->cols;
+  b->H = b->Ly / b->rows;
+  if (b->pad == 0) {
+    double dw = b->W - wmin, dh = b->H - hmin;
+    b->pad = dw > dh ? dw : dh;
+  }
+  b->cells = (ivec *)calloc((size_t)b->ncells, sizeof(ivec));
+  b->cell_nbrs = (int *)malloc((size_t)b->ncells * 8 * sizeof(int));
+  if (!b->cells || !b->cell_nbrs) return -1;
+  for (int c = 0; c < b->ncells; c++) {
+    int row = c / b->cols, col = c % b->cols;
+    int right = (col + 1) % b->cols, left = (b->cols + col - 1) % b->cols;
+    int up = (row + 1) % b->rows, down = (b->rows + row - 1) % b->rows;
+    int *t = b->cell_nbrs + 8 * c;
+    /* table order of the reference: same row (+1, -1), row above (0, +1, -1),
+     * row below (0, +1, -1) */
+    t[0] = row * b->cols + right;
+    t[1] = row * b->cols + left;
+    t[2] = up * b->cols + col;
+    t[3] = up * b->cols + right;
+    t[4] = up * b->cols + left;
+    t[5] = down * b->cols + col;
+    t[6] = down * b->cols + right;
+    t[7] = down * b->cols + left;
+  }
+  return 0;
+}
+
+/* find_cells, spherocyl_box.cpp:270-301 */
+static void find_cells(orc_box *b) {
+  for (int c = 0; c < b->ncells; c++) b->cells[c].len = 0;
+  for (int p = 0; p < b->n; p++) {
+    wrap_particle(b, p);
+    int col = (int)(b->x[p] / b->W);
+    int row = (int)(b->y[p] / b->H);
+    /* A coordinate exactly equal to the box length survives the wrap and would
+     * index one column/row past the grid in the reference; clamp it.  A
+     * non-finite coordinate (crossing spines give 0/0 forces) is an error here,
+     * where the reference would index out of bounds. */
+    if (!isfinite(b->x[p]) || !isfinite(b->y[p])) b->err = 1;
+    if (col >= b->cols || col < 0) col = col < 0 ? 0 : b->cols - 1;
+    if (row >= b->rows || row < 0) row = row < 0 ? 0 : b->rows - 1;
+    int c = col + row * b->cols;
+    b->cell[p] = c;
+    if (ivec_push(&b->cells[c], p)) b->err = 1;
+  }
+}
+
+/* check_neighbors, spherocyl_box.cpp:303-318 */
+static int check_neighbors(const orc_box *b, int p, int q) {
+  double sig = b->R[p] + b->A[p] + b->R[q] + b->A[q];
+  double dy = b->y[p] - b->y[q];
+  dy += b->Ly * ((dy < -0.5 * b->Ly) - (dy > 0.5 * b->Ly));
+  if (fabs(dy) < sig + b->pad) {
+    double dx = b->x[p] - b->x[q];
+    dx += b->Lx * ((dx < -0.5 * b->Lx) - (dx > 0.5 * b->Lx));
+    double dxmax = dx + 0.5 * dy;
+    dx += b->gamma * dy;
+    if (fabs(dx) < sig + b->pad || fabs(dxmax) < sig + b->pad) return 1;
+  }
+  return 0;
+}
+
+/* find_neighbors, spherocyl_box.cpp:320-355 */
+static void find_neighbors(orc_box *b) {
+  b->n_rebuilds++;
+  find_cells(b);
+  for (int p = 0; p < b->n; p++) {
+    b->nbrs[p].len = 0;
+    b->xm[p] = 0.0;
+    b->ym[p] = 0.0;
+  }
+  for (int p = 0; p < b->n - 1; p++) {
+    int c = b->cell[p];
+    for (int k = -1; k < 8; k++) {
+      int cc = k < 0 ? c : b->cell_nbrs[8 * c + k];
+      const ivec *cl = &b->cells[cc];
+      for (int m = 0; m < cl->len; m++) {
+        int q = cl->data[m];
+        if (q > p && check_neighbors(b, p, q))
+          if (ivec_push(&b->nbrs[p], q)) b->err = 1;
+      }
+    }
+  }
+}
+
+/* ---- pair force.  calc_force_pair, strain_dynamics.cpp:17-75 (state copy),
+ * calc_temp_force_pair :77-135 (predictor copy, gamma + dt*rate), and
+ * calc_se_force_pair, spherocyl_box.cpp:425-500 (adds energy and stress). ---- */
+typedef struct {
+  const double *x, *y, *phi;
+  double *fx, *fy, *tau;
+} pview;
+
+static void force_pair(orc_box *b, const pview *v, int p, int q, double gamma, double Lx, double Ly,
+                       int with_se) {
+  double dX = v->x[p] - v->x[q];
+  double dY = v->y[p] - v->y[q];
+  double phiP = v->phi[p], phiQ = v->phi[q];
+  double sig = b->R[p] + b->R[q];
+  double aP = b->A[p], aQ = b->A[q];
+  dX += Lx * ((dX < -0.5 * Lx) - (dX > 0.5 * Lx));
+  dY += Ly * ((dY < -0.5 * Ly) - (dY > 0.5 * Ly));
+  dX += gamma * dY; /* sheared -> lab frame */
+
+  double nxA = aP * cos(phiP), nyA = aP * sin(phiP);
+  double nxB = aQ * cos(phiQ), nyB = aQ * sin(phiQ);
+  double a = aP * aP;
+  double bb = -(nxA * nxB + nyA * nyB);
+  double c = aQ * aQ;
+  double d = nxA * dX + nyA * dY;
+  double e = -nxB * dX - nyB * dY;
+  double delta = a * c - bb * bb;
+
+  /* closest points of the two spines, clamped to the segments */
+  double t = fmin(fmax((bb * d - a * e) / delta, -1.), 1.);
+  double s = -(bb * t + d) / a;
+  double sarg = fabs(s);
+  s = fmin(fmax(s, -1.), 1.);
+  if (sarg > 1) t = fmin(fmax(-(bb * s + e) / c, -1.), 1.);
+
+  double dDx = dX + s * nxA - t * nxB;
+  double dDy = dY + s * nyA - t * nyB;
+  double dsq = dDx * dDx + dDy * dDy;
+  if (dsq < sig * sig) {
+    double dij = sqrt(dsq);
+    double dvij = (1.0 - dij / sig) / sig;
+    double Fx = dDx * dvij / dij;
+    double Fy = dDy * dvij / dij;
+    double tauP = s * nxA * Fy - s * nyA * Fx;
+    double tauQ = t * nyB * Fx - t * nxB * Fy;
+    v->fx[p] += Fx;
+    v->fy[p] += Fy;
+    v->tau[p] += tauP;
+    v->fx[q] -= Fx;
+    v->fy[q] -= Fy;
+    v->tau[q] += tauQ;
+    if (with_se) {
+      /* stress arms and accumulation exactly as written in the reference,
+       * including its three slips (spherocyl_box.cpp:486 uses nxB in the y arm,
+       * :493 adds a Pxy term into Pxx, and Pyx is never reset by calc_se) */
+      double CxA = s * nxA - 0.5 * dDx;
+      double CyA = s * nyA - 0.5 * dDy;
+      double CxB = t * nxB + 0.5 * dDx;
+      double CyB = t * nxB + 0.5 * dDy;
+      b->E += dvij * sig * (1.0 - dij / sig) / (2.0 * b->n);
+      b->Pxx += Fx * CxA / (Lx * Ly);
+      b->Pxx -= Fx * CxB / (Lx * Ly);
+      b->Pyy += Fy * CyA / (Lx * Ly);
+      b->Pyy -= Fy * CyB / (Lx * Ly);
+      b->Pxy += Fy * CxA / (Lx * Ly);
+      b->Pxx -= Fy * CxB / (Lx * Ly);
+      b->Pyx += Fx * CyA / (Lx * Ly);
+      b->Pyx -= Fx * CyB / (Lx * Ly);
+    }
+  }
+}
+
+static void zero3(double *a, double *b2, double *c, int n) {
+  for (int i = 0; i < n; i++) {
+    a[i] = 0.0;
+    b2[i] = 0.0;
+    c[i] = 0.0;
+  }
+}
+
+static void loop_pairs(orc_box *b, const pview *v, double gamma, double Lx, double Ly, int with_se) {
+  for (int p = 0; p < b->n; p++) {
+    const ivec *nl = &b->nbrs[p];
+    for (int j = 0; j < nl->len; j++) {
+      int q = nl->data[j];
+      if (q > p) force_pair(b, v, p, q, gamma, Lx, Ly, with_se);
+    }
+  }
+}
+
+/* calc_forces, strain_dynamics.cpp:137-153 */
+void orc_calc_forces(orc_box *b) {
+  pview v = {b->x, b->y, b->phi, b->fx, b->fy, b->tau};
+  zero3(b->fx, b->fy, b->tau, b->n);
+  loop_pairs(b, &v, b->gamma, b->Lx, b->Ly, 0);
+}
+
+/* calc_temp_forces, strain_dynamics.cpp:156-172 (also what calc_resized_forces,
+ * resize_dynamics.cpp:89-104, calls: the box lengths are the pre-resize ones) */
+static void calc_temp_forces(orc_box *b) {
+  pview v = {b->tx, b->ty, b->tphi, b->tfx, b->tfy, b->ttau};
+  zero3(b->tfx, b->tfy, b->ttau, b->n);
+  loop_pairs(b, &v, b->gamma + b->step * b->strain_rate, b->Lx, b->Ly, 0);
+}
+
+/* calc_se, spherocyl_box.cpp:502-522.  Pyx is deliberately not reset. */
+void orc_calc_se(orc_box *b) {
+  pview v = {b->x, b->y, b->phi, b->fx, b->fy, b->tau};
+  zero3(b->fx, b->fy, b->tau, b->n);
+  b->E = 0.0;
+  b->Pxx = 0.0;
+  b->Pyy = 0.0;
+  b->Pxy = 0.0;
+  loop_pairs(b, &v, b->gamma, b->Lx, b->Ly, 1);
+}
+
+void orc_zero_pyx(orc_box *b) { b->Pyx = 0.0; }
+
+/* isolated_rotation, strain_dynamics.cpp:174-177 */
+static double isolated_rotation(double RC, double phi) { return 0.5 * (1 - RC * cos(2 * phi)); }
+
+static int moved_too_far(const orc_box *b, int i) {
+  return b->xm[i] > 0.5 * b->pad || b->xm[i] < -0.5 * b->pad || b->ym[i] > 0.5 * b->pad ||
+         b->ym[i] < -0.5 * b->pad;
+}
+
+/* set_back_gamma, spherocyl_box.cpp:524-545 */
+static void set_back_gamma(orc_box *b) {
+  for (int i = 0; i < b->n; i++) {
+    if (b->y[i] < 0)
+      b->y[i] += b->Ly;
+    else if (b->y[i] > b->Ly)
+      b->y[i] -= b->Ly;
+    b->x[i] += b->y[i];
+    if (b->x[i] < 0)
+      b->x[i] += b->Lx;
+    else {
+      while (b->x[i] > b->Lx) b->x[i] -= b->Lx;
+    }
+  }
+  b->gamma -= 1.0;
+  b->gamma_total = (int)(b->gamma_total + 1) + b->gamma;
+  find_neighbors(b);
+}
+
+/* strain_step, strain_dynamics.cpp:179-235 (Heun predictor-corrector under
+ * Lees-Edwards shear, neighbour rebuild inside the corrector loop) */
+int orc_strain_step(orc_box *b) {
+  int n = b->n;
+  double *fx0 = (double *)malloc(3 * (size_t)n * sizeof(double));
+  if (!fx0) return -1;
+  double *fy0 = fx0 + n, *tau0 = fy0 + n;
+  for (int i = 0; i < n; i++) {
+    fx0[i] = b->fx[i] - b->gamma * b->fy[i];
+    fy0[i] = b->fy[i];
+    tau0[i] = b->tau[i] / b->I[i] - b->strain_rate * isolated_rotation(b->RC[i], b->phi[i]);
+    b->tx[i] = b->x[i] + b->step * fx0[i];
+    b->ty[i] = b->y[i] + b->step * fy0[i];
+    b->tphi[i] = b->phi[i] + b->step * tau0[i];
+  }
+  calc_temp_forces(b);
+  for (int i = 0; i < n; i++) {
+    double fx1 = b->tfx[i] - (b->gamma + b->step * b->strain_rate) * b->tfy[i];
+    double fy1 = b->tfy[i];
+    double tau1 = b->ttau[i] / b->I[i] - b->strain_rate * isolated_rotation(b->RC[i], b->tphi[i]);
+    double ddx = 0.5 * b->step * (fx0[i] + fx1);
+    double ddy = 0.5 * b->step * (fy0[i] + fy1);
+    double ddphi = 0.5 * b->step * (tau0[i] + tau1);
+    b->x[i] += ddx;
+    b->y[i] += ddy;
+    b->phi[i] += ddphi;
+    b->xm[i] += ddx;
+    b->ym[i] += ddy;
+    if (moved_too_far(b, i)) find_neighbors(b);
+  }
+  free(fx0);
+  b->gamma += b->strain_rate * b->step;
+  b->gamma_total += b->strain_rate * b->step;
+  if (b->gamma >= 0.5) set_back_gamma(b);
+  return b->err ? -1 : 0;
+}
+
+/* reconfigure_cells, resize_dynamics.cpp:106-121 (note the reference pairs the
+ * row count with Lx and the column count with Ly; the boxes here are square) */
+static void reconfigure_cells(orc_box *b) {
+  double wmin = 2.24 * (b->Rmax + b->Amax) + b->pad;
+  double hmin = 2 * (b->Rmax + b->Amax) + b->pad;
+  int rows = (int)(b->Lx / hmin);
+  int cols = (int)(b->Ly / wmin);
+  if (rows < 1) rows = 1;
+  if (cols < 1) cols = 1;
+  if (rows != b->rows || cols != b->cols) {
+    if (configure_cells(b)) b->err = 1;
+    find_neighbors(b);
+  } else {
+    b->W = b->Lx / b->cols;
+    b->H = b->Ly / b->rows;
+  }
+}
+
+/* resize_step, resize_dynamics.cpp:164-243 (Heun at the set strain rate's gamma
+ * with an affine scale of (1-rate)^dt applied to the predicted and corrected
+ * positions; the box shrinks after the corrector loop) */
+int orc_resize_step(orc_box *b, int shrink) {
+  int n = b->n;
+  double *fx0 = (double *)malloc(3 * (size_t)n * sizeof(double));
+  if (!fx0) return -1;
+  double *fy0 = fx0 + n, *tau0 = fy0 + n;
+  for (int i = 0; i < n; i++) {
+    fx0[i] = b->fx[i];
+    fy0[i] = b->fy[i];
+    tau0[i] = b->tau[i];
+    b->tx[i] = b->x[i] + b->step * fx0[i];
+    b->ty[i] = b->y[i] + b->step * fy0[i];
+    b->tphi[i] = b->phi[i] + b->step * tau0[i] / b->I[i];
+    if (shrink) {
+      b->tx[i] *= pow(1.0 - b->resize_rate, b->step);
+      b->ty[i] *= pow(1.0 - b->resize_rate, b->step);
+    } else {
+      b->tx[i] /= pow(1.0 - b->resize_rate, b->step);
+      b->ty[i] /= pow(1.0 - b->resize_rate, b->step);
+    }
+  }
+  calc_temp_forces(b);
+  for (int i = 0; i < n; i++) {
+    double ddx = 0.5 * b->step * (fx0[i] + b->tfx[i]);
+    double ddy = 0.5 * b->step * (fy0[i] + b->tfy[i]);
+    double ddphi = 0.5 * b->step * (tau0[i] + b->ttau[i]) / b->I[i];
+    double x0 = b->x[i], y0 = b->y[i];
+    b->x[i] += ddx;
+    b->y[i] += ddy;
+    b->phi[i] += ddphi;
+    if (shrink) {
+      b->x[i] *= pow(1.0 - b->resize_rate, b->step);
+      b->y[i] *= pow(1.0 - b->resize_rate, b->step);
+    } else {
+      b->x[i] /= pow(1.0 - b->resize_rate, b->step);
+      b->y[i] /= pow(1.0 - b->resize_rate, b->step);
+    }
+    b->xm[i] += b->x[i] - x0;
+    b->ym[i] += b->y[i] - y0;
+    reconfigure_cells(b);
+    if (moved_too_far(b, i)) find_neighbors(b);
+  }
+  free(fx0);
+  if (shrink) {
+    b->Lx *= pow(1.0 - b->resize_rate, b->step);
+    b->Ly *= pow(1.0 - b->resize_rate, b->step);
+  } else {
+    b->Lx /= pow(1.0 - b->resize_rate, b->step);
+    b->Ly /= pow(1.0 - b->resize_rate, b->step);
+  }
+  return b->err ? -1 : 0;
+}
+
+/* gradient_relax_step, relaxation_dynamics.cpp:11-31 */
+int orc_gd_step(orc_box *b) {
+  for (int i = 0; i < b->n; i++) {
+    double ddx = b->step * b->fx[i];
+    double ddy = b->step * b->fy[i];
+    b->x[i] += ddx;
+    b->y[i] += ddy;
+    b->phi[i] += b->step * b->tau[i] / b->I[i];
+    b->xm[i] += ddx;
+    b->ym[i] += ddy;
+    if (moved_too_far(b, i)) find_neighbors(b);
+  }
+  return b->err ? -1 : 0;
+}
+
+/* ---- construction: SpherocylBox(L, N, x, y, phi, A*, R*, pad),
+ * spherocyl_box.cpp:152-173 ---- */
+orc_box *orc_create(int n, double L, const double *x, const double *y, const double *phi,
+                    const double *A, const double *R, double pad) {
+  if (n <= 0 || !(L > 0)) return NULL;
+  orc_box *b = (orc_box *)calloc(1, sizeof(orc_box));
+  if (!b) return NULL;
+  b->n = n;
+  b->Lx = L;
+  b->Ly = L;
+  b->step = 0.05; /* set_defaults, spherocyl_box.cpp:16-53 */
+  size_t nd = (size_t)n;
+  double **arrs[] = {&b->x,  &b->y,   &b->phi, &b->R,  &b->A,  &b->I,   &b->RC, &b->fx, &b->fy,
+                     &b->tau, &b->xm, &b->ym,  &b->tx, &b->ty, &b->tphi, &b->tfx, &b->tfy, &b->ttau};
+  for (size_t k = 0; k < sizeof(arrs) / sizeof(arrs[0]); k++) {
+    *arrs[k] = (double *)calloc(nd, sizeof(double));
+    if (!*arrs[k]) {
+      orc_destroy(b);
+      return NULL;
+    }
+  }
+  b->cell = (int *)calloc(nd, sizeof(int));
+  b->nbrs = (ivec *)calloc(nd, sizeof(ivec));
+  if (!b->cell || !b->nbrs) {
+    orc_destroy(b);
+    return NULL;
+  }
+  for (int p = 0; p < n; p++) set_particle(b, p, x[p], y[p], phi[p], A[p], R[p]);
+  b->packing = packing_fraction(b);
+  b->pad = pad;
+  if (configure_cells(b)) {
+    orc_destroy(b);
+    return NULL;
+  }
+  find_neighbors(b);
+  return b;
+}
+
+void orc_destroy(orc_box *b) {
+  if (!b) return;
+  double *arrs[] = {b->x,  b->y,  b->phi, b->R,  b->A,  b->I,   b->RC,  b->fx,  b->fy,
+                    b->tau, b->xm, b->ym, b->tx, b->ty, b->tphi, b->tfx, b->tfy, b->ttau};
+  for (size_t k = 0; k < sizeof(arrs) / sizeof(arrs[0]); k++) free(arrs[k]);
+  free(b->cell);
+  ivec_free_array(b->nbrs, b->n);
+  ivec_free_array(b->cells, b->ncells);
+  free(b->cell_nbrs);
+  free(b);
+}
+
+/* setters mirror spherocyl_box.h:110-119 */
+void orc_set_strain_rate(orc_box *b, double v) { b->strain_rate = v; }
+void orc_set_resize_rate(orc_box *b, double v) { b->resize_rate = v; }
+void orc_set_step(orc_box *b, double v) { b->step = v; }
+void orc_set_gamma(orc_box *b, double v) { b->gamma = v; }
+void orc_set_total_gamma(orc_box *b, double v) { b->gamma_total = v; }
+void orc_find_neighbors(orc_box *b) { find_neighbors(b); }
+
+int orc_n(const orc_box *b) { return b->n; }
+
+void orc_get_state(const orc_box *b, double *x, double *y, double *phi) {
+  memcpy(x, b->x, (size_t)b->n * sizeof(double));
+  memcpy(y, b->y, (size_t)b->n * sizeof(double));
+  memcpy(phi, b->phi, (size_t)b->n * sizeof(double));
+}
+
+void orc_get_forces(const orc_box *b, double *fx, double *fy, double *tau) {
+  memcpy(fx, b->fx, (size_t)b->n * sizeof(double));
+  memcpy(fy, b->fy, (size_t)b->n * sizeof(double));
+  memcpy(tau, b->tau, (size_t)b->n * sizeof(double));
+}
+
+void orc_get_moved(const orc_box *b, double *xm, double *ym) {
+  memcpy(xm, b->xm, (size_t)b->n * sizeof(double));
+  memcpy(ym, b->ym, (size_t)b->n * sizeof(double));
+}
+
+void orc_get_consts(const orc_box *b, double *I, double *RC) {
+  memcpy(I, b->I, (size_t)b->n * sizeof(double));
+  memcpy(RC, b->RC, (size_t)b->n * sizeof(double));
+}
+
+/* out[0..9]: Lx Ly gamma gamma_total pad W H packing rows cols */
+void orc_get_scalars(const orc_box *b, double *out) {
+  out[0] = b->Lx;
+  out[1] = b->Ly;
+  out[2] = b->gamma;
+  out[3] = b->gamma_total;
+  out[4] = b->pad;
+  out[5] = b->W;
+  out[6] = b->H;
+  out[7] = b->packing;
+  out[8] = b->rows;
+  out[9] = b->cols;
+}
+
+/* out[0..4]: E Pxx Pyy Pxy Pyx as the reference accumulates them */
+void orc_get_se(const orc_box *b, double *out) {
+  out[0] = b->E;
+  out[1] = b->Pxx;
+  out[2] = b->Pyy;
+  out[3] = b->Pxy;
+  out[4] = b->Pyx;
+}
+
+long orc_n_rebuilds(const orc_box *b) { return b->n_rebuilds; }
+
+/* Number of half-list pairs; when pairs != NULL writes (p, q) pairs in list order. */
+long orc_get_pairs(const orc_box *b, int *pairs, long cap) {
+  long k = 0;
+  for (int p = 0; p < b->n; p++) {
+    for (int j = 0; j < b->nbrs[p].len; j++) {
+      if (pairs && k < cap) {
+        pairs[2 * k] = p;
+        pairs[2 * k + 1] = b->nbrs[p].data[j];
+      }
+      k++;
+    }
+  }
+  return k;
+}
+
+/* Inner loop of run_strain, strain_dynamics.cpp:285-296: strain_step followed by
+ * calc_forces (or calc_se on stress-save steps).  se_out receives 5 values per
+ * step when non-NULL (then calc_se runs every step). */
+int orc_run_strain_steps(orc_box *b, int nsteps, double *se_out) {
+  for (int k = 0; k < nsteps; k++) {
+    if (orc_strain_step(b)) return -1;
+    if (se_out) {
+      orc_calc_se(b);
+      orc_get_se(b, se_out + 5 * (size_t)k);
+    } else {
+      orc_calc_forces(b);
+    }
+  }
+  return 0;
+}
+
+/* Inner loop of resize_box, resize_dynamics.cpp:297-307 */
+int orc_run_resize_steps(orc_box *b, int nsteps, int shrink, double *se_out) {
+  for (int k = 0; k < nsteps; k++) {
+    if (orc_resize_step(b, shrink)) return -1;
+    if (se_out) {
+      orc_calc_se(b);
+      orc_get_se(b, se_out + 5 * (size_t)k);
+    } else {
+      orc_calc_forces(b);
+    }
+  }
+  return 0;
+}
+
+/* Loop body of gradient_descent_minimize, relaxation_dynamics.cpp:38-60
+ * (calc_se, then a gradient step), without the file output.  Returns the number
+ * of steps taken before E <= emin (or nsteps). */
+int orc_run_gd_steps(orc_box *b, int nsteps, double emin, double *e_out) {
+  int s;
+  for (s = 0; s < nsteps; s++) {
+    orc_calc_se(b);
+    if (e_out) e_out[s] = b->E;
+    if (b->E <= emin) break;
+    if (orc_gd_step(b)) return -1;
+  }
+  return s;
+}

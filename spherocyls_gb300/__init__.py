@@ -1,0 +1,11 @@
+"""spherocyls_gb300 -- GB300 (sm_103a) implementation of the overdamped-dynamics hot
+path of tmarschall/spherocyls: 2D bidisperse spherocylinder packings under
+Lees-Edwards shear and affine box resize, plus energy minimisation.
+
+The work is done by ``libspherocyl`` (C++ host runtime + hand-written CUDA kernels,
+C ABI in ``include/spherocyl.h``); this package binds it with ctypes.
+"""
+from ._lib import ScError, lib
+from .box import BoxBatch, SpherocylBox, generate_packing
+
+__all__ = ["BoxBatch", "SpherocylBox", "generate_packing", "ScError", "lib"]

@@ -1,0 +1,202 @@
+"""Python mirror of the reference's box object over the C ABI.
+
+``SpherocylBox`` follows the interface of tmarschall/spherocyls' ``SpherocylBox``
+(src/cpp/spherocyl_box.h:86-119): the constructor takes the box side, particle
+arrays and the cell padding; setters for strain rate, resize rate, step, gamma and
+total gamma; ``find_neighbors``, ``calc_forces``, ``calc_se``; the per-step
+routines of ``run_strain`` / ``resize_box`` / ``gradient_descent_minimize``.  A
+box may hold several independent systems that advance together (``BoxBatch``).
+All work happens in libspherocyl on the GPU; this module only moves arrays.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import PREC, STRESS, ScOptions, check, lib
+
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(_dp)
+
+
+def generate_packing(n: int, packing: float, a_over_r: float, r_small: float = 0.5,
+                     r_ratio: float = 1.4, seed: int = 0, min_sep: float = 0.1):
+    """Seeded crossing-free bidisperse packing: returns (L, x, y, phi, R, A)."""
+    x, y, p, R, A = (np.empty(n) for _ in range(5))
+    L = ctypes.c_double()
+    st = lib().sc_generate_packing(int(n), float(packing), float(a_over_r), float(r_small),
+                                   float(r_ratio), ctypes.c_uint64(int(seed)), float(min_sep),
+                                   _ptr(x), _ptr(y), _ptr(p), _ptr(R), _ptr(A), ctypes.byref(L))
+    if st != 0:
+        raise _lib.ScError(st, "packing generation failed")
+    return L.value, x, y, p, R, A
+
+
+class BoxBatch:
+    """One or more independent periodic boxes advanced together on one GPU."""
+
+    def __init__(self, n_per_sys, L, x, y, phi, A, R, pad=0.0, *, precision: str = "fp64",
+                 stress: str = "compat", device: int = 0, max_nbrs: int = 0,
+                 use_graphs: bool = True, block: int = 0, profile: bool = False):
+        n_per_sys = np.ascontiguousarray(np.atleast_1d(n_per_sys), dtype=np.int32)
+        self.nsys = int(n_per_sys.shape[0])
+        self.n_per_sys = n_per_sys
+        self.ntot = int(n_per_sys.sum())
+        L = _f64(np.broadcast_to(np.asarray(L, dtype=np.float64), (self.nsys,)))
+        pad = _f64(np.broadcast_to(np.asarray(pad, dtype=np.float64), (self.nsys,)))
+        x, y, phi, A, R = (_f64(v) for v in (x, y, phi, A, R))
+        for v in (x, y, phi, A, R):
+            if v.shape[0] != self.ntot:
+                raise ValueError("particle arrays must hold sum(n_per_sys) entries")
+        opt = ScOptions()
+        lib().sc_default_options(ctypes.byref(opt))
+        opt.precision = PREC[precision]
+        opt.stress_mode = STRESS[stress]
+        opt.device = int(device)
+        opt.max_nbrs = int(max_nbrs)
+        opt.use_graphs = int(bool(use_graphs))
+        opt.block = int(block)
+        opt.profile = int(bool(profile))
+        self.precision = precision
+        h = ctypes.c_void_p()
+        st = lib().sc_create(ctypes.byref(opt), self.nsys,
+                             n_per_sys.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _ptr(L),
+                             _ptr(pad), _ptr(x), _ptr(y), _ptr(phi), _ptr(R), _ptr(A),
+                             ctypes.byref(h))
+        check(st, None)
+        self.h = h
+
+    # --- lifetime ---------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            lib().sc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _chk(self, st):
+        check(st, self.h)
+
+    # --- setters (spherocyl_box.h:112-119) ----------------------------------
+    def set_strain_rate(self, v, sys=-1):
+        self._chk(lib().sc_set_strain_rate(self.h, sys, float(v)))
+
+    def set_resize_rate(self, v, sys=-1):
+        self._chk(lib().sc_set_resize_rate(self.h, sys, float(v)))
+
+    def set_step(self, v, sys=-1):
+        self._chk(lib().sc_set_step(self.h, sys, float(v)))
+
+    def set_gamma(self, v, sys=-1):
+        self._chk(lib().sc_set_gamma(self.h, sys, float(v)))
+
+    def set_total_gamma(self, v, sys=-1):
+        self._chk(lib().sc_set_total_gamma(self.h, sys, float(v)))
+
+    def set_stream(self, stream_ptr: int | None):
+        self._chk(lib().sc_set_stream(self.h, ctypes.c_void_p(stream_ptr or 0)))
+
+    def synchronize(self):
+        self._chk(lib().sc_synchronize(self.h))
+
+    # --- compute ----------------------------------------------------------
+    def find_neighbors(self):
+        self._chk(lib().sc_find_neighbors(self.h))
+
+    def calc_forces(self):
+        self._chk(lib().sc_calc_forces(self.h))
+
+    def calc_se(self) -> np.ndarray:
+        """(nsys, 5): E, Pxx, Pyy, Pxy, Pyx per system."""
+        out = np.empty((self.nsys, 5))
+        self._chk(lib().sc_calc_se(self.h, _ptr(out)))
+        return out
+
+    def strain_steps(self, nsteps: int, se_every: int = 0):
+        out = None
+        if se_every > 0 and nsteps // se_every > 0:
+            out = np.empty((nsteps // se_every, self.nsys, 5))
+        self._chk(lib().sc_strain_steps(self.h, int(nsteps), int(se_every),
+                                        _ptr(out) if out is not None else None))
+        return out
+
+    def resize_steps(self, nsteps: int, shrink: bool = True, se_every: int = 0):
+        out = None
+        if se_every > 0 and nsteps // se_every > 0:
+            out = np.empty((nsteps // se_every, self.nsys, 5))
+        self._chk(lib().sc_resize_steps(self.h, int(nsteps), int(bool(shrink)), int(se_every),
+                                        _ptr(out) if out is not None else None))
+        return out
+
+    def gd_minimize(self, max_steps: int, e_min: float = 0.0):
+        steps = ctypes.c_int()
+        ef = ctypes.c_double()
+        self._chk(lib().sc_gd_minimize(self.h, int(max_steps), float(e_min), ctypes.byref(steps),
+                                       ctypes.byref(ef)))
+        return steps.value, ef.value
+
+    # --- state ------------------------------------------------------------
+    def state(self):
+        x, y, p = (np.empty(self.ntot) for _ in range(3))
+        self._chk(lib().sc_get_state(self.h, _ptr(x), _ptr(y), _ptr(p)))
+        return x, y, p
+
+    def forces(self):
+        fx, fy, t = (np.empty(self.ntot) for _ in range(3))
+        self._chk(lib().sc_get_forces(self.h, _ptr(fx), _ptr(fy), _ptr(t)))
+        return fx, fy, t
+
+    def box(self, sys: int = 0) -> dict:
+        out = np.empty(10)
+        self._chk(lib().sc_get_box(self.h, int(sys), _ptr(out)))
+        keys = ("Lx", "Ly", "gamma", "gamma_total", "pad", "W", "H", "packing", "rows", "cols")
+        return dict(zip(keys, out.tolist()))
+
+    def pairs(self, sys: int = 0) -> np.ndarray:
+        n = ctypes.c_long()
+        self._chk(lib().sc_get_pairs(self.h, int(sys), None, 0, ctypes.byref(n)))
+        out = np.empty((max(n.value, 1), 2), dtype=np.int32)
+        self._chk(lib().sc_get_pairs(self.h, int(sys), out.ctypes.data_as(
+            ctypes.POINTER(ctypes.c_int)), n.value, ctypes.byref(n)))
+        return out[: n.value]
+
+    def counters(self) -> dict:
+        out = (ctypes.c_longlong * 3)()
+        self._chk(lib().sc_get_counters(self.h, out))
+        return {"steps": out[0], "rebuilds": out[1], "status": out[2]}
+
+    def pass_times(self) -> dict:
+        out = np.empty(6)
+        self._chk(lib().sc_get_pass_times(self.h, _ptr(out)))
+        return {"corr_ms": out[0], "pred_ms": out[1], "rebuild_ms": out[2],
+                "n_corr": int(out[3]), "n_pred": int(out[4]), "n_rebuild": int(out[5])}
+
+
+class SpherocylBox(BoxBatch):
+    """A single periodic square box: SpherocylBox(L, N, x, y, phi, A*, R*, pad)."""
+
+    def __init__(self, L, x, y, phi, A, R, pad=0.0, **kw):
+        x = _f64(x)
+        super().__init__([x.shape[0]], [L], x, y, phi, A, R, [pad], **kw)
+
+    def calc_se(self) -> np.ndarray:
+        return super().calc_se()[0]

@@ -1,0 +1,522 @@
+// sc_api.cpp -- extern "C" entry points of libspherocyl (include/spherocyl.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/spherocyl.h"
+#include "sc_host.hpp"
+#include "sc_internal.hpp"
+
+struct sc_handle {
+  sc::Handle h;
+};
+
+namespace {
+
+const double kRefPi = 3.14159265358979;  // src/cpp/spherocyl_box.cpp:12
+thread_local std::string g_create_error;
+
+bool finite_all(const double* a, size_t n) {
+  for (size_t i = 0; i < n; i++)
+    if (!std::isfinite(a[i])) return false;
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* sc_version(void) { return "spherocyls_gb300 0.1 (sm_103a)"; }
+
+const char* sc_status_string(int status) {
+  switch (status) {
+    case SC_OK: return "ok";
+    case SC_E_ARG: return "invalid argument";
+    case SC_E_IO: return "file i/o error";
+    case SC_E_NAN: return "non-finite state";
+    case SC_E_OVERFLOW: return "capacity exceeded";
+    case SC_E_NOCONV: return "not converged";
+    case SC_E_TIMEOUT: return "device wait timed out";
+    case SC_E_CUDA: return "cuda error";
+    case SC_E_STATE: return "invalid state";
+    case SC_E_NOMEM: return "out of memory";
+  }
+  return "unknown status";
+}
+
+void sc_default_options(sc_options* opt) {
+  if (!opt) return;
+  std::memset(opt, 0, sizeof *opt);
+  opt->precision = SC_PREC_FP64;
+  opt->stress_mode = SC_STRESS_COMPAT;
+  opt->device = 0;
+  opt->max_nbrs = 0;
+  opt->use_graphs = 1;
+  opt->block = 0;
+  opt->profile = 0;
+}
+
+const char* sc_last_error(const sc_handle* h) {
+  if (!h) return g_create_error.c_str();
+  return h->h.err.c_str();
+}
+
+int sc_create(const sc_options* opt_in, int n_sys, const int* n_per_sys, const double* L,
+              const double* pad, const double* x, const double* y, const double* phi,
+              const double* R, const double* A, sc_handle** out) {
+  g_create_error.clear();
+  if (!out) return SC_E_ARG;
+  *out = nullptr;
+  if (n_sys <= 0 || !n_per_sys || !L || !x || !y || !phi || !R || !A) {
+    g_create_error = "sc_create: missing arrays or n_sys <= 0";
+    return SC_E_ARG;
+  }
+  sc_options opt;
+  if (opt_in)
+    opt = *opt_in;
+  else
+    sc_default_options(&opt);
+  if (opt.precision != SC_PREC_FP64 && opt.precision != SC_PREC_MIXED) {
+    g_create_error = "sc_create: unknown precision";
+    return SC_E_ARG;
+  }
+  long long ntot_ll = 0;
+  for (int s = 0; s < n_sys; s++) {
+    if (n_per_sys[s] < 2 || !(L[s] > 0) || !std::isfinite(L[s]) || (pad && !(pad[s] >= 0))) {
+      char buf[160];
+      snprintf(buf, sizeof buf, "sc_create: system %d needs n >= 2, L > 0 and pad >= 0", s);
+      g_create_error = buf;
+      return SC_E_ARG;
+    }
+    ntot_ll += n_per_sys[s];
+  }
+  if (ntot_ll > (1LL << 30)) {
+    g_create_error = "sc_create: too many particles";
+    return SC_E_ARG;
+  }
+  const int ntot = (int)ntot_ll;
+  if (!finite_all(x, ntot) || !finite_all(y, ntot) || !finite_all(phi, ntot) ||
+      !finite_all(R, ntot) || !finite_all(A, ntot)) {
+    g_create_error = "sc_create: non-finite input";
+    return SC_E_NAN;
+  }
+  for (int i = 0; i < ntot; i++)
+    if (!(R[i] > 0) || !(A[i] >= 0)) {
+      g_create_error = "sc_create: every R must be > 0 and every A >= 0";
+      return SC_E_ARG;
+    }
+
+  sc_handle* H = new (std::nothrow) sc_handle;
+  if (!H) return SC_E_NOMEM;
+  sc::Handle& h = H->h;
+  h.opt = opt;
+  h.device = opt.device;
+  h.prec = opt.precision;
+  h.block = opt.block > 0 ? opt.block : 128;
+  h.nsys = n_sys;
+  h.ntot = ntot;
+  auto bail = [&](int code) {
+    g_create_error = h.err.empty() ? std::string("sc_create failed") : h.err;
+    delete H;
+    return code;
+  };
+  if (!h.cuda_ok(cudaSetDevice(h.device), "cudaSetDevice")) return bail(SC_E_CUDA);
+  if (!h.cuda_ok(cudaStreamCreateWithFlags(&h.stream, cudaStreamNonBlocking), "stream"))
+    return bail(SC_E_CUDA);
+  h.own_stream = true;
+  if (!h.cuda_ok(cudaMallocHost((void**)&h.h_pinned, (16 + 12 * (size_t)n_sys) * sizeof(int)),
+                 "pinned"))
+    return bail(SC_E_NOMEM);
+
+  // host-side particle constants: set_particle, src/cpp/spherocyl_box.cpp:188-221
+  std::vector<double> hx(x, x + ntot), hy(y, y + ntot), hp(phi, phi + ntot);
+  std::vector<double> hI(ntot), hRC(ntot);
+  h.hs.resize(n_sys);
+  int p0 = 0;
+  for (int s = 0; s < n_sys; s++) {
+    sc::HostSys& S = h.hs[s];
+    S.n = n_per_sys[s];
+    S.p0 = p0;
+    S.Lx = S.Ly = L[s];
+    S.pad = pad ? pad[s] : 0.0;
+    double filled = 0.0;
+    for (int k = 0; k < S.n; k++) {
+      int i = p0 + k;
+      double al = A[i] / R[i];
+      double C = (3 * kRefPi + 24 * al + 6 * kRefPi * al * al + 8 * al * al * al);
+      double area = R[i] * (kRefPi * R[i] + 4 * A[i]);
+      hI[i] = R[i] * R[i] * R[i] * R[i] * C / (6 * area);
+      hRC[i] = (8 * al + 6 * kRefPi * al * al + 8 * al * al * al) / C;
+      while (hx[i] > S.Lx) hx[i] -= S.Lx;
+      while (hx[i] < 0.0) hx[i] += S.Lx;
+      while (hy[i] > S.Ly) hy[i] -= S.Ly;
+      while (hy[i] < 0.0) hy[i] += S.Ly;
+      while (hp[i] > kRefPi) hp[i] -= 2 * kRefPi;
+      while (hp[i] < -kRefPi) hp[i] += 2 * kRefPi;
+      if (A[i] > S.Amax) S.Amax = A[i];
+      if (R[i] > S.Rmax) S.Rmax = R[i];
+      filled += (kRefPi * R[i] + 4.0 * A[i]) * R[i];
+    }
+    S.packing = filled / (S.Lx * S.Ly);
+    S.configure(true);
+    p0 += S.n;
+  }
+
+  // device arrays
+  const size_t N = ntot;
+  sc::Dev& d = h.d;
+  d.ntot = ntot;
+  d.nsys = n_sys;
+  d.stress_mode = opt.stress_mode == SC_STRESS_VIRIAL ? sc::STRESS_VIRIAL : sc::STRESS_COMPAT;
+  d.maxn = opt.max_nbrs > 0 ? opt.max_nbrs : 64;
+  std::vector<int> pchunk_sys, pchunk_p0, pchunk_np;
+  for (int s = 0; s < n_sys; s++) {
+    const sc::HostSys& S = h.hs[s];
+    for (int k = 0; k < S.n; k += sc::kSeChunk) {
+      pchunk_sys.push_back(s);
+      pchunk_p0.push_back(S.p0 + k);
+      pchunk_np.push_back(std::min(sc::kSeChunk, S.n - k));
+    }
+  }
+  d.npchunks = (int)pchunk_sys.size();
+  bool ok = true;
+  sc::SysGeom* geom = nullptr;
+  int *psys = nullptr, *pcs = nullptr, *pcp = nullptr, *pcn = nullptr;
+  ok = ok && h.dalloc(&geom, n_sys, "geom") && h.dalloc(&psys, N, "psys");
+  ok = ok && h.dalloc(&d.xy, N, "xy") && h.dalloc(&d.ph, N, "ph") && h.dalloc(&d.ra, N, "ra") &&
+       h.dalloc(&d.irc, N, "irc") && h.dalloc(&d.id, N, "id") && h.dalloc(&d.cell, N, "cell");
+  ok = ok && h.dalloc(&d.nxy, N, "nxy") && h.dalloc(&d.xy_t, N, "xy_t") &&
+       h.dalloc(&d.ph_t, N, "ph_t") && h.dalloc(&d.nxy_t, N, "nxy_t");
+  ok = ok && h.dalloc(&d.v0x, N, "v0x") && h.dalloc(&d.v0y, N, "v0y") &&
+       h.dalloc(&d.v0p, N, "v0p") && h.dalloc(&d.fx, N, "fx") && h.dalloc(&d.fy, N, "fy") &&
+       h.dalloc(&d.tau, N, "tau") && h.dalloc(&d.moved, N, "moved");
+  if (h.prec == sc::PREC_MIXED)
+    ok = ok && h.dalloc(&d.rec, N, "rec") && h.dalloc(&d.rec_t, N, "rec_t") &&
+         h.dalloc(&d.raf, N, "raf");
+  else
+    ok = ok && h.dalloc(&d.nbr, N * d.maxn, "nbr");
+  ok = ok && h.dalloc(&d.nbr_n, N, "nbr_n");
+  ok = ok && h.dalloc(&d.cell_tmp, N, "cell_tmp") && h.dalloc(&d.rank, N, "rank") &&
+       h.dalloc(&d.perm, N, "perm");
+  ok = ok && h.dalloc(&d.s_xy, N, "s_xy") && h.dalloc(&d.s_ph, N, "s_ph") &&
+       h.dalloc(&d.s_ra, N, "s_ra") && h.dalloc(&d.s_irc, N, "s_irc") &&
+       h.dalloc(&d.s_id, N, "s_id") && h.dalloc(&d.s_cell, N, "s_cell");
+  ok = ok && h.dalloc(&d.se_part, 5 * N, "se_part") &&
+       h.dalloc(&d.se_chunk, 5 * (size_t)d.npchunks, "se_chunk") &&
+       h.dalloc(&d.se_sys, 5 * (size_t)n_sys, "se_sys");
+  ok = ok && h.dalloc(&pcs, d.npchunks, "pchunk") && h.dalloc(&pcp, d.npchunks, "pchunk") &&
+       h.dalloc(&pcn, d.npchunks, "pchunk");
+  ok = ok && h.dalloc(&d.flags, n_sys, "flags") && h.dalloc(&d.any, 1, "any") &&
+       h.dalloc(&d.status, 2, "status");
+  if (!ok) return bail(h.last_status ? h.last_status : SC_E_NOMEM);
+  d.geom = geom;
+  d.psys = psys;
+  d.pchunk_sys = pcs;
+  d.pchunk_p0 = pcp;
+  d.pchunk_np = pcn;
+
+  // initial slots: the input order
+  std::vector<double2> xy(N), ra(N), irc(N);
+  std::vector<int> id(N), ps(N);
+  for (int s = 0; s < n_sys; s++) {
+    const sc::HostSys& S = h.hs[s];
+    for (int k = 0; k < S.n; k++) {
+      int i = S.p0 + k;
+      xy[i] = make_double2(hx[i], hy[i]);
+      ra[i] = make_double2(R[i], A[i]);
+      irc[i] = make_double2(hI[i], hRC[i]);
+      id[i] = k;
+      ps[i] = s;
+    }
+  }
+  cudaStream_t st = h.stream;
+  ok = h.cuda_ok(cudaMemcpyAsync(d.xy, xy.data(), N * sizeof(double2), cudaMemcpyHostToDevice, st),
+                 "upload") &&
+       h.cuda_ok(cudaMemcpyAsync(d.ph, hp.data(), N * sizeof(double), cudaMemcpyHostToDevice, st),
+                 "upload") &&
+       h.cuda_ok(cudaMemcpyAsync(d.ra, ra.data(), N * sizeof(double2), cudaMemcpyHostToDevice, st),
+                 "upload") &&
+       h.cuda_ok(cudaMemcpyAsync(d.irc, irc.data(), N * sizeof(double2), cudaMemcpyHostToDevice,
+                                 st), "upload") &&
+       h.cuda_ok(cudaMemcpyAsync(d.id, id.data(), N * sizeof(int), cudaMemcpyHostToDevice, st),
+                 "upload") &&
+       h.cuda_ok(cudaMemcpyAsync(psys, ps.data(), N * sizeof(int), cudaMemcpyHostToDevice, st),
+                 "upload") &&
+       h.cuda_ok(cudaMemcpyAsync(pcs, pchunk_sys.data(), d.npchunks * sizeof(int),
+                                 cudaMemcpyHostToDevice, st), "upload") &&
+       h.cuda_ok(cudaMemcpyAsync(pcp, pchunk_p0.data(), d.npchunks * sizeof(int),
+                                 cudaMemcpyHostToDevice, st), "upload") &&
+       h.cuda_ok(cudaMemcpyAsync(pcn, pchunk_np.data(), d.npchunks * sizeof(int),
+                                 cudaMemcpyHostToDevice, st), "upload") &&
+       h.cuda_ok(cudaMemsetAsync(d.moved, 0, N * sizeof(double2), st), "memset") &&
+       h.cuda_ok(cudaMemsetAsync(d.flags, 0, n_sys * sizeof(int), st), "memset") &&
+       h.cuda_ok(cudaMemsetAsync(d.any, 0, sizeof(int), st), "memset") &&
+       h.cuda_ok(cudaMemsetAsync(d.status, 0, 2 * sizeof(int), st), "memset") &&
+       h.cuda_ok(cudaMemsetAsync(d.nbr_n, 0, N * sizeof(int), st), "memset") &&
+       h.cuda_ok(cudaMemsetAsync(d.fx, 0, N * sizeof(double), st), "memset") &&
+       h.cuda_ok(cudaMemsetAsync(d.fy, 0, N * sizeof(double), st), "memset") &&
+       h.cuda_ok(cudaMemsetAsync(d.tau, 0, N * sizeof(double), st), "memset") &&
+       h.cuda_ok(cudaStreamSynchronize(st), "upload sync");
+  if (!ok) return bail(h.last_status);
+  if (!h.layout_cells() || !h.rebuild_all() || !h.check_status("create"))
+    return bail(h.last_status);
+  *out = H;
+  return SC_OK;
+}
+
+int sc_destroy(sc_handle* h) {
+  delete h;
+  return SC_OK;
+}
+
+int sc_set_stream(sc_handle* H, void* stream) {
+  if (!H) return SC_E_ARG;
+  sc::Handle& h = H->h;
+  cudaSetDevice(h.device);
+  cudaStreamSynchronize(h.stream);
+  if (h.own_stream && h.stream) cudaStreamDestroy(h.stream);
+  if (stream) {
+    h.stream = (cudaStream_t)stream;
+    h.own_stream = false;
+  } else {
+    cudaStreamCreateWithFlags(&h.stream, cudaStreamNonBlocking);
+    h.own_stream = true;
+  }
+  return SC_OK;
+}
+
+int sc_synchronize(sc_handle* H) {
+  if (!H) return SC_E_ARG;
+  sc::Handle& h = H->h;
+  cudaSetDevice(h.device);
+  return h.check_status("synchronize") ? SC_OK : h.last_status;
+}
+
+static int set_scalar(sc_handle* H, int sys, double v, double sc::HostSys::*field, bool rebuild,
+                      const char* what) {
+  if (!H) return SC_E_ARG;
+  sc::Handle& h = H->h;
+  if (sys < -1 || sys >= h.nsys || !std::isfinite(v)) {
+    h.fail(SC_E_ARG, "%s: bad system index or value", what);
+    return SC_E_ARG;
+  }
+  for (int s = 0; s < h.nsys; s++)
+    if (sys < 0 || s == sys) h.hs[s].*field = v;
+  h.pred_valid = false;
+  if (rebuild) {
+    cudaSetDevice(h.device);
+    if (!h.rebuild_all() || !h.check_status(what)) return h.last_status;
+  }
+  return SC_OK;
+}
+
+int sc_set_strain_rate(sc_handle* h, int sys, double v) {
+  return set_scalar(h, sys, v, &sc::HostSys::strain_rate, false, "sc_set_strain_rate");
+}
+int sc_set_resize_rate(sc_handle* h, int sys, double v) {
+  return set_scalar(h, sys, v, &sc::HostSys::resize_rate, false, "sc_set_resize_rate");
+}
+int sc_set_step(sc_handle* h, int sys, double v) {
+  return set_scalar(h, sys, v, &sc::HostSys::step, false, "sc_set_step");
+}
+// The neighbour criterion depends on gamma, so a new gamma rebuilds the lists.
+int sc_set_gamma(sc_handle* h, int sys, double v) {
+  return set_scalar(h, sys, v, &sc::HostSys::gamma, true, "sc_set_gamma");
+}
+int sc_set_total_gamma(sc_handle* h, int sys, double v) {
+  return set_scalar(h, sys, v, &sc::HostSys::gamma_total, false, "sc_set_total_gamma");
+}
+
+int sc_find_neighbors(sc_handle* H) {
+  if (!H) return SC_E_ARG;
+  sc::Handle& h = H->h;
+  cudaSetDevice(h.device);
+  if (!h.rebuild_all() || !h.check_status("sc_find_neighbors")) return h.last_status;
+  return SC_OK;
+}
+
+int sc_calc_forces(sc_handle* H) {
+  if (!H) return SC_E_ARG;
+  return H->h.calc(false, nullptr);
+}
+
+int sc_calc_se(sc_handle* H, double* se_out) {
+  if (!H) return SC_E_ARG;
+  return H->h.calc(true, se_out);
+}
+
+int sc_strain_steps(sc_handle* H, int nsteps, int se_every, double* se_out) {
+  if (!H) return SC_E_ARG;
+  return H->h.run_steps(false, 0, nsteps, se_every, se_out);
+}
+
+int sc_resize_steps(sc_handle* H, int nsteps, int shrink, int se_every, double* se_out) {
+  if (!H) return SC_E_ARG;
+  return H->h.run_steps(true, shrink ? 1 : 0, nsteps, se_every, se_out);
+}
+
+int sc_gd_minimize(sc_handle* H, int max_steps, double e_min, int* steps_taken, double* e_final) {
+  if (!H) return SC_E_ARG;
+  if (max_steps < 0) {
+    H->h.fail(SC_E_ARG, "max_steps must be >= 0");
+    return SC_E_ARG;
+  }
+  return H->h.gd_minimize(max_steps, e_min, steps_taken, e_final);
+}
+
+// slot -> original index (systems concatenated)
+static bool read_ids(sc::Handle& h, std::vector<int>& gid) {
+  std::vector<int> id(h.ntot);
+  if (!h.cuda_ok(cudaMemcpyAsync(id.data(), h.d.id, h.ntot * sizeof(int), cudaMemcpyDeviceToHost,
+                                 h.stream), "read ids"))
+    return false;
+  if (!h.cuda_ok(cudaStreamSynchronize(h.stream), "read ids")) return false;
+  gid.resize(h.ntot);
+  for (int s = 0; s < h.nsys; s++)
+    for (int k = 0; k < h.hs[s].n; k++) {
+      int i = h.hs[s].p0 + k;
+      gid[i] = h.hs[s].p0 + id[i];
+    }
+  return true;
+}
+
+int sc_get_state(sc_handle* H, double* x, double* y, double* phi) {
+  if (!H) return SC_E_ARG;
+  sc::Handle& h = H->h;
+  cudaSetDevice(h.device);
+  std::vector<double2> xy(h.ntot);
+  std::vector<double> ph(h.ntot);
+  std::vector<int> gid;
+  if (!h.cuda_ok(cudaMemcpyAsync(xy.data(), h.d.xy, h.ntot * sizeof(double2),
+                                 cudaMemcpyDeviceToHost, h.stream), "read state") ||
+      !h.cuda_ok(cudaMemcpyAsync(ph.data(), h.d.ph, h.ntot * sizeof(double),
+                                 cudaMemcpyDeviceToHost, h.stream), "read state") ||
+      !read_ids(h, gid))
+    return h.last_status;
+  for (int i = 0; i < h.ntot; i++) {
+    if (x) x[gid[i]] = xy[i].x;
+    if (y) y[gid[i]] = xy[i].y;
+    if (phi) phi[gid[i]] = ph[i];
+  }
+  return SC_OK;
+}
+
+int sc_get_forces(sc_handle* H, double* fx, double* fy, double* tau) {
+  if (!H) return SC_E_ARG;
+  sc::Handle& h = H->h;
+  cudaSetDevice(h.device);
+  std::vector<double> a(h.ntot), b(h.ntot), c(h.ntot);
+  std::vector<int> gid;
+  if (!h.cuda_ok(cudaMemcpyAsync(a.data(), h.d.fx, h.ntot * sizeof(double),
+                                 cudaMemcpyDeviceToHost, h.stream), "read forces") ||
+      !h.cuda_ok(cudaMemcpyAsync(b.data(), h.d.fy, h.ntot * sizeof(double),
+                                 cudaMemcpyDeviceToHost, h.stream), "read forces") ||
+      !h.cuda_ok(cudaMemcpyAsync(c.data(), h.d.tau, h.ntot * sizeof(double),
+                                 cudaMemcpyDeviceToHost, h.stream), "read forces") ||
+      !read_ids(h, gid))
+    return h.last_status;
+  for (int i = 0; i < h.ntot; i++) {
+    if (fx) fx[gid[i]] = a[i];
+    if (fy) fy[gid[i]] = b[i];
+    if (tau) tau[gid[i]] = c[i];
+  }
+  return SC_OK;
+}
+
+int sc_get_box(sc_handle* H, int sys, double* out) {
+  if (!H || !out) return SC_E_ARG;
+  sc::Handle& h = H->h;
+  if (sys < 0 || sys >= h.nsys) {
+    h.fail(SC_E_ARG, "sc_get_box: bad system index");
+    return SC_E_ARG;
+  }
+  const sc::HostSys& S = h.hs[sys];
+  out[0] = S.Lx;
+  out[1] = S.Ly;
+  out[2] = S.gamma;
+  out[3] = S.gamma_total;
+  out[4] = S.pad;
+  out[5] = S.Lx / S.cols;
+  out[6] = S.Ly / S.rows;
+  out[7] = S.packing;
+  out[8] = S.rows;
+  out[9] = S.cols;
+  return SC_OK;
+}
+
+int sc_get_pairs(sc_handle* H, int sys, int* pairs, long cap, long* n_pairs) {
+  if (!H) return SC_E_ARG;
+  sc::Handle& h = H->h;
+  if (sys < 0 || sys >= h.nsys) {
+    h.fail(SC_E_ARG, "sc_get_pairs: bad system index");
+    return SC_E_ARG;
+  }
+  cudaSetDevice(h.device);
+  sc::Dev& d = h.d;
+  if (h.prec == sc::PREC_MIXED) {
+    // the mixed form keeps no list; build one from a fresh cell sort
+    if (!d.nbr && !h.dalloc(&d.nbr, (size_t)d.ntot * d.maxn, "nbr")) return h.last_status;
+    if (!h.rebuild_all()) return h.last_status;
+    sc::launch_force_rebuild_all(d, h.stream);
+    sc::launch_build_nbrs(d, h.d_tab, 0, h.stream);
+    sc::launch_clear_flags(d, h.stream);
+  }
+  if (!h.check_status("sc_get_pairs")) return h.last_status;
+  const sc::HostSys& S = h.hs[sys];
+  std::vector<int> nn(S.n), ids(S.n), lst((size_t)S.n * d.maxn);
+  if (!h.cuda_ok(cudaMemcpyAsync(nn.data(), d.nbr_n + S.p0, S.n * sizeof(int),
+                                 cudaMemcpyDeviceToHost, h.stream), "read lists") ||
+      !h.cuda_ok(cudaMemcpyAsync(ids.data(), d.id + S.p0, S.n * sizeof(int),
+                                 cudaMemcpyDeviceToHost, h.stream), "read lists") ||
+      !h.cuda_ok(cudaMemcpy2DAsync(lst.data(), S.n * sizeof(int), d.nbr + S.p0,
+                                   (size_t)d.ntot * sizeof(int), S.n * sizeof(int), d.maxn,
+                                   cudaMemcpyDeviceToHost, h.stream), "read lists") ||
+      !h.cuda_ok(cudaStreamSynchronize(h.stream), "read lists"))
+    return h.last_status;
+  std::vector<std::pair<int, int>> pr;
+  for (int k = 0; k < S.n; k++) {
+    int c = std::min(nn[k], d.maxn);
+    for (int m = 0; m < c; m++) {
+      int j = lst[(size_t)m * S.n + k] - S.p0;
+      if (j < 0 || j >= S.n) continue;
+      int a = ids[k], b = ids[j];
+      if (a < b) pr.emplace_back(a, b);
+    }
+  }
+  std::sort(pr.begin(), pr.end());
+  if (n_pairs) *n_pairs = (long)pr.size();
+  if (pairs)
+    for (long k = 0; k < (long)pr.size() && k < cap; k++) {
+      pairs[2 * k] = pr[k].first;
+      pairs[2 * k + 1] = pr[k].second;
+    }
+  return SC_OK;
+}
+
+int sc_get_counters(sc_handle* H, long long* out) {
+  if (!H || !out) return SC_E_ARG;
+  out[0] = H->h.steps;
+  out[1] = H->h.dev_rebuilds;
+  out[2] = H->h.dev_status;
+  return SC_OK;
+}
+
+int sc_get_pass_times(sc_handle* H, double* out) {
+  if (!H || !out) return SC_E_ARG;
+  sc::Handle& h = H->h;
+  for (int k = 0; k < 3; k++) {
+    out[k] = h.pass_n[k] ? h.pass_ms[k] / h.pass_n[k] : 0.0;
+    out[3 + k] = (double)h.pass_n[k];
+    h.pass_ms[k] = 0;
+    h.pass_n[k] = 0;
+  }
+  return SC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,434 @@
+// sc_cells.cu -- cell-list build (counting sort of particles by cell), Lees-Edwards
+// set-back, stress/energy reductions and the gradient-descent update.
+//
+// The rebuild follows the reference's find_cells / find_neighbors
+// (tmarschall/spherocyls src/cpp/spherocyl_box.cpp:270-355): positions are wrapped
+// into the box, each particle is hashed to cell col + row*cols, and the cell lists
+// hold particles in increasing particle index.  On the GPU the lists are a
+// counting sort of the particle arrays themselves into cell order:
+//
+//   zero counts -> hash (atomic rank inside the cell) -> per-chunk sums ->
+//   per-system scan of chunk sums -> per-chunk scan = cell starts -> scatter ->
+//   sort each cell's slots by particle index (makes the order deterministic and
+//   equal to the reference's cell-list order) -> gather into scratch -> commit.
+//
+// Only systems whose flag is set are rebuilt; every kernel exits at once when no
+// system is flagged, so the chain can sit in every step of a captured graph.
+// Compiled with -fmad=false: the wrap arithmetic and the set-back are the
+// reference's IEEE operations.
+#include "sc_internal.hpp"
+#include "sc_pair.cuh"
+#include "sc_rec.cuh"
+
+namespace sc {
+
+namespace {
+
+constexpr double kRefPi = 3.14159265358979;  // src/cpp/spherocyl_box.cpp:12
+
+// The reference's wrap loops (while v > hi: v -= period; while v < lo: v += period).
+// A runaway value would make them spin for ever; after 64 periods the wrap
+// finishes with floor() and flags the state as non-finite instead.
+__device__ __forceinline__ double wrap_bounded(double v, double lo, double hi, double period,
+                                               int* status) {
+  int it = 0;
+  while (v > hi && it < 64) {
+    v -= period;
+    it++;
+  }
+  while (v < lo && it < 64) {
+    v += period;
+    it++;
+  }
+  if (it >= 64) {
+    v -= period * floor((v - lo) / period);
+    atomicOr(status, ST_NAN);
+  }
+  return v;
+}
+
+__global__ void k_rb_zero(Dev d) {
+  if (*d.any == 0) return;
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= d.ncells) return;
+  if (d.flags[d.cell_sys[c]]) d.cell_count[c] = 0;
+}
+
+// find_cells, spherocyl_box.cpp:270-301: wrap, then hash.
+__global__ void k_rb_hash(Dev d, const StepScalars* __restrict__ tab, int row) {
+  if (*d.any == 0) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.ntot) return;
+  int s = d.psys[i];
+  if (d.flags[s] == 0) return;
+  const SysGeom& g = d.geom[s];
+  const StepScalars& ts = tab[row * d.nsys + s];
+  double Lx = ts.Lx_p, Ly = ts.Ly_p;
+  double2 p = d.xy[i];
+  double phi = d.ph[i];
+  p.x = wrap_bounded(p.x, 0.0, Lx, Lx, d.status);
+  p.y = wrap_bounded(p.y, 0.0, Ly, Ly, d.status);
+  phi = wrap_bounded(phi, -kRefPi, kRefPi, 2 * kRefPi, d.status);
+  d.xy[i] = p;
+  d.ph[i] = phi;
+  int col = (int)(p.x / ts.W_p);
+  int rw = (int)(p.y / ts.H_p);
+  // a coordinate equal to the box length survives the wrap; keep it on the grid
+  if (col >= g.cols) col = g.cols - 1;
+  if (rw >= g.rows) rw = g.rows - 1;
+  if (col < 0) col = 0;
+  if (rw < 0) rw = 0;
+  int c = g.c0 + col + rw * g.cols;
+  d.cell_tmp[i] = c;
+  d.rank[i] = atomicAdd(&d.cell_count[c], 1);
+}
+
+__device__ __forceinline__ int block_sum_int(int v, int* sh) {
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  int nw = blockDim.x >> 5;
+  if (w == 0) {
+    v = lane < nw ? sh[lane] : 0;
+    for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  }
+  return v;  // valid in thread 0
+}
+
+__global__ void k_rb_chunksum(Dev d) {
+  if (*d.any == 0) return;
+  int ch = blockIdx.x;
+  if (d.flags[d.chunk_sys[ch]] == 0) return;
+  __shared__ int sh[32];
+  int c0 = d.chunk_c0[ch], nc = d.chunk_nc[ch];
+  int v = 0;
+  for (int k = threadIdx.x; k < nc; k += blockDim.x) v += d.cell_count[c0 + k];
+  v = block_sum_int(v, sh);
+  if (threadIdx.x == 0) d.chunk_sum[ch] = v;
+}
+
+// One thread per system: exclusive scan of its chunk sums (a system owns at most a
+// few hundred chunks).
+__global__ void k_rb_sysscan(Dev d) {
+  if (*d.any == 0) return;
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= d.nsys || d.flags[s] == 0) return;
+  const SysGeom& g = d.geom[s];
+  int off = 0;
+  for (int k = 0; k < g.nchunks; k++) {
+    d.chunk_off[g.chunk0 + k] = off;
+    off += d.chunk_sum[g.chunk0 + k];
+  }
+  if (off != g.n) atomicOr(d.status, ST_CELL_OVERFLOW);
+}
+
+// One 1024-thread block per chunk: exclusive scan of cell counts.
+__global__ void __launch_bounds__(1024) k_rb_cellscan(Dev d) {
+  if (*d.any == 0) return;
+  int ch = blockIdx.x;
+  int s = d.chunk_sys[ch];
+  if (d.flags[s] == 0) return;
+  __shared__ int warp_tot[32];
+  int c0 = d.chunk_c0[ch], nc = d.chunk_nc[ch];
+  int k = threadIdx.x;
+  int v = k < nc ? d.cell_count[c0 + k] : 0;
+  int lane = k & 31, w = k >> 5;
+  int x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_tot[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    int t = warp_tot[lane];
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    warp_tot[lane] = t;  // inclusive
+  }
+  __syncthreads();
+  int excl = x - v + (w > 0 ? warp_tot[w - 1] : 0);
+  if (k < nc) d.cell_start[c0 + k] = d.geom[s].p0 + d.chunk_off[ch] + excl;
+}
+
+__global__ void k_rb_scatter(Dev d) {
+  if (*d.any == 0) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.ntot) return;
+  if (d.flags[d.psys[i]] == 0) return;
+  d.perm[d.cell_start[d.cell_tmp[i]] + d.rank[i]] = i;
+}
+
+// Order each cell's slots by particle index: the reference's cell lists are
+// filled in particle order (spherocyl_box.cpp:277-298).
+__global__ void k_rb_cellsort(Dev d) {
+  if (*d.any == 0) return;
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= d.ncells) return;
+  if (d.flags[d.cell_sys[c]] == 0) return;
+  int st = d.cell_start[c], n = d.cell_count[c];
+  if (n <= 1) return;
+  int* P = d.perm + st;
+  if (n <= kMaxCellSort) {
+    int key[kMaxCellSort], val[kMaxCellSort];
+    for (int k = 0; k < n; k++) {
+      val[k] = P[k];
+      key[k] = d.id[val[k]];
+    }
+    for (int k = 1; k < n; k++) {
+      int kk = key[k], vv = val[k], m = k - 1;
+      while (m >= 0 && key[m] > kk) {
+        key[m + 1] = key[m];
+        val[m + 1] = val[m];
+        m--;
+      }
+      key[m + 1] = kk;
+      val[m + 1] = vv;
+    }
+    for (int k = 0; k < n; k++) P[k] = val[k];
+  } else {
+    for (int k = 1; k < n; k++) {
+      int vv = P[k], kk = d.id[vv], m = k - 1;
+      while (m >= 0 && d.id[P[m]] > kk) {
+        P[m + 1] = P[m];
+        m--;
+      }
+      P[m + 1] = vv;
+    }
+  }
+}
+
+__global__ void k_rb_gather(Dev d) {
+  if (*d.any == 0) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.ntot) return;
+  if (d.flags[d.psys[i]] == 0) return;
+  int src = d.perm[i];
+  d.s_xy[i] = d.xy[src];
+  d.s_ph[i] = d.ph[src];
+  d.s_ra[i] = d.ra[src];
+  d.s_irc[i] = d.irc[src];
+  d.s_id[i] = d.id[src];
+  d.s_cell[i] = d.cell_tmp[src];
+}
+
+__global__ void k_rb_commit(Dev d, const StepScalars* __restrict__ tab, int row, int mixed) {
+  if (*d.any == 0) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.ntot) return;
+  int s = d.psys[i];
+  if (d.flags[s] == 0) return;
+  double2 p = d.s_xy[i];
+  double phi = d.s_ph[i];
+  double2 ra = d.s_ra[i];
+  int c = d.s_cell[i];
+  d.xy[i] = p;
+  d.ph[i] = phi;
+  d.ra[i] = ra;
+  d.irc[i] = d.s_irc[i];
+  d.id[i] = d.s_id[i];
+  d.cell[i] = c;
+  d.moved[i] = make_double2(0.0, 0.0);
+  if (mixed) {
+    const SysGeom& g = d.geom[s];
+    const StepScalars& ts = tab[row * d.nsys + s];
+    int lc = c - g.c0;
+    d.rec[i] = make_rec(p, phi, ra.y, lc % g.cols, lc / g.cols, ts.W_p, ts.H_p);
+    d.raf[i] = make_float2((float)ra.x, (float)ra.y);
+  } else {
+    double sn, cs;
+    sincos(phi, &sn, &cs);
+    d.nxy[i] = make_double2(ra.y * cs, ra.y * sn);
+  }
+}
+
+__global__ void k_rb_clear(Dev d) {
+  if (*d.any == 0) return;
+  for (int s = threadIdx.x; s < d.nsys; s += blockDim.x) d.flags[s] = 0;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    *d.any = 0;
+    d.status[1] += 1;  // rebuild chains executed
+  }
+}
+
+__global__ void k_force_all(Dev d) {
+  for (int s = threadIdx.x; s < d.nsys; s += blockDim.x) d.flags[s] = 2;
+  if (threadIdx.x == 0) *d.any = 1;
+}
+
+// set_back_gamma, spherocyl_box.cpp:524-545 (positions; gamma itself is advanced
+// on the host), for the systems whose table row says so.
+__global__ void k_setback(Dev d, const StepScalars* __restrict__ tab, int row) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.ntot) return;
+  int s = d.psys[i];
+  const StepScalars& ts = tab[row * d.nsys + s];
+  if (!ts.setback) return;
+  double Lx = ts.Lx_p, Ly = ts.Ly_p;
+  double2 p = d.xy[i];
+  if (p.y < 0)
+    p.y += Ly;
+  else if (p.y > Ly)
+    p.y -= Ly;
+  p.x += p.y;
+  if (p.x < 0)
+    p.x += Lx;
+  else
+    p.x = wrap_bounded(p.x, -1.0, Lx, Lx, d.status);  // only the "> Lx" loop applies
+  d.xy[i] = p;
+  if (i == d.geom[s].p0) {
+    atomicOr(&d.flags[s], 2);
+    atomicExch(d.any, 1);
+  }
+}
+
+// Recompute the derived per-particle geometry (shaft vectors, FP32 records) from
+// the FP64 state, e.g. after the host replaced positions.
+__global__ void k_refresh(Dev d, const StepScalars* __restrict__ tab, int row, int mixed) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.ntot) return;
+  int s = d.psys[i];
+  double2 p = d.xy[i];
+  double phi = d.ph[i];
+  double2 ra = d.ra[i];
+  if (mixed) {
+    const SysGeom& g = d.geom[s];
+    const StepScalars& ts = tab[row * d.nsys + s];
+    int lc = d.cell[i] - g.c0;
+    d.rec[i] = make_rec(p, phi, ra.y, lc % g.cols, lc / g.cols, ts.W_p, ts.H_p);
+    d.raf[i] = make_float2((float)ra.x, (float)ra.y);
+  } else {
+    double sn, cs;
+    sincos(phi, &sn, &cs);
+    d.nxy[i] = make_double2(ra.y * cs, ra.y * sn);
+  }
+}
+
+// gradient_relax_step, src/cpp/relaxation_dynamics.cpp:11-31
+__global__ void k_gd_update(Dev d, const StepScalars* __restrict__ tab, int row, int mixed) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.ntot) return;
+  int s = d.psys[i];
+  const SysGeom& g = d.geom[s];
+  const double step = tab[row * d.nsys + s].step;
+  if (step == 0.0) return;
+  double ddx = step * d.fx[i];
+  double ddy = step * d.fy[i];
+  double2 p = d.xy[i];
+  p.x += ddx;
+  p.y += ddy;
+  double phi = d.ph[i] + step * d.tau[i] / d.irc[i].x;
+  d.xy[i] = p;
+  d.ph[i] = phi;
+  double2 m = d.moved[i];
+  m.x += ddx;
+  m.y += ddy;
+  d.moved[i] = m;
+  double2 ra = d.ra[i];
+  if (mixed) {
+    const StepScalars& ts = tab[row * d.nsys + s];
+    int lc = d.cell[i] - g.c0;
+    d.rec[i] = make_rec(p, phi, ra.y, lc % g.cols, lc / g.cols, ts.W_p, ts.H_p);
+  } else {
+    double sn, cs;
+    sincos(phi, &sn, &cs);
+    d.nxy[i] = make_double2(ra.y * cs, ra.y * sn);
+  }
+  if (!(isfinite(p.x) && isfinite(p.y) && isfinite(phi))) atomicOr(d.status, ST_NAN);
+  // the reference tests and rebuilds inside the update loop
+  if (m.x > 0.5 * g.pad || m.x < -0.5 * g.pad || m.y > 0.5 * g.pad || m.y < -0.5 * g.pad) {
+    if (d.flags[s] == 0) atomicOr(&d.flags[s], 1);
+    if (*d.any == 0) atomicExch(d.any, 1);
+  }
+}
+
+// Stress/energy: deterministic two-level reduction of the per-slot contributions.
+__global__ void k_se_chunk(Dev d) {
+  int ch = blockIdx.x;
+  int p0 = d.pchunk_p0[ch], np = d.pchunk_np[ch];
+  __shared__ double sh[5][32];
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int comp = 0; comp < 5; comp++) {
+    const double* src = d.se_part + (size_t)comp * d.ntot + p0;
+    double v = 0.0;
+    for (int k = threadIdx.x; k < np; k += blockDim.x) v += src[k];
+    for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[comp][w] = v;
+  }
+  __syncthreads();
+  if (w < 5) {
+    double v = lane < nw ? sh[w][lane] : 0.0;
+    for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) d.se_chunk[(size_t)w * d.npchunks + ch] = v;
+  }
+}
+
+__global__ void k_se_sys(Dev d) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= d.nsys) return;
+  // particle chunks of a system are contiguous and ordered; find them by scan
+  for (int comp = 0; comp < 5; comp++) {
+    double v = 0.0;
+    for (int ch = 0; ch < d.npchunks; ch++)
+      if (d.pchunk_sys[ch] == s) v += d.se_chunk[(size_t)comp * d.npchunks + ch];
+    d.se_sys[(size_t)comp * d.nsys + s] = v;
+  }
+}
+
+// se_sys is [5][nsys]; a record is [nsys][5]
+__global__ void k_se_store(Dev d, double* dst) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= d.nsys) return;
+  for (int k = 0; k < 5; k++) dst[5 * s + k] = d.se_sys[(size_t)k * d.nsys + s];
+}
+
+inline int nblk(int n, int b) { return (n + b - 1) / b; }
+
+}  // namespace
+
+void launch_rebuild(const Dev& d, bool mixed, const StepScalars* tab, int row, cudaStream_t st) {
+  const int B = 256;
+  k_rb_zero<<<nblk(d.ncells, B), B, 0, st>>>(d);
+  k_rb_hash<<<nblk(d.ntot, B), B, 0, st>>>(d, tab, row);
+  k_rb_chunksum<<<d.nchunks, 256, 0, st>>>(d);
+  k_rb_sysscan<<<nblk(d.nsys, 128), 128, 0, st>>>(d);
+  k_rb_cellscan<<<d.nchunks, 1024, 0, st>>>(d);
+  k_rb_scatter<<<nblk(d.ntot, B), B, 0, st>>>(d);
+  k_rb_cellsort<<<nblk(d.ncells, 128), 128, 0, st>>>(d);
+  k_rb_gather<<<nblk(d.ntot, B), B, 0, st>>>(d);
+  k_rb_commit<<<nblk(d.ntot, B), B, 0, st>>>(d, tab, row, mixed ? 1 : 0);
+  if (!mixed) launch_build_nbrs(d, tab, row, st);
+  k_rb_clear<<<1, 256, 0, st>>>(d);
+}
+
+void launch_force_rebuild_all(const Dev& d, cudaStream_t st) { k_force_all<<<1, 256, 0, st>>>(d); }
+
+void launch_clear_flags(const Dev& d, cudaStream_t st) { k_rb_clear<<<1, 256, 0, st>>>(d); }
+
+void launch_setback(const Dev& d, const StepScalars* tab, int row, cudaStream_t st) {
+  k_setback<<<nblk(d.ntot, 256), 256, 0, st>>>(d, tab, row);
+}
+
+void launch_refresh_geometry(const Dev& d, bool mixed, const StepScalars* tab, int row,
+                             cudaStream_t st) {
+  k_refresh<<<nblk(d.ntot, 256), 256, 0, st>>>(d, tab, row, mixed ? 1 : 0);
+}
+
+void launch_gd_update(const Dev& d, bool mixed, const StepScalars* tab, int row, cudaStream_t st) {
+  k_gd_update<<<nblk(d.ntot, 256), 256, 0, st>>>(d, tab, row, mixed ? 1 : 0);
+}
+
+void launch_se_store(const Dev& d, double* dst, cudaStream_t st) {
+  k_se_store<<<nblk(d.nsys, 128), 128, 0, st>>>(d, dst);
+}
+
+void launch_se_reduce(const Dev& d, cudaStream_t st) {
+  k_se_chunk<<<d.npchunks, 256, 0, st>>>(d);
+  k_se_sys<<<nblk(d.nsys, 128), 128, 0, st>>>(d);
+}
+
+}  // namespace sc

@@ -1,0 +1,542 @@
+// sc_host.cpp -- host runtime of libspherocyl: handle lifetime, device memory,
+// per-step scalar tables, the step loops (eager or captured in CUDA graphs) and
+// the C-ABI entry points declared in include/spherocyl.h.
+//
+// The host keeps an exact mirror of every per-system scalar the reference keeps
+// (gamma, total gamma, box lengths, cell grid) and advances it with the
+// reference's own floating-point operations (strain_step, resize_step and
+// set_back_gamma: tmarschall/spherocyls src/cpp/strain_dynamics.cpp:231-234,
+// src/cpp/resize_dynamics.cpp:230-238, src/cpp/spherocyl_box.cpp:542-543).  The
+// device receives those values as tables, one row per step, so the only
+// device-side decision is the displacement-triggered neighbour rebuild.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/spherocyl.h"
+#include "sc_internal.hpp"
+#include "sc_host.hpp"
+
+namespace sc {
+
+static const double kRefPi = 3.14159265358979;  // src/cpp/spherocyl_box.cpp:12
+
+void Handle::fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  err = buf;
+  last_status = code;
+}
+
+bool Handle::cuda_ok(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return true;
+  fail(SC_E_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  return false;
+}
+
+void Handle::dfree(void* p) {
+  if (!p) return;
+  auto it = std::find(allocs.begin(), allocs.end(), p);
+  if (it != allocs.end()) allocs.erase(it);
+  cudaFree(p);
+}
+
+Handle::~Handle() {
+  if (device >= 0) cudaSetDevice(device);
+  if (graph_exec) cudaGraphExecDestroy(graph_exec);
+  for (auto& e : ev_pool) cudaEventDestroy(e);
+  for (void* p : allocs) cudaFree(p);
+  if (h_pinned) cudaFreeHost(h_pinned);
+  if (own_stream && stream) cudaStreamDestroy(stream);
+}
+
+// ---- per-system geometry (set_particle and configure_cells on the host) ----
+
+// configure_cells, src/cpp/spherocyl_box.cpp:223-241
+void HostSys::configure(bool set_pad) {
+  double wmin = 2.24 * (Rmax + Amax) + pad;
+  double hmin = 2 * (Rmax + Amax) + pad;
+  rows = std::max(static_cast<int>(Ly / hmin), 1);
+  cols = std::max(static_cast<int>(Lx / wmin), 1);
+  if (set_pad && pad == 0) pad = std::max(Lx / cols - wmin, Ly / rows - hmin);
+}
+
+// reconfigure_cells' test, src/cpp/resize_dynamics.cpp:106-121 (rows from Lx,
+// columns from Ly, as written there)
+bool HostSys::grid_changes(double Lx_now, double Ly_now) const {
+  double wmin = 2.24 * (Rmax + Amax) + pad;
+  double hmin = 2 * (Rmax + Amax) + pad;
+  int r = std::max(static_cast<int>(Lx_now / hmin), 1);
+  int c = std::max(static_cast<int>(Ly_now / wmin), 1);
+  return r != rows || c != cols;
+}
+
+StepScalars Handle::row_current(int s) const {
+  const HostSys& h = hs[s];
+  StepScalars t;
+  std::memset(&t, 0, sizeof t);
+  t.gamma_c = h.gamma + h.step * h.strain_rate;
+  t.gamma_p = h.gamma;
+  t.Lx_c = t.Lx_p = h.Lx;
+  t.Ly_c = t.Ly_p = h.Ly;
+  t.W_c = t.W_p = h.Lx / h.cols;
+  t.H_c = t.H_p = h.Ly / h.rows;
+  t.rate = h.strain_rate;
+  t.step = h.step;
+  t.scale = 1.0;
+  return t;
+}
+
+// ---- device layout ----
+
+bool Handle::layout_cells() {
+  // cells, scan chunks and particle chunks for all systems
+  int c = 0, ch = 0;
+  std::vector<int> chunk_sys, chunk_c0, chunk_nc, cell_sys;
+  for (int s = 0; s < nsys; s++) {
+    HostSys& h = hs[s];
+    h.c0 = c;
+    int nc = h.rows * h.cols;
+    h.chunk0 = ch;
+    h.nchunks = (nc + kScanChunk - 1) / kScanChunk;
+    for (int k = 0; k < h.nchunks; k++) {
+      chunk_sys.push_back(s);
+      chunk_c0.push_back(c + k * kScanChunk);
+      chunk_nc.push_back(std::min(kScanChunk, nc - k * kScanChunk));
+    }
+    for (int k = 0; k < nc; k++) cell_sys.push_back(s);
+    c += nc;
+    ch += h.nchunks;
+  }
+  int ncells = c, nchunks = ch;
+  if (ncells > cell_cap) {
+    dfree(d.cell_start);
+    dfree(d.cell_count);
+    dfree((void*)d.cell_sys);
+    int cap = ncells + ncells / 4 + 64;
+    int *cs = nullptr, *cn = nullptr, *csys = nullptr;
+    if (!dalloc(&cs, cap, "cell_start") || !dalloc(&cn, cap, "cell_count") ||
+        !dalloc(&csys, cap, "cell_sys"))
+      return false;
+    d.cell_start = cs;
+    d.cell_count = cn;
+    d.cell_sys = csys;
+    cell_cap = cap;
+  }
+  if (nchunks > chunk_cap) {
+    dfree(d.chunk_sum);
+    dfree(d.chunk_off);
+    dfree((void*)d.chunk_sys);
+    dfree((void*)d.chunk_c0);
+    dfree((void*)d.chunk_nc);
+    int cap = nchunks + nchunks / 4 + 16;
+    int *a = nullptr, *b = nullptr, *e = nullptr, *f = nullptr, *g = nullptr;
+    if (!dalloc(&a, cap, "chunk_sum") || !dalloc(&b, cap, "chunk_off") ||
+        !dalloc(&e, cap, "chunk_sys") || !dalloc(&f, cap, "chunk_c0") ||
+        !dalloc(&g, cap, "chunk_nc"))
+      return false;
+    d.chunk_sum = a;
+    d.chunk_off = b;
+    d.chunk_sys = e;
+    d.chunk_c0 = f;
+    d.chunk_nc = g;
+    chunk_cap = cap;
+  }
+  d.ncells = ncells;
+  d.nchunks = nchunks;
+  invalidate_graph();  // captured kernels hold the old layout
+  std::vector<SysGeom> g(nsys);
+  for (int s = 0; s < nsys; s++) {
+    const HostSys& h = hs[s];
+    SysGeom& o = g[s];
+    std::memset(&o, 0, sizeof o);
+    o.n = h.n;
+    o.p0 = h.p0;
+    o.c0 = h.c0;
+    o.cols = h.cols;
+    o.rows = h.rows;
+    o.chunk0 = h.chunk0;
+    o.nchunks = h.nchunks;
+    o.pad = h.pad;
+    o.inv_n = 1.0 / h.n;
+  }
+  bool ok = cuda_ok(cudaMemcpyAsync((void*)d.geom, g.data(), nsys * sizeof(SysGeom),
+                                    cudaMemcpyHostToDevice, stream), "upload geometry") &&
+            cuda_ok(cudaMemcpyAsync((void*)d.cell_sys, cell_sys.data(), ncells * sizeof(int),
+                                    cudaMemcpyHostToDevice, stream), "upload cell map") &&
+            cuda_ok(cudaMemcpyAsync((void*)d.chunk_sys, chunk_sys.data(), nchunks * sizeof(int),
+                                    cudaMemcpyHostToDevice, stream), "upload chunks") &&
+            cuda_ok(cudaMemcpyAsync((void*)d.chunk_c0, chunk_c0.data(), nchunks * sizeof(int),
+                                    cudaMemcpyHostToDevice, stream), "upload chunks") &&
+            cuda_ok(cudaMemcpyAsync((void*)d.chunk_nc, chunk_nc.data(), nchunks * sizeof(int),
+                                    cudaMemcpyHostToDevice, stream), "upload chunks");
+  if (!ok) return false;
+  // host copies must outlive the async copies
+  return cuda_ok(cudaStreamSynchronize(stream), "layout sync");
+}
+
+bool Handle::ensure_table(int rows) {
+  if (rows * nsys <= tab_cap) return true;
+  dfree(d_tab);
+  int cap = std::max(rows * nsys, 2 * tab_cap);
+  StepScalars* t = nullptr;
+  if (!dalloc(&t, cap, "step table")) return false;
+  d_tab = t;
+  tab_cap = cap;
+  invalidate_graph();
+  return true;
+}
+
+bool Handle::upload_table(const std::vector<StepScalars>& rows) {
+  int nrows = (int)(rows.size() / nsys);
+  if (!ensure_table(nrows)) return false;
+  // the host table is a member, so it outlives the asynchronous copy
+  h_tab = rows;
+  return cuda_ok(cudaMemcpyAsync(d_tab, h_tab.data(), h_tab.size() * sizeof(StepScalars),
+                                 cudaMemcpyHostToDevice, stream),
+                 "upload step table");
+}
+
+bool Handle::check_status(const char* where) {
+  if (!cuda_ok(cudaMemcpyAsync(h_pinned, d.status, 2 * sizeof(int), cudaMemcpyDeviceToHost,
+                               stream), "read status") ||
+      !cuda_ok(cudaStreamSynchronize(stream), where))
+    return false;
+  int st = h_pinned[0];
+  dev_rebuilds = h_pinned[1];
+  dev_status |= st;
+  if (st & ST_NAN) {
+    fail(SC_E_NAN, "%s: a position or angle became non-finite", where);
+    return false;
+  }
+  if (st & ST_NBR_OVERFLOW) {
+    fail(SC_E_OVERFLOW, "%s: a neighbour list exceeded max_nbrs=%d", where, d.maxn);
+    return false;
+  }
+  if (st & ST_CELL_OVERFLOW) {
+    fail(SC_E_OVERFLOW, "%s: cell sort lost particles", where);
+    return false;
+  }
+  return true;
+}
+
+// full rebuild of every system at the current state (constructor / setters)
+bool Handle::rebuild_all() {
+  std::vector<StepScalars> rows(nsys);
+  for (int s = 0; s < nsys; s++) rows[s] = row_current(s);
+  if (!upload_table(rows)) return false;
+  launch_force_rebuild_all(d, stream);
+  launch_rebuild(d, prec == PREC_MIXED, d_tab, 0, stream);
+  pred_valid = false;
+  rebuilds++;
+  return cuda_ok(cudaGetLastError(), "rebuild launch");
+}
+
+void Handle::launch_pass(int mode, bool se, int row) {
+  if (prec == PREC_MIXED)
+    launch_pass_mixed(d, mode, se, d_tab, row, stream, block);
+  else
+    launch_pass_fp64(d, mode, se, d_tab, row, stream);
+}
+
+cudaEvent_t Handle::next_event() {
+  if (ev_used == (int)ev_pool.size()) {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    ev_pool.push_back(e);
+  }
+  return ev_pool[ev_used++];
+}
+
+void Handle::timed(int kind, bool on, const std::function<void()>& f) {
+  if (!on) {
+    f();
+    return;
+  }
+  cudaEvent_t a = next_event(), b = next_event();
+  cudaEventRecord(a, stream);
+  f();
+  cudaEventRecord(b, stream);
+  ev_marks.push_back({kind, a, b});
+}
+
+void Handle::collect_times() {
+  if (ev_marks.empty()) return;
+  cudaStreamSynchronize(stream);
+  for (auto& m : ev_marks) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, m.a, m.b);
+    pass_ms[m.kind] += ms;
+    pass_n[m.kind] += 1;
+  }
+  ev_marks.clear();
+  ev_used = 0;
+}
+
+// One Heun step (rows k of the uploaded table), strain or resize form.
+void Handle::enqueue_step(bool resize, int k, bool se, bool prof) {
+  timed(0, prof, [&] { launch_pass(resize ? PASS_CORR_RESIZE : PASS_CORR_STRAIN, false, k); });
+  if (!resize) launch_setback(d, d_tab, k, stream);
+  timed(2, prof, [&] { launch_rebuild(d, prec == PREC_MIXED, d_tab, k, stream); });
+  timed(1, prof, [&] { launch_pass(resize ? PASS_PRED_RESIZE : PASS_PRED_STRAIN, se, k); });
+}
+
+void Handle::invalidate_graph() {
+  if (graph_exec) cudaGraphExecDestroy(graph_exec);
+  graph_exec = nullptr;
+  graph_key = GraphKey{};
+}
+
+// Capture `nsteps` steps (rows 1..nsteps) as one graph; reused while the table
+// pointer, the shapes and the step kind stay the same (the table contents change
+// from call to call, the graph reads them from device memory).
+bool Handle::run_graph(bool resize, int nsteps, int se_every) {
+  GraphKey key{resize, nsteps, se_every, prec};
+  if (!graph_exec || !(key == graph_key)) {
+    invalidate_graph();
+    cudaGraph_t g = nullptr;
+    if (!cuda_ok(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal),
+                 "begin capture"))
+      return false;
+    int r = 0;
+    for (int k = 1; k <= nsteps; k++) {
+      bool se = se_every > 0 && k % se_every == 0;
+      enqueue_step(resize, k, se, false);
+      if (se) enqueue_se_record(r++);
+    }
+    cudaError_t e = cudaStreamEndCapture(stream, &g);
+    if (!cuda_ok(e, "end capture")) return false;
+    e = cudaGraphInstantiate(&graph_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (!cuda_ok(e, "graph instantiate")) {
+      graph_exec = nullptr;
+      return false;
+    }
+    graph_key = key;
+  }
+  return cuda_ok(cudaGraphLaunch(graph_exec, stream), "graph launch");
+}
+
+bool Handle::ensure_se_hist(int nrec) {
+  if (nrec * nsys * 5 <= se_hist_cap) return true;
+  dfree(d_se_hist);
+  int cap = std::max(nrec * nsys * 5, 2 * se_hist_cap);
+  double* p = nullptr;
+  if (!dalloc(&p, cap, "se history")) return false;
+  d_se_hist = p;
+  se_hist_cap = cap;
+  invalidate_graph();
+  return true;
+}
+
+void Handle::enqueue_se_record(int rec) {
+  launch_se_reduce(d, stream);
+  launch_se_store(d, d_se_hist + (size_t)rec * nsys * 5, stream);
+}
+
+// ---- protocols ----
+
+// Advance one system's host mirror by one step and fill its table row
+// (strain_step, strain_dynamics.cpp:231-234 with set_back_gamma,
+// spherocyl_box.cpp:542-543; resize_step, resize_dynamics.cpp:230-238).
+static void advance(HostSys& h, bool resize, int shrink, StepScalars& t) {
+  std::memset(&t, 0, sizeof t);
+  t.rate = h.strain_rate;
+  t.step = h.step;
+  t.gamma_c = h.gamma + h.step * h.strain_rate;
+  t.Lx_c = h.Lx;
+  t.Ly_c = h.Ly;
+  t.W_c = h.Lx / h.cols;
+  t.H_c = h.Ly / h.rows;
+  t.scale = 1.0;
+  if (resize) {
+    t.scale = std::pow(1.0 - h.resize_rate, h.step);
+    t.mode = shrink ? 1 : 2;
+    if (shrink) {
+      h.Lx *= std::pow(1.0 - h.resize_rate, h.step);
+      h.Ly *= std::pow(1.0 - h.resize_rate, h.step);
+    } else {
+      h.Lx /= std::pow(1.0 - h.resize_rate, h.step);
+      h.Ly /= std::pow(1.0 - h.resize_rate, h.step);
+    }
+  } else {
+    h.gamma += h.strain_rate * h.step;
+    h.gamma_total += h.strain_rate * h.step;
+    if (h.gamma >= 0.5) {
+      h.gamma -= 1.0;
+      h.gamma_total = static_cast<int>(h.gamma_total + 1) + h.gamma;
+      t.setback = 1;
+    }
+  }
+  t.gamma_p = h.gamma;
+  t.Lx_p = h.Lx;
+  t.Ly_p = h.Ly;
+  t.W_p = h.Lx / h.cols;
+  t.H_p = h.Ly / h.rows;
+}
+
+int Handle::run_steps(bool resize, int shrink, int nsteps, int se_every, double* se_out) {
+  if (nsteps < 0 || se_every < 0) {
+    fail(SC_E_ARG, "nsteps and se_every must be >= 0");
+    return SC_E_ARG;
+  }
+  if (nsteps == 0) return SC_OK;
+  if (resize) {
+    for (int s = 0; s < nsys; s++)
+      if (!(hs[s].resize_rate > 0 && hs[s].resize_rate < 1)) {
+        fail(SC_E_ARG, "resize rate of system %d must be in (0, 1)", s);
+        return SC_E_ARG;
+      }
+  }
+  cudaSetDevice(device);
+  int nrec_total = (se_every > 0) ? nsteps / se_every : 0;
+  std::vector<double> se_host((size_t)nrec_total * nsys * 5);
+  int done = 0, rec_done = 0;
+  while (done < nsteps) {
+    // chunk length: at most kChunk steps, a multiple of the recording period when
+    // possible, and ending before any system's cell grid would change
+    // (reconfigure_cells, resize_dynamics.cpp:106-121)
+    int want = std::min(nsteps - done, kChunk);
+    if (se_every > 0 && want >= se_every) want = (want / se_every) * se_every;
+    int nk = want;
+    bool regrid = false;
+    if (resize) {
+      std::vector<HostSys> sim = hs;
+      StepScalars tmp;
+      for (int k = 0; k < want; k++) {
+        bool change = false;
+        for (int s = 0; s < nsys; s++)
+          if (sim[s].grid_changes(sim[s].Lx, sim[s].Ly)) change = true;
+        if (change) {
+          nk = k;
+          regrid = true;
+          break;
+        }
+        for (int s = 0; s < nsys; s++) advance(sim[s], resize, shrink, tmp);
+      }
+    }
+    if (nk == 0) {
+      // the grid changes before the next step: re-grid, rebuild, continue
+      for (int s = 0; s < nsys; s++) hs[s].configure(false);
+      if (!layout_cells() || !rebuild_all()) return last_status;
+      continue;
+    }
+    std::vector<HostSys> sim = hs;
+    std::vector<StepScalars> rows((size_t)(nk + 1) * nsys);
+    for (int s = 0; s < nsys; s++) rows[s] = row_current(s);
+    for (int k = 1; k <= nk; k++)
+      for (int s = 0; s < nsys; s++) advance(sim[s], resize, shrink, rows[(size_t)k * nsys + s]);
+    if (!upload_table(rows)) return last_status;
+    // records of this chunk: steps done+k with (done+k) % se_every == 0
+    int first_rec = rec_done;
+    int nrec = 0;
+    for (int k = 1; k <= nk; k++)
+      if (se_every > 0 && (done + k) % se_every == 0) nrec++;
+    if (nrec > 0 && !ensure_se_hist(nrec)) return last_status;
+    if (!pred_valid) {
+      launch_pass(resize ? PASS_PRED_RESIZE : PASS_PRED_STRAIN, false, 0);
+      pred_valid = true;
+    }
+    bool aligned = se_every == 0 || done % se_every == 0;
+    bool use_graph = opt.use_graphs && !opt.profile && nk == kChunk && aligned;
+    if (use_graph) {
+      if (!run_graph(resize, nk, se_every)) return last_status;
+    } else {
+      int r = 0;
+      for (int k = 1; k <= nk; k++) {
+        bool se = se_every > 0 && (done + k) % se_every == 0;
+        enqueue_step(resize, k, se, opt.profile != 0);
+        if (se) enqueue_se_record(r++);
+      }
+    }
+    if (!cuda_ok(cudaGetLastError(), "step launch")) return last_status;
+    if (nrec > 0) {
+      if (!cuda_ok(cudaMemcpyAsync(se_host.data() + (size_t)first_rec * nsys * 5, d_se_hist,
+                                   (size_t)nrec * nsys * 5 * sizeof(double),
+                                   cudaMemcpyDeviceToHost, stream),
+                   "read se records"))
+        return last_status;
+    }
+    collect_times();
+    if (!check_status(resize ? "resize steps" : "strain steps")) return last_status;
+    hs = sim;
+    rec_done += nrec;
+    done += nk;
+    steps += nk;
+    if (regrid) {
+      for (int s = 0; s < nsys; s++) hs[s].configure(false);
+      if (!layout_cells() || !rebuild_all()) return last_status;
+    }
+  }
+  if (se_out && nrec_total > 0)
+    std::memcpy(se_out, se_host.data(), se_host.size() * sizeof(double));
+  return SC_OK;
+}
+
+int Handle::calc(bool se, double* se_out) {
+  cudaSetDevice(device);
+  std::vector<StepScalars> rows(nsys);
+  for (int s = 0; s < nsys; s++) rows[s] = row_current(s);
+  if (!upload_table(rows)) return last_status;
+  launch_pass(PASS_FORCE, se, 0);
+  if (se) {
+    launch_se_reduce(d, stream);
+    if (!cuda_ok(cudaMemcpyAsync(h_pinned + 8, d.se_sys, 5 * nsys * sizeof(double),
+                                 cudaMemcpyDeviceToHost, stream),
+                 "read se"))
+      return last_status;
+  }
+  if (!check_status("calc")) return last_status;
+  if (se && se_out) {
+    const double* src = reinterpret_cast<const double*>(h_pinned + 8);
+    for (int s = 0; s < nsys; s++)
+      for (int k = 0; k < 5; k++) se_out[5 * s + k] = src[(size_t)k * nsys + s];
+  }
+  return SC_OK;
+}
+
+int Handle::gd_minimize(int max_steps, double e_min, int* steps_taken, double* e_final) {
+  // gradient_descent_minimize, relaxation_dynamics.cpp:33-85: calc_se, test,
+  // then one fixed-size gradient step; a rebuild follows any step that moved a
+  // particle beyond pad/2.
+  cudaSetDevice(device);
+  std::vector<double> se(5 * (size_t)nsys);
+  int s;
+  for (s = 0; s < max_steps; s++) {
+    int rc = calc(true, se.data());
+    if (rc) return rc;
+    bool all_done = true;
+    for (int q = 0; q < nsys; q++)
+      if (!(se[5 * q] <= e_min)) all_done = false;
+    if (all_done) break;
+    // one table row with the current scalars; the step size is per system
+    std::vector<StepScalars> rows(nsys);
+    for (int q = 0; q < nsys; q++) {
+      rows[q] = row_current(q);
+      if (se[5 * q] <= e_min) rows[q].step = 0.0;  // this system has finished
+    }
+    if (!upload_table(rows)) return last_status;
+    launch_gd_update(d, prec == PREC_MIXED, d_tab, 0, stream);
+    launch_rebuild(d, prec == PREC_MIXED, d_tab, 0, stream);
+    pred_valid = false;
+  }
+  if (steps_taken) *steps_taken = s;
+  if (e_final) {
+    double emax = 0;
+    for (int q = 0; q < nsys; q++) emax = std::max(emax, se[5 * q]);
+    *e_final = emax;
+  }
+  return check_status("gd minimize") ? SC_OK : last_status;
+}
+
+}  // namespace sc

@@ -1,0 +1,122 @@
+// sc_host.hpp -- the handle behind the C ABI (host side only).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <functional>
+#include <string>
+#include <vector>
+
+#include "../../include/spherocyl.h"
+#include "sc_internal.hpp"
+
+namespace sc {
+
+// Host mirror of one system: the scalars the reference's SpherocylBox keeps
+// (src/cpp/spherocyl_box.h:29-61), advanced with the reference's arithmetic.
+struct HostSys {
+  int n = 0, p0 = 0;
+  double Lx = 0, Ly = 0;
+  double gamma = 0, gamma_total = 0;
+  double strain_rate = 0, resize_rate = 0;
+  double step = 0.05;  // set_defaults, src/cpp/spherocyl_box.cpp:24
+  double pad = 0;
+  double Rmax = 0, Amax = 0;
+  double packing = 0;
+  int rows = 1, cols = 1;
+  int c0 = 0, chunk0 = 0, nchunks = 0;
+
+  void configure(bool set_pad);
+  bool grid_changes(double Lx_now, double Ly_now) const;
+};
+
+struct GraphKey {
+  bool resize = false;
+  int nsteps = 0, se_every = -1;
+  int prec = -1;
+  bool operator==(const GraphKey& o) const {
+    return resize == o.resize && nsteps == o.nsteps && se_every == o.se_every && prec == o.prec;
+  }
+};
+
+struct Handle {
+  static constexpr int kChunk = 100;  // steps per table upload / captured graph
+
+  sc_options opt{};
+  int device = -1;
+  int prec = PREC_FP64;
+  int block = 128;
+  int nsys = 0, ntot = 0;
+  std::vector<HostSys> hs;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  Dev d{};
+  std::vector<void*> allocs;
+  int cell_cap = 0, chunk_cap = 0;
+  StepScalars* d_tab = nullptr;
+  int tab_cap = 0;
+  std::vector<StepScalars> h_tab;
+  double* d_se_hist = nullptr;
+  int se_hist_cap = 0;
+  int* h_pinned = nullptr;  // status word + scratch for small reads
+  bool pred_valid = false;
+  long long steps = 0, rebuilds = 0;
+  int dev_status = 0;
+  long long dev_rebuilds = 0;  // rebuild chains the device executed
+  int last_status = SC_OK;
+  std::string err;
+  // CUDA graph of one chunk of steps
+  cudaGraphExec_t graph_exec = nullptr;
+  GraphKey graph_key{};
+  // profiling: per-pass events
+  struct Mark {
+    int kind;
+    cudaEvent_t a, b;
+  };
+  std::vector<cudaEvent_t> ev_pool;
+  int ev_used = 0;
+  std::vector<Mark> ev_marks;
+  double pass_ms[3] = {0, 0, 0};
+  long long pass_n[3] = {0, 0, 0};
+
+  ~Handle();
+  void fail(int code, const char* fmt, ...);
+  bool cuda_ok(cudaError_t e, const char* what);
+  template <class T>
+  bool dalloc(T** p, size_t count, const char* what) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+    if (e != cudaSuccess) {
+      fail(SC_E_NOMEM, "cudaMalloc %s (%zu bytes): %s", what, count * sizeof(T),
+           cudaGetErrorString(e));
+      *p = nullptr;
+      return false;
+    }
+    allocs.push_back((void*)*p);
+    return true;
+  }
+  void dfree(void* p);
+
+  StepScalars row_current(int s) const;
+  bool layout_cells();
+  bool ensure_table(int rows);
+  bool upload_table(const std::vector<StepScalars>& rows);
+  bool ensure_se_hist(int nrec);
+  bool check_status(const char* where);
+  bool rebuild_all();
+  void launch_pass(int mode, bool se, int row);
+  cudaEvent_t next_event();
+  void timed(int kind, bool on, const std::function<void()>& f);
+  void collect_times();
+  void enqueue_step(bool resize, int k, bool se, bool prof);
+  void enqueue_se_record(int rec);
+  void invalidate_graph();
+  bool run_graph(bool resize, int nsteps, int se_every);
+
+  int run_steps(bool resize, int shrink, int nsteps, int se_every, double* se_out);
+  int calc(bool se, double* se_out);
+  int gd_minimize(int max_steps, double e_min, int* steps_taken, double* e_final);
+};
+
+}  // namespace sc

@@ -1,0 +1,150 @@
+// sc_internal.hpp -- data layout shared by the host runtime and the sm_103a kernels.
+//
+// Layout in HBM (all arrays indexed by "slot": particles sorted by cell, systems
+// contiguous; system s owns slots [p0, p0+n) and global cells [c0, c0+cols*rows)):
+//   xy  double2  centre position in sheared (Lees-Edwards) coordinates
+//   ph  double   orientation angle
+//   ra  double2  (R, A): radius and half shaft length
+//   irc double2  (I, RC): rotational drag factor and isolated-rotation coefficient
+//   id  int      particle index within its system (the reference's particle order)
+//   cell int     global cell index assigned at the last rebuild
+// plus per-pass working arrays (predictor copy, Heun velocities, forces, moved
+// distance) and, for the mixed form, an FP32 geometry record per particle.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace sc {
+
+enum Precision { PREC_FP64 = 0, PREC_MIXED = 1 };
+enum StressMode { STRESS_COMPAT = 0, STRESS_VIRIAL = 1 };
+
+// Per-system constants of the current cell grid; changed only by the host.
+struct SysGeom {
+  int n, p0;           // particle count and first slot
+  int c0, cols, rows;  // first global cell and grid dimensions
+  int chunk0, nchunks; // cell-scan chunks owned by the system
+  int pad_;
+  double pad;          // neighbour padding (configure_cells auto-value applied)
+  double inv_n;        // 1/n, energy normalisation
+};
+
+// Per-(step, system) scalars, computed on the host with the reference's own
+// floating-point operations so that gamma and the box lengths are bit-identical
+// to the reference's accumulation.  Row 0 of a table primes the first step
+// (only the *_p fields are used); rows 1..K are the K steps.
+struct StepScalars {
+  double gamma_c;    // gamma of the corrector force pass (gamma_k + dt*rate)
+  double gamma_p;    // gamma of the following pass (gamma_{k+1}, after any set-back)
+  double Lx_c, Ly_c; // box of the corrector pass minimum image
+  double Lx_p, Ly_p; // box after the step (predictor pass and the next corrector)
+  double W_c, H_c;   // cell size matching Lx_c, Ly_c
+  double W_p, H_p;   // cell size matching Lx_p, Ly_p
+  double rate;       // strain rate
+  double step;       // integration step
+  double scale;      // resize factor pow(1-rate, dt)
+  int mode;          // 0 none, 1 multiply by scale (shrink), 2 divide by scale (grow)
+  int setback;       // set back gamma at the end of this step
+};
+
+// Device pointers handed to every kernel by value.
+struct Dev {
+  int ntot, nsys, ncells, nchunks, npchunks;
+  int maxn;                 // neighbour-list capacity per particle (FP64 form)
+  int stress_mode;
+  const SysGeom* geom;      // [nsys]
+  const int* psys;          // [ntot] system of each slot
+  const int* cell_sys;      // [ncells] system of each cell
+  // state
+  double2* xy;
+  double* ph;
+  double2* ra;
+  double2* irc;
+  int* id;
+  int* cell;
+  double2* nxy;             // (A cos phi, A sin phi) of the state positions
+  // predictor copy
+  double2* xy_t;
+  double* ph_t;
+  double2* nxy_t;
+  // Heun velocities of the predictor, forces, moved distance
+  double* v0x;
+  double* v0y;
+  double* v0p;
+  double* fx;
+  double* fy;
+  double* tau;
+  double2* moved;
+  // mixed form: FP32 geometry records (x_local, y_local, nx, ny) and (R, A)
+  float4* rec;
+  float4* rec_t;
+  float2* raf;
+  // cell lists
+  int* cell_start;          // [ncells] first slot
+  int* cell_count;          // [ncells]
+  // neighbour list (FP64 form), column-major [k * ntot + slot]
+  int* nbr;
+  int* nbr_n;
+  // rebuild scratch
+  int* cell_tmp;
+  int* rank;
+  int* perm;
+  int* chunk_sum;
+  int* chunk_off;
+  const int* chunk_sys;     // [nchunks] system of each chunk
+  const int* chunk_c0;      // [nchunks] first global cell of each chunk
+  const int* chunk_nc;      // [nchunks] cells in the chunk
+  double2* s_xy;
+  double* s_ph;
+  double2* s_ra;
+  double2* s_irc;
+  int* s_id;
+  int* s_cell;
+  // stress/energy: per-slot contributions and per-chunk partials
+  double* se_part;          // [5][ntot]
+  double* se_chunk;         // [5][npchunks]
+  double* se_sys;           // [5][nsys]
+  const int* pchunk_sys;    // particle chunks for reductions
+  const int* pchunk_p0;
+  const int* pchunk_np;
+  // flags
+  int* flags;               // [nsys] bit0 moved-rebuild, bit1 forced rebuild
+  int* any;                 // [1] set when any system needs a rebuild
+  int* status;              // [2] sticky error bits (ST_*), rebuild-chain count
+};
+
+// sticky device status bits
+enum { ST_NBR_OVERFLOW = 1, ST_NAN = 2, ST_CELL_OVERFLOW = 4 };
+
+constexpr int kScanChunk = 1024;  // cells per scan chunk
+constexpr int kSeChunk = 1024;    // particles per reduction chunk
+constexpr int kMaxCellSort = 48;  // cells above this occupancy use the in-place slow sort
+
+// pass modes for the force kernels
+enum PassMode {
+  PASS_FORCE = 0,        // forces at the state positions
+  PASS_CORR_STRAIN = 1,  // forces at the predictor copy + Heun corrector (shear)
+  PASS_PRED_STRAIN = 2,  // forces at the state + predictor for the next step (shear)
+  PASS_CORR_RESIZE = 3,  // forces at the predictor copy + corrector (affine resize)
+  PASS_PRED_RESIZE = 4   // forces at the state + predictor (affine resize)
+};
+
+// ---- kernel launchers (defined in the .cu files) ----
+// tab: device table, row `row` holds nsys StepScalars.
+void launch_pass_fp64(const Dev& d, int mode, bool se, const StepScalars* tab, int row,
+                      cudaStream_t st);
+void launch_pass_mixed(const Dev& d, int mode, bool se, const StepScalars* tab, int row,
+                       cudaStream_t st, int block);
+void launch_setback(const Dev& d, const StepScalars* tab, int row, cudaStream_t st);
+void launch_rebuild(const Dev& d, bool mixed, const StepScalars* tab, int row, cudaStream_t st);
+void launch_force_rebuild_all(const Dev& d, cudaStream_t st);
+void launch_clear_flags(const Dev& d, cudaStream_t st);
+void launch_se_reduce(const Dev& d, cudaStream_t st);
+void launch_gd_update(const Dev& d, bool mixed, const StepScalars* tab, int row, cudaStream_t st);
+void launch_se_store(const Dev& d, double* dst, cudaStream_t st);
+void launch_refresh_geometry(const Dev& d, bool mixed, const StepScalars* tab, int row,
+                             cudaStream_t st);
+void launch_build_nbrs(const Dev& d, const StepScalars* tab, int row, cudaStream_t st);
+
+}  // namespace sc

@@ -1,0 +1,291 @@
+// sc_pass64.cu -- the plain FP64 form: neighbour-list build and force passes.
+//
+// Compiled with -fmad=false: together with the operation order of sc_pair.cuh and
+// the explicit Heun arithmetic below, every pair contribution and every position
+// update is the reference's own sequence of IEEE operations
+// (tmarschall/spherocyls src/cpp/strain_dynamics.cpp:17-235,
+// src/cpp/resize_dynamics.cpp:164-243, src/cpp/spherocyl_box.cpp:303-355).
+//
+// One thread per particle slot gathers over the particle's full neighbour list
+// (column-major, one coalesced index load per entry) and computes each pair with
+// the lower particle index as the reference's "p", so the two threads that visit a
+// pair compute bit-identical contributions.  The epilogue fuses the Heun
+// predictor or corrector for the slot.
+#include "sc_internal.hpp"
+#include "sc_pair.cuh"
+
+namespace sc {
+
+namespace {
+
+// check_neighbors, src/cpp/spherocyl_box.cpp:303-318, with p the lower index.
+__device__ __forceinline__ bool nbr_criterion(double2 pp, double2 pq, double sig, double pad,
+                                              double gamma, double Lx, double Ly) {
+  double dY = pp.y - pq.y;
+  dY += Ly * (double)((dY < -0.5 * Ly) - (dY > 0.5 * Ly));
+  if (fabs(dY) < sig + pad) {
+    double dX = pp.x - pq.x;
+    dX += Lx * (double)((dX < -0.5 * Lx) - (dX > 0.5 * Lx));
+    double dXmax = dX + 0.5 * dY;  // dX at the largest gamma of the list lifetime
+    dX += gamma * dY;
+    if (fabs(dX) < sig + pad || fabs(dXmax) < sig + pad) return true;
+  }
+  return false;
+}
+
+__global__ void __launch_bounds__(128) k_build_nbrs(Dev d, const StepScalars* __restrict__ tab,
+                                                   int row) {
+  if (*d.any == 0) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.ntot) return;
+  int s = d.psys[i];
+  if (d.flags[s] == 0) return;
+  const SysGeom g = d.geom[s];
+  const StepScalars ts = tab[row * d.nsys + s];
+  double2 pi = d.xy[i];
+  double2 rai = d.ra[i];
+  int idi = d.id[i];
+  int c = d.cell[i] - g.c0;
+  int col = c % g.cols, rw = c / g.cols;
+  // 3x3 block of cells; a dimension with fewer than three cells is scanned once
+  // per distinct cell (the reference would list such cells twice).
+  int ncx = g.cols < 3 ? g.cols : 3, ncy = g.rows < 3 ? g.rows : 3;
+  int cnt = 0;
+  for (int a = 0; a < ncy; a++) {
+    int r2 = ncy == 3 ? wrap_index(rw + a - 1, g.rows) : a;
+    for (int b = 0; b < ncx; b++) {
+      int c2 = ncx == 3 ? wrap_index(col + b - 1, g.cols) : b;
+      int cc = g.c0 + r2 * g.cols + c2;
+      int st = d.cell_start[cc], nn = d.cell_count[cc];
+      for (int j = st; j < st + nn; j++) {
+        if (j == i) continue;
+        int idj = d.id[j];
+        double2 pj = d.xy[j];
+        double2 raj = d.ra[j];
+        bool ip = idi < idj;
+        // S = R_p + A_p + R_q + A_q summed in the reference's order
+        double sig = ip ? rai.x + rai.y + raj.x + raj.y : raj.x + raj.y + rai.x + rai.y;
+        bool hit = ip ? nbr_criterion(pi, pj, sig, g.pad, ts.gamma_p, ts.Lx_p, ts.Ly_p)
+                      : nbr_criterion(pj, pi, sig, g.pad, ts.gamma_p, ts.Lx_p, ts.Ly_p);
+        if (hit) {
+          if (cnt < d.maxn) d.nbr[(size_t)cnt * d.ntot + i] = j;
+          cnt++;
+        }
+      }
+    }
+  }
+  d.nbr_n[i] = cnt;
+  if (cnt > d.maxn) atomicOr(d.status, ST_NBR_OVERFLOW);
+}
+
+__device__ __forceinline__ void flag_moved(const Dev& d, int s, double2 m, double pad) {
+  if (m.x > 0.5 * pad || m.x < -0.5 * pad || m.y > 0.5 * pad || m.y < -0.5 * pad) {
+    if (d.flags[s] == 0) atomicOr(&d.flags[s], 1);
+    if (*d.any == 0) atomicExch(d.any, 1);
+  }
+}
+
+template <int MODE, bool SE>
+__global__ void __launch_bounds__(128) k_pass64(Dev d, const StepScalars* __restrict__ tab,
+                                               int row) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.ntot) return;
+  constexpr bool kPred = (MODE == PASS_CORR_STRAIN || MODE == PASS_CORR_RESIZE);
+  int s = d.psys[i];
+  const SysGeom& g = d.geom[s];
+  const StepScalars ts = tab[row * d.nsys + s];
+  const double2* __restrict__ XY = kPred ? d.xy_t : d.xy;
+  const double2* __restrict__ NXY = kPred ? d.nxy_t : d.nxy;
+  const double gamma = kPred ? ts.gamma_c : ts.gamma_p;
+  const double Lx = kPred ? ts.Lx_c : ts.Lx_p;
+  const double Ly = kPred ? ts.Ly_c : ts.Ly_p;
+  const bool virial = d.stress_mode == STRESS_VIRIAL;
+  const double two_n = 2.0 * g.n;
+
+  double2 pi = XY[i];
+  double2 ni = NXY[i];
+  double2 rai = d.ra[i];
+  int idi = d.id[i];
+  double fx = 0.0, fy = 0.0, tq = 0.0;
+  double se0 = 0.0, se1 = 0.0, se2 = 0.0, se3 = 0.0, se4 = 0.0;
+  int cnt = d.nbr_n[i];
+  if (cnt > d.maxn) cnt = d.maxn;
+  for (int k = 0; k < cnt; k++) {
+    int j = d.nbr[(size_t)k * d.ntot + i];
+    double2 pj = XY[j];
+    double2 nj = NXY[j];
+    double2 raj = d.ra[j];
+    int idj = d.id[j];
+    bool ip = idi < idj;
+    PairF64 o;
+    bool hit;
+    if (ip)
+      hit = pair_fp64<SE>(pi.x - pj.x, pi.y - pj.y, ni.x, ni.y, rai.y, nj.x, nj.y, raj.y,
+                          rai.x + raj.x, gamma, Lx, Ly, virial, two_n, o);
+    else
+      hit = pair_fp64<false>(pj.x - pi.x, pj.y - pi.y, nj.x, nj.y, raj.y, ni.x, ni.y, rai.y,
+                             raj.x + rai.x, gamma, Lx, Ly, virial, two_n, o);
+    if (hit) {
+      if (ip) {
+        fx += o.fx;
+        fy += o.fy;
+        tq += o.tp;
+        if (SE) {
+          se0 += o.e;
+          se1 += o.pxx;
+          se2 += o.pyy;
+          se3 += o.pxy;
+          se4 += o.pyx;
+        }
+      } else {
+        fx -= o.fx;
+        fy -= o.fy;
+        tq += o.tq;
+      }
+    }
+  }
+  if (SE) {
+    d.se_part[i] = se0;
+    d.se_part[(size_t)d.ntot + i] = se1;
+    d.se_part[(size_t)2 * d.ntot + i] = se2;
+    d.se_part[(size_t)3 * d.ntot + i] = se3;
+    d.se_part[(size_t)4 * d.ntot + i] = se4;
+  }
+
+  const double2 irc = d.irc[i];  // (I, RC)
+  const double dt = ts.step;
+  if (MODE == PASS_FORCE) {
+    d.fx[i] = fx;
+    d.fy[i] = fy;
+    d.tau[i] = tq;
+  } else if (MODE == PASS_PRED_STRAIN) {
+    // strain_step predictor, strain_dynamics.cpp:187-199
+    d.fx[i] = fx;
+    d.fy[i] = fy;
+    d.tau[i] = tq;
+    double phi = d.ph[i];
+    double v0x = fx - gamma * fy;
+    double v0y = fy;
+    double v0p = tq / irc.x - ts.rate * iso_rot64(irc.y, phi);
+    d.v0x[i] = v0x;
+    d.v0y[i] = v0y;
+    d.v0p[i] = v0p;
+    double2 p = d.xy[i];
+    double2 pt = make_double2(p.x + dt * v0x, p.y + dt * v0y);
+    double pht = phi + dt * v0p;
+    d.xy_t[i] = pt;
+    d.ph_t[i] = pht;
+    double sn, cs;
+    sincos(pht, &sn, &cs);
+    d.nxy_t[i] = make_double2(rai.y * cs, rai.y * sn);
+  } else if (MODE == PASS_CORR_STRAIN) {
+    // strain_step corrector, strain_dynamics.cpp:203-219
+    double pht = d.ph_t[i];
+    double v1x = fx - gamma * fy;
+    double v1y = fy;
+    double v1p = tq / irc.x - ts.rate * iso_rot64(irc.y, pht);
+    double ddx = 0.5 * dt * (d.v0x[i] + v1x);
+    double ddy = 0.5 * dt * (d.v0y[i] + v1y);
+    double ddp = 0.5 * dt * (d.v0p[i] + v1p);
+    double2 p = d.xy[i];
+    p.x += ddx;
+    p.y += ddy;
+    double phi = d.ph[i] + ddp;
+    d.xy[i] = p;
+    d.ph[i] = phi;
+    double2 m = d.moved[i];
+    m.x += ddx;
+    m.y += ddy;
+    d.moved[i] = m;
+    double sn, cs;
+    sincos(phi, &sn, &cs);
+    d.nxy[i] = make_double2(rai.y * cs, rai.y * sn);
+    if (!(isfinite(p.x) && isfinite(p.y) && isfinite(phi))) atomicOr(d.status, ST_NAN);
+    flag_moved(d, s, m, g.pad);
+  } else if (MODE == PASS_PRED_RESIZE) {
+    // resize_step predictor, resize_dynamics.cpp:172-191
+    d.fx[i] = fx;
+    d.fy[i] = fy;
+    d.tau[i] = tq;
+    d.v0x[i] = fx;
+    d.v0y[i] = fy;
+    d.v0p[i] = tq;
+    double2 p = d.xy[i];
+    double2 pt = make_double2(p.x + dt * fx, p.y + dt * fy);
+    double pht = d.ph[i] + dt * tq / irc.x;
+    if (ts.mode == 1) {
+      pt.x *= ts.scale;
+      pt.y *= ts.scale;
+    } else if (ts.mode == 2) {
+      pt.x /= ts.scale;
+      pt.y /= ts.scale;
+    }
+    d.xy_t[i] = pt;
+    d.ph_t[i] = pht;
+    double sn, cs;
+    sincos(pht, &sn, &cs);
+    d.nxy_t[i] = make_double2(rai.y * cs, rai.y * sn);
+  } else if (MODE == PASS_CORR_RESIZE) {
+    // resize_step corrector, resize_dynamics.cpp:194-218
+    double ddx = 0.5 * dt * (d.v0x[i] + fx);
+    double ddy = 0.5 * dt * (d.v0y[i] + fy);
+    double ddp = 0.5 * dt * (d.v0p[i] + tq) / irc.x;
+    double2 p0 = d.xy[i];
+    double2 p = make_double2(p0.x + ddx, p0.y + ddy);
+    double phi = d.ph[i] + ddp;
+    if (ts.mode == 1) {
+      p.x *= ts.scale;
+      p.y *= ts.scale;
+    } else if (ts.mode == 2) {
+      p.x /= ts.scale;
+      p.y /= ts.scale;
+    }
+    d.xy[i] = p;
+    d.ph[i] = phi;
+    double2 m = d.moved[i];
+    m.x += p.x - p0.x;
+    m.y += p.y - p0.y;
+    d.moved[i] = m;
+    double sn, cs;
+    sincos(phi, &sn, &cs);
+    d.nxy[i] = make_double2(rai.y * cs, rai.y * sn);
+    if (!(isfinite(p.x) && isfinite(p.y) && isfinite(phi))) atomicOr(d.status, ST_NAN);
+    flag_moved(d, s, m, g.pad);
+  }
+}
+
+template <int MODE, bool SE>
+void launch_one(const Dev& d, const StepScalars* tab, int row, cudaStream_t st) {
+  int block = 128;
+  int grid = (d.ntot + block - 1) / block;
+  k_pass64<MODE, SE><<<grid, block, 0, st>>>(d, tab, row);
+}
+
+}  // namespace
+
+void launch_pass_fp64(const Dev& d, int mode, bool se, const StepScalars* tab, int row,
+                      cudaStream_t st) {
+  switch (mode) {
+    case PASS_FORCE:
+      se ? launch_one<PASS_FORCE, true>(d, tab, row, st) : launch_one<PASS_FORCE, false>(d, tab, row, st);
+      break;
+    case PASS_CORR_STRAIN: launch_one<PASS_CORR_STRAIN, false>(d, tab, row, st); break;
+    case PASS_PRED_STRAIN:
+      se ? launch_one<PASS_PRED_STRAIN, true>(d, tab, row, st)
+         : launch_one<PASS_PRED_STRAIN, false>(d, tab, row, st);
+      break;
+    case PASS_CORR_RESIZE: launch_one<PASS_CORR_RESIZE, false>(d, tab, row, st); break;
+    case PASS_PRED_RESIZE:
+      se ? launch_one<PASS_PRED_RESIZE, true>(d, tab, row, st)
+         : launch_one<PASS_PRED_RESIZE, false>(d, tab, row, st);
+      break;
+  }
+}
+
+void launch_build_nbrs(const Dev& d, const StepScalars* tab, int row, cudaStream_t st) {
+  int block = 128;
+  int grid = (d.ntot + block - 1) / block;
+  k_build_nbrs<<<grid, block, 0, st>>>(d, tab, row);
+}
+
+}  // namespace sc
