@@ -1,0 +1,304 @@
+"""Benchmark: particle-steps/s of Lees-Edwards shear on one GB300.
+
+Workload (default): N = 1,048,576 bidisperse spherocylinders (R = 0.5 / 0.7
+alternating, A = R), packing fraction 0.84, strain rate 1e-4, dt = 0.02, seeded
+crossing-free synthetic packing (seed 3).  A "step" is one Heun step (two force
+passes) of every particle.  The headline line times the mixed-precision form; the
+plain FP64 form, the force-pass roofline, the CPU baseline (the oracle restatement
+of the reference's CPU path on host cores) and an end-to-end run through the C ABI
+with host buffers are reported in the same JSON line.
+
+    python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (N, packing, a/R, strain rate, dt, seed)
+    "shear_n1048576_phi084": (1 << 20, 0.84, 1.0, 1e-4, 0.02, 3),
+    "shear_n16384_phi086": (16384, 0.86, 1.0, 1e-4, 0.02, 1),
+}
+# algorithmic bytes per particle per force pass of the mixed cell-tile pass
+# (positions/angle FP64 24 B + (R, A) FP32 8 B + FP32 record 16 B read; forces and
+# Heun state: v0 24 B, new position 24 B, moved 16 B r/w amortised, record 16 B write):
+# the 152 B per particle-step of the mixed form with no stored list, halved.
+BYTES_PER_PASS_MIXED = 76.0
+BYTES_PER_PASS_FP64 = 116.0 + 4 * 8.6  # (232 + 8 n)/2 with the measured list length
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    def __init__(self):
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        cmd = ["nvidia-smi",
+               "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+               "--format=csv,noheader,nounits", "-lms", "200"]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                                         text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([v.strip() for v in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self, device=0):
+        rows = [s for s in self.samples if s and s[0] == str(device)]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4)
+                          if len(r) > 5 + k and r[5 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def make_workload(name):
+    from spherocyls_gb300 import generate_packing
+
+    n, phi, a, rate, dt, seed = WORKLOADS[name]
+    L, x, y, p, R, A = generate_packing(n, phi, a, seed=seed)
+    return dict(n=n, phi=phi, a=a, rate=rate, dt=dt, seed=seed, L=L, x=x, y=y, p=p, R=R, A=A)
+
+
+def time_steps(box, steps, torch):
+    """Device time of `steps` steps with CUDA events on the library's stream."""
+    stream = torch.cuda.current_stream()
+    box.set_stream(stream.cuda_stream)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    box.strain_steps(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1e3
+
+
+def cpu_baseline(w, sample_n, steps, threads):
+    """The oracle restatement of the reference's CPU path on host cores: `threads`
+    independent replicas of a sample box (same density, shape, rate, step)."""
+    import oracle
+    from spherocyls_gb300 import generate_packing
+
+    oracle.build(with_ref=False)
+    kind = "port"
+    cls = oracle.OracleBox
+    if oracle.ref_available():
+        kind, cls = "reference", oracle.RefBox
+    L, x, y, p, R, A = generate_packing(sample_n, w["phi"], w["a"], seed=w["seed"])
+    boxes = [cls(L, x, y, p, A, R, 0.1, strain_rate=w["rate"], step=w["dt"]) for _ in range(threads)]
+    for b in boxes:
+        b.run_strain_steps(1)
+
+    def run(b):
+        b.run_strain_steps(steps)
+
+    ts = [threading.Thread(target=run, args=(b,)) for b in boxes]
+    t0 = time.perf_counter()
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    dt = time.perf_counter() - t0
+    return {"value": threads * sample_n * steps / dt, "unit": "particle-steps/s",
+            "cores": threads, "kind": kind,
+            "sample": f"{threads} independent box(es) of N={sample_n} (same packing, a/R, rate, dt), "
+                      f"{steps} Heun steps each, {dt:.1f} s"}
+
+
+def run_reference_arm(args, w, rank):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    steps = max(args.steps // 10, 5)
+    base = cpu_baseline(w, 65536, steps, threads)
+    line = {"impl": "reference", "metric": "particle-steps/s (Lees-Edwards shear, Heun step)",
+            "value": base["value"], "unit": "particle-steps/s", "n_gpus": args.gpus,
+            "steps": steps, "warmup": 1, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "N": w["n"], "sample_N": 65536},
+            "cpu_baseline": base,
+            "e2e": {"value": base["value"], "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="shear_n1048576_phi084", choices=list(WORKLOADS))
+    ap.add_argument("--fp64-steps", type=int, default=20)
+    ap.add_argument("--cpu-steps", type=int, default=5)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    w = make_workload(args.workload)
+    if args.impl == "reference":
+        run_reference_arm(args, w, rank)
+        return
+
+    import torch
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    import __graft_entry__
+
+    __graft_entry__.build()
+    from spherocyls_gb300 import SpherocylBox
+
+    n = w["n"]
+
+    def new_box(precision, profile=False):
+        b = SpherocylBox(w["L"], w["x"], w["y"], w["p"], w["A"], w["R"], 0.1, precision=precision,
+                         device=local, profile=profile)
+        b.set_strain_rate(w["rate"])
+        b.set_step(w["dt"])
+        return b
+
+    # ---- mixed precision, device-resident: the headline value ----
+    box = new_box("mixed")
+    box.strain_steps(args.warmup)
+    counters0 = box.counters()
+    if world > 1:
+        torch.distributed.barrier()
+    with ClockSampler() as clk:
+        secs = time_steps(box, args.steps, torch)
+    if world > 1:
+        t = torch.tensor([secs], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        secs = float(t.item())
+    value = world * n * args.steps / secs
+    k_before = counters0["kernels"]
+    counters = box.counters()
+    launches = counters["kernels"] - k_before
+
+    # ---- force-pass timing with per-pass CUDA events (same workload, same state) ----
+    prof = new_box("mixed", profile=True)
+    prof.strain_steps(args.warmup)
+    prof.pass_times()
+    prof.strain_steps(min(args.steps, 100))
+    pt = prof.pass_times()
+    pass_ms = 0.5 * (pt["corr_ms"] + pt["pred_ms"])
+    peak, peak_kind = _peaks()
+    achieved = BYTES_PER_PASS_MIXED * n / (pass_ms / 1e3) / 1e9
+    prof.close()
+
+    # ---- plain FP64 form on the same workload ----
+    b64 = new_box("fp64")
+    b64.strain_steps(3)
+    secs64 = time_steps(b64, args.fp64_steps, torch)
+    value64 = n * args.fp64_steps / secs64
+    b64.close()
+
+    # ---- end to end through the C ABI with host buffers ----
+    box.close()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_box = new_box("mixed")
+    rec_every = 100
+    h2d = 40 * n  # x, y, phi, R, A
+    d2h = 0
+    done = 0
+    while done < args.steps:
+        k = min(rec_every, args.steps - done)
+        e2e_box.strain_steps(k, se_every=k)
+        e2e_box.state()
+        d2h += 24 * n + 40
+        done += k
+    torch.cuda.synchronize()
+    e2e_secs = time.perf_counter() - t0
+    e2e_box.close()
+    e2e = {"value": n * args.steps / e2e_secs, "unit": "particle-steps/s",
+           "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
+           "note": "sc_create from host arrays, steps in chunks of 100 with stress/energy and "
+                   "positions read back after each chunk"}
+
+    base = None
+    if rank == 0 and not args.no_cpu:
+        base = cpu_baseline(w, 65536, args.cpu_steps, 1)
+
+    if rank == 0:
+        line = {
+            "metric": "particle-steps/s (Lees-Edwards shear, Heun step), mixed precision",
+            "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic (seeded crossing-free packing)",
+            "config": {"workload": args.workload, "N": n, "packing": w["phi"], "a_over_r": w["a"],
+                       "strain_rate": w["rate"], "dt": w["dt"], "seed": w["seed"], "pad": 0.1,
+                       "l2": "state larger than L2 (~200 MB per step touched)",
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "plain_fp64": {"value": value64, "unit": "particle-steps/s",
+                           "ms_per_step": 1e3 * secs64 / args.fp64_steps,
+                           "steps": args.fp64_steps, "mixed_over_fp64": value / value64},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                         "kernel": "k_pass_mixed (corrector/predictor force passes)",
+                         "pass_ms": pass_ms, "bytes_per_particle_pass": BYTES_PER_PASS_MIXED,
+                         "rebuild_ms_mean": pt["rebuild_ms"]},
+            "cpu_baseline": base,
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "clocks": clk.summary(local),
+            "rebuild_chains": counters["rebuilds"],
+        }
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -120,7 +120,8 @@ int sc_get_box(sc_handle *h, int sys, double *out);
 /* Half neighbour list of one system as (p, q) pairs with p < q, sorted; with
  * pairs == NULL only *n_pairs is written.  (The reference's m_pvNeighbors.) */
 int sc_get_pairs(sc_handle *h, int sys, int *pairs, long cap, long *n_pairs);
-/* Counters: out[0] steps, out[1] neighbour rebuilds, out[2] device status bits. */
+/* Counters: out[0] steps, out[1] rebuild chains executed on the device, out[2]
+ * device status bits, out[3] kernels launched so far. */
 int sc_get_counters(sc_handle *h, long long *out);
 /* Mean device time per force pass of the last run call with profiling on:
  * out[0] corrector passes (ms), out[1] predictor passes (ms), out[2] rebuild

@@ -138,6 +138,10 @@ class _BoxBase:
             raise RuntimeError("oracle box creation failed")
         self.set_params(strain_rate=strain_rate, resize_rate=resize_rate, step=step, gamma=gamma,
                         total_gamma=total_gamma)
+        # The reference's constructor leaves the forces uninitialised (new Spherocyl[n]);
+        # its run methods always call calc_se/calc_forces before the first step
+        # (src/cpp/strain_dynamics.cpp:242-279), so do the same here.
+        self.calc_forces()
 
     def set_params(self, *, strain_rate, resize_rate, step, gamma, total_gamma):
         L = self._L

@@ -180,9 +180,9 @@ class BoxBatch:
         return out[: n.value]
 
     def counters(self) -> dict:
-        out = (ctypes.c_longlong * 3)()
+        out = (ctypes.c_longlong * 4)()
         self._chk(lib().sc_get_counters(self.h, out))
-        return {"steps": out[0], "rebuilds": out[1], "status": out[2]}
+        return {"steps": out[0], "rebuilds": out[1], "status": out[2], "kernels": out[3]}
 
     def pass_times(self) -> dict:
         out = np.empty(6)

@@ -504,6 +504,7 @@ int sc_get_counters(sc_handle* H, long long* out) {
   out[0] = H->h.steps;
   out[1] = H->h.dev_rebuilds;
   out[2] = H->h.dev_status;
+  out[3] = H->h.kernels;
   return SC_OK;
 }
 

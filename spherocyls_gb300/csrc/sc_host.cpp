@@ -243,6 +243,7 @@ bool Handle::rebuild_all() {
 }
 
 void Handle::launch_pass(int mode, bool se, int row) {
+  kernels += 1;
   if (prec == PREC_MIXED)
     launch_pass_mixed(d, mode, se, d_tab, row, stream, block);
   else
@@ -286,8 +287,12 @@ void Handle::collect_times() {
 // One Heun step (rows k of the uploaded table), strain or resize form.
 void Handle::enqueue_step(bool resize, int k, bool se, bool prof) {
   timed(0, prof, [&] { launch_pass(resize ? PASS_CORR_RESIZE : PASS_CORR_STRAIN, false, k); });
-  if (!resize) launch_setback(d, d_tab, k, stream);
+  if (!resize) {
+    launch_setback(d, d_tab, k, stream);
+    kernels += 1;
+  }
   timed(2, prof, [&] { launch_rebuild(d, prec == PREC_MIXED, d_tab, k, stream); });
+  kernels += prec == PREC_MIXED ? 10 : 11;
   timed(1, prof, [&] { launch_pass(resize ? PASS_PRED_RESIZE : PASS_PRED_STRAIN, se, k); });
 }
 
@@ -309,11 +314,14 @@ bool Handle::run_graph(bool resize, int nsteps, int se_every) {
                  "begin capture"))
       return false;
     int r = 0;
+    long long k0 = kernels;
     for (int k = 1; k <= nsteps; k++) {
       bool se = se_every > 0 && k % se_every == 0;
       enqueue_step(resize, k, se, false);
       if (se) enqueue_se_record(r++);
     }
+    graph_kernels = kernels - k0;
+    kernels = k0;
     cudaError_t e = cudaStreamEndCapture(stream, &g);
     if (!cuda_ok(e, "end capture")) return false;
     e = cudaGraphInstantiate(&graph_exec, g, 0);
@@ -324,6 +332,7 @@ bool Handle::run_graph(bool resize, int nsteps, int se_every) {
     }
     graph_key = key;
   }
+  kernels += graph_kernels;
   return cuda_ok(cudaGraphLaunch(graph_exec, stream), "graph launch");
 }
 
@@ -340,6 +349,7 @@ bool Handle::ensure_se_hist(int nrec) {
 }
 
 void Handle::enqueue_se_record(int rec) {
+  kernels += 3;
   launch_se_reduce(d, stream);
   launch_se_store(d, d_se_hist + (size_t)rec * nsys * 5, stream);
 }

@@ -63,6 +63,8 @@ struct Handle {
   long long steps = 0, rebuilds = 0;
   int dev_status = 0;
   long long dev_rebuilds = 0;  // rebuild chains the device executed
+  long long kernels = 0;       // kernels launched (eagerly or inside graphs)
+  long long graph_kernels = 0; // kernels in the captured chunk graph
   int last_status = SC_OK;
   std::string err;
   // CUDA graph of one chunk of steps

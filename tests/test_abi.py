@@ -1,0 +1,89 @@
+"""CPU checks of the C ABI: the library loads, exports every declared entry point,
+validates arguments without touching a GPU, and its host-side packing generator
+is reproducible and crossing-free."""
+from __future__ import annotations
+
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def _declared_symbols() -> list[str]:
+    hdr = open(os.path.join(ROOT, "include", "spherocyl.h")).read()
+    hdr = re.sub(r"/\*.*?\*/", "", hdr, flags=re.S)
+    return sorted(set(re.findall(r"\b(sc_[a-z0-9_]+)\s*\(", hdr)))
+
+
+def test_library_exports_every_declared_symbol(library):
+    names = _declared_symbols()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(library, n), n
+
+
+def test_binding_covers_header():
+    from spherocyls_gb300 import _lib
+
+    bound = {s[0] for s in _lib.SIGNATURES}
+    assert set(_declared_symbols()) <= bound
+
+
+def test_create_rejects_bad_arguments_without_gpu(library):
+    import ctypes
+
+    from spherocyls_gb300 import _lib
+
+    h = ctypes.c_void_p()
+    n = (ctypes.c_int * 1)(1)
+    L = (ctypes.c_double * 1)(10.0)
+    a = (ctypes.c_double * 1)(0.5)
+    st = library.sc_create(None, 1, n, L, None, a, a, a, a, a, ctypes.byref(h))
+    assert st == _lib.SC_E_ARG  # a system needs at least two particles
+    assert b"n >= 2" in library.sc_last_error(None)
+    n2 = (ctypes.c_int * 1)(2)
+    bad = (ctypes.c_double * 2)(float("nan"), 1.0)
+    ok = (ctypes.c_double * 2)(0.5, 0.5)
+    st = library.sc_create(None, 1, n2, L, None, bad, ok, ok, ok, ok, ctypes.byref(h))
+    assert st == _lib.SC_E_NAN
+    assert library.sc_status_string(_lib.SC_E_OVERFLOW) == b"capacity exceeded"
+
+
+def test_generator_reproducible_and_crossing_free(library):
+    from spherocyls_gb300 import generate_packing
+
+    L1, x1, y1, p1, R1, A1 = generate_packing(300, 0.85, 1.0, seed=5)
+    L2, x2, y2, p2, R2, A2 = generate_packing(300, 0.85, 1.0, seed=5)
+    assert L1 == L2 and np.array_equal(x1, x2) and np.array_equal(p1, p2)
+    _, x3, *_ = generate_packing(300, 0.85, 1.0, seed=6)
+    assert not np.array_equal(x1, x3)
+    # bidisperse alternation and packing fraction
+    assert np.all(R1[0::2] == 0.5) and np.allclose(R1[1::2], 0.7) and np.allclose(A1, R1)
+    phi = np.sum(np.pi * R1 ** 2 + 4 * A1 * R1) / L1 ** 2
+    assert abs(phi - 0.85) < 1e-12
+    assert np.all((x1 >= 0) & (x1 < L1) & (p1 >= 0) & (p1 < np.pi))
+    # minimum spine separation >= 0.1 sigma (brute force, sampled segments)
+    s = np.linspace(-1, 1, 41)
+    ux, uy = A1 * np.cos(p1), A1 * np.sin(p1)
+    worst = np.inf
+    for i in range(len(x1)):
+        dx = x1[i] - x1
+        dy = y1[i] - y1
+        dx -= L1 * np.round(dx / L1)
+        dy -= L1 * np.round(dy / L1)
+        near = np.nonzero((dx ** 2 + dy ** 2 < (2 * A1.max() + 0.2) ** 2) & (np.arange(len(x1)) != i))[0]
+        for j in near:
+            ax = dx[j] + s[:, None] * ux[i] - s[None, :] * ux[j]
+            ay = dy[j] + s[:, None] * uy[i] - s[None, :] * uy[j]
+            worst = min(worst, np.sqrt(ax ** 2 + ay ** 2).min() / (R1[i] + R1[j]))
+    assert worst >= 0.1 - 1e-9
+
+
+def test_generator_rejects_bad_arguments(library):
+    from spherocyls_gb300 import ScError, generate_packing
+
+    with pytest.raises(ScError):
+        generate_packing(10, 1.5, 1.0)

@@ -1,0 +1,242 @@
+"""Parity of the CUDA library (through its C ABI) with the reference's CPU path.
+
+Plain FP64 form: positions, angles, forces, stress and energy agree with the
+reference's own outputs (tests/golden/, made by the reference itself) and with the
+oracle within TOL = 1e-12 relative over the first 100 steps, the tolerance the
+plain form is specified to meet.  Neighbour lists agree as sets of pairs, exactly.
+
+Positions are compared modulo the box and angles modulo 2*pi_ref: the reference
+wraps them only when it rebuilds its lists, and rebuild timing is not part of
+the result (any list that contains all pairs within reach gives the same forces).
+Pyx is compared only on the first stress evaluation: the reference never resets
+it between calls (src/cpp/spherocyl_box.cpp:509-512), the library does.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import REF_PI, load_golden, periodic_diff
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12  # relative tolerance of the plain FP64 form
+
+
+@pytest.fixture(scope="module")
+def sc(library):
+    import spherocyls_gb300
+
+    return spherocyls_gb300
+
+
+def _gpu_box(sc, g, pad, precision="fp64", **kw):
+    return sc.SpherocylBox(float(g["L"]), g["x"], g["y"], g["phi"], g["A"], g["R"], pad,
+                           precision=precision, **kw)
+
+
+def _assert_state(box, g, prefix, L, tol=TOL):
+    x, y, p = box.state()
+    ex = np.max(np.abs(periodic_diff(x, g[prefix + "x"], L)))
+    ey = np.max(np.abs(periodic_diff(y, g[prefix + "y"], L)))
+    ep = np.max(np.abs(periodic_diff(p, g[prefix + "phi"], 2 * REF_PI)))
+    assert ex <= tol * L and ey <= tol * L, (prefix, ex, ey)
+    assert ep <= tol * 2 * REF_PI, (prefix, ep)
+
+
+def _assert_forces(box, g, prefix, tol=TOL):
+    f = np.array(box.forces())
+    fg = np.stack([g[prefix + "fx"], g[prefix + "fy"], g[prefix + "tau"]])
+    rms = np.sqrt(np.mean(fg ** 2))
+    err = np.max(np.abs(f - fg))
+    assert err <= tol * rms, (prefix, err, rms)
+
+
+def _assert_se(se, sg, ncols=4, tol=TOL):
+    scale = max(abs(sg[0]), np.max(np.abs(sg[1:4])))
+    for k in range(ncols):
+        assert abs(se[k] - sg[k]) <= tol * scale, (k, se[k], sg[k])
+
+
+@pytest.mark.parametrize("name", ["shear_n1024_phi085", "shear_n256_setback", "shear_n512_autopad"])
+@pytest.mark.parametrize("graphs", [False, True])
+def test_fp64_shear_matches_reference(sc, name, graphs):
+    g = load_golden(name)
+    rate, dt, pad = g["params"]
+    L = float(g["L"])
+    box = _gpu_box(sc, g, pad, use_graphs=graphs)
+    box.set_strain_rate(rate)
+    box.set_step(dt)
+    # neighbour list of the initial state: the same set of pairs
+    pairs = box.pairs()
+    ref_pairs = np.sort(g["pairs0"].view([("p", np.int32), ("q", np.int32)]), axis=0)
+    assert np.array_equal(pairs, ref_pairs.view(np.int32).reshape(-1, 2))
+    se0 = box.calc_se()
+    _assert_se(se0, g["s0_se"], ncols=5)
+    _assert_forces(box, g, "s0_")
+    done = 0
+    traces = []
+    for cp in g["checkpoints"]:
+        cp = int(cp)
+        rec = box.strain_steps(cp - done, se_every=1 if "se_trace" in g else 0)
+        if rec is not None:
+            traces.append(rec[:, 0, :])
+        done = cp
+        bx = g[f"s{cp}_box"]
+        b = box.box()
+        assert b["gamma"] == bx[2] and b["gamma_total"] == bx[3]
+        _assert_state(box, g, f"s{cp}_", L)
+        box.calc_se()
+        _assert_forces(box, g, f"s{cp}_")
+        _assert_se(box.calc_se(), g[f"s{cp}_se"])
+    if traces:
+        tr = np.concatenate(traces)
+        ref = g["se_trace"]
+        for k in range(4):
+            assert np.max(np.abs(tr[:, k] - ref[:, k])) <= TOL * np.max(np.abs(ref[:, :4]))
+
+
+@pytest.mark.parametrize("name", ["resize_n256_shrink", "resize_n256_grow"])
+def test_fp64_resize_matches_reference(sc, name):
+    g = load_golden(name)
+    rate, dt, pad, shrink = g["params"]
+    box = _gpu_box(sc, g, pad)
+    box.set_resize_rate(rate)
+    box.set_step(dt)
+    done = 0
+    for cp in g["checkpoints"]:
+        cp = int(cp)
+        box.resize_steps(cp - done, shrink=bool(shrink))
+        done = cp
+        bx = g[f"s{cp}_box"]
+        b = box.box()
+        assert b["Lx"] == bx[0] and b["Ly"] == bx[1]
+        _assert_state(box, g, f"s{cp}_", bx[0])
+        box.calc_se()
+        _assert_forces(box, g, f"s{cp}_")
+        _assert_se(box.calc_se(), g[f"s{cp}_se"])
+
+
+def test_fp64_gradient_descent_matches_reference(sc):
+    g = load_golden("gd_n256")
+    dt, pad, nsteps = g["params"]
+    box = _gpu_box(sc, g, pad)
+    box.set_step(dt)
+    steps, e_final = box.gd_minimize(int(nsteps), 0.0)
+    assert steps == int(g["steps"])
+    _assert_state(box, g, "end_", float(g["L"]))
+    se = box.calc_se()
+    _assert_se(se, g["end_se"])
+
+
+def test_fp64_pair_geometry_matches_reference(sc):
+    g = load_golden("pair_geometry")
+    for name in g["names"]:
+        x0, y0, p0, x1, y1, p1, gam = g[name + "_in"]
+        box = sc.SpherocylBox(float(g["L"]), [x0, x1], [y0, y1], [p0, p1], g["A"], g["R"], 0.1)
+        box.set_gamma(gam)
+        se = box.calc_se()
+        f = np.array(box.forces())
+        fg = g[name + "_f"]
+        assert np.max(np.abs(f - fg)) <= TOL * max(np.abs(fg).max(), 1e-300), name
+        _assert_se(se, g[name + "_se"], ncols=5)
+        assert np.array_equal(box.pairs(), g[name + "_pairs"]), name
+        box.close()
+
+
+def test_fp64_matches_oracle_long_run_with_setback(sc, oracle_built):
+    """Oracle and library side by side over 600 steps through a gamma set-back."""
+    g = load_golden("shear_n256_setback")
+    L = float(g["L"])
+    kw = dict(strain_rate=0.05, step=0.02)
+    ob = oracle_built.OracleBox(L, g["x"], g["y"], g["phi"], g["A"], g["R"], 0.1, **kw)
+    box = _gpu_box(sc, g, 0.1)
+    box.set_strain_rate(kw["strain_rate"])
+    box.set_step(kw["step"])
+    for _ in range(6):
+        se_o = ob.run_strain_steps(100, record_se=True)
+        se_g = box.strain_steps(100, se_every=10)[:, 0, :]
+        x, y, p = box.state()
+        ox, oy, op = ob.state()
+        assert np.max(np.abs(periodic_diff(x, ox, L))) <= TOL * L
+        assert np.max(np.abs(periodic_diff(y, oy, L))) <= TOL * L
+        _assert_se(se_g[-1], se_o[-1])
+    assert box.box()["gamma"] == ob.scalars()["gamma"]
+
+
+def test_neighbour_lists_equal_reference_sets_random_states(sc, oracle_built):
+    """Bit-exact list sets for identical positions at several gamma values."""
+    for seed, gam in [(1, 0.0), (2, 0.37), (3, -0.49), (4, 0.4999)]:
+        L, x, y, p, R, A = sc.generate_packing(400, 0.84, 1.5, seed=seed)
+        ob = oracle_built.OracleBox(L, x, y, p, A, R, 0.15, gamma=gam)
+        ob.find_neighbors()
+        box = sc.SpherocylBox(L, x, y, p, A, R, 0.15)
+        box.set_gamma(gam)
+        ref = ob.pairs()
+        ref = ref[np.lexsort((ref[:, 1], ref[:, 0]))]
+        assert np.array_equal(box.pairs(), ref), (seed, gam)
+
+
+def test_mixed_precision_against_fp64(sc, oracle_built):
+    """FP32 pair geometry: forces within 1e-4 of the RMS force, energy and stress
+    within 2e-6 relative of the FP64 oracle on the same configuration."""
+    g = load_golden("shear_n1024_phi085")
+    L = float(g["L"])
+    for prefix in ("s0_", "s100_"):
+        box = sc.SpherocylBox(L, g[prefix + "x"], g[prefix + "y"], g[prefix + "phi"], g["A"],
+                              g["R"], 0.1, precision="mixed")
+        box.set_gamma(g[prefix + "box"][2])
+        se = box.calc_se()
+        _assert_forces(box, g, prefix, tol=1e-4)
+        sg = g[prefix + "se"]
+        assert abs(se[0] - sg[0]) <= 2e-6 * abs(sg[0])
+        for k in (1, 2, 3):
+            assert abs(se[k] - sg[k]) <= 2e-6 * max(abs(sg[1]), abs(sg[2]))
+
+
+def test_mixed_precision_shear_tracks_fp64(sc):
+    """100 mixed steps stay close to 100 FP64 steps (short-time, before chaos)."""
+    g = load_golden("shear_n1024_phi085")
+    L = float(g["L"])
+    rate, dt, pad = g["params"]
+    a = _gpu_box(sc, g, pad, precision="fp64")
+    b = _gpu_box(sc, g, pad, precision="mixed")
+    for box in (a, b):
+        box.set_strain_rate(rate)
+        box.set_step(dt)
+    sa = a.strain_steps(100, se_every=10)
+    sb = b.strain_steps(100, se_every=10)
+    xa, ya, _ = a.state()
+    xb, yb, _ = b.state()
+    assert np.max(np.abs(periodic_diff(xa, xb, L))) < 1e-4
+    assert np.all(np.abs(sa[:, 0, 0] - sb[:, 0, 0]) <= 1e-4 * np.abs(sa[:, 0, 0]))
+
+
+def test_batched_systems_match_single_runs(sc):
+    """Several systems of different size in one handle advance exactly as alone."""
+    specs = [(256, 0.85, 1.0, 1e-3, 21), (400, 0.80, 0.5, 5e-4, 22), (300, 0.88, 2.0, 2e-3, 23)]
+    packs = [sc.generate_packing(n, phi, a, seed=s) for n, phi, a, _, s in specs]
+    singles = []
+    for (n, phi, a, rate, s), (L, x, y, p, R, A) in zip(specs, packs):
+        box = sc.SpherocylBox(L, x, y, p, A, R, 0.1)
+        box.set_strain_rate(rate)
+        box.set_step(0.02)
+        box.strain_steps(150)
+        singles.append(np.concatenate(box.state()))
+    batch = sc.BoxBatch([sp[0] for sp in specs], [pk[0] for pk in packs],
+                        np.concatenate([pk[1] for pk in packs]),
+                        np.concatenate([pk[2] for pk in packs]),
+                        np.concatenate([pk[3] for pk in packs]),
+                        np.concatenate([pk[5] for pk in packs]),
+                        np.concatenate([pk[4] for pk in packs]), 0.1)
+    for i, sp in enumerate(specs):
+        batch.set_strain_rate(sp[3], sys=i)
+    batch.set_step(0.02)
+    batch.strain_steps(150)
+    x, y, p = batch.state()
+    off = 0
+    for i, sp in enumerate(specs):
+        n = sp[0]
+        got = np.concatenate([x[off:off + n], y[off:off + n], p[off:off + n]])
+        assert np.array_equal(got, singles[i]), i
+        off += n
