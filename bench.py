@@ -103,9 +103,16 @@ def make_workload(name):
     return dict(n=n, phi=phi, a=a, rate=rate, dt=dt, seed=seed, L=L, x=x, y=y, p=p, R=R, A=A)
 
 
+_STREAM = None
+
+
 def time_steps(box, steps, torch):
-    """Device time of `steps` steps with CUDA events on the library's stream."""
-    stream = torch.cuda.current_stream()
+    """Device time of `steps` steps with CUDA events on the library's stream (a
+    dedicated non-default stream shared with torch's events)."""
+    global _STREAM
+    if _STREAM is None:
+        _STREAM = torch.cuda.Stream()
+    stream = _STREAM
     box.set_stream(stream.cuda_stream)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -176,6 +183,8 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=20)
     ap.add_argument("--cpu-steps", type=int, default=5)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--only", choices=["mixed", "fp64"], default=None,
+                    help="time one form only (for profiler captures)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -207,6 +216,16 @@ def main():
         b.set_strain_rate(w["rate"])
         b.set_step(w["dt"])
         return b
+
+    if args.only:
+        b = new_box(args.only)
+        b.strain_steps(args.warmup)
+        secs = time_steps(b, args.steps, torch)
+        if rank == 0:
+            print(json.dumps({"only": args.only, "workload": args.workload, "steps": args.steps,
+                              "ms_per_step": 1e3 * secs / args.steps,
+                              "value": n * args.steps / secs}))
+        return
 
     # ---- mixed precision, device-resident: the headline value ----
     box = new_box("mixed")

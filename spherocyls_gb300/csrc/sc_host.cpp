@@ -443,7 +443,14 @@ int Handle::run_steps(bool resize, int shrink, int nsteps, int se_every, double*
     }
     std::vector<HostSys> sim = hs;
     std::vector<StepScalars> rows((size_t)(nk + 1) * nsys);
-    for (int s = 0; s < nsys; s++) rows[s] = row_current(s);
+    for (int s = 0; s < nsys; s++) {
+      // row 0 primes the predictor of the first step, which scales like any step
+      rows[s] = row_current(s);
+      if (resize) {
+        rows[s].scale = std::pow(1.0 - hs[s].resize_rate, hs[s].step);
+        rows[s].mode = shrink ? 1 : 2;
+      }
+    }
     for (int k = 1; k <= nk; k++)
       for (int s = 0; s < nsys; s++) advance(sim[s], resize, shrink, rows[(size_t)k * nsys + s]);
     if (!upload_table(rows)) return last_status;
@@ -453,9 +460,11 @@ int Handle::run_steps(bool resize, int shrink, int nsteps, int se_every, double*
     for (int k = 1; k <= nk; k++)
       if (se_every > 0 && (done + k) % se_every == 0) nrec++;
     if (nrec > 0 && !ensure_se_hist(nrec)) return last_status;
-    if (!pred_valid) {
+    const int kind = resize ? (shrink ? 2 : 3) : 1;
+    if (!pred_valid || pred_kind != kind) {
       launch_pass(resize ? PASS_PRED_RESIZE : PASS_PRED_STRAIN, false, 0);
       pred_valid = true;
+      pred_kind = kind;
     }
     bool aligned = se_every == 0 || done % se_every == 0;
     bool use_graph = opt.use_graphs && !opt.profile && nk == kChunk && aligned;

@@ -59,7 +59,8 @@ struct Handle {
   double* d_se_hist = nullptr;
   int se_hist_cap = 0;
   int* h_pinned = nullptr;  // status word + scratch for small reads
-  bool pred_valid = false;
+  bool pred_valid = false;  // predictor copy consistent with the state
+  int pred_kind = 0;        // 1 strain, 2 shrink, 3 grow
   long long steps = 0, rebuilds = 0;
   int dev_status = 0;
   long long dev_rebuilds = 0;  // rebuild chains the device executed
