@@ -30,12 +30,11 @@ WORKLOADS = {
     "shear_n1048576_phi084": (1 << 20, 0.84, 1.0, 1e-4, 0.02, 3),
     "shear_n16384_phi086": (16384, 0.86, 1.0, 1e-4, 0.02, 1),
 }
-# algorithmic bytes per particle per force pass of the mixed cell-tile pass
-# (positions/angle FP64 24 B + (R, A) FP32 8 B + FP32 record 16 B read; forces and
-# Heun state: v0 24 B, new position 24 B, moved 16 B r/w amortised, record 16 B write):
-# the 152 B per particle-step of the mixed form with no stored list, halved.
-BYTES_PER_PASS_MIXED = 76.0
-BYTES_PER_PASS_FP64 = 116.0 + 4 * 8.6  # (232 + 8 n)/2 with the measured list length
+# Algorithmic bytes per particle-step (two force passes plus the state update):
+# mixed form 152 + 8 n, plain FP64 form 232 + 8 n, n the mean length of the full
+# neighbour list actually used (4 bytes per entry and pass).  Per force pass: half.
+def bytes_per_pass(precision: str, nbar: float) -> float:
+    return (152.0 if precision == "mixed" else 232.0) / 2 + 4.0 * nbar
 
 
 def _peaks():
@@ -252,7 +251,9 @@ def main():
     pt = prof.pass_times()
     pass_ms = 0.5 * (pt["corr_ms"] + pt["pred_ms"])
     peak, peak_kind = _peaks()
-    achieved = BYTES_PER_PASS_MIXED * n / (pass_ms / 1e3) / 1e9
+    nbar = 2.0 * len(prof.pairs()) / n
+    bpp = bytes_per_pass("mixed", nbar)
+    achieved = bpp * n / (pass_ms / 1e3) / 1e9
     prof.close()
 
     # ---- plain FP64 form on the same workload ----
@@ -306,7 +307,7 @@ def main():
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
                          "kernel": "k_pass_mixed (corrector/predictor force passes)",
-                         "pass_ms": pass_ms, "bytes_per_particle_pass": BYTES_PER_PASS_MIXED,
+                         "pass_ms": pass_ms, "bytes_per_particle_pass": bpp, "mean_list_length": nbar,
                          "rebuild_ms_mean": pt["rebuild_ms"]},
             "cpu_baseline": base,
             "e2e": e2e,

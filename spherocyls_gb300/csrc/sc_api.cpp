@@ -198,9 +198,9 @@ int sc_create(const sc_options* opt_in, int n_sys, const int* n_per_sys, const d
        h.dalloc(&d.tau, N, "tau") && h.dalloc(&d.moved, N, "moved");
   if (h.prec == sc::PREC_MIXED)
     ok = ok && h.dalloc(&d.rec, N, "rec") && h.dalloc(&d.rec_t, N, "rec_t") &&
-         h.dalloc(&d.raf, N, "raf");
-  else
-    ok = ok && h.dalloc(&d.nbr, N * d.maxn, "nbr");
+         h.dalloc(&d.mc, N, "mc") && h.dalloc(&d.mv, N, "mv") && h.dalloc(&d.mm, N, "mm") &&
+         h.dalloc(&d.pa, N, "pa") && h.dalloc(&d.cellp, N, "cellp");
+  ok = ok && h.dalloc(&d.nbr, N * d.maxn, "nbr");
   ok = ok && h.dalloc(&d.nbr_n, N, "nbr_n");
   ok = ok && h.dalloc(&d.cell_tmp, N, "cell_tmp") && h.dalloc(&d.rank, N, "rank") &&
        h.dalloc(&d.perm, N, "perm");
@@ -212,7 +212,8 @@ int sc_create(const sc_options* opt_in, int n_sys, const int* n_per_sys, const d
        h.dalloc(&d.se_sys, 5 * (size_t)n_sys, "se_sys");
   ok = ok && h.dalloc(&pcs, d.npchunks, "pchunk") && h.dalloc(&pcp, d.npchunks, "pchunk") &&
        h.dalloc(&pcn, d.npchunks, "pchunk");
-  ok = ok && h.dalloc(&d.flags, n_sys, "flags") && h.dalloc(&d.any, 1, "any") &&
+  ok = ok && h.dalloc(&d.flags, n_sys, "flags") && h.dalloc(&d.istar, n_sys, "istar") &&
+       h.dalloc(&d.any, 1, "any") &&
        h.dalloc(&d.status, 2, "status");
   if (!ok) return bail(h.last_status ? h.last_status : SC_E_NOMEM);
   d.geom = geom;
@@ -256,6 +257,7 @@ int sc_create(const sc_options* opt_in, int n_sys, const int* n_per_sys, const d
                                  cudaMemcpyHostToDevice, st), "upload") &&
        h.cuda_ok(cudaMemsetAsync(d.moved, 0, N * sizeof(double2), st), "memset") &&
        h.cuda_ok(cudaMemsetAsync(d.flags, 0, n_sys * sizeof(int), st), "memset") &&
+       h.cuda_ok(cudaMemsetAsync(d.istar, 0x7f, n_sys * sizeof(int), st), "memset") &&
        h.cuda_ok(cudaMemsetAsync(d.any, 0, sizeof(int), st), "memset") &&
        h.cuda_ok(cudaMemsetAsync(d.status, 0, 2 * sizeof(int), st), "memset") &&
        h.cuda_ok(cudaMemsetAsync(d.nbr_n, 0, N * sizeof(int), st), "memset") &&
@@ -367,6 +369,10 @@ int sc_gd_minimize(sc_handle* H, int max_steps, double e_min, int* steps_taken, 
     H->h.fail(SC_E_ARG, "max_steps must be >= 0");
     return SC_E_ARG;
   }
+  if (H->h.prec != sc::PREC_FP64) {
+    H->h.fail(SC_E_STATE, "sc_gd_minimize is the reference's FP64 protocol; use an FP64 handle");
+    return SC_E_STATE;
+  }
   return H->h.gd_minimize(max_steps, e_min, steps_taken, e_final);
 }
 
@@ -390,6 +396,7 @@ int sc_get_state(sc_handle* H, double* x, double* y, double* phi) {
   if (!H) return SC_E_ARG;
   sc::Handle& h = H->h;
   cudaSetDevice(h.device);
+  if (!h.materialize()) return h.last_status;
   std::vector<double2> xy(h.ntot);
   std::vector<double> ph(h.ntot);
   std::vector<int> gid;
@@ -411,6 +418,11 @@ int sc_get_forces(sc_handle* H, double* fx, double* fy, double* tau) {
   if (!H) return SC_E_ARG;
   sc::Handle& h = H->h;
   cudaSetDevice(h.device);
+  // the mixed form's step passes do not keep the forces: evaluate them
+  if (h.prec == sc::PREC_MIXED && !h.forces_valid) {
+    int rc = h.calc(false, nullptr);
+    if (rc) return rc;
+  }
   std::vector<double> a(h.ntot), b(h.ntot), c(h.ntot);
   std::vector<int> gid;
   if (!h.cuda_ok(cudaMemcpyAsync(a.data(), h.d.fx, h.ntot * sizeof(double),
@@ -459,14 +471,6 @@ int sc_get_pairs(sc_handle* H, int sys, int* pairs, long cap, long* n_pairs) {
   }
   cudaSetDevice(h.device);
   sc::Dev& d = h.d;
-  if (h.prec == sc::PREC_MIXED) {
-    // the mixed form keeps no list; build one from a fresh cell sort
-    if (!d.nbr && !h.dalloc(&d.nbr, (size_t)d.ntot * d.maxn, "nbr")) return h.last_status;
-    if (!h.rebuild_all()) return h.last_status;
-    sc::launch_force_rebuild_all(d, h.stream);
-    sc::launch_build_nbrs(d, h.d_tab, 0, h.stream);
-    sc::launch_clear_flags(d, h.stream);
-  }
   if (!h.check_status("sc_get_pairs")) return h.last_status;
   const sc::HostSys& S = h.hs[sys];
   std::vector<int> nn(S.n), ids(S.n), lst((size_t)S.n * d.maxn);
@@ -483,7 +487,7 @@ int sc_get_pairs(sc_handle* H, int sys, int* pairs, long cap, long* n_pairs) {
   for (int k = 0; k < S.n; k++) {
     int c = std::min(nn[k], d.maxn);
     for (int m = 0; m < c; m++) {
-      int j = lst[(size_t)m * S.n + k] - S.p0;
+      int j = (int)((unsigned)lst[(size_t)m * S.n + k] & sc::kSlotMask) - S.p0;
       if (j < 0 || j >= S.n) continue;
       int a = ids[k], b = ids[j];
       if (a < b) pr.emplace_back(a, b);

@@ -18,7 +18,6 @@
 // reference's IEEE operations.
 #include "sc_internal.hpp"
 #include "sc_pair.cuh"
-#include "sc_rec.cuh"
 
 namespace sc {
 
@@ -55,7 +54,16 @@ __global__ void k_rb_zero(Dev d) {
 }
 
 // find_cells, spherocyl_box.cpp:270-301: wrap, then hash.
-__global__ void k_rb_hash(Dev d, const StepScalars* __restrict__ tab, int row) {
+//
+// A displacement-triggered rebuild happens in the reference inside the corrector
+// loop, at the first particle i* whose accumulated displacement exceeds pad/2:
+// particles up to i* are wrapped after their update, the others before it, and
+// the displacement counters of the latter restart from this step's move.  The
+// reference wraps with the box length of the loop (before a resize shrinks it).
+// Reproducing that matters under resize, where the reference's predictor pass
+// uses the pre-resize box for the minimum image and so depends on which image a
+// particle sits at.  Forced rebuilds and set-back steps wrap every particle.
+__global__ void k_rb_hash(Dev d, const StepScalars* __restrict__ tab, int row, int mixed) {
   if (*d.any == 0) return;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.ntot) return;
@@ -63,17 +71,37 @@ __global__ void k_rb_hash(Dev d, const StepScalars* __restrict__ tab, int row) {
   if (d.flags[s] == 0) return;
   const SysGeom& g = d.geom[s];
   const StepScalars& ts = tab[row * d.nsys + s];
-  double Lx = ts.Lx_p, Ly = ts.Ly_p;
+  const double Lx = ts.Lx_c, Ly = ts.Ly_c;
   double2 p = d.xy[i];
   double phi = d.ph[i];
-  p.x = wrap_bounded(p.x, 0.0, Lx, Lx, d.status);
-  p.y = wrap_bounded(p.y, 0.0, Ly, Ly, d.status);
-  phi = wrap_bounded(phi, -kRefPi, kRefPi, 2 * kRefPi, d.status);
+  double2 mv = make_double2(0.0, 0.0);
+  const int istar = d.istar[s];
+  if (!mixed && istar != kNoTrigger && !ts.setback && d.id[i] > istar) {
+    double2 p0 = d.s_xy[i];
+    p0.x = wrap_bounded(p0.x, 0.0, Lx, Lx, d.status);
+    p0.y = wrap_bounded(p0.y, 0.0, Ly, Ly, d.status);
+    double ph0 = wrap_bounded(d.s_ph[i], -kRefPi, kRefPi, 2 * kRefPi, d.status);
+    p = make_double2(p0.x + d.v0x[i], p0.y + d.v0y[i]);
+    phi = ph0 + d.v0p[i];
+    if (ts.mode == 1) {
+      p.x *= ts.scale;
+      p.y *= ts.scale;
+    } else if (ts.mode == 2) {
+      p.x /= ts.scale;
+      p.y /= ts.scale;
+    }
+    mv = make_double2(p.x - p0.x, p.y - p0.y);
+  } else {
+    p.x = wrap_bounded(p.x, 0.0, Lx, Lx, d.status);
+    p.y = wrap_bounded(p.y, 0.0, Ly, Ly, d.status);
+    phi = wrap_bounded(phi, -kRefPi, kRefPi, 2 * kRefPi, d.status);
+  }
   d.xy[i] = p;
   d.ph[i] = phi;
+  d.nxy_t[i] = mv;  // displacement counter to carry into the new slot
   int col = (int)(p.x / ts.W_p);
   int rw = (int)(p.y / ts.H_p);
-  // a coordinate equal to the box length survives the wrap; keep it on the grid
+  // a coordinate at (or, after a resize, just past) the box edge stays on the grid
   if (col >= g.cols) col = g.cols - 1;
   if (rw >= g.rows) rw = g.rows - 1;
   if (col < 0) col = 0;
@@ -213,6 +241,9 @@ __global__ void k_rb_gather(Dev d) {
   d.s_irc[i] = d.irc[src];
   d.s_id[i] = d.id[src];
   d.s_cell[i] = d.cell_tmp[src];
+  double2 mv = d.nxy_t[src];
+  d.v0x[i] = mv.x;
+  d.v0y[i] = mv.y;
 }
 
 __global__ void k_rb_commit(Dev d, const StepScalars* __restrict__ tab, int row, int mixed) {
@@ -224,21 +255,14 @@ __global__ void k_rb_commit(Dev d, const StepScalars* __restrict__ tab, int row,
   double2 p = d.s_xy[i];
   double phi = d.s_ph[i];
   double2 ra = d.s_ra[i];
-  int c = d.s_cell[i];
   d.xy[i] = p;
   d.ph[i] = phi;
   d.ra[i] = ra;
   d.irc[i] = d.s_irc[i];
   d.id[i] = d.s_id[i];
-  d.cell[i] = c;
-  d.moved[i] = make_double2(0.0, 0.0);
-  if (mixed) {
-    const SysGeom& g = d.geom[s];
-    const StepScalars& ts = tab[row * d.nsys + s];
-    int lc = c - g.c0;
-    d.rec[i] = make_rec(p, phi, ra.y, lc % g.cols, lc / g.cols, ts.W_p, ts.H_p);
-    d.raf[i] = make_float2((float)ra.x, (float)ra.y);
-  } else {
+  d.cell[i] = d.s_cell[i];
+  d.moved[i] = make_double2(d.v0x[i], d.v0y[i]);
+  if (!mixed) {
     double sn, cs;
     sincos(phi, &sn, &cs);
     d.nxy[i] = make_double2(ra.y * cs, ra.y * sn);
@@ -247,7 +271,10 @@ __global__ void k_rb_commit(Dev d, const StepScalars* __restrict__ tab, int row,
 
 __global__ void k_rb_clear(Dev d) {
   if (*d.any == 0) return;
-  for (int s = threadIdx.x; s < d.nsys; s += blockDim.x) d.flags[s] = 0;
+  for (int s = threadIdx.x; s < d.nsys; s += blockDim.x) {
+    d.flags[s] = 0;
+    d.istar[s] = kNoTrigger;
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
     *d.any = 0;
@@ -286,30 +313,20 @@ __global__ void k_setback(Dev d, const StepScalars* __restrict__ tab, int row) {
   }
 }
 
-// Recompute the derived per-particle geometry (shaft vectors, FP32 records) from
-// the FP64 state, e.g. after the host replaced positions.
-__global__ void k_refresh(Dev d, const StepScalars* __restrict__ tab, int row, int mixed) {
+// Recompute the shaft vectors of the FP64 form from the state, e.g. after the
+// host replaced positions.
+__global__ void k_refresh(Dev d) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.ntot) return;
-  int s = d.psys[i];
-  double2 p = d.xy[i];
   double phi = d.ph[i];
   double2 ra = d.ra[i];
-  if (mixed) {
-    const SysGeom& g = d.geom[s];
-    const StepScalars& ts = tab[row * d.nsys + s];
-    int lc = d.cell[i] - g.c0;
-    d.rec[i] = make_rec(p, phi, ra.y, lc % g.cols, lc / g.cols, ts.W_p, ts.H_p);
-    d.raf[i] = make_float2((float)ra.x, (float)ra.y);
-  } else {
-    double sn, cs;
-    sincos(phi, &sn, &cs);
-    d.nxy[i] = make_double2(ra.y * cs, ra.y * sn);
-  }
+  double sn, cs;
+  sincos(phi, &sn, &cs);
+  d.nxy[i] = make_double2(ra.y * cs, ra.y * sn);
 }
 
 // gradient_relax_step, src/cpp/relaxation_dynamics.cpp:11-31
-__global__ void k_gd_update(Dev d, const StepScalars* __restrict__ tab, int row, int mixed) {
+__global__ void k_gd_update(Dev d, const StepScalars* __restrict__ tab, int row) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.ntot) return;
   int s = d.psys[i];
@@ -318,30 +335,31 @@ __global__ void k_gd_update(Dev d, const StepScalars* __restrict__ tab, int row,
   if (step == 0.0) return;
   double ddx = step * d.fx[i];
   double ddy = step * d.fy[i];
-  double2 p = d.xy[i];
-  p.x += ddx;
-  p.y += ddy;
-  double phi = d.ph[i] + step * d.tau[i] / d.irc[i].x;
+  double ddp = step * d.tau[i] / d.irc[i].x;
+  const double2 p0 = d.xy[i];
+  const double phi0 = d.ph[i];
+  double2 p = make_double2(p0.x + ddx, p0.y + ddy);
+  double phi = phi0 + ddp;
   d.xy[i] = p;
   d.ph[i] = phi;
+  d.s_xy[i] = p0;
+  d.s_ph[i] = phi0;
+  d.v0x[i] = ddx;
+  d.v0y[i] = ddy;
+  d.v0p[i] = ddp;
   double2 m = d.moved[i];
   m.x += ddx;
   m.y += ddy;
   d.moved[i] = m;
   double2 ra = d.ra[i];
-  if (mixed) {
-    const StepScalars& ts = tab[row * d.nsys + s];
-    int lc = d.cell[i] - g.c0;
-    d.rec[i] = make_rec(p, phi, ra.y, lc % g.cols, lc / g.cols, ts.W_p, ts.H_p);
-  } else {
-    double sn, cs;
-    sincos(phi, &sn, &cs);
-    d.nxy[i] = make_double2(ra.y * cs, ra.y * sn);
-  }
+  double sn, cs;
+  sincos(phi, &sn, &cs);
+  d.nxy[i] = make_double2(ra.y * cs, ra.y * sn);
   if (!(isfinite(p.x) && isfinite(p.y) && isfinite(phi))) atomicOr(d.status, ST_NAN);
   // the reference tests and rebuilds inside the update loop
   if (m.x > 0.5 * g.pad || m.x < -0.5 * g.pad || m.y > 0.5 * g.pad || m.y < -0.5 * g.pad) {
     if (d.flags[s] == 0) atomicOr(&d.flags[s], 1);
+    atomicMin(&d.istar[s], d.id[i]);
     if (*d.any == 0) atomicExch(d.any, 1);
   }
 }
@@ -393,7 +411,7 @@ inline int nblk(int n, int b) { return (n + b - 1) / b; }
 void launch_rebuild(const Dev& d, bool mixed, const StepScalars* tab, int row, cudaStream_t st) {
   const int B = 256;
   k_rb_zero<<<nblk(d.ncells, B), B, 0, st>>>(d);
-  k_rb_hash<<<nblk(d.ntot, B), B, 0, st>>>(d, tab, row);
+  k_rb_hash<<<nblk(d.ntot, B), B, 0, st>>>(d, tab, row, mixed ? 1 : 0);
   k_rb_chunksum<<<d.nchunks, 256, 0, st>>>(d);
   k_rb_sysscan<<<nblk(d.nsys, 128), 128, 0, st>>>(d);
   k_rb_cellscan<<<d.nchunks, 1024, 0, st>>>(d);
@@ -401,7 +419,12 @@ void launch_rebuild(const Dev& d, bool mixed, const StepScalars* tab, int row, c
   k_rb_cellsort<<<nblk(d.ncells, 128), 128, 0, st>>>(d);
   k_rb_gather<<<nblk(d.ntot, B), B, 0, st>>>(d);
   k_rb_commit<<<nblk(d.ntot, B), B, 0, st>>>(d, tab, row, mixed ? 1 : 0);
-  if (!mixed) launch_build_nbrs(d, tab, row, st);
+  if (mixed) {
+    launch_mx_local(d, tab, row, false, st);
+    launch_mx_build_list(d, tab, row, false, st);
+  } else {
+    launch_build_nbrs(d, tab, row, st);
+  }
   k_rb_clear<<<1, 256, 0, st>>>(d);
 }
 
@@ -415,11 +438,15 @@ void launch_setback(const Dev& d, const StepScalars* tab, int row, cudaStream_t 
 
 void launch_refresh_geometry(const Dev& d, bool mixed, const StepScalars* tab, int row,
                              cudaStream_t st) {
-  k_refresh<<<nblk(d.ntot, 256), 256, 0, st>>>(d, tab, row, mixed ? 1 : 0);
+  if (mixed)
+    launch_mx_local(d, tab, row, true, st);
+  else
+    k_refresh<<<nblk(d.ntot, 256), 256, 0, st>>>(d);
 }
 
 void launch_gd_update(const Dev& d, bool mixed, const StepScalars* tab, int row, cudaStream_t st) {
-  k_gd_update<<<nblk(d.ntot, 256), 256, 0, st>>>(d, tab, row, mixed ? 1 : 0);
+  (void)mixed;  // the CPU-compatible gradient descent is a plain FP64 protocol
+  k_gd_update<<<nblk(d.ntot, 256), 256, 0, st>>>(d, tab, row);
 }
 
 void launch_se_store(const Dev& d, double* dst, cudaStream_t st) {

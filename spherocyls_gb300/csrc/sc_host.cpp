@@ -81,6 +81,19 @@ bool HostSys::grid_changes(double Lx_now, double Ly_now) const {
   return r != rows || c != cols;
 }
 
+// FP32 copies of a row, for the mixed form
+static void fill_f32(StepScalars& t) {
+  t.f_gamma_c = (float)t.gamma_c;
+  t.f_gamma_p = (float)t.gamma_p;
+  t.f_Wc = (float)t.W_c;
+  t.f_Hc = (float)t.H_c;
+  t.f_Wp = (float)t.W_p;
+  t.f_Hp = (float)t.H_p;
+  t.f_rate = (float)t.rate;
+  t.f_step = (float)t.step;
+  t.f_factor = t.mode == 1 ? (float)t.scale : (t.mode == 2 ? (float)(1.0 / t.scale) : 1.0f);
+}
+
 StepScalars Handle::row_current(int s) const {
   const HostSys& h = hs[s];
   StepScalars t;
@@ -202,6 +215,7 @@ bool Handle::upload_table(const std::vector<StepScalars>& rows) {
   if (!ensure_table(nrows)) return false;
   // the host table is a member, so it outlives the asynchronous copy
   h_tab = rows;
+  for (auto& t : h_tab) fill_f32(t);
   return cuda_ok(cudaMemcpyAsync(d_tab, h_tab.data(), h_tab.size() * sizeof(StepScalars),
                                  cudaMemcpyHostToDevice, stream),
                  "upload step table");
@@ -230,8 +244,21 @@ bool Handle::check_status(const char* where) {
   return true;
 }
 
+// mixed form: bring the FP64 copy of the state up to date
+bool Handle::materialize() {
+  if (prec != PREC_MIXED || fp64_valid) return true;
+  std::vector<StepScalars> rows(nsys);
+  for (int s = 0; s < nsys; s++) rows[s] = row_current(s);
+  if (!upload_table(rows)) return false;
+  launch_mx_materialize(d, d_tab, 0, true, stream);
+  kernels += 1;
+  fp64_valid = true;
+  return cuda_ok(cudaGetLastError(), "materialize");
+}
+
 // full rebuild of every system at the current state (constructor / setters)
 bool Handle::rebuild_all() {
+  if (!materialize()) return false;
   std::vector<StepScalars> rows(nsys);
   for (int s = 0; s < nsys; s++) rows[s] = row_current(s);
   if (!upload_table(rows)) return false;
@@ -287,12 +314,17 @@ void Handle::collect_times() {
 // One Heun step (rows k of the uploaded table), strain or resize form.
 void Handle::enqueue_step(bool resize, int k, bool se, bool prof) {
   timed(0, prof, [&] { launch_pass(resize ? PASS_CORR_RESIZE : PASS_CORR_STRAIN, false, k); });
+  if (prec == PREC_MIXED) {
+    // FP64 positions of the systems about to be sorted or set back
+    launch_mx_materialize(d, d_tab, k, false, stream);
+    kernels += 1;
+  }
   if (!resize) {
     launch_setback(d, d_tab, k, stream);
     kernels += 1;
   }
   timed(2, prof, [&] { launch_rebuild(d, prec == PREC_MIXED, d_tab, k, stream); });
-  kernels += prec == PREC_MIXED ? 10 : 11;
+  kernels += prec == PREC_MIXED ? 12 : 11;
   timed(1, prof, [&] { launch_pass(resize ? PASS_PRED_RESIZE : PASS_PRED_STRAIN, se, k); });
 }
 
@@ -488,6 +520,8 @@ int Handle::run_steps(bool resize, int shrink, int nsteps, int se_every, double*
     }
     collect_times();
     if (!check_status(resize ? "resize steps" : "strain steps")) return last_status;
+    fp64_valid = prec != PREC_MIXED;
+    forces_valid = false;
     hs = sim;
     rec_done += nrec;
     done += nk;
@@ -508,6 +542,7 @@ int Handle::calc(bool se, double* se_out) {
   for (int s = 0; s < nsys; s++) rows[s] = row_current(s);
   if (!upload_table(rows)) return last_status;
   launch_pass(PASS_FORCE, se, 0);
+  forces_valid = true;
   if (se) {
     launch_se_reduce(d, stream);
     if (!cuda_ok(cudaMemcpyAsync(h_pinned + 8, d.se_sys, 5 * nsys * sizeof(double),

@@ -61,6 +61,8 @@ struct Handle {
   int* h_pinned = nullptr;  // status word + scratch for small reads
   bool pred_valid = false;  // predictor copy consistent with the state
   int pred_kind = 0;        // 1 strain, 2 shrink, 3 grow
+  bool fp64_valid = true;   // mixed form: FP64 copy of the state is current
+  bool forces_valid = false;// mixed form: fx/fy/tau hold the forces of the state
   long long steps = 0, rebuilds = 0;
   int dev_status = 0;
   long long dev_rebuilds = 0;  // rebuild chains the device executed
@@ -119,6 +121,7 @@ struct Handle {
 
   int run_steps(bool resize, int shrink, int nsteps, int se_every, double* se_out);
   int calc(bool se, double* se_out);
+  bool materialize();
   int gd_minimize(int max_steps, double e_min, int* steps_taken, double* e_final);
 };
 

@@ -46,6 +46,10 @@ struct StepScalars {
   double scale;      // resize factor pow(1-rate, dt)
   int mode;          // 0 none, 1 multiply by scale (shrink), 2 divide by scale (grow)
   int setback;       // set back gamma at the end of this step
+  // FP32 copies for the mixed form (no FP64 arithmetic in its passes)
+  float f_gamma_c, f_gamma_p, f_Wc, f_Hc, f_Wp, f_Hp, f_rate, f_step;
+  float f_factor;    // scale (mode 1), 1/scale (mode 2), 1 (mode 0)
+  float f_pad_;
 };
 
 // Device pointers handed to every kernel by value.
@@ -76,10 +80,14 @@ struct Dev {
   double* fy;
   double* tau;
   double2* moved;
-  // mixed form: FP32 geometry records (x_local, y_local, nx, ny) and (R, A)
-  float4* rec;
-  float4* rec_t;
-  float2* raf;
+  // mixed form (FP32 state relative to the cell centre, compensated):
+  float4* rec;    // (x_local, y_local, A cos phi, A sin phi) of the state
+  float4* rec_t;  // the same for the predictor copy
+  float4* mc;     // (x compensation, y compensation, phi, phi compensation)
+  float4* mv;     // (v0x, v0y, v0phi, predicted phi)
+  float2* mm;     // displacement since the last rebuild
+  float4* pa;     // (R, A, 1/I, RC)
+  int* cellp;     // local cell packed as col | row << 16
   // cell lists
   int* cell_start;          // [ncells] first slot
   int* cell_count;          // [ncells]
@@ -110,6 +118,7 @@ struct Dev {
   const int* pchunk_np;
   // flags
   int* flags;               // [nsys] bit0 moved-rebuild, bit1 forced rebuild
+  int* istar;               // [nsys] lowest particle index that triggered a rebuild
   int* any;                 // [1] set when any system needs a rebuild
   int* status;              // [2] sticky error bits (ST_*), rebuild-chain count
 };
@@ -119,7 +128,11 @@ enum { ST_NBR_OVERFLOW = 1, ST_NAN = 2, ST_CELL_OVERFLOW = 4 };
 
 constexpr int kScanChunk = 1024;  // cells per scan chunk
 constexpr int kSeChunk = 1024;    // particles per reduction chunk
-constexpr int kMaxCellSort = 48;  // cells above this occupancy use the in-place slow sort
+constexpr int kMaxCellSort = 48;
+constexpr int kNoTrigger = 0x7f7f7f7f;  // istar value when no particle triggered
+// mixed-form list entries: slot in the low 28 bits, cell offset (dc+1, dr+1) above
+constexpr int kSlotBits = 28;
+constexpr unsigned kSlotMask = (1u << kSlotBits) - 1u;  // cells above this occupancy use the in-place slow sort
 
 // pass modes for the force kernels
 enum PassMode {
@@ -146,5 +159,11 @@ void launch_se_store(const Dev& d, double* dst, cudaStream_t st);
 void launch_refresh_geometry(const Dev& d, bool mixed, const StepScalars* tab, int row,
                              cudaStream_t st);
 void launch_build_nbrs(const Dev& d, const StepScalars* tab, int row, cudaStream_t st);
+// mixed form
+void launch_mx_materialize(const Dev& d, const StepScalars* tab, int row, bool all,
+                           cudaStream_t st);
+void launch_mx_local(const Dev& d, const StepScalars* tab, int row, bool all, cudaStream_t st);
+void launch_mx_build_list(const Dev& d, const StepScalars* tab, int row, bool all,
+                          cudaStream_t st);
 
 }  // namespace sc

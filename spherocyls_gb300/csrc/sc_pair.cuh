@@ -104,8 +104,16 @@ __device__ __forceinline__ bool pair_fp32(float dX, float dY, float nxA, float n
   float c = aQ * aQ;
   float d = nxA * dX + nyA * dY;
   float e = -(nxB * dX + nyB * dY);
-  float delta = a * c - b * b;
-  float t = fminf(fmaxf(__fdividef(b * d - a * e, delta), -1.f), 1.f);
+  // Unclamped spine parameter of Q.  The reference's (b d - a e)/(a c - b^2) is,
+  // by the Binet-Cauchy identity, cross(u_A, D)/cross(u_A, u_B); the cross-product
+  // form keeps FP32 accurate for nearly parallel spines, where a c - b^2 cancels.
+  // Exactly parallel spines give 0/0 in the reference, which its clamp turns into
+  // t = -1; the same value is used here.
+  float w = nyA * nxB;
+  float uxv = fmaf(nxA, nyB, -w) + fmaf(-nyA, nxB, w);  // cross(u_A, u_B), error-compensated
+  float w2 = nyA * dX;
+  float uxD = fmaf(nxA, dY, -w2) + fmaf(-nyA, dX, w2);  // cross(u_A, D)
+  float t = uxv == 0.f ? -1.f : fminf(fmaxf(__fdividef(uxD, uxv), -1.f), 1.f);
   float s = -__fdividef(b * t + d, a);
   float sarg = fabsf(s);
   s = fminf(fmaxf(s, -1.f), 1.f);

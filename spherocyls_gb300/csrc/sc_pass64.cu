@@ -78,9 +78,14 @@ __global__ void __launch_bounds__(128) k_build_nbrs(Dev d, const StepScalars* __
   if (cnt > d.maxn) atomicOr(d.status, ST_NBR_OVERFLOW);
 }
 
-__device__ __forceinline__ void flag_moved(const Dev& d, int s, double2 m, double pad) {
+// The reference rebuilds inside its corrector loop as soon as particle i has
+// moved more than pad/2 (strain_dynamics.cpp:220-225, resize_dynamics.cpp:222-227);
+// the lowest such index per system is kept so the rebuild can reproduce which
+// particles the reference wrapped before, and which after, their update.
+__device__ __forceinline__ void flag_moved(const Dev& d, int s, int id, double2 m, double pad) {
   if (m.x > 0.5 * pad || m.x < -0.5 * pad || m.y > 0.5 * pad || m.y < -0.5 * pad) {
     if (d.flags[s] == 0) atomicOr(&d.flags[s], 1);
+    atomicMin(&d.istar[s], id);
     if (*d.any == 0) atomicExch(d.any, 1);
   }
 }
@@ -188,11 +193,19 @@ __global__ void __launch_bounds__(128) k_pass64(Dev d, const StepScalars* __rest
     double ddy = 0.5 * dt * (d.v0y[i] + v1y);
     double ddp = 0.5 * dt * (d.v0p[i] + v1p);
     double2 p = d.xy[i];
+    const double2 p0 = p;
+    const double phi0 = d.ph[i];
     p.x += ddx;
     p.y += ddy;
-    double phi = d.ph[i] + ddp;
+    double phi = phi0 + ddp;
     d.xy[i] = p;
     d.ph[i] = phi;
+    // pre-step state and increments, for a rebuild that follows this step
+    d.s_xy[i] = p0;
+    d.s_ph[i] = phi0;
+    d.v0x[i] = ddx;
+    d.v0y[i] = ddy;
+    d.v0p[i] = ddp;
     double2 m = d.moved[i];
     m.x += ddx;
     m.y += ddy;
@@ -201,7 +214,7 @@ __global__ void __launch_bounds__(128) k_pass64(Dev d, const StepScalars* __rest
     sincos(phi, &sn, &cs);
     d.nxy[i] = make_double2(rai.y * cs, rai.y * sn);
     if (!(isfinite(p.x) && isfinite(p.y) && isfinite(phi))) atomicOr(d.status, ST_NAN);
-    flag_moved(d, s, m, g.pad);
+    flag_moved(d, s, idi, m, g.pad);
   } else if (MODE == PASS_PRED_RESIZE) {
     // resize_step predictor, resize_dynamics.cpp:172-191
     d.fx[i] = fx;
@@ -231,8 +244,9 @@ __global__ void __launch_bounds__(128) k_pass64(Dev d, const StepScalars* __rest
     double ddy = 0.5 * dt * (d.v0y[i] + fy);
     double ddp = 0.5 * dt * (d.v0p[i] + tq) / irc.x;
     double2 p0 = d.xy[i];
+    const double phi0 = d.ph[i];
     double2 p = make_double2(p0.x + ddx, p0.y + ddy);
-    double phi = d.ph[i] + ddp;
+    double phi = phi0 + ddp;
     if (ts.mode == 1) {
       p.x *= ts.scale;
       p.y *= ts.scale;
@@ -242,6 +256,11 @@ __global__ void __launch_bounds__(128) k_pass64(Dev d, const StepScalars* __rest
     }
     d.xy[i] = p;
     d.ph[i] = phi;
+    d.s_xy[i] = p0;
+    d.s_ph[i] = phi0;
+    d.v0x[i] = ddx;
+    d.v0y[i] = ddy;
+    d.v0p[i] = ddp;
     double2 m = d.moved[i];
     m.x += p.x - p0.x;
     m.y += p.y - p0.y;
@@ -250,7 +269,7 @@ __global__ void __launch_bounds__(128) k_pass64(Dev d, const StepScalars* __rest
     sincos(phi, &sn, &cs);
     d.nxy[i] = make_double2(rai.y * cs, rai.y * sn);
     if (!(isfinite(p.x) && isfinite(p.y) && isfinite(phi))) atomicOr(d.status, ST_NAN);
-    flag_moved(d, s, m, g.pad);
+    flag_moved(d, s, idi, m, g.pad);
   }
 }
 

@@ -1,118 +1,148 @@
-// sc_pass_mixed.cu -- the mixed-precision form: cell-tile force passes.
+// sc_pass_mixed.cu -- the mixed-precision form.
 //
-// Pair geometry and forces in FP32, positions/orientations and the Heun update in
-// FP64, stress and energy accumulated in FP64.  No neighbour list is stored: each
-// thread takes one particle slot (slots are sorted by cell) and scans the 3x3 block
-// of cells around its own cell, whose particles are contiguous slot ranges.  The
-// rebuild rule is the reference's (a rebuild when a particle's accumulated
-// displacement exceeds pad/2 in x or y, tmarschall/spherocyls
-// src/cpp/strain_dynamics.cpp:220-225), and the cell size is the reference's
-// (src/cpp/spherocyl_box.cpp:228-232), which bounds every possible contact to the
-// 3x3 block, so the set of interacting pairs is exactly the reference's.
+// State: each particle's centre is kept relative to the centre of the cell it was
+// last sorted into, as an FP32 value plus an FP32 compensation term (Kahan), and
+// its angle likewise; the absolute FP64 position is (col+1/2)W + x_local + x_comp,
+// materialised only for the cell sort, the Lees-Edwards set-back and for output.
+// Pair geometry and forces are FP32; stress and energy accumulate in FP64.  No
+// FP64 instruction runs in the force passes except the stress/energy sums on the
+// steps that record them.
 //
-// A pair is computed with the lower particle index as the reference's "p" from
-// both sides, so both threads produce the same FP32 contribution and Newton's
-// third law holds exactly pair by pair.
+// Neighbour list: the reference's padded list (tmarschall/spherocyls
+// src/cpp/spherocyl_box.cpp:303-355, criterion |dy| < S+pad and
+// (|dx + gamma dy| < S+pad or |dx + dy/2| < S+pad)), evaluated in FP32 with the
+// bound inflated by 1e-5 relative so that it contains every pair the FP64
+// criterion accepts.  Each entry packs the neighbour's slot with the cell offset
+// (dc, dr) between the two cells, so the displacement is
+// rec_i - rec_j - (dc W, dr H) with no box length in the FP32 arithmetic.
+//
+// Force pass: one thread per slot, two phases -- a cheap bounding test over the
+// list (centres closer than R_i+A_i+R_j+A_j), collecting the survivors, then the
+// segment-segment contact for the survivors only, which keeps the expensive code
+// path free of the divergence of the bounding test.
 #include "sc_internal.hpp"
 #include "sc_pair.cuh"
-#include "sc_rec.cuh"
 
 namespace sc {
 
 namespace {
 
-__device__ __forceinline__ void flag_moved(const Dev& d, int s, double2 m, double pad) {
-  if (m.x > 0.5 * pad || m.x < -0.5 * pad || m.y > 0.5 * pad || m.y < -0.5 * pad) {
+constexpr int kHits = 24;  // survivors buffered per phase
+
+__device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
+  float y = v + c;
+  float t = s + y;
+  c = y - (t - s);
+  s = t;
+}
+
+// (s + c) <- (s + c + v) * f, keeping the rounding error of the product in c
+__device__ __forceinline__ void kahan_add_scale(float& s, float& c, float v, float f) {
+  float y = v + c;
+  float t = s + y;
+  float e = y - (t - s);
+  float p = t * f;
+  float pe = fmaf(t, f, -p) + e * f;
+  s = p;
+  c = pe;
+}
+
+__device__ __forceinline__ void flag_moved32(const Dev& d, int s, float2 m, float pad) {
+  float h = 0.5f * pad;
+  if (m.x > h || m.x < -h || m.y > h || m.y < -h) {
     if (d.flags[s] == 0) atomicOr(&d.flags[s], 1);
     if (*d.any == 0) atomicExch(d.any, 1);
   }
 }
 
 template <int MODE, bool SE>
-__global__ void __launch_bounds__(256) k_pass_mixed(Dev d, const StepScalars* __restrict__ tab,
+__global__ void __launch_bounds__(128) k_pass_mixed(Dev d, const StepScalars* __restrict__ tab,
                                                    int row) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.ntot) return;
   constexpr bool kPred = (MODE == PASS_CORR_STRAIN || MODE == PASS_CORR_RESIZE);
   const int s = d.psys[i];
   const SysGeom& g = d.geom[s];
   const StepScalars& ts = tab[row * d.nsys + s];
   const float4* __restrict__ REC = kPred ? d.rec_t : d.rec;
-  const double Wd = kPred ? ts.W_c : ts.W_p;
-  const double Hd = kPred ? ts.H_c : ts.H_p;
-  const float W = (float)Wd, H = (float)Hd;
-  const float gam = (float)(kPred ? ts.gamma_c : ts.gamma_p);
+  const float W = kPred ? ts.f_Wc : ts.f_Wp;
+  const float H = kPred ? ts.f_Hc : ts.f_Hp;
+  const float gam = kPred ? ts.f_gamma_c : ts.f_gamma_p;
+  const bool smallx = g.cols < 3, smally = g.rows < 3;
+  const float Lxf = W * g.cols, Lyf = H * g.rows;
   const bool virial = d.stress_mode == STRESS_VIRIAL;
 
   const float4 ri = REC[i];
-  const float2 rai = d.raf[i];
+  const float4 pai = d.pa[i];  // (R, A, 1/I, RC)
   const int idi = d.id[i];
-  const int lc = d.cell[i] - g.c0;
-  const int col = lc % g.cols, rw = lc / g.cols;
-  const int ncx = g.cols < 3 ? g.cols : 3, ncy = g.rows < 3 ? g.rows : 3;
-  const bool smallx = ncx < 3, smally = ncy < 3;
-  const float Lxf = W * g.cols, Lyf = H * g.rows;
+  int cnt = d.nbr_n[i];
+  if (cnt > d.maxn) cnt = d.maxn;
+  const unsigned* __restrict__ L = reinterpret_cast<const unsigned*>(d.nbr) + i;
+  const size_t stride = d.ntot;
 
   float fx = 0.f, fy = 0.f, tq = 0.f;
   double e_acc = 0.0, pxx = 0.0, pyy = 0.0, pxy = 0.0, pyx = 0.0;
-
-  for (int a = 0; a < ncy; a++) {
-    int dr = smally ? a - rw : a - 1;  // small grids: absolute row a
-    int r2 = smally ? a : wrap_index(rw + dr, g.rows);
-    float oy = -(float)dr * H;
-    for (int b = 0; b < ncx; b++) {
-      int dc = smallx ? b - col : b - 1;
-      int c2 = smallx ? b : wrap_index(col + dc, g.cols);
-      float ox = -(float)dc * W;
-      int cc = g.c0 + r2 * g.cols + c2;
-      int st = d.cell_start[cc];
-      int en = st + d.cell_count[cc];
-      for (int j = st; j < en; j++) {
-        if (j == i) continue;
-        float4 rj = REC[j];
-        float dx = (ri.x - rj.x) + ox;
-        float dy = (ri.y - rj.y) + oy;
-        if (smallx) dx += Lxf * (float)((dx < -0.5f * Lxf) - (dx > 0.5f * Lxf));
-        if (smally) dy += Lyf * (float)((dy < -0.5f * Lyf) - (dy > 0.5f * Lyf));
-        // quick reject: centres farther apart than R+A+R+A (sheared frame bound)
-        float2 raj = d.raf[j];
-        float reach = rai.x + rai.y + raj.x + raj.y;
-        float dxl = fmaf(gam, dy, dx);
-        if (dxl * dxl + dy * dy >= reach * reach) continue;
-        int idj = d.id[j];
-        bool ip = idi < idj;
-        PairF32 o;
-        bool hit;
-        if (ip)
-          hit = pair_fp32<SE>(dx, dy, ri.z, ri.w, rai.y, rj.z, rj.w, raj.y, rai.x + raj.x, gam,
+  unsigned hit[kHits];
+  int k = 0;
+  while (k < cnt) {
+    // phase 1: bounding test over the list
+    int nh = 0;
+    for (; k < cnt && nh < kHits; k++) {
+      unsigned e = __ldg(L + (size_t)k * stride);
+      int j = (int)(e & kSlotMask);
+      float4 rj = REC[j];
+      float2 raj = *reinterpret_cast<const float2*>(&d.pa[j]);
+      float dx = ri.x - rj.x + (float)(1 - (int)((e >> 28) & 3u)) * W;
+      float dy = ri.y - rj.y + (float)(1 - (int)(e >> 30)) * H;
+      if (smallx) dx += Lxf * (float)((dx < -0.5f * Lxf) - (dx > 0.5f * Lxf));
+      if (smally) dy += Lyf * (float)((dy < -0.5f * Lyf) - (dy > 0.5f * Lyf));
+      float reach = pai.x + pai.y + raj.x + raj.y;
+      float dxl = fmaf(gam, dy, dx);
+      if (dxl * dxl + dy * dy < reach * reach) hit[nh++] = e;
+    }
+    // phase 2: contacts of the survivors
+    for (int h = 0; h < nh; h++) {
+      unsigned e = hit[h];
+      int j = (int)(e & kSlotMask);
+      float4 rj = REC[j];
+      float2 raj = *reinterpret_cast<const float2*>(&d.pa[j]);
+      int idj = d.id[j];
+      float dx = ri.x - rj.x + (float)(1 - (int)((e >> 28) & 3u)) * W;
+      float dy = ri.y - rj.y + (float)(1 - (int)(e >> 30)) * H;
+      if (smallx) dx += Lxf * (float)((dx < -0.5f * Lxf) - (dx > 0.5f * Lxf));
+      if (smally) dy += Lyf * (float)((dy < -0.5f * Lyf) - (dy > 0.5f * Lyf));
+      const bool ip = idi < idj;
+      PairF32 o;
+      bool touch;
+      if (ip)
+        touch = pair_fp32<SE>(dx, dy, ri.z, ri.w, pai.y, rj.z, rj.w, raj.y, pai.x + raj.x, gam,
                               virial, o);
-        else
-          hit = pair_fp32<false>(-dx, -dy, rj.z, rj.w, raj.y, ri.z, ri.w, rai.y, raj.x + rai.x,
+      else
+        touch = pair_fp32<false>(-dx, -dy, rj.z, rj.w, raj.y, ri.z, ri.w, pai.y, raj.x + pai.x,
                                  gam, virial, o);
-        if (!hit) continue;
-        if (ip) {
-          fx += o.fx;
-          fy += o.fy;
-          tq += o.tp;
-          if (SE) {
-            e_acc += (double)(o.ov * o.ov);
-            if (!virial) {
-              pxx += (double)(o.fx * o.cxa) - (double)(o.fx * o.cxb) - (double)(o.fy * o.cxb);
-              pyy += (double)(o.fy * o.cya) - (double)(o.fy * o.cyb);
-              pxy += (double)(o.fy * o.cxa);
-              pyx += (double)(o.fx * o.cya) - (double)(o.fx * o.cyb);
-            } else {
-              pxx += (double)(o.fx * o.cxa) - (double)(o.fx * o.cxb);
-              pyy += (double)(o.fy * o.cya) - (double)(o.fy * o.cyb);
-              pxy += (double)(o.fy * o.cxa) - (double)(o.fy * o.cxb);
-              pyx += (double)(o.fx * o.cya) - (double)(o.fx * o.cyb);
-            }
+      if (!touch) continue;
+      if (ip) {
+        fx += o.fx;
+        fy += o.fy;
+        tq += o.tp;
+        if (SE) {
+          e_acc += (double)(o.ov * o.ov);
+          if (!virial) {
+            pxx += (double)(o.fx * o.cxa) - (double)(o.fx * o.cxb) - (double)(o.fy * o.cxb);
+            pyy += (double)(o.fy * o.cya) - (double)(o.fy * o.cyb);
+            pxy += (double)(o.fy * o.cxa);
+            pyx += (double)(o.fx * o.cya) - (double)(o.fx * o.cyb);
+          } else {
+            pxx += (double)(o.fx * o.cxa) - (double)(o.fx * o.cxb);
+            pyy += (double)(o.fy * o.cya) - (double)(o.fy * o.cyb);
+            pxy += (double)(o.fy * o.cxa) - (double)(o.fy * o.cxb);
+            pyx += (double)(o.fx * o.cya) - (double)(o.fx * o.cyb);
           }
-        } else {
-          fx -= o.fx;
-          fy -= o.fy;
-          tq += o.tq;
         }
+      } else {
+        fx -= o.fx;
+        fy -= o.fy;
+        tq += o.tq;
       }
     }
   }
@@ -126,89 +156,85 @@ __global__ void __launch_bounds__(256) k_pass_mixed(Dev d, const StepScalars* __
     d.se_part[(size_t)4 * d.ntot + i] = pyx * inv_area;
   }
 
-  const double2 irc = d.irc[i];
-  const double dt = ts.step;
-  const double Fx = fx, Fy = fy, T = tq;
-  const double A = rai.y;
+  const float dt = ts.f_step;
+  const float A = pai.y, invI = pai.z, RC = pai.w;
   if (MODE == PASS_FORCE) {
-    d.fx[i] = Fx;
-    d.fy[i] = Fy;
-    d.tau[i] = T;
+    d.fx[i] = fx;
+    d.fy[i] = fy;
+    d.tau[i] = tq;
   } else if (MODE == PASS_PRED_STRAIN || MODE == PASS_PRED_RESIZE) {
-    d.fx[i] = Fx;
-    d.fy[i] = Fy;
-    d.tau[i] = T;
-    double phi = d.ph[i];
-    double v0x, v0y, v0p;
+    const float4 c = d.mc[i];
+    float v0x, v0y, v0p;
     if (MODE == PASS_PRED_STRAIN) {
-      const double gamma = ts.gamma_p;
-      v0x = Fx - gamma * Fy;
-      v0y = Fy;
-      float iso = 0.5f * (1.f - (float)irc.y * cosf(2.f * (float)phi));
-      v0p = T / irc.x - ts.rate * (double)iso;
+      // strain_step predictor, strain_dynamics.cpp:187-199
+      float phi = c.z + c.w;
+      v0x = fx - gam * fy;
+      v0y = fy;
+      v0p = tq * invI - ts.f_rate * (0.5f * (1.f - RC * __cosf(2.f * phi)));
     } else {
-      v0x = Fx;
-      v0y = Fy;
-      v0p = T / irc.x;
+      // resize_step predictor, resize_dynamics.cpp:172-191
+      v0x = fx;
+      v0y = fy;
+      v0p = tq * invI;
     }
-    d.v0x[i] = v0x;
-    d.v0y[i] = v0y;
-    d.v0p[i] = v0p;
-    double2 p = d.xy[i];
-    double2 pt = make_double2(p.x + dt * v0x, p.y + dt * v0y);
-    double pht = phi + dt * v0p;
+    float xt = ri.x + (c.x + dt * v0x);
+    float yt = ri.y + (c.y + dt * v0y);
+    float pt = c.z + (c.w + dt * v0p);
     if (MODE == PASS_PRED_RESIZE) {
-      if (ts.mode == 1) {
-        pt.x *= ts.scale;
-        pt.y *= ts.scale;
-      } else if (ts.mode == 2) {
-        pt.x /= ts.scale;
-        pt.y /= ts.scale;
-      }
+      xt *= ts.f_factor;  // about the (equally scaled) cell centre
+      yt *= ts.f_factor;
     }
-    d.xy_t[i] = pt;
-    d.ph_t[i] = pht;
-    // the next consumer of the predictor record is the corrector pass of the next
-    // step, whose box is the one after this step
-    d.rec_t[i] = make_rec(pt, pht, A, col, rw, ts.W_p, ts.H_p);
+    float sn, cs;
+    sincosf(pt, &sn, &cs);
+    d.rec_t[i] = make_float4(xt, yt, A * cs, A * sn);
+    d.mv[i] = make_float4(v0x, v0y, v0p, pt);
   } else {
-    double pht = d.ph_t[i];
-    double ddx, ddy, ddp;
+    const float4 v0 = d.mv[i];
+    float4 c = d.mc[i];
+    float4 r = d.rec[i];
+    float ddx, ddy, ddp;
     if (MODE == PASS_CORR_STRAIN) {
-      const double gamma = ts.gamma_c;
-      double v1x = Fx - gamma * Fy;
-      double v1y = Fy;
-      float iso = 0.5f * (1.f - (float)irc.y * cosf(2.f * (float)pht));
-      double v1p = T / irc.x - ts.rate * (double)iso;
-      ddx = 0.5 * dt * (d.v0x[i] + v1x);
-      ddy = 0.5 * dt * (d.v0y[i] + v1y);
-      ddp = 0.5 * dt * (d.v0p[i] + v1p);
+      // strain_step corrector, strain_dynamics.cpp:203-219
+      float v1x = fx - gam * fy;
+      float v1y = fy;
+      float v1p = tq * invI - ts.f_rate * (0.5f * (1.f - RC * __cosf(2.f * v0.w)));
+      ddx = 0.5f * dt * (v0.x + v1x);
+      ddy = 0.5f * dt * (v0.y + v1y);
+      ddp = 0.5f * dt * (v0.z + v1p);
     } else {
-      ddx = 0.5 * dt * (d.v0x[i] + Fx);
-      ddy = 0.5 * dt * (d.v0y[i] + Fy);
-      ddp = 0.5 * dt * (d.v0p[i] + T / irc.x);
+      // resize_step corrector, resize_dynamics.cpp:194-218
+      ddx = 0.5f * dt * (v0.x + fx);
+      ddy = 0.5f * dt * (v0.y + fy);
+      ddp = 0.5f * dt * (v0.z + tq * invI);
     }
-    double2 p0 = d.xy[i];
-    double2 p = make_double2(p0.x + ddx, p0.y + ddy);
-    double phi = d.ph[i] + ddp;
+    float2 m = d.mm[i];
     if (MODE == PASS_CORR_RESIZE) {
-      if (ts.mode == 1) {
-        p.x *= ts.scale;
-        p.y *= ts.scale;
-      } else if (ts.mode == 2) {
-        p.x /= ts.scale;
-        p.y /= ts.scale;
-      }
+      const float f = ts.f_factor;
+      const int cp = d.cellp[i];
+      // the cell centre moves with the affine scale as well
+      float cx = ((float)(cp & 0xffff) + 0.5f) * ts.f_Wc;
+      float cy = ((float)(cp >> 16) + 0.5f) * ts.f_Hc;
+      float x0 = r.x, y0 = r.y;
+      kahan_add_scale(r.x, c.x, ddx, f);
+      kahan_add_scale(r.y, c.y, ddy, f);
+      m.x += (r.x - x0) + cx * (f - 1.f);
+      m.y += (r.y - y0) + cy * (f - 1.f);
+    } else {
+      kahan_add(r.x, c.x, ddx);
+      kahan_add(r.y, c.y, ddy);
+      m.x += ddx;
+      m.y += ddy;
     }
-    d.xy[i] = p;
-    d.ph[i] = phi;
-    double2 m = d.moved[i];
-    m.x += p.x - p0.x;
-    m.y += p.y - p0.y;
-    d.moved[i] = m;
-    d.rec[i] = make_rec(p, phi, A, col, rw, ts.W_p, ts.H_p);
-    if (!(isfinite(p.x) && isfinite(p.y) && isfinite(phi))) atomicOr(d.status, ST_NAN);
-    flag_moved(d, s, m, g.pad);
+    kahan_add(c.z, c.w, ddp);
+    float sn, cs;
+    sincosf(c.z + c.w, &sn, &cs);
+    r.z = A * cs;
+    r.w = A * sn;
+    d.rec[i] = r;
+    d.mc[i] = c;
+    d.mm[i] = m;
+    if (!(isfinite(r.x) && isfinite(r.y) && isfinite(c.z))) atomicOr(d.status, ST_NAN);
+    flag_moved32(d, s, m, (float)g.pad);
   }
 }
 
@@ -217,6 +243,103 @@ void launch_one(const Dev& d, const StepScalars* tab, int row, cudaStream_t st, 
   int grid = (d.ntot + block - 1) / block;
   k_pass_mixed<MODE, SE><<<grid, block, 0, st>>>(d, tab, row);
 }
+
+// ---- rebuild support ----
+
+// FP64 absolute state from the compensated local state (flagged systems, systems
+// that set back gamma at this step, or all).
+__global__ void k_mx_materialize(Dev d, const StepScalars* __restrict__ tab, int row, int all) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.ntot) return;
+  int s = d.psys[i];
+  const StepScalars& ts = tab[row * d.nsys + s];
+  if (!all && d.flags[s] == 0 && !ts.setback) return;
+  int cp = d.cellp[i];
+  float4 r = d.rec[i];
+  float4 c = d.mc[i];
+  double x = ((cp & 0xffff) + 0.5) * ts.W_p + ((double)r.x + (double)c.x);
+  double y = ((cp >> 16) + 0.5) * ts.H_p + ((double)r.y + (double)c.y);
+  d.xy[i] = make_double2(x, y);
+  d.ph[i] = (double)c.z + (double)c.w;
+}
+
+// Compensated local state from the FP64 state after a cell sort.
+__global__ void k_mx_local(Dev d, const StepScalars* __restrict__ tab, int row, int all) {
+  if (!all && *d.any == 0) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.ntot) return;
+  int s = d.psys[i];
+  if (!all && d.flags[s] == 0) return;
+  const SysGeom& g = d.geom[s];
+  const StepScalars& ts = tab[row * d.nsys + s];
+  int lc = d.cell[i] - g.c0;
+  int col = lc % g.cols, rw = lc / g.cols;
+  d.cellp[i] = col | (rw << 16);
+  double2 p = d.xy[i];
+  double lx = p.x - (col + 0.5) * ts.W_p;
+  double ly = p.y - (rw + 0.5) * ts.H_p;
+  double phi = d.ph[i];
+  float xl = (float)lx, yl = (float)ly, pf = (float)phi;
+  double2 ra = d.ra[i];
+  double2 irc = d.irc[i];
+  float A = (float)ra.y;
+  float sn, cs;
+  sincosf(pf, &sn, &cs);
+  d.rec[i] = make_float4(xl, yl, A * cs, A * sn);
+  d.mc[i] = make_float4((float)(lx - xl), (float)(ly - yl), pf, (float)(phi - pf));
+  d.mm[i] = make_float2(0.f, 0.f);
+  d.pa[i] = make_float4((float)ra.x, A, (float)(1.0 / irc.x), (float)irc.y);
+}
+
+// The padded neighbour list in FP32 (see the file comment).
+__global__ void __launch_bounds__(128) k_mx_build_list(Dev d, const StepScalars* __restrict__ tab,
+                                                      int row, int all) {
+  if (!all && *d.any == 0) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.ntot) return;
+  int s = d.psys[i];
+  if (!all && d.flags[s] == 0) return;
+  const SysGeom& g = d.geom[s];
+  const StepScalars& ts = tab[row * d.nsys + s];
+  const float W = ts.f_Wp, H = ts.f_Hp, gam = ts.f_gamma_p, pad = (float)g.pad;
+  const float Lxf = W * g.cols, Lyf = H * g.rows;
+  const int cp = d.cellp[i];
+  const int col = cp & 0xffff, rw = cp >> 16;
+  const float4 ri = d.rec[i];
+  const float4 pai = d.pa[i];
+  const int ncx = g.cols < 3 ? g.cols : 3, ncy = g.rows < 3 ? g.rows : 3;
+  const bool smallx = ncx < 3, smally = ncy < 3;
+  int cnt = 0;
+  for (int a = 0; a < ncy; a++) {
+    int dr = smally ? a - rw : a - 1;
+    int r2 = smally ? a : wrap_index(rw + dr, g.rows);
+    for (int b = 0; b < ncx; b++) {
+      int dc = smallx ? b - col : b - 1;
+      int c2 = smallx ? b : wrap_index(col + dc, g.cols);
+      int cc = g.c0 + r2 * g.cols + c2;
+      int st = d.cell_start[cc], en = st + d.cell_count[cc];
+      unsigned code = ((unsigned)(dc + 1) << 28) | ((unsigned)(dr + 1) << 30);
+      for (int j = st; j < en; j++) {
+        if (j == i) continue;
+        float4 rj = d.rec[j];
+        float4 paj = d.pa[j];
+        float dx = ri.x - rj.x - (float)dc * W;
+        float dy = ri.y - rj.y - (float)dr * H;
+        if (smallx) dx += Lxf * (float)((dx < -0.5f * Lxf) - (dx > 0.5f * Lxf));
+        if (smally) dy += Lyf * (float)((dy < -0.5f * Lyf) - (dy > 0.5f * Lyf));
+        float lim = (pai.x + pai.y + paj.x + paj.y + pad) * 1.00001f + 1e-6f;
+        if (fabsf(dy) < lim && (fabsf(fmaf(gam, dy, dx)) < lim || fabsf(fmaf(0.5f, dy, dx)) < lim)) {
+          if (cnt < d.maxn) d.nbr[(size_t)cnt * d.ntot + i] = (int)((unsigned)j | code);
+          cnt++;
+        }
+      }
+    }
+  }
+  d.nbr_n[i] = cnt;
+  if (cnt > d.maxn) atomicOr(d.status, ST_NBR_OVERFLOW);
+}
+
+inline int nblk(int n, int b) { return (n + b - 1) / b; }
 
 }  // namespace
 
@@ -239,6 +362,20 @@ void launch_pass_mixed(const Dev& d, int mode, bool se, const StepScalars* tab, 
          : launch_one<PASS_PRED_RESIZE, false>(d, tab, row, st, block);
       break;
   }
+}
+
+void launch_mx_materialize(const Dev& d, const StepScalars* tab, int row, bool all,
+                           cudaStream_t st) {
+  k_mx_materialize<<<nblk(d.ntot, 256), 256, 0, st>>>(d, tab, row, all ? 1 : 0);
+}
+
+void launch_mx_local(const Dev& d, const StepScalars* tab, int row, bool all, cudaStream_t st) {
+  k_mx_local<<<nblk(d.ntot, 256), 256, 0, st>>>(d, tab, row, all ? 1 : 0);
+}
+
+void launch_mx_build_list(const Dev& d, const StepScalars* tab, int row, bool all,
+                          cudaStream_t st) {
+  k_mx_build_list<<<nblk(d.ntot, 128), 128, 0, st>>>(d, tab, row, all ? 1 : 0);
 }
 
 }  // namespace sc
