@@ -138,6 +138,27 @@ int sc_generate_packing(int n, double packing, double a_over_r, double r_small, 
                         uint64_t seed, double min_sep, double *x, double *y, double *phi,
                         double *R, double *A, double *L);
 
+/* ---- allocation-free force evaluation (no counterpart in the reference) ----
+ * For callers that cannot let a library allocate device memory -- a host program
+ * that has divided the GPU's memory among its own solvers and passes only
+ * pre-allocated buffers, or a loop that must never reach the allocator.  Computes,
+ * for one periodic square box of side L at shear offset gamma, the contact forces
+ * and torques that sc_calc_forces gives on an FP64 handle, from caller-owned device
+ * arrays (x, y, phi, R, A in; fx, fy, tau out; n entries each) on the given stream
+ * (NULL: the default stream), asynchronously.  The cell lists live in one fixed
+ * file-scope device array (about 0.9 MB, resident on every GPU that loads the
+ * library until the process exits); no cudaMalloc, cudaFree or other allocation is
+ * made.  n above SC_NOALLOC_MAX_PARTICLES is rejected with SC_E_ARG.  The first call
+ * on a device looks up the array's address on that device: make it before any
+ * stream capture.  Calls share the array, so calls that overlap on the GPU race;
+ * serialise them.  sc_noalloc_last_error() describes the last failure. */
+#define SC_NOALLOC_MAX_PARTICLES 65536
+int sc_forces_noalloc(int n, double L, double gamma, double pad, const double *d_x,
+                      const double *d_y, const double *d_phi, const double *d_R,
+                      const double *d_A, double *d_fx, double *d_fy, double *d_tau,
+                      void *cuda_stream);
+const char *sc_noalloc_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

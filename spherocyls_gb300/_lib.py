@@ -76,6 +76,10 @@ SIGNATURES = [
     ("sc_generate_packing", ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                            ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
                                            ctypes.c_double, _dp, _dp, _dp, _dp, _dp, _dp]),
+    ("sc_forces_noalloc", ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                         ctypes.c_double, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                         _vp]),
+    ("sc_noalloc_last_error", ctypes.c_char_p, []),
 ]
 
 _LIB = None

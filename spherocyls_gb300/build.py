@@ -27,6 +27,7 @@ CU_UNITS = {
     "sc_pass64.cu": False,
     "sc_cells.cu": False,
     "sc_pass_mixed.cu": True,
+    "sc_noalloc.cu": False,
 }
 CPP_UNITS = ["sc_host.cpp", "sc_api.cpp", "sc_generate.cpp", "sc_io.cpp"]
 CLI_UNITS = {
