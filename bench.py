@@ -184,6 +184,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--only", choices=["mixed", "fp64"], default=None,
                     help="time one form only (for profiler captures)")
+    ap.add_argument("--pad", type=float, default=0.1, help="neighbour-list padding")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -210,8 +211,8 @@ def main():
     n = w["n"]
 
     def new_box(precision, profile=False):
-        b = SpherocylBox(w["L"], w["x"], w["y"], w["p"], w["A"], w["R"], 0.1, precision=precision,
-                         device=local, profile=profile)
+        b = SpherocylBox(w["L"], w["x"], w["y"], w["p"], w["A"], w["R"], args.pad,
+                         precision=precision, device=local, profile=profile)
         b.set_strain_rate(w["rate"])
         b.set_step(w["dt"])
         return b
@@ -219,11 +220,15 @@ def main():
     if args.only:
         b = new_box(args.only)
         b.strain_steps(args.warmup)
+        c0 = b.counters()
         secs = time_steps(b, args.steps, torch)
+        c1 = b.counters()
         if rank == 0:
             print(json.dumps({"only": args.only, "workload": args.workload, "steps": args.steps,
-                              "ms_per_step": 1e3 * secs / args.steps,
-                              "value": n * args.steps / secs}))
+                              "pad": args.pad, "ms_per_step": 1e3 * secs / args.steps,
+                              "value": n * args.steps / secs,
+                              "rebuilds": c1["rebuilds"] - c0["rebuilds"],
+                              "mean_list_length": 2.0 * len(b.pairs()) / n}))
         return
 
     # ---- mixed precision, device-resident: the headline value ----

@@ -432,6 +432,30 @@ void launch_force_rebuild_all(const Dev& d, cudaStream_t st) { k_force_all<<<1, 
 
 void launch_clear_flags(const Dev& d, cudaStream_t st) { k_rb_clear<<<1, 256, 0, st>>>(d); }
 
+// Inside a captured step: mark the systems that set back gamma at this step and
+// switch the graph's conditional rebuild body on when any system needs a rebuild.
+__global__ void k_pre_rebuild(Dev d, const StepScalars* __restrict__ tab, int row,
+                              cudaGraphConditionalHandle cond) {
+  __shared__ int need;
+  if (threadIdx.x == 0) need = 0;
+  __syncthreads();
+  for (int s = threadIdx.x; s < d.nsys; s += blockDim.x)
+    if (tab[row * d.nsys + s].setback) {
+      d.flags[s] |= 2;
+      need = 1;
+    }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (need) *d.any = 1;
+    cudaGraphSetConditional(cond, (need || *d.any) ? 1u : 0u);
+  }
+}
+
+void launch_pre_rebuild(const Dev& d, const StepScalars* tab, int row,
+                        cudaGraphConditionalHandle cond, cudaStream_t st) {
+  k_pre_rebuild<<<1, 256, 0, st>>>(d, tab, row, cond);
+}
+
 void launch_setback(const Dev& d, const StepScalars* tab, int row, cudaStream_t st) {
   k_setback<<<nblk(d.ntot, 256), 256, 0, st>>>(d, tab, row);
 }

@@ -54,6 +54,7 @@ void Handle::dfree(void* p) {
 Handle::~Handle() {
   if (device >= 0) cudaSetDevice(device);
   if (graph_exec) cudaGraphExecDestroy(graph_exec);
+  if (stream2) cudaStreamDestroy(stream2);
   for (auto& e : ev_pool) cudaEventDestroy(e);
   for (void* p : allocs) cudaFree(p);
   if (h_pinned) cudaFreeHost(h_pinned);
@@ -182,6 +183,8 @@ bool Handle::layout_cells() {
     o.nchunks = h.nchunks;
     o.pad = h.pad;
     o.inv_n = 1.0 / h.n;
+    o.smax = (float)(2.0 * (h.Rmax + h.Amax));
+    o.fpad = (float)h.pad;
   }
   bool ok = cuda_ok(cudaMemcpyAsync((void*)d.geom, g.data(), nsys * sizeof(SysGeom),
                                     cudaMemcpyHostToDevice, stream), "upload geometry") &&
@@ -311,27 +314,110 @@ void Handle::collect_times() {
   ev_used = 0;
 }
 
-// One Heun step (rows k of the uploaded table), strain or resize form.
-void Handle::enqueue_step(bool resize, int k, bool se, bool prof) {
+// One Heun step (row k of the uploaded table), strain or resize form, in three
+// parts: the corrector pass, the rebuild body (run only when a system needs it;
+// every kernel in it also exits at once when none does), the predictor pass.
+void Handle::enqueue_corr(bool resize, int k, bool prof) {
   timed(0, prof, [&] { launch_pass(resize ? PASS_CORR_RESIZE : PASS_CORR_STRAIN, false, k); });
+}
+
+int Handle::enqueue_rebuild_body(bool resize, int k, bool prof, cudaStream_t st) {
+  int n = 0;
+  cudaStream_t keep = stream;
+  stream = st;
   if (prec == PREC_MIXED) {
     // FP64 positions of the systems about to be sorted or set back
-    launch_mx_materialize(d, d_tab, k, false, stream);
-    kernels += 1;
+    launch_mx_materialize(d, d_tab, k, false, st);
+    n++;
   }
   if (!resize) {
-    launch_setback(d, d_tab, k, stream);
-    kernels += 1;
+    launch_setback(d, d_tab, k, st);
+    n++;
   }
-  timed(2, prof, [&] { launch_rebuild(d, prec == PREC_MIXED, d_tab, k, stream); });
-  kernels += prec == PREC_MIXED ? 12 : 11;
+  timed(2, prof, [&] { launch_rebuild(d, prec == PREC_MIXED, d_tab, k, st); });
+  n += prec == PREC_MIXED ? 12 : 11;
+  stream = keep;
+  return n;
+}
+
+void Handle::enqueue_pred(bool resize, int k, bool se, bool prof) {
   timed(1, prof, [&] { launch_pass(resize ? PASS_PRED_RESIZE : PASS_PRED_STRAIN, se, k); });
+}
+
+void Handle::enqueue_step(bool resize, int k, bool se, bool prof) {
+  enqueue_corr(resize, k, prof);
+  kernels += enqueue_rebuild_body(resize, k, prof, stream);
+  enqueue_pred(resize, k, se, prof);
 }
 
 void Handle::invalidate_graph() {
   if (graph_exec) cudaGraphExecDestroy(graph_exec);
   graph_exec = nullptr;
   graph_key = GraphKey{};
+}
+
+// Capture the per-step sequence with the rebuild body inside a conditional graph
+// node (skipped when no system needs a rebuild).  Returns false, with the capture
+// ended, when any capture step fails.
+bool Handle::capture_conditional(bool resize, int nsteps, int se_every, cudaGraph_t* out) {
+  if (!stream2 && !cuda_ok(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking), "stream"))
+    return false;
+  if (!cuda_ok(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture"))
+    return false;
+  cudaError_t e = cudaSuccess;
+  int r = 0;
+  long long fixed = 0;
+  for (int k = 1; k <= nsteps && e == cudaSuccess; k++) {
+    bool se = se_every > 0 && k % se_every == 0;
+    enqueue_corr(resize, k, false);
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t gcap = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    e = cudaStreamGetCaptureInfo(stream, &cs, nullptr, &gcap, &deps, nullptr, &nd);
+    cudaGraphConditionalHandle hcond;
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&hcond, gcap, 0, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) break;
+    launch_pre_rebuild(d, d_tab, k, hcond, stream);
+    e = cudaStreamGetCaptureInfo(stream, &cs, nullptr, &gcap, &deps, nullptr, &nd);
+    if (e != cudaSuccess) break;
+    // zeroed raw storage: the struct's union has no default constructor in C++
+    alignas(cudaGraphNodeParams) unsigned char cp_buf[sizeof(cudaGraphNodeParams)] = {};
+    cudaGraphNodeParams& cp = *reinterpret_cast<cudaGraphNodeParams*>(cp_buf);
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = hcond;
+    cp.conditional.type = cudaGraphCondTypeIf;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cn;
+    e = cudaGraphAddNode(&cn, gcap, deps, nullptr, nd, &cp);
+    if (e == cudaSuccess)
+      e = cudaStreamUpdateCaptureDependencies(stream, &cn, nullptr, 1,
+                                              cudaStreamSetCaptureDependencies);
+    if (e != cudaSuccess) break;
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    e = cudaStreamBeginCaptureToGraph(stream2, body, nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) break;
+    body_kernels = enqueue_rebuild_body(resize, k, false, stream2);
+    e = cudaStreamEndCapture(stream2, &body);
+    if (e != cudaSuccess) break;
+    enqueue_pred(resize, k, se, false);
+    fixed += 3;
+    if (se) {
+      enqueue_se_record(r++);
+      fixed += 3;
+    }
+  }
+  cudaGraph_t g = nullptr;
+  cudaError_t e2 = cudaStreamEndCapture(stream, &g);
+  if (e != cudaSuccess || e2 != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    return false;
+  }
+  graph_kernels = fixed;
+  *out = g;
+  return true;
 }
 
 // Capture `nsteps` steps (rows 1..nsteps) as one graph; reused while the table
@@ -342,21 +428,26 @@ bool Handle::run_graph(bool resize, int nsteps, int se_every) {
   if (!graph_exec || !(key == graph_key)) {
     invalidate_graph();
     cudaGraph_t g = nullptr;
-    if (!cuda_ok(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal),
-                 "begin capture"))
-      return false;
-    int r = 0;
     long long k0 = kernels;
-    for (int k = 1; k <= nsteps; k++) {
-      bool se = se_every > 0 && k % se_every == 0;
-      enqueue_step(resize, k, se, false);
-      if (se) enqueue_se_record(r++);
-    }
-    graph_kernels = kernels - k0;
+    graph_conditional = use_conditional && capture_conditional(resize, nsteps, se_every, &g);
     kernels = k0;
-    cudaError_t e = cudaStreamEndCapture(stream, &g);
-    if (!cuda_ok(e, "end capture")) return false;
-    e = cudaGraphInstantiate(&graph_exec, g, 0);
+    if (!graph_conditional) {
+      use_conditional = false;  // plain capture: the rebuild kernels exit early
+      if (!cuda_ok(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal),
+                   "begin capture"))
+        return false;
+      int r = 0;
+      for (int k = 1; k <= nsteps; k++) {
+        bool se = se_every > 0 && k % se_every == 0;
+        enqueue_step(resize, k, se, false);
+        if (se) enqueue_se_record(r++);
+      }
+      graph_kernels = kernels - k0;
+      kernels = k0;
+      body_kernels = 0;
+      if (!cuda_ok(cudaStreamEndCapture(stream, &g), "end capture")) return false;
+    }
+    cudaError_t e = cudaGraphInstantiate(&graph_exec, g, 0);
     cudaGraphDestroy(g);
     if (!cuda_ok(e, "graph instantiate")) {
       graph_exec = nullptr;
@@ -519,7 +610,9 @@ int Handle::run_steps(bool resize, int shrink, int nsteps, int se_every, double*
         return last_status;
     }
     collect_times();
+    long long rb0 = dev_rebuilds;
     if (!check_status(resize ? "resize steps" : "strain steps")) return last_status;
+    if (use_graph && graph_conditional) kernels += (dev_rebuilds - rb0) * body_kernels;
     fp64_valid = prec != PREC_MIXED;
     forces_valid = false;
     hs = sim;

@@ -73,6 +73,10 @@ struct Handle {
   // CUDA graph of one chunk of steps
   cudaGraphExec_t graph_exec = nullptr;
   GraphKey graph_key{};
+  cudaStream_t stream2 = nullptr;  // captures the conditional rebuild bodies
+  bool use_conditional = true;     // conditional graph nodes available
+  bool graph_conditional = false;  // the current graph uses them
+  long long body_kernels = 0;      // kernels in one rebuild body
   // profiling: per-pass events
   struct Mark {
     int kind;
@@ -115,6 +119,10 @@ struct Handle {
   void timed(int kind, bool on, const std::function<void()>& f);
   void collect_times();
   void enqueue_step(bool resize, int k, bool se, bool prof);
+  void enqueue_corr(bool resize, int k, bool prof);
+  int enqueue_rebuild_body(bool resize, int k, bool prof, cudaStream_t st);
+  void enqueue_pred(bool resize, int k, bool se, bool prof);
+  bool capture_conditional(bool resize, int nsteps, int se_every, cudaGraph_t* out);
   void enqueue_se_record(int rec);
   void invalidate_graph();
   bool run_graph(bool resize, int nsteps, int se_every);

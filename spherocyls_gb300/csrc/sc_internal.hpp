@@ -28,6 +28,8 @@ struct SysGeom {
   int pad_;
   double pad;          // neighbour padding (configure_cells auto-value applied)
   double inv_n;        // 1/n, energy normalisation
+  float smax;          // largest R_i + A_i + R_j + A_j of the system
+  float fpad;          // pad in FP32
 };
 
 // Per-(step, system) scalars, computed on the host with the reference's own
@@ -86,8 +88,10 @@ struct Dev {
   float4* mc;     // (x compensation, y compensation, phi, phi compensation)
   float4* mv;     // (v0x, v0y, v0phi, predicted phi)
   float2* mm;     // displacement since the last rebuild
-  float4* pa;     // (R, A, 1/I, RC)
+  float4* pa;     // (R, A, particle index as int bits, 1/I)
+  float* rcf;     // isolated-rotation coefficient RC
   int* cellp;     // local cell packed as col | row << 16
+  float* gbuild;  // [nsys] gamma at which each system's list was built
   // cell lists
   int* cell_start;          // [ncells] first slot
   int* cell_count;          // [ncells]
@@ -153,6 +157,8 @@ void launch_setback(const Dev& d, const StepScalars* tab, int row, cudaStream_t 
 void launch_rebuild(const Dev& d, bool mixed, const StepScalars* tab, int row, cudaStream_t st);
 void launch_force_rebuild_all(const Dev& d, cudaStream_t st);
 void launch_clear_flags(const Dev& d, cudaStream_t st);
+void launch_pre_rebuild(const Dev& d, const StepScalars* tab, int row,
+                        cudaGraphConditionalHandle cond, cudaStream_t st);
 void launch_se_reduce(const Dev& d, cudaStream_t st);
 void launch_gd_update(const Dev& d, bool mixed, const StepScalars* tab, int row, cudaStream_t st);
 void launch_se_store(const Dev& d, double* dst, cudaStream_t st);

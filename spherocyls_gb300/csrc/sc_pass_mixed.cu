@@ -8,26 +8,26 @@
 // FP64 instruction runs in the force passes except the stress/energy sums on the
 // steps that record them.
 //
-// Neighbour list: the reference's padded list (tmarschall/spherocyls
-// src/cpp/spherocyl_box.cpp:303-355, criterion |dy| < S+pad and
-// (|dx + gamma dy| < S+pad or |dx + dy/2| < S+pad)), evaluated in FP32 with the
-// bound inflated by 1e-5 relative so that it contains every pair the FP64
-// criterion accepts.  Each entry packs the neighbour's slot with the cell offset
-// (dc, dr) between the two cells, so the displacement is
-// rec_i - rec_j - (dc W, dr H) with no box length in the FP32 arithmetic.
+// Neighbour list: every pair whose centres, in the Lees-Edwards frame of the
+// build, are closer than R_i+A_i+R_j+A_j+pad (the reach of a contact plus the
+// padding; FP32, bound inflated by 2e-5 relative).  It is rebuilt when a particle's
+// displacement since the build, plus this step's displacement as an allowance for
+// the next predictor excursion, exceeds half of what is left of the padding once
+// the shear accumulated since the build, |gamma - gamma_build| (S_max + pad), is
+// taken off.  Then no pair outside the list can come into contact, so the set of
+// interacting pairs is exactly the reference's (whose own padded list is larger).
+// Each entry packs the neighbour's slot with the cell offset (dc, dr) between the
+// two cells, so the displacement is rec_i - rec_j - (dc W, dr H) with no box
+// length in the FP32 arithmetic.
 //
-// Force pass: one thread per slot, two phases -- a cheap bounding test over the
-// list (centres closer than R_i+A_i+R_j+A_j), collecting the survivors, then the
-// segment-segment contact for the survivors only, which keeps the expensive code
-// path free of the divergence of the bounding test.
+// Force pass: one thread per slot gathers over its list; each pair is computed
+// with the lower particle index as the reference's "p".
 #include "sc_internal.hpp"
 #include "sc_pair.cuh"
 
 namespace sc {
 
 namespace {
-
-constexpr int kHits = 24;  // survivors buffered per phase
 
 __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
   float y = v + c;
@@ -47,17 +47,10 @@ __device__ __forceinline__ void kahan_add_scale(float& s, float& c, float v, flo
   c = pe;
 }
 
-__device__ __forceinline__ void flag_moved32(const Dev& d, int s, float2 m, float pad) {
-  float h = 0.5f * pad;
-  if (m.x > h || m.x < -h || m.y > h || m.y < -h) {
-    if (d.flags[s] == 0) atomicOr(&d.flags[s], 1);
-    if (*d.any == 0) atomicExch(d.any, 1);
-  }
-}
-
 template <int MODE, bool SE>
-__global__ void __launch_bounds__(128) k_pass_mixed(Dev d, const StepScalars* __restrict__ tab,
-                                                   int row) {
+__global__ void __launch_bounds__(128, 10) k_pass_mixed(Dev d,
+                                                       const StepScalars* __restrict__ tab,
+                                                       int row) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.ntot) return;
   constexpr bool kPred = (MODE == PASS_CORR_STRAIN || MODE == PASS_CORR_RESIZE);
@@ -73,77 +66,70 @@ __global__ void __launch_bounds__(128) k_pass_mixed(Dev d, const StepScalars* __
   const bool virial = d.stress_mode == STRESS_VIRIAL;
 
   const float4 ri = REC[i];
-  const float4 pai = d.pa[i];  // (R, A, 1/I, RC)
-  const int idi = d.id[i];
+  const float4 pai = d.pa[i];  // (R, A, index bits, 1/I)
+  const int idi = __float_as_int(pai.z);
   int cnt = d.nbr_n[i];
   if (cnt > d.maxn) cnt = d.maxn;
-  const unsigned* __restrict__ L = reinterpret_cast<const unsigned*>(d.nbr) + i;
+  const unsigned* __restrict__ Lst = reinterpret_cast<const unsigned*>(d.nbr) + i;
   const size_t stride = d.ntot;
 
   float fx = 0.f, fy = 0.f, tq = 0.f;
   double e_acc = 0.0, pxx = 0.0, pyy = 0.0, pxy = 0.0, pyx = 0.0;
-  unsigned hit[kHits];
-  int k = 0;
-  while (k < cnt) {
-    // phase 1: bounding test over the list
-    int nh = 0;
-    for (; k < cnt && nh < kHits; k++) {
-      unsigned e = __ldg(L + (size_t)k * stride);
-      int j = (int)(e & kSlotMask);
-      float4 rj = REC[j];
-      float2 raj = *reinterpret_cast<const float2*>(&d.pa[j]);
-      float dx = ri.x - rj.x + (float)(1 - (int)((e >> 28) & 3u)) * W;
-      float dy = ri.y - rj.y + (float)(1 - (int)(e >> 30)) * H;
-      if (smallx) dx += Lxf * (float)((dx < -0.5f * Lxf) - (dx > 0.5f * Lxf));
-      if (smally) dy += Lyf * (float)((dy < -0.5f * Lyf) - (dy > 0.5f * Lyf));
-      float reach = pai.x + pai.y + raj.x + raj.y;
-      float dxl = fmaf(gam, dy, dx);
-      if (dxl * dxl + dy * dy < reach * reach) hit[nh++] = e;
+  // software pipeline: the list entry two ahead and the neighbour data one ahead
+  // are in flight while the current pair is computed
+  unsigned e1 = cnt > 0 ? __ldg(Lst) : 0u;
+  unsigned e2 = cnt > 1 ? __ldg(Lst + stride) : 0u;
+  float4 r1 = make_float4(0.f, 0.f, 0.f, 0.f), p1 = r1;
+  if (cnt > 0) {
+    r1 = REC[e1 & kSlotMask];
+    p1 = d.pa[e1 & kSlotMask];
+  }
+  for (int k = 0; k < cnt; k++) {
+    const unsigned e = e1;
+    const float4 rj = r1;
+    const float4 paj = p1;
+    e1 = e2;
+    if (k + 1 < cnt) {
+      r1 = REC[e1 & kSlotMask];
+      p1 = d.pa[e1 & kSlotMask];
     }
-    // phase 2: contacts of the survivors
-    for (int h = 0; h < nh; h++) {
-      unsigned e = hit[h];
-      int j = (int)(e & kSlotMask);
-      float4 rj = REC[j];
-      float2 raj = *reinterpret_cast<const float2*>(&d.pa[j]);
-      int idj = d.id[j];
-      float dx = ri.x - rj.x + (float)(1 - (int)((e >> 28) & 3u)) * W;
-      float dy = ri.y - rj.y + (float)(1 - (int)(e >> 30)) * H;
-      if (smallx) dx += Lxf * (float)((dx < -0.5f * Lxf) - (dx > 0.5f * Lxf));
-      if (smally) dy += Lyf * (float)((dy < -0.5f * Lyf) - (dy > 0.5f * Lyf));
-      const bool ip = idi < idj;
-      PairF32 o;
-      bool touch;
-      if (ip)
-        touch = pair_fp32<SE>(dx, dy, ri.z, ri.w, pai.y, rj.z, rj.w, raj.y, pai.x + raj.x, gam,
-                              virial, o);
-      else
-        touch = pair_fp32<false>(-dx, -dy, rj.z, rj.w, raj.y, ri.z, ri.w, pai.y, raj.x + pai.x,
-                                 gam, virial, o);
-      if (!touch) continue;
-      if (ip) {
-        fx += o.fx;
-        fy += o.fy;
-        tq += o.tp;
-        if (SE) {
-          e_acc += (double)(o.ov * o.ov);
-          if (!virial) {
-            pxx += (double)(o.fx * o.cxa) - (double)(o.fx * o.cxb) - (double)(o.fy * o.cxb);
-            pyy += (double)(o.fy * o.cya) - (double)(o.fy * o.cyb);
-            pxy += (double)(o.fy * o.cxa);
-            pyx += (double)(o.fx * o.cya) - (double)(o.fx * o.cyb);
-          } else {
-            pxx += (double)(o.fx * o.cxa) - (double)(o.fx * o.cxb);
-            pyy += (double)(o.fy * o.cya) - (double)(o.fy * o.cyb);
-            pxy += (double)(o.fy * o.cxa) - (double)(o.fy * o.cxb);
-            pyx += (double)(o.fx * o.cya) - (double)(o.fx * o.cyb);
-          }
+    if (k + 2 < cnt) e2 = __ldg(Lst + (size_t)(k + 2) * stride);
+    float dx = ri.x - rj.x + (float)(1 - (int)((e >> 28) & 3u)) * W;
+    float dy = ri.y - rj.y + (float)(1 - (int)(e >> 30)) * H;
+    if (smallx) dx += Lxf * (float)((dx < -0.5f * Lxf) - (dx > 0.5f * Lxf));
+    if (smally) dy += Lyf * (float)((dy < -0.5f * Lyf) - (dy > 0.5f * Lyf));
+    const bool ip = idi < __float_as_int(paj.z);
+    PairF32 o;
+    bool touch;
+    if (ip)
+      touch = pair_fp32<SE>(dx, dy, ri.z, ri.w, pai.y, rj.z, rj.w, paj.y, pai.x + paj.x, gam,
+                            virial, o);
+    else
+      touch = pair_fp32<false>(-dx, -dy, rj.z, rj.w, paj.y, ri.z, ri.w, pai.y, paj.x + pai.x, gam,
+                               virial, o);
+    if (!touch) continue;
+    if (ip) {
+      fx += o.fx;
+      fy += o.fy;
+      tq += o.tp;
+      if (SE) {
+        e_acc += (double)(o.ov * o.ov);
+        if (!virial) {
+          pxx += (double)(o.fx * o.cxa) - (double)(o.fx * o.cxb) - (double)(o.fy * o.cxb);
+          pyy += (double)(o.fy * o.cya) - (double)(o.fy * o.cyb);
+          pxy += (double)(o.fy * o.cxa);
+          pyx += (double)(o.fx * o.cya) - (double)(o.fx * o.cyb);
+        } else {
+          pxx += (double)(o.fx * o.cxa) - (double)(o.fx * o.cxb);
+          pyy += (double)(o.fy * o.cya) - (double)(o.fy * o.cyb);
+          pxy += (double)(o.fy * o.cxa) - (double)(o.fy * o.cxb);
+          pyx += (double)(o.fx * o.cya) - (double)(o.fx * o.cyb);
         }
-      } else {
-        fx -= o.fx;
-        fy -= o.fy;
-        tq += o.tq;
       }
+    } else {
+      fx -= o.fx;
+      fy -= o.fy;
+      tq += o.tq;
     }
   }
   if (SE) {
@@ -157,7 +143,7 @@ __global__ void __launch_bounds__(128) k_pass_mixed(Dev d, const StepScalars* __
   }
 
   const float dt = ts.f_step;
-  const float A = pai.y, invI = pai.z, RC = pai.w;
+  const float A = pai.y, invI = pai.w;
   if (MODE == PASS_FORCE) {
     d.fx[i] = fx;
     d.fy[i] = fy;
@@ -168,6 +154,7 @@ __global__ void __launch_bounds__(128) k_pass_mixed(Dev d, const StepScalars* __
     if (MODE == PASS_PRED_STRAIN) {
       // strain_step predictor, strain_dynamics.cpp:187-199
       float phi = c.z + c.w;
+      const float RC = d.rcf[i];
       v0x = fx - gam * fy;
       v0y = fy;
       v0p = tq * invI - ts.f_rate * (0.5f * (1.f - RC * __cosf(2.f * phi)));
@@ -195,6 +182,7 @@ __global__ void __launch_bounds__(128) k_pass_mixed(Dev d, const StepScalars* __
     float ddx, ddy, ddp;
     if (MODE == PASS_CORR_STRAIN) {
       // strain_step corrector, strain_dynamics.cpp:203-219
+      const float RC = d.rcf[i];
       float v1x = fx - gam * fy;
       float v1y = fy;
       float v1p = tq * invI - ts.f_rate * (0.5f * (1.f - RC * __cosf(2.f * v0.w)));
@@ -234,7 +222,14 @@ __global__ void __launch_bounds__(128) k_pass_mixed(Dev d, const StepScalars* __
     d.mc[i] = c;
     d.mm[i] = m;
     if (!(isfinite(r.x) && isfinite(r.y) && isfinite(c.z))) atomicOr(d.status, ST_NAN);
-    flag_moved32(d, s, m, (float)g.pad);
+    // padding left after the shear since the list was built (next corrector's gamma)
+    float dg = fabsf(ts.f_gamma_p - d.gbuild[s]) + 2.f * fabsf(ts.f_rate * dt);
+    float h = 0.5f * (g.fpad - dg * (g.smax + g.fpad));
+    float reach = sqrtf(m.x * m.x + m.y * m.y) + sqrtf(ddx * ddx + ddy * ddy);
+    if (!(reach < h)) {
+      if (d.flags[s] == 0) atomicOr(&d.flags[s], 1);
+      if (*d.any == 0) atomicExch(d.any, 1);
+    }
   }
 }
 
@@ -288,7 +283,8 @@ __global__ void k_mx_local(Dev d, const StepScalars* __restrict__ tab, int row, 
   d.rec[i] = make_float4(xl, yl, A * cs, A * sn);
   d.mc[i] = make_float4((float)(lx - xl), (float)(ly - yl), pf, (float)(phi - pf));
   d.mm[i] = make_float2(0.f, 0.f);
-  d.pa[i] = make_float4((float)ra.x, A, (float)(1.0 / irc.x), (float)irc.y);
+  d.pa[i] = make_float4((float)ra.x, A, __int_as_float(d.id[i]), (float)(1.0 / irc.x));
+  d.rcf[i] = (float)irc.y;
 }
 
 // The padded neighbour list in FP32 (see the file comment).
@@ -327,8 +323,9 @@ __global__ void __launch_bounds__(128) k_mx_build_list(Dev d, const StepScalars*
         float dy = ri.y - rj.y - (float)dr * H;
         if (smallx) dx += Lxf * (float)((dx < -0.5f * Lxf) - (dx > 0.5f * Lxf));
         if (smally) dy += Lyf * (float)((dy < -0.5f * Lyf) - (dy > 0.5f * Lyf));
-        float lim = (pai.x + pai.y + paj.x + paj.y + pad) * 1.00001f + 1e-6f;
-        if (fabsf(dy) < lim && (fabsf(fmaf(gam, dy, dx)) < lim || fabsf(fmaf(0.5f, dy, dx)) < lim)) {
+        float lim = (pai.x + pai.y + paj.x + paj.y + pad) * 1.00002f + 1e-6f;
+        float dxl = fmaf(gam, dy, dx);
+        if (dxl * dxl + dy * dy < lim * lim) {
           if (cnt < d.maxn) d.nbr[(size_t)cnt * d.ntot + i] = (int)((unsigned)j | code);
           cnt++;
         }
@@ -337,6 +334,7 @@ __global__ void __launch_bounds__(128) k_mx_build_list(Dev d, const StepScalars*
   }
   d.nbr_n[i] = cnt;
   if (cnt > d.maxn) atomicOr(d.status, ST_NBR_OVERFLOW);
+  if (i == g.p0) d.gbuild[s] = gam;
 }
 
 inline int nblk(int n, int b) { return (n + b - 1) / b; }
