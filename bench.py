@@ -185,6 +185,9 @@ def main():
     ap.add_argument("--only", choices=["mixed", "fp64"], default=None,
                     help="time one form only (for profiler captures)")
     ap.add_argument("--pad", type=float, default=0.1, help="neighbour-list padding")
+    ap.add_argument("--no-graphs", action="store_true",
+                    help="launch eagerly instead of through CUDA graphs (profiler captures: "
+                         "kernels inside graphs with conditional nodes cannot be profiled)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -212,7 +215,8 @@ def main():
 
     def new_box(precision, profile=False):
         b = SpherocylBox(w["L"], w["x"], w["y"], w["p"], w["A"], w["R"], args.pad,
-                         precision=precision, device=local, profile=profile)
+                         precision=precision, device=local, profile=profile,
+                         use_graphs=not args.no_graphs)
         b.set_strain_rate(w["rate"])
         b.set_step(w["dt"])
         return b

@@ -121,16 +121,15 @@ __global__ void __launch_bounds__(128) k_pass64(Dev d, const StepScalars* __rest
     double2 nj = NXY[j];
     double2 raj = d.ra[j];
     int idj = d.id[j];
-    bool ip = idi < idj;
+    // the lower particle index plays the reference's "p": select the operands (one
+    // copy of the pair code per warp) rather than branch into two
+    const bool ip = idi < idj;
+    const double2 pP = ip ? pi : pj, pQ = ip ? pj : pi;
+    const double2 nP = ip ? ni : nj, nQ = ip ? nj : ni;
+    const double2 rP = ip ? rai : raj, rQ = ip ? raj : rai;
     PairF64 o;
-    bool hit;
-    if (ip)
-      hit = pair_fp64<SE>(pi.x - pj.x, pi.y - pj.y, ni.x, ni.y, rai.y, nj.x, nj.y, raj.y,
-                          rai.x + raj.x, gamma, Lx, Ly, virial, two_n, o);
-    else
-      hit = pair_fp64<false>(pj.x - pi.x, pj.y - pi.y, nj.x, nj.y, raj.y, ni.x, ni.y, rai.y,
-                             raj.x + rai.x, gamma, Lx, Ly, virial, two_n, o);
-    if (hit) {
+    if (pair_fp64<SE>(pP.x - pQ.x, pP.y - pQ.y, nP.x, nP.y, rP.y, nQ.x, nQ.y, rQ.y, rP.x + rQ.x,
+                      gamma, Lx, Ly, virial, two_n, o)) {
       if (ip) {
         fx += o.fx;
         fy += o.fy;

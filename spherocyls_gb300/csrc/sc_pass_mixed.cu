@@ -98,21 +98,21 @@ __global__ void __launch_bounds__(128, 10) k_pass_mixed(Dev d,
     float dy = ri.y - rj.y + (float)(1 - (int)(e >> 30)) * H;
     if (smallx) dx += Lxf * (float)((dx < -0.5f * Lxf) - (dx > 0.5f * Lxf));
     if (smally) dy += Lyf * (float)((dy < -0.5f * Lyf) - (dy > 0.5f * Lyf));
+    // the lower particle index plays the reference's "p"; select the operands
+    // instead of branching so that the warp runs one copy of the pair code
     const bool ip = idi < __float_as_int(paj.z);
+    const float sg = ip ? 1.f : -1.f;
     PairF32 o;
-    bool touch;
-    if (ip)
-      touch = pair_fp32<SE>(dx, dy, ri.z, ri.w, pai.y, rj.z, rj.w, paj.y, pai.x + paj.x, gam,
-                            virial, o);
-    else
-      touch = pair_fp32<false>(-dx, -dy, rj.z, rj.w, paj.y, ri.z, ri.w, pai.y, paj.x + pai.x, gam,
-                               virial, o);
+    const bool touch = pair_fp32<SE>(sg * dx, sg * dy, ip ? ri.z : rj.z, ip ? ri.w : rj.w,
+                                     ip ? pai.y : paj.y, ip ? rj.z : ri.z, ip ? rj.w : ri.w,
+                                     ip ? paj.y : pai.y, ip ? pai.x + paj.x : paj.x + pai.x, gam,
+                                     virial, o);
     if (!touch) continue;
-    if (ip) {
-      fx += o.fx;
-      fy += o.fy;
-      tq += o.tp;
-      if (SE) {
+    fx += sg * o.fx;
+    fy += sg * o.fy;
+    tq += ip ? o.tp : o.tq;
+    if (SE && ip) {
+      {
         e_acc += (double)(o.ov * o.ov);
         if (!virial) {
           pxx += (double)(o.fx * o.cxa) - (double)(o.fx * o.cxb) - (double)(o.fy * o.cxb);
@@ -126,10 +126,6 @@ __global__ void __launch_bounds__(128, 10) k_pass_mixed(Dev d,
           pyx += (double)(o.fx * o.cya) - (double)(o.fx * o.cyb);
         }
       }
-    } else {
-      fx -= o.fx;
-      fy -= o.fy;
-      tq += o.tq;
     }
   }
   if (SE) {
