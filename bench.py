@@ -29,7 +29,27 @@ WORKLOADS = {
     # name: (N, packing, a/R, strain rate, dt, seed)
     "shear_n1048576_phi084": (1 << 20, 0.84, 1.0, 1e-4, 0.02, 3),
     "shear_n16384_phi086": (16384, 0.86, 1.0, 1e-4, 0.02, 1),
+    # 512 independent systems: N log-uniform in [64, 8192] (even), packing U[0.75, 0.90],
+    # a/R U[0.2, 2.0], strain rate log-uniform in [1e-6, 1e-3], seed 2
+    "batch512": (512, None, None, None, 0.02, 2),
 }
+
+
+def make_batch(seed=2, nsys=512):
+    from spherocyls_gb300 import generate_packing
+
+    rng = np.random.default_rng(seed)
+    ns = (np.exp(rng.uniform(np.log(64), np.log(8192), nsys)) / 2).round().astype(int) * 2
+    phis = rng.uniform(0.75, 0.90, nsys)
+    aors = rng.uniform(0.2, 2.0, nsys)
+    rates = np.exp(rng.uniform(np.log(1e-6), np.log(1e-3), nsys))
+    parts = [generate_packing(int(n), float(f), float(a), seed=int(seed * 100000 + k))
+             for k, (n, f, a) in enumerate(zip(ns, phis, aors))]
+    return dict(ns=ns, phis=phis, aors=aors, rates=rates,
+                L=np.array([pk[0] for pk in parts]),
+                x=np.concatenate([pk[1] for pk in parts]), y=np.concatenate([pk[2] for pk in parts]),
+                p=np.concatenate([pk[3] for pk in parts]), R=np.concatenate([pk[4] for pk in parts]),
+                A=np.concatenate([pk[5] for pk in parts]))
 # Algorithmic bytes per particle-step (two force passes plus the state update):
 # mixed form 152 + 8 n, plain FP64 form 232 + 8 n, n the mean length of the full
 # neighbour list actually used (4 bytes per entry and pass).  Per force pass: half.
@@ -97,12 +117,21 @@ class ClockSampler:
 def make_workload(name):
     from spherocyls_gb300 import generate_packing
 
+    if name == "batch512":
+        b = make_batch()
+        b.update(n=int(b["ns"].sum()), phi=None, a=None, rate=None, dt=0.02, seed=2)
+        return b
     n, phi, a, rate, dt, seed = WORKLOADS[name]
     L, x, y, p, R, A = generate_packing(n, phi, a, seed=seed)
     return dict(n=n, phi=phi, a=a, rate=rate, dt=dt, seed=seed, L=L, x=x, y=y, p=p, R=R, A=A)
 
 
 _STREAM = None
+
+
+def mean_list_length(box):
+    """Mean full-list length (2 x half-list pairs / N) of the first system."""
+    return 2.0 * len(box.pairs(0)) / int(box.n_per_sys[0])
 
 
 def time_steps(box, steps, torch):
@@ -214,10 +243,19 @@ def main():
     n = w["n"]
 
     def new_box(precision, profile=False):
-        b = SpherocylBox(w["L"], w["x"], w["y"], w["p"], w["A"], w["R"], args.pad,
+        if args.workload == "batch512":
+            from spherocyls_gb300 import BoxBatch
+
+            b = BoxBatch(w["ns"], w["L"], w["x"], w["y"], w["p"], w["A"], w["R"], args.pad,
                          precision=precision, device=local, profile=profile,
                          use_graphs=not args.no_graphs)
-        b.set_strain_rate(w["rate"])
+            for k, r in enumerate(w["rates"]):
+                b.set_strain_rate(float(r), sys=k)
+        else:
+            b = SpherocylBox(w["L"], w["x"], w["y"], w["p"], w["A"], w["R"], args.pad,
+                             precision=precision, device=local, profile=profile,
+                             use_graphs=not args.no_graphs)
+            b.set_strain_rate(w["rate"])
         b.set_step(w["dt"])
         return b
 
@@ -232,7 +270,7 @@ def main():
                               "pad": args.pad, "ms_per_step": 1e3 * secs / args.steps,
                               "value": n * args.steps / secs,
                               "rebuilds": c1["rebuilds"] - c0["rebuilds"],
-                              "mean_list_length": 2.0 * len(b.pairs()) / n}))
+                              "mean_list_length": mean_list_length(b)}))
         return
 
     # ---- mixed precision, device-resident: the headline value ----
@@ -260,7 +298,7 @@ def main():
     pt = prof.pass_times()
     pass_ms = 0.5 * (pt["corr_ms"] + pt["pred_ms"])
     peak, peak_kind = _peaks()
-    nbar = 2.0 * len(prof.pairs()) / n
+    nbar = mean_list_length(prof)
     bpp = bytes_per_pass("mixed", nbar)
     achieved = bpp * n / (pass_ms / 1e3) / 1e9
     prof.close()
@@ -296,7 +334,7 @@ def main():
                    "positions read back after each chunk"}
 
     base = None
-    if rank == 0 and not args.no_cpu:
+    if rank == 0 and not args.no_cpu and w.get("phi") is not None:
         base = cpu_baseline(w, 65536, args.cpu_steps, 1)
 
     if rank == 0:

@@ -138,6 +138,37 @@ int sc_generate_packing(int n, double packing, double a_over_r, double r_small, 
                         uint64_t seed, double min_sep, double *x, double *y, double *phi,
                         double *R, double *A, double *L);
 
+/* ---- files and run protocols with output (single-system handles) ---- */
+
+/* Read a position file (DatFileInput with a header row, src/cpp/file_input.h:24-76).
+ * Both header layouts are accepted: the src/cpp one, "N L packing gamma
+ * gamma_total rate dt" (7 fields), and the src/cuda one, "N Lx Ly packing gamma
+ * gamma_total rate dt" (8 fields, src/cuda/main.cpp:201).  Rows are "x y phi R A".
+ * Call once with x == NULL to get *n and hdr; then with arrays of *n entries.
+ * hdr[0..6] = Lx Ly packing gamma gamma_total rate dt. */
+int sc_read_positions(const char *path, int *n, double *hdr, double *x, double *y, double *phi,
+                      double *R, double *A);
+/* save_positions: SC_FMT_SP as src/cpp/spherocyl_box.cpp:410-423 (precision 14),
+ * SC_FMT_SD as src/cuda/strain_dynamics.cu:820-843 (%.17g rows). */
+int sc_save_positions(sc_handle *h, int sys, const char *path, int format);
+
+/* run_strain with output, src/cpp/strain_dynamics.cpp:238-319: t runs from t_start
+ * to t_start + round(run_gamma/rate) in units of 1/dt steps; stress/energy lines
+ * every se_save strain (SE file sp_strain_se.dat, or sd_stress_energy.dat for
+ * SC_FMT_SD) and position files every pos_save strain, named sp%010lu.dat /
+ * sd%010lu.dat; t_start > 0 continues an earlier run, rewriting the SE file from
+ * the line of time t_start.  *t_end receives the final time. */
+int sc_run_strain(sc_handle *h, const char *out_dir, double run_gamma, double pos_save,
+                  double se_save, unsigned long t_start, int format, unsigned long *t_end);
+/* resize_box with output, src/cpp/resize_dynamics.cpp:246-330 (SE file
+ * sp_resize_se.dat with the packing fraction as second column). */
+int sc_run_resize(sc_handle *h, const char *out_dir, double final_packing, double pos_save,
+                  double se_save, unsigned long t_start, int format, unsigned long *t_end);
+/* gradient_descent_minimize with output, src/cpp/relaxation_dynamics.cpp:33-85 (SE
+ * file sr_strain_se.dat, position files sr%010lu.dat every pos_save_n steps). */
+int sc_run_minimize(sc_handle *h, const char *out_dir, int max_steps, double e_min,
+                    int pos_save_n, int *steps_taken);
+
 /* ---- allocation-free force evaluation (no counterpart in the reference) ----
  * For callers that cannot let a library allocate device memory -- a host program
  * that has divided the GPU's memory among its own solvers and passes only

@@ -6,6 +6,6 @@ The work is done by ``libspherocyl`` (C++ host runtime + hand-written CUDA kerne
 C ABI in ``include/spherocyl.h``); this package binds it with ctypes.
 """
 from ._lib import ScError, lib
-from .box import BoxBatch, SpherocylBox, generate_packing
+from .box import BoxBatch, SpherocylBox, generate_packing, read_positions
 
-__all__ = ["BoxBatch", "SpherocylBox", "generate_packing", "ScError", "lib"]
+__all__ = ["BoxBatch", "SpherocylBox", "generate_packing", "read_positions", "ScError", "lib"]

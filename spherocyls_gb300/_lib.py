@@ -76,6 +76,16 @@ SIGNATURES = [
     ("sc_generate_packing", ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                            ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
                                            ctypes.c_double, _dp, _dp, _dp, _dp, _dp, _dp]),
+    ("sc_read_positions", ctypes.c_int, [ctypes.c_char_p, _ip, _dp, _dp, _dp, _dp, _dp, _dp]),
+    ("sc_save_positions", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_int]),
+    ("sc_run_strain", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_double, ctypes.c_double,
+                                     ctypes.c_double, ctypes.c_ulong, ctypes.c_int,
+                                     ctypes.POINTER(ctypes.c_ulong)]),
+    ("sc_run_resize", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_double, ctypes.c_double,
+                                     ctypes.c_double, ctypes.c_ulong, ctypes.c_int,
+                                     ctypes.POINTER(ctypes.c_ulong)]),
+    ("sc_run_minimize", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_double,
+                                       ctypes.c_int, _ip]),
     ("sc_forces_noalloc", ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                          ctypes.c_double, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                          _vp]),

@@ -41,6 +41,26 @@ def generate_packing(n: int, packing: float, a_over_r: float, r_small: float = 0
     return L.value, x, y, p, R, A
 
 
+FMT = {"sp": 0, "sd": 1}
+
+
+def read_positions(path: str):
+    """Read a position file (src/cpp or src/cuda header); returns (hdr, x, y, phi, R, A)
+    with hdr = dict(Lx, Ly, packing, gamma, gamma_total, rate, dt)."""
+    n = ctypes.c_int(0)
+    hdr = np.empty(7)
+    L = lib()
+    st = L.sc_read_positions(path.encode(), ctypes.byref(n), _ptr(hdr), None, None, None, None,
+                             None)
+    check(st, None)
+    x, y, p, R, A = (np.empty(n.value) for _ in range(5))
+    st = L.sc_read_positions(path.encode(), ctypes.byref(n), _ptr(hdr), _ptr(x), _ptr(y), _ptr(p),
+                             _ptr(R), _ptr(A))
+    check(st, None)
+    keys = ("Lx", "Ly", "packing", "gamma", "gamma_total", "rate", "dt")
+    return dict(zip(keys, hdr.tolist())), x, y, p, R, A
+
+
 class BoxBatch:
     """One or more independent periodic boxes advanced together on one GPU."""
 
@@ -153,6 +173,32 @@ class BoxBatch:
         self._chk(lib().sc_gd_minimize(self.h, int(max_steps), float(e_min), ctypes.byref(steps),
                                        ctypes.byref(ef)))
         return steps.value, ef.value
+
+    # --- runs with file output (single-system handles) -------------------------
+    def save_positions(self, path: str, fmt: str = "sp", sys: int = 0):
+        self._chk(lib().sc_save_positions(self.h, int(sys), path.encode(), FMT[fmt]))
+
+    def run_strain(self, out_dir: str, run_gamma: float, pos_save: float, se_save: float,
+                   t_start: int = 0, fmt: str = "sp") -> int:
+        t = ctypes.c_ulong()
+        self._chk(lib().sc_run_strain(self.h, out_dir.encode(), float(run_gamma), float(pos_save),
+                                      float(se_save), int(t_start), FMT[fmt], ctypes.byref(t)))
+        return t.value
+
+    def run_resize(self, out_dir: str, final_packing: float, pos_save: float, se_save: float,
+                   t_start: int = 0, fmt: str = "sp") -> int:
+        t = ctypes.c_ulong()
+        self._chk(lib().sc_run_resize(self.h, out_dir.encode(), float(final_packing),
+                                      float(pos_save), float(se_save), int(t_start), FMT[fmt],
+                                      ctypes.byref(t)))
+        return t.value
+
+    def run_minimize(self, out_dir: str, max_steps: int, e_min: float = 0.0,
+                     pos_save_n: int = 1000) -> int:
+        s = ctypes.c_int()
+        self._chk(lib().sc_run_minimize(self.h, out_dir.encode(), int(max_steps), float(e_min),
+                                        int(pos_save_n), ctypes.byref(s)))
+        return s.value
 
     # --- state ------------------------------------------------------------
     def state(self):

@@ -1,0 +1,82 @@
+// spherocyl_strain -- Lees-Edwards shear run (new or continued) on the GPU.
+//
+// Arguments in the order of input/input_key.txt:7-22 (the src/cuda driver's order,
+// src/cuda/main.cpp:63-125): data file or "r", output directory, N, strain rate,
+// step, run length (strain), position save interval (strain), stress save interval
+// (strain), cell padding, shear-direction change (only 0 is supported), and for
+// "r": packing fraction, aspect ratio A/R (R1 = 0.5), bidispersity R2/R1, initial
+// configuration type (only 0, random, is supported).  SC_PRECISION=mixed selects
+// the mixed form, SC_OUTPUT_FORMAT=sd the src/cuda file layout, SC_SEED the seed of
+// the random configuration.
+#include <chrono>
+#include <vector>
+
+#include "cli_common.hpp"
+
+int main(int argc, char** argv) {
+  cli::Args a{argc, argv};
+  std::string file = a.s("Data file ('r' for random)");
+  std::string dir = a.s("Output data directory");
+  int n = a.i("Number of particles");
+  double rate = a.f("Strain rate");
+  double dt = a.f("Integration step size");
+  double run = a.f("Strain run length (gamma)");
+  double pos_save = a.f("Position data save rate");
+  double se_save = a.f("Stress data save rate");
+  double pad = a.f("Cell padding");
+  int flip = a.i("Change shear direction (0: no)");
+  if (flip != 0) {
+    std::cerr << "shear-direction changes are not supported" << std::endl;
+    return 1;
+  }
+  std::vector<double> x, y, p, R, A;
+  double L = 0, gamma = 0, gamma_total = 0;
+  unsigned long t0 = 0;
+  if (file == "r") {
+    double phi = a.f("Packing Fraction");
+    double aspect = a.f("Aspect ratio (A/R)");
+    double bidisp = a.f("Bidispersity ratio (R2/R1)");
+    int config = a.more() ? a.i("Initial configuration (0: random)") : 0;
+    if (config != 0) {
+      std::cerr << "only random initial configurations (0) are supported" << std::endl;
+      return 1;
+    }
+    x.resize(n), y.resize(n), p.resize(n), R.resize(n), A.resize(n);
+    int rc = sc_generate_packing(n, phi, aspect, 0.5, bidisp, cli::env_int("SC_SEED", 0), 0.1,
+                                 x.data(), y.data(), p.data(), R.data(), A.data(), &L);
+    if (rc) return cli::fail("packing", rc);
+  } else {
+    int nf = 0;
+    double hdr[7];
+    int rc = sc_read_positions(file.c_str(), &nf, hdr, nullptr, nullptr, nullptr, nullptr, nullptr);
+    if (rc) return cli::fail("read", rc);
+    if (nf != n) std::cerr << "Warning: Number of particles in data file may not match requested number" << std::endl;
+    x.resize(nf), y.resize(nf), p.resize(nf), R.resize(nf), A.resize(nf);
+    rc = sc_read_positions(file.c_str(), &nf, hdr, x.data(), y.data(), p.data(), R.data(), A.data());
+    if (rc) return cli::fail("read", rc);
+    n = nf;
+    L = hdr[0];
+    gamma = hdr[3];
+    gamma_total = hdr[4];
+    if (hdr[5] != rate) std::cerr << "Warning: Strain rate in data file does not match the requested rate" << std::endl;
+    if (hdr[6] != dt) std::cerr << "Warning: Integration step size in data file does not match requested step" << std::endl;
+    t0 = cli::time_from_name(file);
+  }
+  auto start = std::chrono::steady_clock::now();
+  sc_options opt;
+  sc_default_options(&opt);
+  opt.precision = cli::precision();
+  sc_handle* h = nullptr;
+  int rc = sc_create(&opt, 1, &n, &L, &pad, x.data(), y.data(), p.data(), R.data(), A.data(), &h);
+  if (rc) return cli::fail("create", rc);
+  if ((rc = sc_set_strain_rate(h, -1, rate)) || (rc = sc_set_step(h, -1, dt)) ||
+      (rc = sc_set_gamma(h, -1, gamma)) || (rc = sc_set_total_gamma(h, -1, gamma_total)))
+    return cli::fail("setup", rc, h);
+  unsigned long t_end = 0;
+  rc = sc_run_strain(h, dir.c_str(), run, pos_save, se_save, t0, cli::out_format(), &t_end);
+  if (rc) return cli::fail("run", rc, h);
+  double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - start).count();
+  std::cout << "\nRun Time: " << secs << std::endl;
+  sc_destroy(h);
+  return 0;
+}

@@ -13,14 +13,14 @@
 #include "sc_host.hpp"
 #include "sc_internal.hpp"
 
-struct sc_handle {
-  sc::Handle h;
-};
+namespace sc {
+thread_local std::string g_noh_error;
+}
 
 namespace {
 
 const double kRefPi = 3.14159265358979;  // src/cpp/spherocyl_box.cpp:12
-thread_local std::string g_create_error;
+std::string& g_create_error = sc::g_noh_error;
 
 bool finite_all(const double* a, size_t n) {
   for (size_t i = 0; i < n; i++)
@@ -121,6 +121,8 @@ int sc_create(const sc_options* opt_in, int n_sys, const int* n_per_sys, const d
   h.block = opt.block > 0 ? opt.block : 128;
   h.nsys = n_sys;
   h.ntot = ntot;
+  h.h_R.assign(R, R + ntot);
+  h.h_A.assign(A, A + ntot);
   auto bail = [&](int code) {
     g_create_error = h.err.empty() ? std::string("sc_create failed") : h.err;
     delete H;

@@ -590,7 +590,7 @@ int Handle::run_steps(bool resize, int shrink, int nsteps, int se_every, double*
       pred_kind = kind;
     }
     bool aligned = se_every == 0 || done % se_every == 0;
-    bool use_graph = opt.use_graphs && !opt.profile && nk == kChunk && aligned;
+    bool use_graph = opt.use_graphs && !opt.profile && nk >= 16 && aligned;
     if (use_graph) {
       if (!run_graph(resize, nk, se_every)) return last_status;
     } else {
@@ -652,10 +652,26 @@ int Handle::calc(bool se, double* se_out) {
   return SC_OK;
 }
 
+// One fixed-size gradient step (gradient_relax_step, relaxation_dynamics.cpp:11-31)
+// for every system whose energy is still above e_min; a rebuild follows any step
+// that moved a particle beyond pad/2.
+int Handle::gd_step(const double* se_now, double e_min) {
+  std::vector<StepScalars> rows(nsys);
+  for (int q = 0; q < nsys; q++) {
+    rows[q] = row_current(q);
+    if (se_now && se_now[5 * q] <= e_min) rows[q].step = 0.0;  // this system has finished
+  }
+  if (!upload_table(rows)) return last_status;
+  launch_gd_update(d, prec == PREC_MIXED, d_tab, 0, stream);
+  launch_rebuild(d, prec == PREC_MIXED, d_tab, 0, stream);
+  kernels += 12;
+  pred_valid = false;
+  return cuda_ok(cudaGetLastError(), "gd step") ? SC_OK : last_status;
+}
+
 int Handle::gd_minimize(int max_steps, double e_min, int* steps_taken, double* e_final) {
   // gradient_descent_minimize, relaxation_dynamics.cpp:33-85: calc_se, test,
-  // then one fixed-size gradient step; a rebuild follows any step that moved a
-  // particle beyond pad/2.
+  // then one fixed-size gradient step.
   cudaSetDevice(device);
   std::vector<double> se(5 * (size_t)nsys);
   int s;
@@ -666,16 +682,8 @@ int Handle::gd_minimize(int max_steps, double e_min, int* steps_taken, double* e
     for (int q = 0; q < nsys; q++)
       if (!(se[5 * q] <= e_min)) all_done = false;
     if (all_done) break;
-    // one table row with the current scalars; the step size is per system
-    std::vector<StepScalars> rows(nsys);
-    for (int q = 0; q < nsys; q++) {
-      rows[q] = row_current(q);
-      if (se[5 * q] <= e_min) rows[q].step = 0.0;  // this system has finished
-    }
-    if (!upload_table(rows)) return last_status;
-    launch_gd_update(d, prec == PREC_MIXED, d_tab, 0, stream);
-    launch_rebuild(d, prec == PREC_MIXED, d_tab, 0, stream);
-    pred_valid = false;
+    rc = gd_step(se.data(), e_min);
+    if (rc) return rc;
   }
   if (steps_taken) *steps_taken = s;
   if (e_final) {

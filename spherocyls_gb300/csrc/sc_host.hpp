@@ -48,6 +48,7 @@ struct Handle {
   int block = 128;
   int nsys = 0, ntot = 0;
   std::vector<HostSys> hs;
+  std::vector<double> h_R, h_A;  // particle radii and half shafts, input order
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   Dev d{};
@@ -131,6 +132,14 @@ struct Handle {
   int calc(bool se, double* se_out);
   bool materialize();
   int gd_minimize(int max_steps, double e_min, int* steps_taken, double* e_final);
+  int gd_step(const double* se_now, double e_min);
 };
 
+// last error of calls made without a handle (creation, file reading)
+extern thread_local std::string g_noh_error;
+
 }  // namespace sc
+
+struct sc_handle {
+  sc::Handle h;
+};

@@ -1,0 +1,350 @@
+// sc_io.cpp -- position files, stress/energy time series and the run protocols that
+// write them (host code).
+//
+// Formats follow tmarschall/spherocyls:
+//  * src/cpp position file (save_positions, src/cpp/spherocyl_box.cpp:410-423):
+//    header "N L packing gamma gamma_total rate dt", rows "x y phi R A", written by
+//    an ostream with precision 14; files sp%010lu.dat.
+//  * src/cuda position file (save_positions, src/cuda/strain_dynamics.cu:820-843):
+//    header "%d %.17g %.17g %f %.17g %.14g %g %g" (N Lx Ly packing gamma gamma_total
+//    rate dt), rows "%.17g %.17g %.17g %.2g %.17g"; files sd%010lu.dat.
+//  * stress/energy lines: src/cpp "t E Pxx Pyy Pxy" with the ostream default
+//    precision (strain_dynamics.cpp:245,291,298), src/cuda "%lu %.7g x6"
+//    (t E Pxx Pyy P Pxy Pyx, strain_dynamics.cu:697).
+// The reader is the reference's DatFileInput with a header row
+// (src/cpp/file_input.h:24-76): whitespace-separated columns, header length 7
+// (one box length) or 8 (Lx, Ly; src/cuda/main.cpp:201).
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <iomanip>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/spherocyl.h"
+#include "sc_host.hpp"
+
+namespace {
+
+
+int io_fail(sc::Handle* h, int code, const std::string& msg) {
+  if (h) {
+    h->err = msg;
+    h->last_status = code;
+  } else {
+    sc::g_noh_error = msg;
+  }
+  return code;
+}
+
+std::string pos_name(const std::string& dir, const char* prefix, unsigned long t) {
+  char buf[32];
+  snprintf(buf, sizeof buf, "%s%010lu.dat", prefix, t);
+  return dir + "/" + buf;
+}
+
+// positions of one system in input order
+int system_state(sc_handle* H, int sys, std::vector<double>& x, std::vector<double>& y,
+                 std::vector<double>& p) {
+  sc::Handle& h = H->h;
+  std::vector<double> X(h.ntot), Y(h.ntot), P(h.ntot);
+  int rc = sc_get_state(H, X.data(), Y.data(), P.data());
+  if (rc) return rc;
+  const sc::HostSys& S = h.hs[sys];
+  x.assign(X.begin() + S.p0, X.begin() + S.p0 + S.n);
+  y.assign(Y.begin() + S.p0, Y.begin() + S.p0 + S.n);
+  p.assign(P.begin() + S.p0, P.begin() + S.p0 + S.n);
+  return SC_OK;
+}
+
+// One stress/energy record in the chosen layout.
+void se_line(std::ostream& o, int format, unsigned long t, const double* se, bool resize,
+             double packing) {
+  if (format == SC_FMT_SD) {
+    char buf[256];
+    if (resize)
+      snprintf(buf, sizeof buf, "%lu %.7g %.7g %.7g %.7g %.7g %.7g %.7g\n", t, packing, se[0],
+               se[1], se[2], 0.5 * (se[1] + se[2]), se[3], se[4]);
+    else
+      snprintf(buf, sizeof buf, "%lu %.7g %.7g %.7g %.7g %.7g %.7g\n", t, se[0], se[1], se[2],
+               0.5 * (se[1] + se[2]), se[3], se[4]);
+    o << buf;
+  } else {
+    o << t << " ";
+    if (resize) o << packing << " ";
+    o << se[0] << " " << se[1] << " " << se[2] << " " << se[3] << "\n";
+  }
+}
+
+// Open the stress/energy file: new at t_start == 0, else keep the lines up to the
+// one of time t_start and continue after it (the reference's continue,
+// strain_dynamics.cpp:248-279).
+int open_se(sc::Handle& h, const std::string& path, unsigned long t_start, std::ofstream& out) {
+  if (t_start == 0) {
+    out.open(path, std::ios::out | std::ios::trunc);
+    if (!out) return io_fail(&h, SC_E_IO, "cannot open " + path + " for writing");
+    return SC_OK;
+  }
+  std::ifstream in(path);
+  if (!in) return io_fail(&h, SC_E_IO, "cannot open " + path + " to continue");
+  std::string line, kept;
+  bool found = false;
+  while (std::getline(in, line)) {
+    kept += line + "\n";
+    unsigned long t = std::strtoul(line.c_str(), nullptr, 10);
+    if (!line.empty() && t == t_start) {
+      found = true;
+      break;
+    }
+  }
+  in.close();
+  if (!found) return io_fail(&h, SC_E_IO, "start time not found in " + path);
+  out.open(path, std::ios::out | std::ios::trunc);
+  if (!out) return io_fail(&h, SC_E_IO, "cannot rewrite " + path);
+  out << kept;
+  return SC_OK;
+}
+
+int check_single(sc_handle* H, const char* what) {
+  if (!H) return SC_E_ARG;
+  if (H->h.nsys != 1) return io_fail(&H->h, SC_E_ARG, std::string(what) + ": one system per handle");
+  return SC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sc_read_positions(const char* path, int* n, double* hdr, double* x, double* y, double* phi,
+                      double* R, double* A) {
+  sc::g_noh_error.clear();
+  if (!path || !n) return SC_E_ARG;
+  std::ifstream in(path);
+  if (!in) return io_fail(nullptr, SC_E_IO, std::string("cannot open ") + path);
+  std::string line;
+  if (!std::getline(in, line)) return io_fail(nullptr, SC_E_IO, std::string("empty file ") + path);
+  std::vector<double> head;
+  {
+    std::istringstream hs(line);
+    double v;
+    while (hs >> v) head.push_back(v);
+  }
+  if (head.size() != 7 && head.size() != 8)
+    return io_fail(nullptr, SC_E_IO, "header must have 7 or 8 fields");
+  int N = (int)head[0];
+  double out_hdr[7];
+  if (head.size() == 8) {
+    for (int k = 0; k < 7; k++) out_hdr[k] = head[k + 1];
+  } else {
+    out_hdr[0] = out_hdr[1] = head[1];
+    for (int k = 2; k < 7; k++) out_hdr[k] = head[k];
+  }
+  if (hdr) memcpy(hdr, out_hdr, sizeof out_hdr);
+  if (!x) {
+    *n = N;
+    return SC_OK;
+  }
+  if (*n < N) return io_fail(nullptr, SC_E_ARG, "arrays too short for the file");
+  int row = 0;
+  while (row < N && std::getline(in, line)) {
+    std::istringstream rs(line);
+    double v[5];
+    int k = 0;
+    while (k < 5 && rs >> v[k]) k++;
+    if (k == 0) continue;
+    if (k < 5) return io_fail(nullptr, SC_E_IO, "short row in position file");
+    x[row] = v[0];
+    y[row] = v[1];
+    phi[row] = v[2];
+    R[row] = v[3];
+    A[row] = v[4];
+    row++;
+  }
+  if (row != N) return io_fail(nullptr, SC_E_IO, "fewer rows than the header's N");
+  *n = N;
+  return SC_OK;
+}
+
+int sc_save_positions(sc_handle* H, int sys, const char* path, int format) {
+  if (!H || !path) return SC_E_ARG;
+  sc::Handle& h = H->h;
+  if (sys < 0 || sys >= h.nsys) return io_fail(&h, SC_E_ARG, "sc_save_positions: bad system");
+  std::vector<double> x, y, p;
+  int rc = system_state(H, sys, x, y, p);
+  if (rc) return rc;
+  const sc::HostSys& S = h.hs[sys];
+  double packing = S.packing * (h.hs[sys].Lx > 0 ? 1.0 : 0.0);
+  if (format == SC_FMT_SD) {
+    FILE* f = fopen(path, "w");
+    if (!f) return io_fail(&h, SC_E_IO, std::string("cannot open ") + path);
+    fprintf(f, "%d %.17g %.17g %f %.17g %.14g %g %g\n", S.n, S.Lx, S.Ly, packing, S.gamma,
+            S.gamma_total, S.strain_rate, S.step);
+    for (int k = 0; k < S.n; k++)
+      fprintf(f, "%.17g %.17g %.17g %.2g %.17g\n", x[k], y[k], p[k], h.h_R[S.p0 + k],
+              h.h_A[S.p0 + k]);
+    bool ok = fclose(f) == 0;
+    return ok ? SC_OK : io_fail(&h, SC_E_IO, std::string("write failed: ") + path);
+  }
+  std::ofstream o(path);
+  if (!o) return io_fail(&h, SC_E_IO, std::string("cannot open ") + path);
+  o.precision(14);
+  o << S.n << " " << S.Lx << " " << packing << " " << S.gamma << " " << S.gamma_total << " "
+    << S.strain_rate << " " << S.step << std::endl;
+  for (int k = 0; k < S.n; k++)
+    o << x[k] << " " << y[k] << " " << p[k] << " " << h.h_R[S.p0 + k] << " " << h.h_A[S.p0 + k]
+      << std::endl;
+  o.close();
+  return o ? SC_OK : io_fail(&h, SC_E_IO, std::string("write failed: ") + path);
+}
+
+int sc_run_strain(sc_handle* H, const char* out_dir, double run_gamma, double pos_save,
+                  double se_save, unsigned long t_start, int format, unsigned long* t_end) {
+  int rc = check_single(H, "sc_run_strain");
+  if (rc) return rc;
+  sc::Handle& h = H->h;
+  sc::HostSys& S = h.hs[0];
+  if (!out_dir || !(S.strain_rate != 0) || !(S.step > 0) || !(run_gamma >= 0))
+    return io_fail(&h, SC_E_ARG, "sc_run_strain: needs an output directory, rate != 0, dt > 0");
+  const double rate = S.strain_rate, dt = S.step;
+  // the drivers' clamps, src/cpp/main.cpp:87-90
+  if (se_save < rate * dt) se_save = rate * dt;
+  if (pos_save < rate) pos_save = rate;
+  const long nT = (long)(run_gamma / rate + 0.5);
+  const int nInt = (int)(1.0 / dt + 0.5);
+  const long nPos = std::max(1L, (long)(pos_save / rate + 0.5));
+  const int nSE = std::max(1, (int)(se_save / (rate * dt) + 0.5));
+  const std::string dir(out_dir);
+  const char* prefix = format == SC_FMT_SD ? "sd" : "sp";
+  const std::string se_path = dir + (format == SC_FMT_SD ? "/sd_stress_energy.dat" : "/sp_strain_se.dat");
+  std::ofstream se_out;
+  if ((rc = open_se(h, se_path, t_start, se_out))) return rc;
+  double se[5] = {0, 0, 0, 0, 0};
+  if (t_start == 0) {
+    if ((rc = sc_calc_se(H, se))) return rc;
+    se_line(se_out, format, 0, se, false, 0);
+    if ((rc = sc_save_positions(H, 0, pos_name(dir, prefix, 0).c_str(), format))) return rc;
+  } else if ((rc = sc_calc_forces(H))) {
+    return rc;
+  }
+  std::vector<double> rec((size_t)(nInt / nSE + 1) * 5);
+  for (unsigned long t = t_start + 1; t <= t_start + (unsigned long)nT; t++) {
+    rc = h.run_steps(false, 0, nInt, nSE, rec.data());
+    if (rc) return rc;
+    for (int k = 0; k < nInt / nSE; k++) {
+      memcpy(se, &rec[5 * (size_t)k], sizeof se);
+      se_line(se_out, format, t, se, false, 0);
+    }
+    if ((t * (unsigned long)nInt) % (unsigned long)nSE == 0) se_line(se_out, format, t, se, false, 0);
+    if (t % (unsigned long)nPos == 0) {
+      se_out.flush();
+      if ((rc = sc_save_positions(H, 0, pos_name(dir, prefix, t).c_str(), format))) return rc;
+    }
+  }
+  se_out.close();
+  unsigned long tend = t_start + (unsigned long)nT;
+  if ((rc = sc_save_positions(H, 0, pos_name(dir, prefix, tend).c_str(), format))) return rc;
+  if (t_end) *t_end = tend;
+  return SC_OK;
+}
+
+int sc_run_resize(sc_handle* H, const char* out_dir, double final_packing, double pos_save,
+                  double se_save, unsigned long t_start, int format, unsigned long* t_end) {
+  int rc = check_single(H, "sc_run_resize");
+  if (rc) return rc;
+  sc::Handle& h = H->h;
+  if (!out_dir || !(h.hs[0].resize_rate > 0 && h.hs[0].resize_rate < 1) || !(h.hs[0].step > 0) ||
+      !(final_packing > 0))
+    return io_fail(&h, SC_E_ARG, "sc_run_resize: needs an output directory, 0 < rate < 1, dt > 0");
+  const double rate = h.hs[0].resize_rate, dt = h.hs[0].step;
+  if (se_save < rate * dt) se_save = rate * dt;  // src/cpp/main_resize.cpp:283-286
+  if (pos_save < rate) pos_save = rate;
+  const int nInt = (int)(1.0 / dt + 0.5);
+  const long nPos = std::max(1L, (long)(pos_save / rate + 0.5));
+  const int nSE = std::max(1, (int)(se_save / (rate * dt) + 0.5));
+  const std::string dir(out_dir);
+  const char* prefix = format == SC_FMT_SD ? "sd" : "sp";
+  const std::string se_path = dir + "/sp_resize_se.dat";
+  // resize_box, resize_dynamics.cpp:246-330: packing follows the box area
+  const double parea = h.hs[0].packing * (h.hs[0].Lx * h.hs[0].Ly);
+  auto packing = [&]() { return parea / (h.hs[0].Lx * h.hs[0].Ly); };
+  const bool shrink = final_packing > packing();
+  std::ofstream se_out;
+  if ((rc = open_se(h, se_path, t_start, se_out))) return rc;
+  double se[5] = {0, 0, 0, 0, 0};
+  if (t_start == 0) {
+    if ((rc = sc_calc_se(H, se))) return rc;
+    se_line(se_out, format, 0, se, true, packing());
+    if ((rc = sc_save_positions(H, 0, pos_name(dir, prefix, 0).c_str(), format))) return rc;
+  } else if ((rc = sc_calc_forces(H))) {
+    return rc;
+  }
+  unsigned long t = t_start;
+  while (shrink ? final_packing > packing() : final_packing < packing()) {
+    t += 1;
+    // in segments of nSE steps so the packing of each record is the host's exact one
+    int done = 0;
+    while (done < nInt) {
+      int seg = std::min(nSE - (done % nSE), nInt - done);
+      bool rec_here = (done + seg) % nSE == 0;
+      double r5[5];
+      rc = h.run_steps(true, shrink ? 1 : 0, seg, rec_here ? seg : 0, rec_here ? r5 : nullptr);
+      if (rc) return rc;
+      done += seg;
+      if (rec_here) {
+        memcpy(se, r5, sizeof se);
+        se_line(se_out, format, t, se, true, packing());
+      }
+    }
+    h.hs[0].packing = packing();
+    if ((t * (unsigned long)nInt) % (unsigned long)nSE == 0) se_line(se_out, format, t, se, true, packing());
+    if (t % (unsigned long)nPos == 0) {
+      se_out.flush();
+      if ((rc = sc_save_positions(H, 0, pos_name(dir, prefix, t).c_str(), format))) return rc;
+    }
+  }
+  se_out.close();
+  if ((rc = sc_save_positions(H, 0, pos_name(dir, prefix, t).c_str(), format))) return rc;
+  if (t_end) *t_end = t;
+  return SC_OK;
+}
+
+int sc_run_minimize(sc_handle* H, const char* out_dir, int max_steps, double e_min,
+                    int pos_save_n, int* steps_taken) {
+  int rc = check_single(H, "sc_run_minimize");
+  if (rc) return rc;
+  sc::Handle& h = H->h;
+  if (!out_dir || max_steps < 0) return io_fail(&h, SC_E_ARG, "sc_run_minimize: bad arguments");
+  if (h.prec != sc::PREC_FP64)
+    return io_fail(&h, SC_E_STATE, "sc_run_minimize is the reference's FP64 protocol");
+  const std::string dir(out_dir);
+  const int nPos = std::max(1, pos_save_n);
+  std::ofstream se_out(dir + "/sr_strain_se.dat");
+  if (!se_out) return io_fail(&h, SC_E_IO, "cannot open " + dir + "/sr_strain_se.dat");
+  double se[5];
+  int s;
+  bool zero = false;
+  for (s = 0; s < max_steps; s++) {
+    if ((rc = sc_calc_se(H, se))) return rc;
+    se_out << s << " " << se[0] << " " << se[1] << " " << se[2] << " " << se[3] << std::endl;
+    if (se[0] <= e_min) {
+      if ((rc = sc_save_positions(H, 0, pos_name(dir, "sr", s).c_str(), SC_FMT_SP))) return rc;
+      zero = true;
+      break;
+    } else if (s % nPos == 0) {
+      if ((rc = sc_save_positions(H, 0, pos_name(dir, "sr", s).c_str(), SC_FMT_SP))) return rc;
+    }
+    if ((rc = h.gd_step(se, e_min))) return rc;
+  }
+  if (!zero) {
+    if ((rc = sc_calc_se(H, se))) return rc;
+    se_out << max_steps << " " << se[0] << " " << se[1] << " " << se[2] << " " << se[3] << std::endl;
+    if ((rc = sc_save_positions(H, 0, pos_name(dir, "sr", max_steps).c_str(), SC_FMT_SP)))
+      return rc;
+  }
+  if (steps_taken) *steps_taken = s;
+  return h.check_status("sc_run_minimize") ? SC_OK : h.last_status;
+}
+
+}  // extern "C"
