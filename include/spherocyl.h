@@ -50,6 +50,10 @@ extern "C" {
 #define SC_STRESS_COMPAT 0 /* stress exactly as src/cpp accumulates it (with its slips) */
 #define SC_STRESS_VIRIAL 1 /* the intended contact virial */
 
+#define SC_CONTACT_ONE 0 /* one closest-point contact per pair (src/cpp) */
+#define SC_CONTACT_TWO 1 /* up to two contacts per pair for near-parallel spines
+                          * (src/cuda/2point_dynamics.cu:385-546), used for jamming */
+
 #define SC_FMT_SP 0 /* src/cpp position file: "N L phi gamma gamma_tot rate dt" */
 #define SC_FMT_SD 1 /* src/cuda position file: "N Lx Ly phi gamma gamma_tot rate dt" */
 
@@ -63,6 +67,7 @@ typedef struct sc_options {
   int use_graphs;  /* capture step chunks in CUDA graphs (1) or launch eagerly (0) */
   int block;       /* threads per block of the mixed force pass, 0 = autotune */
   int profile;     /* record per-pass CUDA events inside run calls (sc_get_pass_times) */
+  int contact_model; /* SC_CONTACT_* */
 } sc_options;
 
 const char *sc_version(void);
@@ -111,6 +116,27 @@ int sc_resize_steps(sc_handle *h, int nsteps, int shrink, int se_every, double *
  * E <= e_min, else x += dt F.  *steps_taken receives the iterations done. */
 int sc_gd_minimize(sc_handle *h, int max_steps, double e_min, int *steps_taken,
                    double *e_final);
+
+/* Production minimiser: FIRE on every system of the handle, on the device, until
+ * every |F_i| and |tau_i|/sqrt(I_i) is below ftol, or max_iter iterations.  Replaces
+ * the reference's conjugate-gradient relaxation (cjpr_relax_2p,
+ * src/cuda/2point_dynamics.cu:4233-4295), whose line search returns to the host on
+ * every probe.  dt0/dt_max: initial and largest FIRE step.  Per-system outputs
+ * (may be NULL): fmax[s], done[s]; *iters the most iterations any system took.
+ * Returns SC_E_NOCONV when some system did not reach ftol. */
+int sc_fire_minimize(sc_handle *h, double ftol, int max_iter, double dt0, double dt_max,
+                     int *iters, double *fmax, int *done);
+/* Affine rescale of box and positions by factor (the src/cuda resize_coords,
+ * src/cuda/strain_dynamics.cu:1111-1122, as one step); sys = -1 for all. */
+int sc_affine_scale(sc_handle *h, int sys, double factor);
+/* Quasistatic compression to jamming: repeated affine steps raising each system's
+ * packing fraction by dphi, each followed by sc_fire_minimize(ftol, max_iter), until
+ * the system's energy per particle exceeds e_jam (compress_qs2p / find_jam_2p,
+ * src/cuda/2point_dynamics.cu:4299-4344, 4582-4606).  phi_jam[s] receives the
+ * packing fraction at which system s jammed (negated when max_increments ran out);
+ * *n_inc the increments made. */
+int sc_quasistatic_compress(sc_handle *h, double dphi, double ftol, double e_jam,
+                            int max_increments, int max_iter, double *phi_jam, int *n_inc);
 
 /* State readers, original particle order, systems concatenated. */
 int sc_get_state(sc_handle *h, double *x, double *y, double *phi);

@@ -102,6 +102,7 @@ class _Lib:
                          "set_total_gamma"):
                 setattr(self, name, fn(name, None, [handle, ctypes.c_double]))
             self.zero_pyx = fn("zero_pyx", None, [handle])
+            self.set_two_point = fn("set_two_point", None, [handle, ctypes.c_int])
         else:
             self.set_params = fn("set_params", None, [handle] + [ctypes.c_double] * 5)
 
@@ -128,7 +129,9 @@ class _BoxBase:
     kind = "orc"
 
     def __init__(self, L, x, y, phi, A, R, pad=0.0, *, strain_rate=0.0, resize_rate=0.0,
-                 step=0.05, gamma=0.0, total_gamma=0.0):
+                 step=0.05, gamma=0.0, total_gamma=0.0, two_point=False):
+        if two_point and self.kind != "orc":
+            raise ValueError("the two-point contact rule exists only in the restatement")
         self._L = _lib(self.kind)
         x, y, phi, A, R = (_f64(v) for v in (x, y, phi, A, R))
         self.n = int(x.shape[0])
@@ -138,6 +141,8 @@ class _BoxBase:
             raise RuntimeError("oracle box creation failed")
         self.set_params(strain_rate=strain_rate, resize_rate=resize_rate, step=step, gamma=gamma,
                         total_gamma=total_gamma)
+        if two_point:
+            self._L.set_two_point(self.h, 1)
         # The reference's constructor leaves the forces uninitialised (new Spherocyl[n]);
         # its run methods always call calc_se/calc_forces before the first step
         # (src/cpp/strain_dynamics.cpp:242-279), so do the same here.

@@ -68,6 +68,7 @@ struct orc_box {
   double E, Pxx, Pyy, Pxy, Pyx;
   long n_rebuilds;
   int err;
+  int two_point; /* contact model: 0 one point (src/cpp), 1 two points (src/cuda 2p) */
 };
 
 /* ---- per-particle constants and wrap: set_particle, spherocyl_box.cpp:188-221 ---- */
@@ -273,6 +274,125 @@ static void force_pair(orc_box *b, const pview *v, int p, int q, double gamma, d
   }
 }
 
+/* ---- two-point contacts: euler_est_2p, src/cuda/2point_dynamics.cu:385-546.
+ * PARITY UNPINNED: the reference implements this rule only in CUDA, which cannot
+ * run here, so this restatement is checked only against its own invariants (forces
+ * are the gradient of the summed contact energies) and the GPU kernels. ---- */
+static void one_contact(orc_box *b, const pview *v, int p, int q, double dX, double dY, double s,
+                        double t, double nxA, double nyA, double nxB, double nyB, double sig,
+                        double Lx, double Ly, int with_se) {
+  double dDx = dX + s * nxA - t * nxB;
+  double dDy = dY + s * nyA - t * nyB;
+  double dsq = dDx * dDx + dDy * dDy;
+  if (!(dsq < sig * sig)) return;
+  double dij = sqrt(dsq);
+  double dvij = (1.0 - dij / sig) / sig;
+  double Fx = dDx * dvij / dij, Fy = dDy * dvij / dij;
+  v->fx[p] += Fx;
+  v->fy[p] += Fy;
+  v->tau[p] += s * nxA * Fy - s * nyA * Fx;
+  v->fx[q] -= Fx;
+  v->fy[q] -= Fy;
+  v->tau[q] += t * nyB * Fx - t * nxB * Fy;
+  if (with_se) {
+    double LL = Lx * Ly;
+    double CxA = s * nxA - 0.5 * dDx, CyA = s * nyA - 0.5 * dDy;
+    double CxB = t * nxB + 0.5 * dDx, CyB = t * nyB + 0.5 * dDy;
+    b->E += dvij * sig * (1.0 - dij / sig) / (2.0 * b->n);
+    b->Pxx += Fx * CxA / LL - Fx * CxB / LL;
+    b->Pyy += Fy * CyA / LL - Fy * CyB / LL;
+    b->Pxy += Fy * CxA / LL - Fy * CxB / LL;
+    b->Pyx += Fx * CyA / LL - Fx * CyB / LL;
+  }
+}
+
+static double clamp1(double v) { return fmin(fmax(v, -1.0), 1.0); }
+
+static void force_pair2(orc_box *b, const pview *v, int p, int q, double gamma, double Lx,
+                        double Ly, int with_se) {
+  double dX = v->x[p] - v->x[q], dY = v->y[p] - v->y[q];
+  double sig = b->R[p] + b->R[q], aP = b->A[p], aQ = b->A[q];
+  dX += Lx * ((dX < -0.5 * Lx) - (dX > 0.5 * Lx));
+  dY += Ly * ((dY < -0.5 * Ly) - (dY > 0.5 * Ly));
+  dX += gamma * dY;
+  double nxA = aP * cos(v->phi[p]), nyA = aP * sin(v->phi[p]);
+  double nxB = aQ * cos(v->phi[q]), nyB = aQ * sin(v->phi[q]);
+  double a = aP * aP, bb = -(nxA * nxB + nyA * nyB), c = aQ * aQ;
+  double d = nxA * dX + nyA * dY, e = -nxB * dX - nyB * dY;
+  double delta = a * c - bb * bb;
+  double s1, t1, s2, t2, s3, t3;
+  if (delta <= 0) {
+    /* parallel spines: the two ends of the overlap */
+    s1 = clamp1(-(bb + d) / a);
+    s2 = clamp1(-(d - bb) / a);
+    if (fabs(s1) == 1)
+      t1 = clamp1(-(bb * s1 + e) / c);
+    else
+      t1 = bb < 0 ? clamp1(-(bb + e) / c) : clamp1(-(e - bb) / c);
+    if (fabs(s2) == 1)
+      t2 = clamp1(-(bb * s2 + e) / c);
+    else
+      t2 = bb < 0 ? clamp1(-(e - bb) / c) : clamp1(-(bb + e) / c);
+    s3 = s2;
+    t3 = t2;
+  } else {
+    t1 = clamp1((bb * d - a * e) / delta);
+    s1 = -(bb * t1 + d) / a;
+    double sarg = fabs(s1);
+    s1 = clamp1(s1);
+    if (sarg >= 1) {
+      /* primary contact at an end of A: the second candidate at A's other end */
+      t1 = clamp1(-(bb * s1 + e) / c);
+      s2 = -s1;
+      t2 = -(bb * s2 + e) / c;
+      double targ = fabs(t2);
+      t2 = clamp1(t2);
+      if (targ > 1) {
+        s2 = clamp1(-(bb * t2 + d) / a);
+        s3 = s2;
+        t3 = t2;
+      } else {
+        t3 = bb < 0 ? -s1 : s1;
+        s3 = -(bb * t3 + d) / a;
+        sarg = fabs(s3);
+        s3 = clamp1(s3);
+        if (sarg >= 1) t3 = clamp1(-(bb * s3 + e) / c);
+      }
+    } else {
+      /* primary contact at an end of B: the second candidate at B's other end */
+      t2 = -t1;
+      s2 = -(bb * t2 + d) / a;
+      sarg = fabs(s2);
+      s2 = clamp1(s2);
+      if (sarg > 1) {
+        t2 = clamp1(-(bb * s2 + e) / c);
+        s3 = s2;
+        t3 = t2;
+      } else {
+        s3 = bb < 0 ? -t1 : t1;
+        t3 = -(bb * s3 + e) / c;
+        double targ = fabs(t3);
+        t3 = clamp1(t3);
+        if (targ >= 1) s3 = clamp1(-(bb * t3 + d) / a);
+      }
+    }
+  }
+  one_contact(b, v, p, q, dX, dY, s1, t1, nxA, nyA, nxB, nyB, sig, Lx, Ly, with_se);
+  if (s1 != s2 && t1 != t2) {
+    if (s3 != s1 && s3 != s2) {
+      double x2 = dX + s2 * nxA - t2 * nxB, y2 = dY + s2 * nyA - t2 * nyB;
+      double x3 = dX + s3 * nxA - t3 * nxB, y3 = dY + s3 * nyA - t3 * nyB;
+      if (x3 * x3 + y3 * y3 < x2 * x2 + y2 * y2) {
+        s2 = s3;
+        t2 = t3;
+      }
+    }
+    one_contact(b, v, p, q, dX, dY, s2, t2, nxA, nyA, nxB, nyB, sig, Lx, Ly, with_se);
+  }
+}
+
+void orc_set_two_point(orc_box *b, int on) { b->two_point = on != 0; }
+
 static void zero3(double *a, double *b2, double *c, int n) {
   for (int i = 0; i < n; i++) {
     a[i] = 0.0;
@@ -286,7 +406,12 @@ static void loop_pairs(orc_box *b, const pview *v, double gamma, double Lx, doub
     const ivec *nl = &b->nbrs[p];
     for (int j = 0; j < nl->len; j++) {
       int q = nl->data[j];
-      if (q > p) force_pair(b, v, p, q, gamma, Lx, Ly, with_se);
+      if (q > p) {
+        if (b->two_point)
+          force_pair2(b, v, p, q, gamma, Lx, Ly, with_se);
+        else
+          force_pair(b, v, p, q, gamma, Lx, Ly, with_se);
+      }
     }
   }
 }

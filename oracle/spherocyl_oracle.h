@@ -24,6 +24,7 @@ void orc_set_step(orc_box *b, double v);
 void orc_set_gamma(orc_box *b, double v);
 void orc_set_total_gamma(orc_box *b, double v);
 void orc_zero_pyx(orc_box *b);
+void orc_set_two_point(orc_box *b, int on);
 
 void orc_find_neighbors(orc_box *b);
 void orc_calc_forces(orc_box *b);

@@ -41,6 +41,7 @@ class ScOptions(ctypes.Structure):
         ("use_graphs", ctypes.c_int),
         ("block", ctypes.c_int),
         ("profile", ctypes.c_int),
+        ("contact_model", ctypes.c_int),
     ]
 
 
@@ -66,6 +67,12 @@ SIGNATURES = [
     ("sc_strain_steps", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp]),
     ("sc_resize_steps", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp]),
     ("sc_gd_minimize", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double, _ip, _dp]),
+    ("sc_fire_minimize", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_int, ctypes.c_double,
+                                        ctypes.c_double, _ip, _dp, _ip]),
+    ("sc_affine_scale", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double]),
+    ("sc_quasistatic_compress", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_double,
+                                               ctypes.c_double, ctypes.c_int, ctypes.c_int, _dp,
+                                               _ip]),
     ("sc_get_state", ctypes.c_int, [_vp, _dp, _dp, _dp]),
     ("sc_get_forces", ctypes.c_int, [_vp, _dp, _dp, _dp]),
     ("sc_get_box", ctypes.c_int, [_vp, ctypes.c_int, _dp]),

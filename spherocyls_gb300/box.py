@@ -66,7 +66,8 @@ class BoxBatch:
 
     def __init__(self, n_per_sys, L, x, y, phi, A, R, pad=0.0, *, precision: str = "fp64",
                  stress: str = "compat", device: int = 0, max_nbrs: int = 0,
-                 use_graphs: bool = True, block: int = 0, profile: bool = False):
+                 use_graphs: bool = True, block: int = 0, profile: bool = False,
+                 contacts: int = 1):
         n_per_sys = np.ascontiguousarray(np.atleast_1d(n_per_sys), dtype=np.int32)
         self.nsys = int(n_per_sys.shape[0])
         self.n_per_sys = n_per_sys
@@ -86,6 +87,9 @@ class BoxBatch:
         opt.use_graphs = int(bool(use_graphs))
         opt.block = int(block)
         opt.profile = int(bool(profile))
+        if int(contacts) not in (1, 2):
+            raise ValueError("contacts must be 1 (one contact per pair) or 2")
+        opt.contact_model = 1 if int(contacts) == 2 else 0
         self.precision = precision
         h = ctypes.c_void_p()
         st = lib().sc_create(ctypes.byref(opt), self.nsys,
@@ -173,6 +177,33 @@ class BoxBatch:
         self._chk(lib().sc_gd_minimize(self.h, int(max_steps), float(e_min), ctypes.byref(steps),
                                        ctypes.byref(ef)))
         return steps.value, ef.value
+
+    # --- minimisation and quasistatic compression -------------------------------
+    def fire_minimize(self, ftol: float, max_iter: int = 100000, dt0: float = 1e-2,
+                      dt_max: float = 0.2):
+        """FIRE until max|F| < ftol per system; returns (iters, fmax[nsys], done[nsys])."""
+        it = ctypes.c_int()
+        fm = np.empty(self.nsys)
+        dn = np.empty(self.nsys, dtype=np.int32)
+        st = lib().sc_fire_minimize(self.h, float(ftol), int(max_iter), float(dt0), float(dt_max),
+                                    ctypes.byref(it), _ptr(fm),
+                                    dn.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+        if st not in (0, _lib.SC_E_NOCONV):
+            self._chk(st)
+        return it.value, fm, dn.astype(bool)
+
+    def affine_scale(self, factor: float, sys: int = -1):
+        self._chk(lib().sc_affine_scale(self.h, int(sys), float(factor)))
+
+    def quasistatic_compress(self, dphi: float, ftol: float, e_jam: float,
+                             max_increments: int = 100000, max_iter: int = 100000):
+        """Affine steps of dphi + FIRE until E/N > e_jam; returns (phi_jam[nsys], n_inc)."""
+        pj = np.empty(self.nsys)
+        n = ctypes.c_int()
+        self._chk(lib().sc_quasistatic_compress(self.h, float(dphi), float(ftol), float(e_jam),
+                                                int(max_increments), int(max_iter), _ptr(pj),
+                                                ctypes.byref(n)))
+        return pj, n.value
 
     # --- runs with file output (single-system handles) -------------------------
     def save_positions(self, path: str, fmt: str = "sp", sys: int = 0):

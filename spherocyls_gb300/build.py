@@ -28,6 +28,7 @@ CU_UNITS = {
     "sc_cells.cu": False,
     "sc_pass_mixed.cu": True,
     "sc_noalloc.cu": False,
+    "sc_fire.cu": True,
 }
 CPP_UNITS = ["sc_host.cpp", "sc_api.cpp", "sc_generate.cpp", "sc_io.cpp"]
 CLI_UNITS = {

@@ -60,6 +60,7 @@ void sc_default_options(sc_options* opt) {
   opt->use_graphs = 1;
   opt->block = 0;
   opt->profile = 0;
+  opt->contact_model = SC_CONTACT_ONE;
 }
 
 const char* sc_last_error(const sc_handle* h) {
@@ -84,6 +85,10 @@ int sc_create(const sc_options* opt_in, int n_sys, const int* n_per_sys, const d
     sc_default_options(&opt);
   if (opt.precision != SC_PREC_FP64 && opt.precision != SC_PREC_MIXED) {
     g_create_error = "sc_create: unknown precision";
+    return SC_E_ARG;
+  }
+  if (opt.contact_model != SC_CONTACT_ONE && opt.contact_model != SC_CONTACT_TWO) {
+    g_create_error = "sc_create: unknown contact model";
     return SC_E_ARG;
   }
   long long ntot_ll = 0;
@@ -176,6 +181,7 @@ int sc_create(const sc_options* opt_in, int n_sys, const int* n_per_sys, const d
   d.ntot = ntot;
   d.nsys = n_sys;
   d.stress_mode = opt.stress_mode == SC_STRESS_VIRIAL ? sc::STRESS_VIRIAL : sc::STRESS_COMPAT;
+  d.contact_model = opt.contact_model == SC_CONTACT_TWO ? 1 : 0;
   d.maxn = opt.max_nbrs > 0 ? opt.max_nbrs : 64;
   std::vector<int> pchunk_sys, pchunk_p0, pchunk_np;
   for (int s = 0; s < n_sys; s++) {
@@ -504,6 +510,31 @@ int sc_get_pairs(sc_handle* H, int sys, int* pairs, long cap, long* n_pairs) {
       pairs[2 * k + 1] = pr[k].second;
     }
   return SC_OK;
+}
+
+int sc_fire_minimize(sc_handle* H, double ftol, int max_iter, double dt0, double dt_max,
+                     int* iters, double* fmax, int* done) {
+  if (!H) return SC_E_ARG;
+  return H->h.fire_minimize(ftol, max_iter, dt0, dt_max, iters, fmax, done);
+}
+
+int sc_affine_scale(sc_handle* H, int sys, double factor) {
+  if (!H) return SC_E_ARG;
+  sc::Handle& h = H->h;
+  if (sys < -1 || sys >= h.nsys || !(factor > 0) || !std::isfinite(factor)) {
+    h.fail(SC_E_ARG, "sc_affine_scale: bad system index or factor");
+    return SC_E_ARG;
+  }
+  std::vector<double> f(h.nsys, 1.0);
+  for (int s = 0; s < h.nsys; s++)
+    if (sys < 0 || s == sys) f[s] = factor;
+  return h.affine_scale(f);
+}
+
+int sc_quasistatic_compress(sc_handle* H, double dphi, double ftol, double e_jam,
+                            int max_increments, int max_iter, double* phi_jam, int* n_inc) {
+  if (!H) return SC_E_ARG;
+  return H->h.quasistatic(dphi, ftol, e_jam, max_increments, max_iter, phi_jam, n_inc);
 }
 
 int sc_get_counters(sc_handle* H, long long* out) {

@@ -244,6 +244,10 @@ __global__ void k_rb_gather(Dev d) {
   double2 mv = d.nxy_t[src];
   d.v0x[i] = mv.x;
   d.v0y[i] = mv.y;
+  if (d.fvx) {  // minimiser velocities travel with their particles (predictor copy is dead here)
+    d.xy_t[i] = make_double2(d.fvx[src], d.fvy[src]);
+    d.ph_t[i] = d.fvp[src];
+  }
 }
 
 __global__ void k_rb_commit(Dev d, const StepScalars* __restrict__ tab, int row, int mixed) {
@@ -262,6 +266,12 @@ __global__ void k_rb_commit(Dev d, const StepScalars* __restrict__ tab, int row,
   d.id[i] = d.s_id[i];
   d.cell[i] = d.s_cell[i];
   d.moved[i] = make_double2(d.v0x[i], d.v0y[i]);
+  if (d.fvx) {
+    double2 v = d.xy_t[i];
+    d.fvx[i] = v.x;
+    d.fvy[i] = v.y;
+    d.fvp[i] = d.ph_t[i];
+  }
   if (!mixed) {
     double sn, cs;
     sincos(phi, &sn, &cs);

@@ -694,4 +694,145 @@ int Handle::gd_minimize(int max_steps, double e_min, int* steps_taken, double* e
   return check_status("gd minimize") ? SC_OK : last_status;
 }
 
+// ---- FIRE minimiser, affine rescale, quasistatic compression ----
+
+bool Handle::ensure_fire() {
+  if (fire.vx) return true;
+  double *vx = nullptr, *vy = nullptr, *vp = nullptr, *part = nullptr;
+  FireSys* sys = nullptr;
+  if (!dalloc(&vx, ntot, "fire vx") || !dalloc(&vy, ntot, "fire vy") ||
+      !dalloc(&vp, ntot, "fire vp") || !dalloc(&sys, nsys, "fire sys") ||
+      !dalloc(&part, 4 * (size_t)d.npchunks, "fire partials"))
+    return false;
+  fire.vx = vx;
+  fire.vy = vy;
+  fire.vp = vp;
+  fire.sys = sys;
+  fire.part = part;
+  d.fvx = vx;  // the rebuild permutes the minimiser's velocities from now on
+  d.fvy = vy;
+  d.fvp = vp;
+  invalidate_graph();
+  return true;
+}
+
+// FIRE on every system until max |F| < ftol (or max_iter iterations); the host
+// looks at the per-system state only between chunks of iterations.
+int Handle::fire_minimize(double ftol, int max_iter, double dt0, double dt_max, int* iters,
+                          double* fmax_out, int* done_out) {
+  if (!(ftol > 0) || max_iter < 0 || !(dt0 > 0) || !(dt_max >= dt0)) {
+    fail(SC_E_ARG, "fire: need ftol > 0, max_iter >= 0, 0 < dt0 <= dt_max");
+    return SC_E_ARG;
+  }
+  cudaSetDevice(device);
+  if (!ensure_fire()) return last_status;
+  std::vector<StepScalars> rows(nsys);
+  for (int s = 0; s < nsys; s++) rows[s] = row_current(s);
+  if (!upload_table(rows)) return last_status;
+  launch_fire_reset(d, fire, dt0, stream);
+  std::vector<FireSys> hsys(nsys);
+  const bool mixed = prec == PREC_MIXED;
+  int it = 0;
+  bool all_done = false;
+  while (it < max_iter && !all_done) {
+    int chunk = std::min(50, max_iter - it);
+    for (int k = 0; k < chunk; k++) {
+      launch_pass(PASS_FORCE, false, 0);
+      launch_fire_iteration_tail(d, fire, ftol, dt_max, mixed, stream);
+      // the mixed form moves only its FP32 local state: the flagged systems'
+      // FP64 copies are refreshed before the cell sort reads them
+      if (mixed) launch_mx_materialize(d, d_tab, 0, false, stream);
+      launch_rebuild(d, mixed, d_tab, 0, stream);
+      kernels += 3 + (mixed ? 13 : 11);
+    }
+    it += chunk;
+    if (!cuda_ok(cudaGetLastError(), "fire launch") ||
+        !cuda_ok(cudaMemcpyAsync(hsys.data(), fire.sys, nsys * sizeof(FireSys),
+                                 cudaMemcpyDeviceToHost, stream), "fire state") ||
+        !check_status("fire"))
+      return last_status;
+    all_done = true;
+    for (auto& q : hsys) all_done = all_done && q.done;
+  }
+  pred_valid = false;
+  forces_valid = false;
+  if (mixed) fp64_valid = false;
+  int max_it = 0;
+  for (int s = 0; s < nsys; s++) {
+    if (fmax_out) fmax_out[s] = hsys[s].fmax;
+    if (done_out) done_out[s] = hsys[s].done;
+    max_it = std::max(max_it, hsys[s].iters);
+  }
+  if (iters) *iters = max_it;
+  return all_done ? SC_OK : SC_E_NOCONV;
+}
+
+// Box and positions of each system scaled by factor[s] (1 leaves it alone).
+int Handle::affine_scale(const std::vector<double>& factor) {
+  cudaSetDevice(device);
+  if (!materialize()) return last_status;
+  double* dfac = nullptr;
+  if (!dalloc(&dfac, nsys, "factors")) return last_status;
+  bool ok = cuda_ok(cudaMemcpyAsync(dfac, factor.data(), nsys * sizeof(double),
+                                    cudaMemcpyHostToDevice, stream), "factors");
+  if (ok) launch_affine(d, dfac, stream);
+  ok = ok && cuda_ok(cudaStreamSynchronize(stream), "affine");
+  dfree(dfac);
+  if (!ok) return last_status;
+  bool regrid = false;
+  for (int s = 0; s < nsys; s++) {
+    if (factor[s] == 1.0) continue;
+    HostSys& h = hs[s];
+    double old = h.Lx;
+    h.Lx *= factor[s];
+    h.Ly *= factor[s];
+    h.packing *= (old / h.Lx) * (old / h.Lx);
+    int r = h.rows, c = h.cols;
+    h.configure(false);
+    if (h.rows != r || h.cols != c) regrid = true;
+  }
+  if (regrid && !layout_cells()) return last_status;
+  return rebuild_all() && check_status("affine scale") ? SC_OK : last_status;
+}
+
+// Quasistatic compression to jamming: affine steps of dphi in packing fraction,
+// each followed by a FIRE minimisation; a system stops once its energy per
+// particle after minimisation exceeds e_jam (compress_qs2p / find_jam_2p,
+// src/cuda/2point_dynamics.cu:4299-4344, 4582-4606, with FIRE for the relaxation).
+int Handle::quasistatic(double dphi, double ftol, double e_jam, int max_inc, int max_iter,
+                        double* phi_jam, int* n_inc) {
+  if (!(dphi > 0) || !(e_jam >= 0) || max_inc < 0) {
+    fail(SC_E_ARG, "quasistatic: need dphi > 0, e_jam >= 0, max_inc >= 0");
+    return SC_E_ARG;
+  }
+  std::vector<char> jammed(nsys, 0);
+  std::vector<double> se(5 * (size_t)nsys);
+  int inc = 0;
+  int rc = fire_minimize(ftol, max_iter, 1e-2, 0.2, nullptr, nullptr, nullptr);
+  if (rc && rc != SC_E_NOCONV) return rc;
+  for (inc = 0; inc < max_inc; inc++) {
+    std::vector<double> f(nsys, 1.0);
+    bool any = false;
+    for (int s = 0; s < nsys; s++)
+      if (!jammed[s]) {
+        f[s] = std::sqrt(hs[s].packing / (hs[s].packing + dphi));
+        any = true;
+      }
+    if (!any) break;
+    if ((rc = affine_scale(f))) return rc;
+    rc = fire_minimize(ftol, max_iter, 1e-2, 0.2, nullptr, nullptr, nullptr);
+    if (rc && rc != SC_E_NOCONV) return rc;
+    if ((rc = calc(true, se.data()))) return rc;
+    for (int s = 0; s < nsys; s++)
+      if (!jammed[s] && se[5 * s] > e_jam) {
+        jammed[s] = 1;
+        if (phi_jam) phi_jam[s] = hs[s].packing;
+      }
+  }
+  for (int s = 0; s < nsys; s++)
+    if (!jammed[s] && phi_jam) phi_jam[s] = -hs[s].packing;  // not jammed: negative
+  if (n_inc) *n_inc = inc;
+  return SC_OK;
+}
+
 }  // namespace sc

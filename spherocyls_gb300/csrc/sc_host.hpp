@@ -133,6 +133,14 @@ struct Handle {
   bool materialize();
   int gd_minimize(int max_steps, double e_min, int* steps_taken, double* e_final);
   int gd_step(const double* se_now, double e_min);
+  // FIRE minimiser and quasistatic compression
+  FireState fire{};
+  bool ensure_fire();
+  int fire_minimize(double ftol, int max_iter, double dt0, double dt_max, int* iters,
+                    double* fmax_out, int* done_out);
+  int affine_scale(const std::vector<double>& factor);
+  int quasistatic(double dphi, double ftol, double e_jam, int max_inc, int max_iter,
+                  double* phi_jam, int* n_inc);
 };
 
 // last error of calls made without a handle (creation, file reading)

@@ -54,11 +54,28 @@ struct StepScalars {
   float f_pad_;
 };
 
+// FIRE minimiser state of one system
+struct FireSys {
+  double dt, alpha;  // current time step and mixing parameter
+  double c1, c2;     // mixing coefficients of the coming update: v <- c1 v + c2 F/m
+  double fmax;       // largest |F_i| (or |tau_i|/sqrt(I_i)) at the last evaluation
+  int npos, zero_v, done, iters;
+};
+
+struct FireState {
+  double* vx;
+  double* vy;
+  double* vp;
+  FireSys* sys;   // [nsys]
+  double* part;   // [4 * npchunks] chunk partials
+};
+
 // Device pointers handed to every kernel by value.
 struct Dev {
   int ntot, nsys, ncells, nchunks, npchunks;
   int maxn;                 // neighbour-list capacity per particle (FP64 form)
   int stress_mode;
+  int contact_model;        // 0 one contact point (src/cpp), 1 two points (src/cuda 2p)
   const SysGeom* geom;      // [nsys]
   const int* psys;          // [ntot] system of each slot
   const int* cell_sys;      // [ncells] system of each cell
@@ -121,6 +138,9 @@ struct Dev {
   const int* pchunk_p0;
   const int* pchunk_np;
   // flags
+  double* fvx;              // FIRE velocities (null until the minimiser is used);
+  double* fvy;              // permuted with the particles by the rebuild
+  double* fvp;
   int* flags;               // [nsys] bit0 moved-rebuild, bit1 forced rebuild
   int* istar;               // [nsys] lowest particle index that triggered a rebuild
   int* any;                 // [1] set when any system needs a rebuild
@@ -165,6 +185,11 @@ void launch_se_store(const Dev& d, double* dst, cudaStream_t st);
 void launch_refresh_geometry(const Dev& d, bool mixed, const StepScalars* tab, int row,
                              cudaStream_t st);
 void launch_build_nbrs(const Dev& d, const StepScalars* tab, int row, cudaStream_t st);
+// FIRE and affine rescale
+void launch_fire_reset(const Dev& d, const FireState& f, double dt0, cudaStream_t st);
+void launch_fire_iteration_tail(const Dev& d, const FireState& f, double ftol, double dt_max,
+                                bool mixed, cudaStream_t st);
+void launch_affine(const Dev& d, const double* factor, cudaStream_t st);
 // mixed form
 void launch_mx_materialize(const Dev& d, const StepScalars* tab, int row, bool all,
                            cudaStream_t st);

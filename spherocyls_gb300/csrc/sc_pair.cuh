@@ -141,6 +141,269 @@ __device__ __forceinline__ bool pair_fp32(float dX, float dY, float nxA, float n
   return true;
 }
 
+// ---- two-point contacts (src/cuda/2point_dynamics.cu:385-546, euler_est_2p) ----
+//
+// For nearly parallel overlapping spines the single closest-point pair jumps from
+// one end of the overlap to the other as the relative angle changes sign, which
+// puts a cusp in the energy at alignment.  The reference's jamming code adds a
+// second contact at the other end of the overlap (the closer of two candidates),
+// each contact carrying its own harmonic overlap energy.  These functions return
+// the spine parameters of both contacts in the reference's case analysis; has2 is
+// false when the second candidate coincides with the first.
+template <class T>
+struct Contacts2 {
+  T s1, t1, s2, t2;
+  bool has2;
+};
+
+__device__ __forceinline__ Contacts2<double> contacts2_fp64(double a, double b, double c, double d,
+                                                            double e, double delta, double dX,
+                                                            double dY, double nxA, double nyA,
+                                                            double nxB, double nyB) {
+  double s1, t1, s2, t2, s3, t3;
+  if (delta <= 0) {
+    s1 = fmin(fmax(-(b + d) / a, -1.0), 1.0);
+    s2 = fmin(fmax(-(d - b) / a, -1.0), 1.0);
+    if (fabs(s1) == 1)
+      t1 = fmin(fmax(-(b * s1 + e) / c, -1.0), 1.0);
+    else if (b < 0)
+      t1 = fmin(fmax(-(b + e) / c, -1.0), 1.0);
+    else
+      t1 = fmin(fmax(-(e - b) / c, -1.0), 1.0);
+    if (fabs(s2) == 1)
+      t2 = fmin(fmax(-(b * s2 + e) / c, -1.0), 1.0);
+    else if (b < 0)
+      t2 = fmin(fmax(-(e - b) / c, -1.0), 1.0);
+    else
+      t2 = fmin(fmax(-(b + e) / c, -1.0), 1.0);
+    s3 = s2;
+    t3 = t2;
+  } else {
+    t1 = fmin(fmax((b * d - a * e) / delta, -1.), 1.);
+    s1 = -(b * t1 + d) / a;
+    double sarg = fabs(s1);
+    s1 = fmin(fmax(s1, -1.), 1.);
+    if (sarg >= 1) {
+      t1 = fmin(fmax(-(b * s1 + e) / c, -1.), 1.);
+      s2 = -s1;
+      t2 = -(b * s2 + e) / c;
+      double targ = fabs(t2);
+      t2 = fmin(fmax(t2, -1.), 1.);
+      if (targ > 1) {
+        s2 = fmin(fmax(-(b * t2 + d) / a, -1.), 1.);
+        s3 = s2;
+        t3 = t2;
+      } else {
+        t3 = b < 0 ? -s1 : s1;
+        s3 = -(b * t3 + d) / a;
+        sarg = fabs(s3);
+        s3 = fmin(fmax(s3, -1.0), 1.0);
+        if (sarg >= 1) t3 = fmin(fmax(-(b * s3 + e) / c, -1.0), 1.0);
+      }
+    } else {
+      t2 = -t1;
+      s2 = -(b * t2 + d) / a;
+      sarg = fabs(s2);
+      s2 = fmin(fmax(s2, -1.), 1.);
+      if (sarg > 1) {
+        t2 = fmin(fmax(-(b * s2 + e) / c, -1.), 1.);
+        s3 = s2;
+        t3 = t2;
+      } else {
+        s3 = b < 0 ? -t1 : t1;
+        t3 = -(b * s3 + e) / c;
+        double targ = fabs(t3);
+        t3 = fmin(fmax(t3, -1.0), 1.0);
+        if (targ >= 1) s3 = fmin(fmax(-(b * t3 + d) / a, -1.0), 1.0);
+      }
+    }
+  }
+  Contacts2<double> r;
+  r.s1 = s1;
+  r.t1 = t1;
+  r.has2 = (s1 != s2 && t1 != t2);
+  if (r.has2 && s3 != s1 && s3 != s2) {
+    double x2 = dX + s2 * nxA - t2 * nxB, y2 = dY + s2 * nyA - t2 * nyB;
+    double x3 = dX + s3 * nxA - t3 * nxB, y3 = dY + s3 * nyA - t3 * nyB;
+    if (x3 * x3 + y3 * y3 < x2 * x2 + y2 * y2) {
+      s2 = s3;
+      t2 = t3;
+    }
+  }
+  r.s2 = s2;
+  r.t2 = t2;
+  return r;
+}
+
+// One harmonic contact at spine parameters (s, t); accumulates into o (no SE arms
+// beyond the virial form: the two-point model is the reference's jamming path).
+template <bool SE>
+__device__ __forceinline__ bool contact_fp64(double dX, double dY, double s, double t, double nxA,
+                                             double nyA, double nxB, double nyB, double sig,
+                                             double LL, double two_n, PairF64& o) {
+  double dDx = dX + s * nxA - t * nxB;
+  double dDy = dY + s * nyA - t * nyB;
+  double dsq = dDx * dDx + dDy * dDy;
+  if (!(dsq < sig * sig)) return false;
+  double dij = sqrt(dsq);
+  double dvij = (1.0 - dij / sig) / sig;
+  double Fx = dDx * dvij / dij;
+  double Fy = dDy * dvij / dij;
+  o.fx += Fx;
+  o.fy += Fy;
+  o.tp += s * nxA * Fy - s * nyA * Fx;
+  o.tq += t * nyB * Fx - t * nxB * Fy;
+  if (SE) {
+    double CxA = s * nxA - 0.5 * dDx, CyA = s * nyA - 0.5 * dDy;
+    double CxB = t * nxB + 0.5 * dDx, CyB = t * nyB + 0.5 * dDy;
+    o.e += dvij * sig * (1.0 - dij / sig) / two_n;
+    o.pxx += Fx * CxA / LL - Fx * CxB / LL;
+    o.pyy += Fy * CyA / LL - Fy * CyB / LL;
+    o.pxy += Fy * CxA / LL - Fy * CxB / LL;
+    o.pyx += Fx * CyA / LL - Fx * CyB / LL;
+  }
+  return true;
+}
+
+// Two-point contact pair in FP64 (minimum image and Lees-Edwards shift applied
+// here, as in pair_fp64).  Stress uses the virial arms.
+template <bool SE>
+__device__ __forceinline__ bool pair2_fp64(double dX, double dY, double nxA, double nyA,
+                                           double aP, double nxB, double nyB, double aQ,
+                                           double sig, double gamma, double Lx, double Ly,
+                                           double two_n, PairF64& o) {
+  dX += Lx * (double)((dX < -0.5 * Lx) - (dX > 0.5 * Lx));
+  dY += Ly * (double)((dY < -0.5 * Ly) - (dY > 0.5 * Ly));
+  dX += gamma * dY;
+  double a = aP * aP;
+  double b = -(nxA * nxB + nyA * nyB);
+  double c = aQ * aQ;
+  double d = nxA * dX + nyA * dY;
+  double e = -nxB * dX - nyB * dY;
+  double delta = a * c - b * b;
+  Contacts2<double> k = contacts2_fp64(a, b, c, d, e, delta, dX, dY, nxA, nyA, nxB, nyB);
+  o.fx = o.fy = o.tp = o.tq = 0.0;
+  o.e = o.pxx = o.pyy = o.pxy = o.pyx = 0.0;
+  const double LL = Lx * Ly;
+  bool hit = contact_fp64<SE>(dX, dY, k.s1, k.t1, nxA, nyA, nxB, nyB, sig, LL, two_n, o);
+  if (k.has2) hit |= contact_fp64<SE>(dX, dY, k.s2, k.t2, nxA, nyA, nxB, nyB, sig, LL, two_n, o);
+  return hit;
+}
+
+// Two-point contact pair in FP32 on a displacement already reduced to the minimum
+// image (as pair_fp32); the primary parameter uses the cross-product form.
+__device__ __forceinline__ bool contact_fp32(float dX, float dY, float s, float t, float nxA,
+                                             float nyA, float nxB, float nyB, float sig,
+                                             PairF32& o) {
+  float dDx = dX + s * nxA - t * nxB;
+  float dDy = dY + s * nyA - t * nyB;
+  float dsq = dDx * dDx + dDy * dDy;
+  if (!(dsq < sig * sig)) return false;
+  float inv_d = rsqrtf(dsq);
+  float inv_sig = __frcp_rn(sig);
+  float ov = 1.f - dsq * inv_d * inv_sig;
+  float f = ov * inv_sig * inv_d;
+  float Fx = dDx * f, Fy = dDy * f;
+  o.fx += Fx;
+  o.fy += Fy;
+  o.tp += s * (nxA * Fy - nyA * Fx);
+  o.tq += t * (nyB * Fx - nxB * Fy);
+  o.ov += ov * ov;  // sum of squared overlaps of the contacts
+  // stress: virial arms summed over the contacts, as force-weighted terms
+  o.cxa += Fx * (s * nxA - 0.5f * dDx - t * nxB - 0.5f * dDx);
+  o.cya += Fy * (s * nyA - 0.5f * dDy - t * nyB - 0.5f * dDy);
+  o.cxb += Fy * (s * nxA - 0.5f * dDx - t * nxB - 0.5f * dDx);
+  o.cyb += Fx * (s * nyA - 0.5f * dDy - t * nyB - 0.5f * dDy);
+  return true;
+}
+
+// For the two-point model the PairF32 fields ov, cxa, cya, cxb, cyb hold summed
+// quantities: sum ov^2, and the force-weighted virial terms Pxx, Pyy, Pxy, Pyx (before
+// the division by the box area).
+__device__ __forceinline__ bool pair2_fp32(float dX, float dY, float nxA, float nyA, float aP,
+                                           float nxB, float nyB, float aQ, float sig, float gamma,
+                                           PairF32& o) {
+  dX = fmaf(gamma, dY, dX);
+  float a = aP * aP, c = aQ * aQ;
+  float b = -(nxA * nxB + nyA * nyB);
+  float d = nxA * dX + nyA * dY;
+  float e = -(nxB * dX + nyB * dY);
+  float w = nyA * nxB;
+  float uxv = fmaf(nxA, nyB, -w) + fmaf(-nyA, nxB, w);
+  float w2 = nyA * dX;
+  float uxD = fmaf(nxA, dY, -w2) + fmaf(-nyA, dX, w2);
+  float s1, t1, s2, t2, s3, t3;
+  auto cl = [](float v) { return fminf(fmaxf(v, -1.f), 1.f); };
+  if (uxv == 0.f) {
+    s1 = cl(-__fdividef(b + d, a));
+    s2 = cl(-__fdividef(d - b, a));
+    if (fabsf(s1) == 1.f)
+      t1 = cl(-__fdividef(b * s1 + e, c));
+    else
+      t1 = cl(b < 0.f ? -__fdividef(b + e, c) : -__fdividef(e - b, c));
+    if (fabsf(s2) == 1.f)
+      t2 = cl(-__fdividef(b * s2 + e, c));
+    else
+      t2 = cl(b < 0.f ? -__fdividef(e - b, c) : -__fdividef(b + e, c));
+    s3 = s2;
+    t3 = t2;
+  } else {
+    t1 = cl(__fdividef(uxD, uxv));
+    s1 = -__fdividef(b * t1 + d, a);
+    float sarg = fabsf(s1);
+    s1 = cl(s1);
+    if (sarg >= 1.f) {
+      t1 = cl(-__fdividef(b * s1 + e, c));
+      s2 = -s1;
+      t2 = -__fdividef(b * s2 + e, c);
+      float targ = fabsf(t2);
+      t2 = cl(t2);
+      if (targ > 1.f) {
+        s2 = cl(-__fdividef(b * t2 + d, a));
+        s3 = s2;
+        t3 = t2;
+      } else {
+        t3 = b < 0.f ? -s1 : s1;
+        s3 = -__fdividef(b * t3 + d, a);
+        sarg = fabsf(s3);
+        s3 = cl(s3);
+        if (sarg >= 1.f) t3 = cl(-__fdividef(b * s3 + e, c));
+      }
+    } else {
+      t2 = -t1;
+      s2 = -__fdividef(b * t2 + d, a);
+      sarg = fabsf(s2);
+      s2 = cl(s2);
+      if (sarg > 1.f) {
+        t2 = cl(-__fdividef(b * s2 + e, c));
+        s3 = s2;
+        t3 = t2;
+      } else {
+        s3 = b < 0.f ? -t1 : t1;
+        t3 = -__fdividef(b * s3 + e, c);
+        float targ = fabsf(t3);
+        t3 = cl(t3);
+        if (targ >= 1.f) s3 = cl(-__fdividef(b * t3 + d, a));
+      }
+    }
+  }
+  o.fx = o.fy = o.tp = o.tq = 0.f;
+  o.ov = o.cxa = o.cya = o.cxb = o.cyb = 0.f;
+  bool hit = contact_fp32(dX, dY, s1, t1, nxA, nyA, nxB, nyB, sig, o);
+  if (s1 != s2 && t1 != t2) {
+    if (s3 != s1 && s3 != s2) {
+      float x2 = dX + s2 * nxA - t2 * nxB, y2 = dY + s2 * nyA - t2 * nyB;
+      float x3 = dX + s3 * nxA - t3 * nxB, y3 = dY + s3 * nyA - t3 * nyB;
+      if (x3 * x3 + y3 * y3 < x2 * x2 + y2 * y2) {
+        s2 = s3;
+        t2 = t3;
+      }
+    }
+    hit |= contact_fp32(dX, dY, s2, t2, nxA, nyA, nxB, nyB, sig, o);
+  }
+  return hit;
+}
+
 // isolated_rotation, src/cpp/strain_dynamics.cpp:174-177
 __device__ __forceinline__ double iso_rot64(double RC, double phi) {
   return 0.5 * (1 - RC * cos(2 * phi));

@@ -105,6 +105,7 @@ __global__ void __launch_bounds__(128) k_pass64(Dev d, const StepScalars* __rest
   const double Lx = kPred ? ts.Lx_c : ts.Lx_p;
   const double Ly = kPred ? ts.Ly_c : ts.Ly_p;
   const bool virial = d.stress_mode == STRESS_VIRIAL;
+  const bool two_point = d.contact_model == 1;
   const double two_n = 2.0 * g.n;
 
   double2 pi = XY[i];
@@ -128,8 +129,12 @@ __global__ void __launch_bounds__(128) k_pass64(Dev d, const StepScalars* __rest
     const double2 nP = ip ? ni : nj, nQ = ip ? nj : ni;
     const double2 rP = ip ? rai : raj, rQ = ip ? raj : rai;
     PairF64 o;
-    if (pair_fp64<SE>(pP.x - pQ.x, pP.y - pQ.y, nP.x, nP.y, rP.y, nQ.x, nQ.y, rQ.y, rP.x + rQ.x,
-                      gamma, Lx, Ly, virial, two_n, o)) {
+    const bool hit =
+        two_point ? pair2_fp64<SE>(pP.x - pQ.x, pP.y - pQ.y, nP.x, nP.y, rP.y, nQ.x, nQ.y, rQ.y,
+                                   rP.x + rQ.x, gamma, Lx, Ly, two_n, o)
+                  : pair_fp64<SE>(pP.x - pQ.x, pP.y - pQ.y, nP.x, nP.y, rP.y, nQ.x, nQ.y, rQ.y,
+                                  rP.x + rQ.x, gamma, Lx, Ly, virial, two_n, o);
+    if (hit) {
       if (ip) {
         fx += o.fx;
         fy += o.fy;

@@ -64,6 +64,7 @@ __global__ void __launch_bounds__(128, 10) k_pass_mixed(Dev d,
   const bool smallx = g.cols < 3, smally = g.rows < 3;
   const float Lxf = W * g.cols, Lyf = H * g.rows;
   const bool virial = d.stress_mode == STRESS_VIRIAL;
+  const bool two_point = d.contact_model == 1;
 
   const float4 ri = REC[i];
   const float4 pai = d.pa[i];  // (R, A, index bits, 1/I)
@@ -103,15 +104,24 @@ __global__ void __launch_bounds__(128, 10) k_pass_mixed(Dev d,
     const bool ip = idi < __float_as_int(paj.z);
     const float sg = ip ? 1.f : -1.f;
     PairF32 o;
-    const bool touch = pair_fp32<SE>(sg * dx, sg * dy, ip ? ri.z : rj.z, ip ? ri.w : rj.w,
-                                     ip ? pai.y : paj.y, ip ? rj.z : ri.z, ip ? rj.w : ri.w,
-                                     ip ? paj.y : pai.y, ip ? pai.x + paj.x : paj.x + pai.x, gam,
-                                     virial, o);
+    const float nxP = ip ? ri.z : rj.z, nyP = ip ? ri.w : rj.w, aPP = ip ? pai.y : paj.y;
+    const float nxQ = ip ? rj.z : ri.z, nyQ = ip ? rj.w : ri.w, aQQ = ip ? paj.y : pai.y;
+    const float sgm = ip ? pai.x + paj.x : paj.x + pai.x;
+    const bool touch =
+        two_point ? pair2_fp32(sg * dx, sg * dy, nxP, nyP, aPP, nxQ, nyQ, aQQ, sgm, gam, o)
+                  : pair_fp32<SE>(sg * dx, sg * dy, nxP, nyP, aPP, nxQ, nyQ, aQQ, sgm, gam, virial,
+                                  o);
     if (!touch) continue;
     fx += sg * o.fx;
     fy += sg * o.fy;
     tq += ip ? o.tp : o.tq;
-    if (SE && ip) {
+    if (SE && ip && two_point) {
+      e_acc += (double)o.ov;
+      pxx += (double)o.cxa;
+      pyy += (double)o.cya;
+      pxy += (double)o.cxb;
+      pyx += (double)o.cyb;
+    } else if (SE && ip) {
       {
         e_acc += (double)(o.ov * o.ov);
         if (!virial) {
