@@ -152,7 +152,7 @@ def time_steps(box, steps, torch):
     return e0.elapsed_time(e1) / 1e3
 
 
-def cpu_baseline(w, sample_n, steps, threads):
+def cpu_baseline(w, sample_n, steps, threads, pad):
     """The oracle restatement of the reference's CPU path on host cores: `threads`
     independent replicas of a sample box (same density, shape, rate, step)."""
     import oracle
@@ -164,7 +164,7 @@ def cpu_baseline(w, sample_n, steps, threads):
     if oracle.ref_available():
         kind, cls = "reference", oracle.RefBox
     L, x, y, p, R, A = generate_packing(sample_n, w["phi"], w["a"], seed=w["seed"])
-    boxes = [cls(L, x, y, p, A, R, 0.1, strain_rate=w["rate"], step=w["dt"]) for _ in range(threads)]
+    boxes = [cls(L, x, y, p, A, R, pad, strain_rate=w["rate"], step=w["dt"]) for _ in range(threads)]
     for b in boxes:
         b.run_strain_steps(1)
 
@@ -184,17 +184,32 @@ def cpu_baseline(w, sample_n, steps, threads):
                       f"{steps} Heun steps each, {dt:.1f} s"}
 
 
-def run_reference_arm(args, w, rank):
+METRIC = "particle-steps/s (Lees-Edwards shear, Heun step)"
+
+
+def config_of(args, w, world):
+    return {"workload": args.workload, "N": w["n"], "packing": w["phi"], "a_over_r": w["a"],
+            "strain_rate": w["rate"], "dt": w["dt"], "seed": w["seed"], "pad": args.pad,
+            "l2": "inputs larger than L2: a mixed step moves 152 + 8 n B per particle "
+                  "(about 200 B, 210 MB at N = 2^20) against 129 MB of L2",
+            "parallelism": "replicas" if world > 1 else "single"}
+
+
+def run_reference_arm(args, w, rank, world):
+    """The reference's CPU path (the compiled reference when present, else the
+    oracle restatement of it) on every host core: one independent N = 65536 box of
+    the workload's density, shape, rate and step per core; each timed step is a
+    bounded sample of the workload."""
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    steps = max(args.steps // 10, 5)
-    base = cpu_baseline(w, 65536, steps, threads)
-    line = {"impl": "reference", "metric": "particle-steps/s (Lees-Edwards shear, Heun step)",
+    steps = max(min(args.steps, args.cpu_steps), 3)
+    base = cpu_baseline(w, 65536, steps, threads, args.pad)
+    line = {"impl": "reference", "metric": METRIC,
             "value": base["value"], "unit": "particle-steps/s", "n_gpus": args.gpus,
             "steps": steps, "warmup": 1, "ms_per_step": None, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": args.workload, "N": w["n"], "sample_N": 65536},
+            "config": config_of(args, w, world),
             "cpu_baseline": base,
             "e2e": {"value": base["value"], "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
@@ -205,15 +220,16 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
-    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=300)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="shear_n1048576_phi084", choices=list(WORKLOADS))
     ap.add_argument("--fp64-steps", type=int, default=20)
-    ap.add_argument("--cpu-steps", type=int, default=5)
+    ap.add_argument("--cpu-steps", type=int, default=60,
+                    help="Heun steps of each N=65536 CPU replica (about 5-10 s of work)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--only", choices=["mixed", "fp64"], default=None,
                     help="time one form only (for profiler captures)")
-    ap.add_argument("--pad", type=float, default=0.1, help="neighbour-list padding")
+    ap.add_argument("--pad", type=float, default=0.2, help="neighbour-list padding")
     ap.add_argument("--no-graphs", action="store_true",
                     help="launch eagerly instead of through CUDA graphs (profiler captures: "
                          "kernels inside graphs with conditional nodes cannot be profiled)")
@@ -224,7 +240,11 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     w = make_workload(args.workload)
     if args.impl == "reference":
-        run_reference_arm(args, w, rank)
+        if w.get("phi") is None:
+            print(json.dumps({"impl": "reference", "unavailable":
+                              "the CPU arm samples single-system workloads only"}))
+            return
+        run_reference_arm(args, w, rank, world)
         return
 
     import torch
@@ -335,19 +355,16 @@ def main():
 
     base = None
     if rank == 0 and not args.no_cpu and w.get("phi") is not None:
-        base = cpu_baseline(w, 65536, args.cpu_steps, 1)
+        base = cpu_baseline(w, 65536, args.cpu_steps, os.cpu_count() or 1, args.pad)
 
     if rank == 0:
         line = {
-            "metric": "particle-steps/s (Lees-Edwards shear, Heun step), mixed precision",
+            "metric": METRIC,
             "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic (seeded crossing-free packing)",
-            "config": {"workload": args.workload, "N": n, "packing": w["phi"], "a_over_r": w["a"],
-                       "strain_rate": w["rate"], "dt": w["dt"], "seed": w["seed"], "pad": 0.1,
-                       "l2": "state larger than L2 (~200 MB per step touched)",
-                       "parallelism": "replicas" if world > 1 else "single"},
+            "config": config_of(args, w, world),
             "plain_fp64": {"value": value64, "unit": "particle-steps/s",
                            "ms_per_step": 1e3 * secs64 / args.fp64_steps,
                            "steps": args.fp64_steps, "mixed_over_fp64": value / value64},

@@ -208,7 +208,9 @@ int sc_create(const sc_options* opt_in, int n_sys, const int* n_per_sys, const d
     ok = ok && h.dalloc(&d.rec, N, "rec") && h.dalloc(&d.rec_t, N, "rec_t") &&
          h.dalloc(&d.mc, N, "mc") && h.dalloc(&d.mv, N, "mv") && h.dalloc(&d.mm, N, "mm") &&
          h.dalloc(&d.pa, N, "pa") && h.dalloc(&d.rcf, N, "rcf") &&
-         h.dalloc(&d.cellp, N, "cellp") && h.dalloc(&d.gbuild, n_sys, "gbuild");
+         h.dalloc(&d.cellp, N, "cellp") && h.dalloc(&d.gbuild, n_sys, "gbuild") &&
+         h.dalloc(&d.ord, N, "ord") && h.dalloc(&d.nbr_p, N * d.maxn, "nbr_p") &&
+         h.dalloc(&d.nbr_pn, N, "nbr_pn");
   ok = ok && h.dalloc(&d.nbr, N * d.maxn, "nbr");
   ok = ok && h.dalloc(&d.nbr_n, N, "nbr_n");
   ok = ok && h.dalloc(&d.cell_tmp, N, "cell_tmp") && h.dalloc(&d.rank, N, "rank") &&

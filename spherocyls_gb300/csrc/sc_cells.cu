@@ -432,6 +432,7 @@ void launch_rebuild(const Dev& d, bool mixed, const StepScalars* tab, int row, c
   if (mixed) {
     launch_mx_local(d, tab, row, false, st);
     launch_mx_build_list(d, tab, row, false, st);
+    launch_mx_order(d, false, st);
   } else {
     launch_build_nbrs(d, tab, row, st);
   }

@@ -335,7 +335,7 @@ int Handle::enqueue_rebuild_body(bool resize, int k, bool prof, cudaStream_t st)
     n++;
   }
   timed(2, prof, [&] { launch_rebuild(d, prec == PREC_MIXED, d_tab, k, st); });
-  n += prec == PREC_MIXED ? 12 : 11;
+  n += prec == PREC_MIXED ? 13 : 11;
   stream = keep;
   return n;
 }
@@ -743,7 +743,7 @@ int Handle::fire_minimize(double ftol, int max_iter, double dt0, double dt_max, 
       // FP64 copies are refreshed before the cell sort reads them
       if (mixed) launch_mx_materialize(d, d_tab, 0, false, stream);
       launch_rebuild(d, mixed, d_tab, 0, stream);
-      kernels += 3 + (mixed ? 13 : 11);
+      kernels += 3 + (mixed ? 14 : 11);
     }
     it += chunk;
     if (!cuda_ok(cudaGetLastError(), "fire launch") ||

@@ -112,9 +112,15 @@ struct Dev {
   // cell lists
   int* cell_start;          // [ncells] first slot
   int* cell_count;          // [ncells]
-  // neighbour list (FP64 form), column-major [k * ntot + slot]
+  // neighbour list, column-major [k * ntot + slot]
   int* nbr;
   int* nbr_n;
+  // mixed form: the same lists reordered for the force pass.  Within each window
+  // of kOrderWindow slots, threads take the slots in order of increasing list
+  // length, so a warp's lanes loop over lists of nearly equal length.
+  int* ord;     // [ntot] position -> slot
+  int* nbr_p;   // column-major [k * ntot + position]
+  int* nbr_pn;  // [ntot] list length at each position (capped at maxn)
   // rebuild scratch
   int* cell_tmp;
   int* rank;
@@ -152,11 +158,12 @@ enum { ST_NBR_OVERFLOW = 1, ST_NAN = 2, ST_CELL_OVERFLOW = 4 };
 
 constexpr int kScanChunk = 1024;  // cells per scan chunk
 constexpr int kSeChunk = 1024;    // particles per reduction chunk
-constexpr int kMaxCellSort = 48;
+constexpr int kMaxCellSort = 48;  // cells above this occupancy use the in-place slow sort
 constexpr int kNoTrigger = 0x7f7f7f7f;  // istar value when no particle triggered
+constexpr int kOrderWindow = 128;  // slots per window of the force-pass ordering
 // mixed-form list entries: slot in the low 28 bits, cell offset (dc+1, dr+1) above
 constexpr int kSlotBits = 28;
-constexpr unsigned kSlotMask = (1u << kSlotBits) - 1u;  // cells above this occupancy use the in-place slow sort
+constexpr unsigned kSlotMask = (1u << kSlotBits) - 1u;
 
 // pass modes for the force kernels
 enum PassMode {
@@ -194,6 +201,7 @@ void launch_affine(const Dev& d, const double* factor, cudaStream_t st);
 void launch_mx_materialize(const Dev& d, const StepScalars* tab, int row, bool all,
                            cudaStream_t st);
 void launch_mx_local(const Dev& d, const StepScalars* tab, int row, bool all, cudaStream_t st);
+void launch_mx_order(const Dev& d, bool all, cudaStream_t st);
 void launch_mx_build_list(const Dev& d, const StepScalars* tab, int row, bool all,
                           cudaStream_t st);
 

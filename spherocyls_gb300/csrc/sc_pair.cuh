@@ -123,7 +123,7 @@ __device__ __forceinline__ bool pair_fp32(float dX, float dY, float nxA, float n
   float dsq = dDx * dDx + dDy * dDy;
   if (!(dsq < sig * sig)) return false;
   float inv_d = rsqrtf(dsq);
-  float inv_sig = __frcp_rn(sig);
+  float inv_sig = __fdividef(1.f, sig);
   float ov = 1.f - dsq * inv_d * inv_sig;   // 1 - d/sigma
   float f = ov * inv_sig * inv_d;           // (1 - d/sigma)/(sigma d)
   float Fx = dDx * f, Fy = dDy * f;
@@ -300,7 +300,7 @@ __device__ __forceinline__ bool contact_fp32(float dX, float dY, float s, float 
   float dsq = dDx * dDx + dDy * dDy;
   if (!(dsq < sig * sig)) return false;
   float inv_d = rsqrtf(dsq);
-  float inv_sig = __frcp_rn(sig);
+  float inv_sig = __fdividef(1.f, sig);
   float ov = 1.f - dsq * inv_d * inv_sig;
   float f = ov * inv_sig * inv_d;
   float Fx = dDx * f, Fy = dDy * f;

@@ -90,7 +90,7 @@ __device__ __forceinline__ void flag_moved(const Dev& d, int s, int id, double2 
   }
 }
 
-template <int MODE, bool SE>
+template <int MODE, bool SE, bool TWO>
 __global__ void __launch_bounds__(128) k_pass64(Dev d, const StepScalars* __restrict__ tab,
                                                int row) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(128) k_pass64(Dev d, const StepScalars* __rest
   const double Lx = kPred ? ts.Lx_c : ts.Lx_p;
   const double Ly = kPred ? ts.Ly_c : ts.Ly_p;
   const bool virial = d.stress_mode == STRESS_VIRIAL;
-  const bool two_point = d.contact_model == 1;
+  constexpr bool two_point = TWO;
   const double two_n = 2.0 * g.n;
 
   double2 pi = XY[i];
@@ -281,7 +281,10 @@ template <int MODE, bool SE>
 void launch_one(const Dev& d, const StepScalars* tab, int row, cudaStream_t st) {
   int block = 128;
   int grid = (d.ntot + block - 1) / block;
-  k_pass64<MODE, SE><<<grid, block, 0, st>>>(d, tab, row);
+  if (d.contact_model == 1)
+    k_pass64<MODE, SE, true><<<grid, block, 0, st>>>(d, tab, row);
+  else
+    k_pass64<MODE, SE, false><<<grid, block, 0, st>>>(d, tab, row);
 }
 
 }  // namespace

@@ -47,12 +47,13 @@ __device__ __forceinline__ void kahan_add_scale(float& s, float& c, float v, flo
   c = pe;
 }
 
-template <int MODE, bool SE>
-__global__ void __launch_bounds__(128, 10) k_pass_mixed(Dev d,
+template <int MODE, bool SE, bool TWO>
+__global__ void __launch_bounds__(128, TWO ? 6 : 10) k_pass_mixed(Dev d,
                                                        const StepScalars* __restrict__ tab,
                                                        int row) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= d.ntot) return;
+  const int pos = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pos >= d.ntot) return;
+  const int i = d.ord[pos];  // the slot this thread works on (lists ordered by length)
   constexpr bool kPred = (MODE == PASS_CORR_STRAIN || MODE == PASS_CORR_RESIZE);
   const int s = d.psys[i];
   const SysGeom& g = d.geom[s];
@@ -64,14 +65,13 @@ __global__ void __launch_bounds__(128, 10) k_pass_mixed(Dev d,
   const bool smallx = g.cols < 3, smally = g.rows < 3;
   const float Lxf = W * g.cols, Lyf = H * g.rows;
   const bool virial = d.stress_mode == STRESS_VIRIAL;
-  const bool two_point = d.contact_model == 1;
+  constexpr bool two_point = TWO;
 
   const float4 ri = REC[i];
   const float4 pai = d.pa[i];  // (R, A, index bits, 1/I)
   const int idi = __float_as_int(pai.z);
-  int cnt = d.nbr_n[i];
-  if (cnt > d.maxn) cnt = d.maxn;
-  const unsigned* __restrict__ Lst = reinterpret_cast<const unsigned*>(d.nbr) + i;
+  const int cnt = d.nbr_pn[pos];
+  const unsigned* __restrict__ Lst = reinterpret_cast<const unsigned*>(d.nbr_p) + pos;
   const size_t stride = d.ntot;
 
   float fx = 0.f, fy = 0.f, tq = 0.f;
@@ -242,7 +242,10 @@ __global__ void __launch_bounds__(128, 10) k_pass_mixed(Dev d,
 template <int MODE, bool SE>
 void launch_one(const Dev& d, const StepScalars* tab, int row, cudaStream_t st, int block) {
   int grid = (d.ntot + block - 1) / block;
-  k_pass_mixed<MODE, SE><<<grid, block, 0, st>>>(d, tab, row);
+  if (d.contact_model == 1)
+    k_pass_mixed<MODE, SE, true><<<grid, block, 0, st>>>(d, tab, row);
+  else
+    k_pass_mixed<MODE, SE, false><<<grid, block, 0, st>>>(d, tab, row);
 }
 
 // ---- rebuild support ----
@@ -343,9 +346,41 @@ __global__ void __launch_bounds__(128) k_mx_build_list(Dev d, const StepScalars*
   if (i == g.p0) d.gbuild[s] = gam;
 }
 
+// Force-pass ordering: within each window of kOrderWindow slots, a stable sort
+// of the slots by list length; the lists are copied to their positions.  A window
+// is redone when any of its slots belongs to a system that was rebuilt.
+__global__ void __launch_bounds__(kOrderWindow) k_mx_order(Dev d, int all) {
+  if (!all && *d.any == 0) return;
+  const int base = blockIdx.x * kOrderWindow;
+  const int i = base + threadIdx.x;
+  const bool valid = i < d.ntot;
+  const bool mine = valid && (all || d.flags[d.psys[i]] != 0);
+  if (!__syncthreads_or(mine)) return;
+  __shared__ int len[kOrderWindow];
+  int c = 0x7fffffff;  // slots past the end sort last
+  if (valid) c = min(d.nbr_n[i], d.maxn);
+  len[threadIdx.x] = c;
+  __syncthreads();
+  int rank = 0;
+  for (int k = 0; k < kOrderWindow; k++) {
+    const int o = len[k];
+    rank += (o < c) | ((o == c) & (k < (int)threadIdx.x));
+  }
+  if (!valid) return;
+  const int pos = base + rank;
+  d.ord[pos] = i;
+  d.nbr_pn[pos] = c;
+  const size_t n = d.ntot;
+  for (int k = 0; k < c; k++) d.nbr_p[k * n + pos] = d.nbr[k * n + i];
+}
+
 inline int nblk(int n, int b) { return (n + b - 1) / b; }
 
 }  // namespace
+
+void launch_mx_order(const Dev& d, bool all, cudaStream_t st) {
+  k_mx_order<<<nblk(d.ntot, kOrderWindow), kOrderWindow, 0, st>>>(d, all ? 1 : 0);
+}
 
 void launch_pass_mixed(const Dev& d, int mode, bool se, const StepScalars* tab, int row,
                        cudaStream_t st, int block) {
