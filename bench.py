@@ -57,6 +57,12 @@ def bytes_per_pass(precision: str, nbar: float) -> float:
     return (152.0 if precision == "mixed" else 232.0) / 2 + 4.0 * nbar
 
 
+# DRAM bytes (read + write) per particle of one mixed force pass, the mean of the
+# predictor and corrector launches in one ncu capture of the default workload
+# (profiles/k_pass_mixed_n1048576.md: 112.0 and 158.7 MB per launch at N = 2^20).
+PASS_DRAM_BYTES_PER_PARTICLE = {"shear_n1048576_phi084": 135.35e6 / (1 << 20)}
+
+
 def _peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -369,7 +375,11 @@ def main():
                            "ms_per_step": 1e3 * secs64 / args.fp64_steps,
                            "steps": args.fp64_steps, "mixed_over_fp64": value / value64},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                         "frac": achieved / peak, "peak_kind": peak_kind,
+                         "traffic": (PASS_DRAM_BYTES_PER_PARTICLE[args.workload] * n
+                                     if args.workload in PASS_DRAM_BYTES_PER_PARTICLE
+                                     else None),
+                         "traffic_unit": "bytes per launch (ncu capture)",
                          "kernel": "k_pass_mixed (corrector/predictor force passes)",
                          "pass_ms": pass_ms, "bytes_per_particle_pass": bpp, "mean_list_length": nbar,
                          "rebuild_ms_mean": pt["rebuild_ms"]},
