@@ -193,6 +193,19 @@ def cpu_baseline(w, sample_n, steps, threads, pad):
 METRIC = "particle-steps/s (Lees-Edwards shear, Heun step)"
 
 
+def max_over_ranks(secs: float, world: int, device: str) -> float:
+    """The slowest rank's time (replicas run independently; this all-reduce is the
+    only collective, outside the timed region)."""
+    if world <= 1:
+        return secs
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([secs], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def config_of(args, w, world):
     return {"workload": args.workload, "N": w["n"], "packing": w["phi"], "a_over_r": w["a"],
             "strain_rate": w["rate"], "dt": w["dt"], "seed": w["seed"], "pad": args.pad,
@@ -308,9 +321,8 @@ def main():
     with ClockSampler() as clk:
         secs = time_steps(box, args.steps, torch)
     if world > 1:
-        t = torch.tensor([secs], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        secs = float(t.item())
+        torch.distributed.barrier()
+    secs = max_over_ranks(secs, world, "cuda")
     value = world * n * args.steps / secs
     k_before = counters0["kernels"]
     counters = box.counters()
