@@ -354,6 +354,46 @@ void Handle::invalidate_graph() {
   if (graph_exec) cudaGraphExecDestroy(graph_exec);
   graph_exec = nullptr;
   graph_key = GraphKey{};
+  if (fire_exec) cudaGraphExecDestroy(fire_exec);
+  fire_exec = nullptr;
+  fire_key_iters = 0;
+}
+
+// Inside a capture on `stream`: k_pre_rebuild for table row `row`, then a
+// conditional IF node it switches on when any system needs a rebuild; `body`
+// enqueues the node's contents on stream2 and returns its kernel count.
+cudaError_t Handle::capture_rebuild_node(int row, const std::function<int(cudaStream_t)>& body) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t gcap = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  cudaError_t e = cudaStreamGetCaptureInfo(stream, &cs, nullptr, &gcap, &deps, nullptr, &nd);
+  cudaGraphConditionalHandle hcond;
+  if (e == cudaSuccess)
+    e = cudaGraphConditionalHandleCreate(&hcond, gcap, 0, cudaGraphCondAssignDefault);
+  if (e != cudaSuccess) return e;
+  launch_pre_rebuild(d, d_tab, row, hcond, stream);
+  e = cudaStreamGetCaptureInfo(stream, &cs, nullptr, &gcap, &deps, nullptr, &nd);
+  if (e != cudaSuccess) return e;
+  // zeroed raw storage: the struct's union has no default constructor in C++
+  alignas(cudaGraphNodeParams) unsigned char cp_buf[sizeof(cudaGraphNodeParams)] = {};
+  cudaGraphNodeParams& cp = *reinterpret_cast<cudaGraphNodeParams*>(cp_buf);
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = hcond;
+  cp.conditional.type = cudaGraphCondTypeIf;
+  cp.conditional.size = 1;
+  cudaGraphNode_t cn;
+  e = cudaGraphAddNode(&cn, gcap, deps, nullptr, nd, &cp);
+  if (e == cudaSuccess)
+    e = cudaStreamUpdateCaptureDependencies(stream, &cn, nullptr, 1,
+                                            cudaStreamSetCaptureDependencies);
+  if (e != cudaSuccess) return e;
+  cudaGraph_t bg = cp.conditional.phGraph_out[0];
+  e = cudaStreamBeginCaptureToGraph(stream2, bg, nullptr, nullptr, 0,
+                                    cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return e;
+  body_kernels = body(stream2);
+  return cudaStreamEndCapture(stream2, &bg);
 }
 
 // Capture the per-step sequence with the rebuild body inside a conditional graph
@@ -370,36 +410,8 @@ bool Handle::capture_conditional(bool resize, int nsteps, int se_every, cudaGrap
   for (int k = 1; k <= nsteps && e == cudaSuccess; k++) {
     bool se = se_every > 0 && k % se_every == 0;
     enqueue_corr(resize, k, false);
-    cudaStreamCaptureStatus cs;
-    cudaGraph_t gcap = nullptr;
-    const cudaGraphNode_t* deps = nullptr;
-    size_t nd = 0;
-    e = cudaStreamGetCaptureInfo(stream, &cs, nullptr, &gcap, &deps, nullptr, &nd);
-    cudaGraphConditionalHandle hcond;
-    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&hcond, gcap, 0, cudaGraphCondAssignDefault);
-    if (e != cudaSuccess) break;
-    launch_pre_rebuild(d, d_tab, k, hcond, stream);
-    e = cudaStreamGetCaptureInfo(stream, &cs, nullptr, &gcap, &deps, nullptr, &nd);
-    if (e != cudaSuccess) break;
-    // zeroed raw storage: the struct's union has no default constructor in C++
-    alignas(cudaGraphNodeParams) unsigned char cp_buf[sizeof(cudaGraphNodeParams)] = {};
-    cudaGraphNodeParams& cp = *reinterpret_cast<cudaGraphNodeParams*>(cp_buf);
-    cp.type = cudaGraphNodeTypeConditional;
-    cp.conditional.handle = hcond;
-    cp.conditional.type = cudaGraphCondTypeIf;
-    cp.conditional.size = 1;
-    cudaGraphNode_t cn;
-    e = cudaGraphAddNode(&cn, gcap, deps, nullptr, nd, &cp);
-    if (e == cudaSuccess)
-      e = cudaStreamUpdateCaptureDependencies(stream, &cn, nullptr, 1,
-                                              cudaStreamSetCaptureDependencies);
-    if (e != cudaSuccess) break;
-    cudaGraph_t body = cp.conditional.phGraph_out[0];
-    e = cudaStreamBeginCaptureToGraph(stream2, body, nullptr, nullptr, 0,
-                                      cudaStreamCaptureModeThreadLocal);
-    if (e != cudaSuccess) break;
-    body_kernels = enqueue_rebuild_body(resize, k, false, stream2);
-    e = cudaStreamEndCapture(stream2, &body);
+    e = capture_rebuild_node(
+        k, [&](cudaStream_t st) { return enqueue_rebuild_body(resize, k, false, st); });
     if (e != cudaSuccess) break;
     enqueue_pred(resize, k, se, false);
     fixed += 3;
@@ -716,6 +728,64 @@ bool Handle::ensure_fire() {
   return true;
 }
 
+// One FIRE iteration, eagerly: force pass, reductions and update, rebuild chain.
+void Handle::enqueue_fire_iteration(double ftol, double dt_max) {
+  const bool mixed = prec == PREC_MIXED;
+  launch_pass(PASS_FORCE, false, 0);
+  launch_fire_iteration_tail(d, fire, ftol, dt_max, mixed, stream);
+  // the mixed form moves only its FP32 local state: the flagged systems'
+  // FP64 copies are refreshed before the cell sort reads them
+  if (mixed) launch_mx_materialize(d, d_tab, 0, false, stream);
+  launch_rebuild(d, mixed, d_tab, 0, stream);
+  kernels += 4 + (mixed ? 14 : 12);
+}
+
+// `iters` FIRE iterations as one CUDA graph: each is force pass, reductions and
+// update, then the rebuild chain inside a conditional node that runs only when a
+// system was flagged.  Captured once per (iters, ftol, dt_max) and relaunched;
+// returns false (nothing launched) when the capture is not possible.
+bool Handle::run_fire_graph(int iters, double ftol, double dt_max) {
+  if (!use_conditional) return false;
+  if (!fire_exec || fire_key_iters != iters || fire_key_ftol != ftol || fire_key_dtmax != dt_max) {
+    if (fire_exec) cudaGraphExecDestroy(fire_exec);
+    fire_exec = nullptr;
+    fire_key_iters = 0;
+    if (!stream2 && !cuda_ok(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking), "stream"))
+      return false;
+    if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    const bool mixed = prec == PREC_MIXED;
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < iters && e == cudaSuccess; k++) {
+      launch_pass(PASS_FORCE, false, 0);
+      launch_fire_iteration_tail(d, fire, ftol, dt_max, mixed, stream);
+      e = capture_rebuild_node(0, [&](cudaStream_t st) {
+        if (mixed) launch_mx_materialize(d, d_tab, 0, false, st);
+        launch_rebuild(d, mixed, d_tab, 0, st);
+        return mixed ? 14 : 12;
+      });
+    }
+    cudaGraph_t g = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(stream, &g);
+    cudaGraphExec_t ex = nullptr;
+    if (e == cudaSuccess && e2 == cudaSuccess) e = cudaGraphInstantiate(&ex, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    fire_exec = ex;
+    fire_key_iters = iters;
+    fire_key_ftol = ftol;
+    fire_key_dtmax = dt_max;
+    fire_graph_kernels = 5LL * iters;
+  }
+  kernels += fire_graph_kernels;
+  return cuda_ok(cudaGraphLaunch(fire_exec, stream), "fire graph launch");
+}
+
 // FIRE on every system until max |F| < ftol (or max_iter iterations); the host
 // looks at the per-system state only between chunks of iterations.
 int Handle::fire_minimize(double ftol, int max_iter, double dt0, double dt_max, int* iters,
@@ -735,16 +805,9 @@ int Handle::fire_minimize(double ftol, int max_iter, double dt0, double dt_max, 
   int it = 0;
   bool all_done = false;
   while (it < max_iter && !all_done) {
-    int chunk = std::min(50, max_iter - it);
-    for (int k = 0; k < chunk; k++) {
-      launch_pass(PASS_FORCE, false, 0);
-      launch_fire_iteration_tail(d, fire, ftol, dt_max, mixed, stream);
-      // the mixed form moves only its FP32 local state: the flagged systems'
-      // FP64 copies are refreshed before the cell sort reads them
-      if (mixed) launch_mx_materialize(d, d_tab, 0, false, stream);
-      launch_rebuild(d, mixed, d_tab, 0, stream);
-      kernels += 3 + (mixed ? 14 : 11);
-    }
+    int chunk = std::min(kFireChunk, max_iter - it);
+    if (!(opt.use_graphs && chunk == kFireChunk && run_fire_graph(chunk, ftol, dt_max)))
+      for (int k = 0; k < chunk; k++) enqueue_fire_iteration(ftol, dt_max);
     it += chunk;
     if (!cuda_ok(cudaGetLastError(), "fire launch") ||
         !cuda_ok(cudaMemcpyAsync(hsys.data(), fire.sys, nsys * sizeof(FireSys),

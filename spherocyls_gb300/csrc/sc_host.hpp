@@ -41,6 +41,7 @@ struct GraphKey {
 
 struct Handle {
   static constexpr int kChunk = 100;  // steps per table upload / captured graph
+  static constexpr int kFireChunk = 50;  // FIRE iterations between host checks
 
   sc_options opt{};
   int device = -1;
@@ -78,6 +79,11 @@ struct Handle {
   bool use_conditional = true;     // conditional graph nodes available
   bool graph_conditional = false;  // the current graph uses them
   long long body_kernels = 0;      // kernels in one rebuild body
+  // CUDA graph of one chunk of FIRE iterations (same conditional rebuild node)
+  cudaGraphExec_t fire_exec = nullptr;
+  int fire_key_iters = 0;
+  double fire_key_ftol = 0, fire_key_dtmax = 0;
+  long long fire_graph_kernels = 0;
   // profiling: per-pass events
   struct Mark {
     int kind;
@@ -123,6 +129,7 @@ struct Handle {
   void enqueue_corr(bool resize, int k, bool prof);
   int enqueue_rebuild_body(bool resize, int k, bool prof, cudaStream_t st);
   void enqueue_pred(bool resize, int k, bool se, bool prof);
+  cudaError_t capture_rebuild_node(int row, const std::function<int(cudaStream_t)>& body);
   bool capture_conditional(bool resize, int nsteps, int se_every, cudaGraph_t* out);
   void enqueue_se_record(int rec);
   void invalidate_graph();
@@ -136,6 +143,8 @@ struct Handle {
   // FIRE minimiser and quasistatic compression
   FireState fire{};
   bool ensure_fire();
+  void enqueue_fire_iteration(double ftol, double dt_max);
+  bool run_fire_graph(int iters, double ftol, double dt_max);
   int fire_minimize(double ftol, int max_iter, double dt0, double dt_max, int* iters,
                     double* fmax_out, int* done_out);
   int affine_scale(const std::vector<double>& factor);
