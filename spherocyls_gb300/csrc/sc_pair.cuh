@@ -141,6 +141,35 @@ __device__ __forceinline__ bool pair_fp32(float dX, float dY, float nxA, float n
   return true;
 }
 
+// Conservative FP32 screen: false only when the two spines (P at the origin, Q at
+// -D in the sheared, minimum-image frame) are certainly farther apart than sig.
+// The closest-point parameters come from the cross-product form; an error in them
+// only moves the evaluated point pair along the spines, which can only raise the
+// distance by the spines' misalignment angle times their length, and both that and
+// the FP32 rounding of the distance stay far below the 1e-4 relative margin.  Both
+// contact rules need the minimum distance below sig for any contact.
+__device__ __forceinline__ bool may_touch_fp32(float dX, float dY, float nxA, float nyA,
+                                               float aP, float nxB, float nyB, float aQ,
+                                               float sig) {
+  float a = aP * aP, c = aQ * aQ;
+  float b = -(nxA * nxB + nyA * nyB);
+  float d = nxA * dX + nyA * dY;
+  float e = -(nxB * dX + nyB * dY);
+  float w = nyA * nxB;
+  float uxv = fmaf(nxA, nyB, -w) + fmaf(-nyA, nxB, w);
+  float w2 = nyA * dX;
+  float uxD = fmaf(nxA, dY, -w2) + fmaf(-nyA, dX, w2);
+  float t = uxv == 0.f ? -1.f : fminf(fmaxf(__fdividef(uxD, uxv), -1.f), 1.f);
+  float s = a > 0.f ? -__fdividef(b * t + d, a) : 0.f;
+  float sarg = fabsf(s);
+  s = fminf(fmaxf(s, -1.f), 1.f);
+  if (sarg > 1.f && c > 0.f) t = fminf(fmaxf(-__fdividef(b * s + e, c), -1.f), 1.f);
+  float dDx = dX + s * nxA - t * nxB;
+  float dDy = dY + s * nyA - t * nyB;
+  float lim = sig * 1.0001f + 1e-5f;
+  return dDx * dDx + dDy * dDy < lim * lim;
+}
+
 // ---- two-point contacts (src/cuda/2point_dynamics.cu:385-546, euler_est_2p) ----
 //
 // For nearly parallel overlapping spines the single closest-point pair jumps from

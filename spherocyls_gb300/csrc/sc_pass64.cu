@@ -116,40 +116,62 @@ __global__ void __launch_bounds__(128) k_pass64(Dev d, const StepScalars* __rest
   double se0 = 0.0, se1 = 0.0, se2 = 0.0, se3 = 0.0, se4 = 0.0;
   int cnt = d.nbr_n[i];
   if (cnt > d.maxn) cnt = d.maxn;
-  for (int k = 0; k < cnt; k++) {
-    int j = d.nbr[(size_t)k * d.ntot + i];
-    double2 pj = XY[j];
-    double2 nj = NXY[j];
-    double2 raj = d.ra[j];
-    int idj = d.id[j];
-    // the lower particle index plays the reference's "p": select the operands (one
-    // copy of the pair code per warp) rather than branch into two
-    const bool ip = idi < idj;
-    const double2 pP = ip ? pi : pj, pQ = ip ? pj : pi;
-    const double2 nP = ip ? ni : nj, nQ = ip ? nj : ni;
-    const double2 rP = ip ? rai : raj, rQ = ip ? raj : rai;
-    PairF64 o;
-    const bool hit =
-        two_point ? pair2_fp64<SE>(pP.x - pQ.x, pP.y - pQ.y, nP.x, nP.y, rP.y, nQ.x, nQ.y, rQ.y,
-                                   rP.x + rQ.x, gamma, Lx, Ly, two_n, o)
-                  : pair_fp64<SE>(pP.x - pQ.x, pP.y - pQ.y, nP.x, nP.y, rP.y, nQ.x, nQ.y, rQ.y,
-                                  rP.x + rQ.x, gamma, Lx, Ly, virial, two_n, o);
-    if (hit) {
-      if (ip) {
-        fx += o.fx;
-        fy += o.fy;
-        tq += o.tp;
-        if (SE) {
-          se0 += o.e;
-          se1 += o.pxx;
-          se2 += o.pyy;
-          se3 += o.pxy;
-          se4 += o.pyx;
+  const float fpi_x = (float)ni.x, fpi_y = (float)ni.y, fai = (float)rai.y;
+  for (int k0 = 0; k0 < cnt; k0 += 64) {
+    // FP32 screen of up to 64 entries: the FP64 contact code then runs only for the
+    // entries that may touch, in list order, so the sums are unchanged bit for bit
+    unsigned long long cand = 0ull;
+    const int kend = cnt - k0 < 64 ? cnt : k0 + 64;
+    for (int k = k0; k < kend; k++) {
+      const int j = d.nbr[(size_t)k * d.ntot + i];
+      const double2 pj = XY[j];
+      const double2 nj = NXY[j];
+      const double2 raj = d.ra[j];
+      double dX = pi.x - pj.x, dY = pi.y - pj.y;
+      dX += Lx * (double)((dX < -0.5 * Lx) - (dX > 0.5 * Lx));
+      dY += Ly * (double)((dY < -0.5 * Ly) - (dY > 0.5 * Ly));
+      dX += gamma * dY;
+      if (may_touch_fp32((float)dX, (float)dY, fpi_x, fpi_y, fai, (float)nj.x, (float)nj.y,
+                         (float)raj.y, (float)(rai.x + raj.x)))
+        cand |= 1ull << (k - k0);
+    }
+    while (cand) {
+      const int k = k0 + __ffsll((long long)cand) - 1;
+      cand &= cand - 1ull;
+      int j = d.nbr[(size_t)k * d.ntot + i];
+      double2 pj = XY[j];
+      double2 nj = NXY[j];
+      double2 raj = d.ra[j];
+      int idj = d.id[j];
+      // the lower particle index plays the reference's "p": select the operands (one
+      // copy of the pair code per warp) rather than branch into two
+      const bool ip = idi < idj;
+      const double2 pP = ip ? pi : pj, pQ = ip ? pj : pi;
+      const double2 nP = ip ? ni : nj, nQ = ip ? nj : ni;
+      const double2 rP = ip ? rai : raj, rQ = ip ? raj : rai;
+      PairF64 o;
+      const bool hit =
+          two_point ? pair2_fp64<SE>(pP.x - pQ.x, pP.y - pQ.y, nP.x, nP.y, rP.y, nQ.x, nQ.y, rQ.y,
+                                     rP.x + rQ.x, gamma, Lx, Ly, two_n, o)
+                    : pair_fp64<SE>(pP.x - pQ.x, pP.y - pQ.y, nP.x, nP.y, rP.y, nQ.x, nQ.y, rQ.y,
+                                    rP.x + rQ.x, gamma, Lx, Ly, virial, two_n, o);
+      if (hit) {
+        if (ip) {
+          fx += o.fx;
+          fy += o.fy;
+          tq += o.tp;
+          if (SE) {
+            se0 += o.e;
+            se1 += o.pxx;
+            se2 += o.pyy;
+            se3 += o.pxy;
+            se4 += o.pyx;
+          }
+        } else {
+          fx -= o.fx;
+          fy -= o.fy;
+          tq += o.tq;
         }
-      } else {
-        fx -= o.fx;
-        fy -= o.fy;
-        tq += o.tq;
       }
     }
   }
