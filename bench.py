@@ -5,8 +5,10 @@ alternating, A = R), packing fraction 0.84, strain rate 1e-4, dt = 0.02, seeded
 crossing-free synthetic packing (seed 3).  A "step" is one Heun step (two force
 passes) of every particle.  The headline line times the mixed-precision form; the
 plain FP64 form, the force-pass roofline, the CPU baseline (the oracle restatement
-of the reference's CPU path on host cores) and an end-to-end run through the C ABI
-with host buffers are reported in the same JSON line.
+of the reference's CPU path on host cores), an end-to-end run through the C ABI
+with host buffers and the minimisation time to tolerance of batched jamming
+replicas (mixed sweeps then FP64 refinement against FP64 alone) are reported in
+the same JSON line.
 
     python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference]
 """
@@ -193,6 +195,73 @@ def cpu_baseline(w, sample_n, steps, threads, pad):
 METRIC = "particle-steps/s (Lees-Edwards shear, Heun step)"
 
 
+def minimise_leg(replicas=32, n=4096, max_iter=20000, ftol=1e-14, device=0):
+    """Minimisation time to tolerance on the jamming workload's shape: replicas of
+    N = 4096 with a/R in {0.25, 0.5, 1, 2} (a quarter each), seeds 100 + k, from
+    packing 0.70.  Untimed preparation: the mixed form compresses every replica to
+    jamming in affine steps of 2e-3 in packing fraction (FIRE to 1e-6 after each,
+    jammed once E/N > 1e-10: residual overlaps of a 1e-6 force tolerance alone give
+    E/N near 1e-12), and each replica is then compressed by one more
+    1e-4 increment.  From that same state the two timed arms minimise to
+    max|F_i|, |tau_i|/sqrt(I_i) < ftol: (a) mixed FIRE to 1e-6, then FP64 FIRE;
+    (b) FP64 FIRE alone.  Each FP64 stage stops after max_iter iterations."""
+    from spherocyls_gb300 import BoxBatch, generate_packing
+
+    aors = [0.25, 0.5, 1.0, 2.0]
+    packs = [generate_packing(n, 0.70, aors[(4 * k) // replicas], seed=100 + k)
+             for k in range(replicas)]
+    cat = lambda i: np.concatenate([pk[i] for pk in packs])  # noqa: E731
+    L0 = np.array([pk[0] for pk in packs])
+    R, A = cat(4), cat(5)
+    kw = dict(contacts=2, device=device)
+    prep = BoxBatch([n] * replicas, L0, cat(1), cat(2), cat(3), A, R, 0.1, precision="mixed",
+                    **kw)
+    t0 = time.perf_counter()
+    prep.fire_minimize(1e-6, 100000)
+    phi_j, n_inc = prep.quasistatic_compress(2e-3, 1e-6, 1e-10, 1000, 100000)
+    t_prep = time.perf_counter() - t0
+    Lj = np.array([prep.box(s)["Lx"] for s in range(replicas)])
+    xs, ys, ps = prep.state()
+    prep.close()
+    f = np.sqrt(phi_j / (phi_j + 1e-4))
+    fp = np.repeat(f, n)
+    L1, x1, y1 = Lj * f, xs * fp, ys * fp
+
+    def run(b, tol, cap):
+        t = time.perf_counter()
+        it, fmax, done = b.fire_minimize(tol, cap)
+        return time.perf_counter() - t, it, fmax, done
+
+    m = BoxBatch([n] * replicas, L1, x1, y1, ps, A, R, 0.1, precision="mixed", **kw)
+    ta, ia, _, da = run(m, 1e-6, 200000)
+    xm, ym, pm = m.state()
+    m.close()
+    r = BoxBatch([n] * replicas, L1, xm, ym, pm, A, R, 0.1, precision="fp64", **kw)
+    tb, ib, fb, db = run(r, ftol, max_iter)
+    e_a = r.calc_se()[:, 0]
+    r.close()
+    p = BoxBatch([n] * replicas, L1, x1, y1, ps, A, R, 0.1, precision="fp64", **kw)
+    tc, ic, fc, dc = run(p, ftol, max_iter)
+    e_c = p.calc_se()[:, 0]
+    p.close()
+    both = da & db & dc & (e_c > 0)
+    return {
+        "workload": f"jam_{replicas}x{n}", "replicas": replicas, "N": n, "ftol": ftol,
+        "prep": {"seconds": t_prep, "increments": n_inc,
+                 "phi_jam_range": [float(phi_j.min()), float(phi_j.max())]},
+        "mixed_then_fp64": {"seconds": ta + tb, "mixed_seconds": ta, "mixed_iters": ia,
+                            "fp64_iters": ib, "converged": int((da & db).sum()),
+                            "max_residual": float(fb.max())},
+        "fp64": {"seconds": tc, "iters": ic, "converged": int(dc.sum()),
+                 "max_residual": float(fc.max())},
+        "speedup": tc / (ta + tb),
+        "energy_rel_diff_max": (float(np.max(np.abs(e_a[both] - e_c[both]) / e_c[both]))
+                                if both.any() else None),
+        "note": "iterations capped at max_iter per FP64 stage; 'converged' counts replicas "
+                "below ftol",
+    }
+
+
 def max_over_ranks(secs: float, world: int, device: str) -> float:
     """The slowest rank's time (replicas run independently; this all-reduce is the
     only collective, outside the timed region)."""
@@ -249,6 +318,11 @@ def main():
     ap.add_argument("--only", choices=["mixed", "fp64"], default=None,
                     help="time one form only (for profiler captures)")
     ap.add_argument("--pad", type=float, default=0.2, help="neighbour-list padding")
+    ap.add_argument("--no-minimise", action="store_true",
+                    help="skip the minimisation time-to-tolerance leg")
+    ap.add_argument("--min-replicas", type=int, default=32)
+    ap.add_argument("--min-iters", type=int, default=20000,
+                    help="FP64 FIRE iteration cap of the minimisation leg")
     ap.add_argument("--no-graphs", action="store_true",
                     help="launch eagerly instead of through CUDA graphs (profiler captures: "
                          "kernels inside graphs with conditional nodes cannot be profiled)")
@@ -371,6 +445,10 @@ def main():
            "note": "sc_create from host arrays, steps in chunks of 100 with stress/energy and "
                    "positions read back after each chunk"}
 
+    mini = None
+    if rank == 0 and not args.no_minimise:
+        mini = minimise_leg(args.min_replicas, 4096, args.min_iters, device=local)
+
     base = None
     if rank == 0 and not args.no_cpu and w.get("phi") is not None:
         base = cpu_baseline(w, 65536, args.cpu_steps, os.cpu_count() or 1, args.pad)
@@ -396,6 +474,7 @@ def main():
                          "pass_ms": pass_ms, "bytes_per_particle_pass": bpp, "mean_list_length": nbar,
                          "rebuild_ms_mean": pt["rebuild_ms"]},
             "cpu_baseline": base,
+            "minimise": mini,
             "e2e": e2e,
             "gpu_launches": launches,
             "clocks": clk.summary(local),
