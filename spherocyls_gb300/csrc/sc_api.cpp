@@ -388,41 +388,12 @@ int sc_gd_minimize(sc_handle* H, int max_steps, double e_min, int* steps_taken, 
 }
 
 // slot -> original index (systems concatenated)
-static bool read_ids(sc::Handle& h, std::vector<int>& gid) {
-  std::vector<int> id(h.ntot);
-  if (!h.cuda_ok(cudaMemcpyAsync(id.data(), h.d.id, h.ntot * sizeof(int), cudaMemcpyDeviceToHost,
-                                 h.stream), "read ids"))
-    return false;
-  if (!h.cuda_ok(cudaStreamSynchronize(h.stream), "read ids")) return false;
-  gid.resize(h.ntot);
-  for (int s = 0; s < h.nsys; s++)
-    for (int k = 0; k < h.hs[s].n; k++) {
-      int i = h.hs[s].p0 + k;
-      gid[i] = h.hs[s].p0 + id[i];
-    }
-  return true;
-}
-
 int sc_get_state(sc_handle* H, double* x, double* y, double* phi) {
   if (!H) return SC_E_ARG;
   sc::Handle& h = H->h;
   cudaSetDevice(h.device);
   if (!h.materialize()) return h.last_status;
-  std::vector<double2> xy(h.ntot);
-  std::vector<double> ph(h.ntot);
-  std::vector<int> gid;
-  if (!h.cuda_ok(cudaMemcpyAsync(xy.data(), h.d.xy, h.ntot * sizeof(double2),
-                                 cudaMemcpyDeviceToHost, h.stream), "read state") ||
-      !h.cuda_ok(cudaMemcpyAsync(ph.data(), h.d.ph, h.ntot * sizeof(double),
-                                 cudaMemcpyDeviceToHost, h.stream), "read state") ||
-      !read_ids(h, gid))
-    return h.last_status;
-  for (int i = 0; i < h.ntot; i++) {
-    if (x) x[gid[i]] = xy[i].x;
-    if (y) y[gid[i]] = xy[i].y;
-    if (phi) phi[gid[i]] = ph[i];
-  }
-  return SC_OK;
+  return h.read_unsorted(false, x, y, phi) ? SC_OK : h.last_status;
 }
 
 int sc_get_forces(sc_handle* H, double* fx, double* fy, double* tau) {
@@ -434,22 +405,7 @@ int sc_get_forces(sc_handle* H, double* fx, double* fy, double* tau) {
     int rc = h.calc(false, nullptr);
     if (rc) return rc;
   }
-  std::vector<double> a(h.ntot), b(h.ntot), c(h.ntot);
-  std::vector<int> gid;
-  if (!h.cuda_ok(cudaMemcpyAsync(a.data(), h.d.fx, h.ntot * sizeof(double),
-                                 cudaMemcpyDeviceToHost, h.stream), "read forces") ||
-      !h.cuda_ok(cudaMemcpyAsync(b.data(), h.d.fy, h.ntot * sizeof(double),
-                                 cudaMemcpyDeviceToHost, h.stream), "read forces") ||
-      !h.cuda_ok(cudaMemcpyAsync(c.data(), h.d.tau, h.ntot * sizeof(double),
-                                 cudaMemcpyDeviceToHost, h.stream), "read forces") ||
-      !read_ids(h, gid))
-    return h.last_status;
-  for (int i = 0; i < h.ntot; i++) {
-    if (fx) fx[gid[i]] = a[i];
-    if (fy) fy[gid[i]] = b[i];
-    if (tau) tau[gid[i]] = c[i];
-  }
-  return SC_OK;
+  return h.read_unsorted(true, fx, fy, tau) ? SC_OK : h.last_status;
 }
 
 int sc_get_box(sc_handle* H, int sys, double* out) {

@@ -414,6 +414,27 @@ __global__ void k_se_store(Dev d, double* dst) {
   for (int k = 0; k < 5; k++) dst[5 * s + k] = d.se_sys[(size_t)k * d.nsys + s];
 }
 
+// Output in the caller's particle order: slot i holds particle p0 + id[i] of its
+// system, so each value goes to out[k * ntot + p0 + id[i]].
+__global__ void k_unsort_state(Dev d, double* __restrict__ out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.ntot) return;
+  const size_t o = (size_t)d.geom[d.psys[i]].p0 + d.id[i];
+  const double2 p = d.xy[i];
+  out[o] = p.x;
+  out[(size_t)d.ntot + o] = p.y;
+  out[(size_t)2 * d.ntot + o] = d.ph[i];
+}
+
+__global__ void k_unsort_forces(Dev d, double* __restrict__ out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.ntot) return;
+  const size_t o = (size_t)d.geom[d.psys[i]].p0 + d.id[i];
+  out[o] = d.fx[i];
+  out[(size_t)d.ntot + o] = d.fy[i];
+  out[(size_t)2 * d.ntot + o] = d.tau[i];
+}
+
 inline int nblk(int n, int b) { return (n + b - 1) / b; }
 
 }  // namespace
@@ -482,6 +503,14 @@ void launch_refresh_geometry(const Dev& d, bool mixed, const StepScalars* tab, i
 void launch_gd_update(const Dev& d, bool mixed, const StepScalars* tab, int row, cudaStream_t st) {
   (void)mixed;  // the CPU-compatible gradient descent is a plain FP64 protocol
   k_gd_update<<<nblk(d.ntot, 256), 256, 0, st>>>(d, tab, row);
+}
+
+void launch_unsort_state(const Dev& d, double* out, cudaStream_t st) {
+  k_unsort_state<<<nblk(d.ntot, 256), 256, 0, st>>>(d, out);
+}
+
+void launch_unsort_forces(const Dev& d, double* out, cudaStream_t st) {
+  k_unsort_forces<<<nblk(d.ntot, 256), 256, 0, st>>>(d, out);
 }
 
 void launch_se_store(const Dev& d, double* dst, cudaStream_t st) {

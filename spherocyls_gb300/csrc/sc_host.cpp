@@ -259,6 +259,25 @@ bool Handle::materialize() {
   return cuda_ok(cudaGetLastError(), "materialize");
 }
 
+// State (x, y, phi) or forces (fx, fy, tau) in the caller's particle order: one
+// device scatter by particle index, then one copy per requested array.
+bool Handle::read_unsorted(bool forces, double* a, double* b, double* c) {
+  if (!d_out3 && !dalloc(&d_out3, 3 * (size_t)ntot, "output staging")) return false;
+  if (forces)
+    launch_unsort_forces(d, d_out3, stream);
+  else
+    launch_unsort_state(d, d_out3, stream);
+  kernels += 1;
+  double* dst[3] = {a, b, c};
+  for (int k = 0; k < 3; k++)
+    if (dst[k] && !cuda_ok(cudaMemcpyAsync(dst[k], d_out3 + (size_t)k * ntot,
+                                           (size_t)ntot * sizeof(double),
+                                           cudaMemcpyDeviceToHost, stream),
+                           "read output"))
+      return false;
+  return cuda_ok(cudaStreamSynchronize(stream), "read output");
+}
+
 // full rebuild of every system at the current state (constructor / setters)
 bool Handle::rebuild_all() {
   if (!materialize()) return false;

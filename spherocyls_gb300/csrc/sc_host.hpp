@@ -59,6 +59,7 @@ struct Handle {
   int tab_cap = 0;
   std::vector<StepScalars> h_tab;
   double* d_se_hist = nullptr;
+  double* d_out3 = nullptr;  // [3 * ntot] output staging in the caller's particle order
   int se_hist_cap = 0;
   int* h_pinned = nullptr;  // status word + scratch for small reads
   bool pred_valid = false;  // predictor copy consistent with the state
@@ -138,6 +139,7 @@ struct Handle {
   int run_steps(bool resize, int shrink, int nsteps, int se_every, double* se_out);
   int calc(bool se, double* se_out);
   bool materialize();
+  bool read_unsorted(bool forces, double* a, double* b, double* c);
   int gd_minimize(int max_steps, double e_min, int* steps_taken, double* e_final);
   int gd_step(const double* se_now, double e_min);
   // FIRE minimiser and quasistatic compression
