@@ -200,8 +200,9 @@ def minimise_leg(replicas=32, n=4096, max_iter=20000, ftol=1e-14, device=0):
     N = 4096 with a/R in {0.25, 0.5, 1, 2} (a quarter each), seeds 100 + k, from
     packing 0.70.  Untimed preparation: the mixed form compresses every replica to
     jamming in affine steps of 2e-3 in packing fraction (FIRE to 1e-6 after each,
-    jammed once E/N > 1e-10: residual overlaps of a 1e-6 force tolerance alone give
-    E/N near 1e-12), and each replica is then compressed by one more
+    jammed once E/N > 1e-12; a replica whose FP64 minimum has E/N <= 1e-16 was not
+    jammed and is left out of the energy comparison), and each replica is then
+    compressed by one more
     1e-4 increment.  From that same state the two timed arms minimise to
     max|F_i|, |tau_i|/sqrt(I_i) < ftol: (a) mixed FIRE to 1e-6, then FP64 FIRE;
     (b) FP64 FIRE alone.  Each FP64 stage stops after max_iter iterations."""
@@ -218,7 +219,7 @@ def minimise_leg(replicas=32, n=4096, max_iter=20000, ftol=1e-14, device=0):
                     **kw)
     t0 = time.perf_counter()
     prep.fire_minimize(1e-6, 100000)
-    phi_j, n_inc = prep.quasistatic_compress(2e-3, 1e-6, 1e-10, 1000, 100000)
+    phi_j, n_inc = prep.quasistatic_compress(2e-3, 1e-6, 1e-12, 1000, 100000)
     t_prep = time.perf_counter() - t0
     Lj = np.array([prep.box(s)["Lx"] for s in range(replicas)])
     xs, ys, ps = prep.state()
@@ -244,7 +245,8 @@ def minimise_leg(replicas=32, n=4096, max_iter=20000, ftol=1e-14, device=0):
     tc, ic, fc, dc = run(p, ftol, max_iter)
     e_c = p.calc_se()[:, 0]
     p.close()
-    both = da & db & dc & (e_c > 0)
+    # jammed replicas (E/N > 1e-16 at the FP64 minimum) that both arms converged
+    both = da & db & dc & (e_c > 1e-16) & (e_a > 1e-16)
     return {
         "workload": f"jam_{replicas}x{n}", "replicas": replicas, "N": n, "ftol": ftol,
         "prep": {"seconds": t_prep, "increments": n_inc,
@@ -323,7 +325,7 @@ def main():
     ap.add_argument("--no-minimise", action="store_true",
                     help="skip the minimisation time-to-tolerance leg")
     ap.add_argument("--min-replicas", type=int, default=32)
-    ap.add_argument("--min-iters", type=int, default=20000,
+    ap.add_argument("--min-iters", type=int, default=40000,
                     help="FP64 FIRE iteration cap of the minimisation leg")
     ap.add_argument("--no-graphs", action="store_true",
                     help="launch eagerly instead of through CUDA graphs (profiler captures: "

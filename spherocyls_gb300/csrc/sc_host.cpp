@@ -291,12 +291,12 @@ bool Handle::rebuild_all() {
   return cuda_ok(cudaGetLastError(), "rebuild launch");
 }
 
-void Handle::launch_pass(int mode, bool se, int row) {
+void Handle::launch_pass(int mode, bool se, int row, bool fast) {
   kernels += 1;
   if (prec == PREC_MIXED)
     launch_pass_mixed(d, mode, se, d_tab, row, stream, block);
   else
-    launch_pass_fp64(d, mode, se, d_tab, row, stream);
+    launch_pass_fp64(d, mode, se, d_tab, row, stream, fast);
 }
 
 cudaEvent_t Handle::next_event() {
@@ -750,7 +750,7 @@ bool Handle::ensure_fire() {
 // One FIRE iteration, eagerly: force pass, reductions and update, rebuild chain.
 void Handle::enqueue_fire_iteration(double ftol, double dt_max) {
   const bool mixed = prec == PREC_MIXED;
-  launch_pass(PASS_FORCE, false, 0);
+  launch_pass(PASS_FORCE, false, 0, true);
   launch_fire_iteration_tail(d, fire, ftol, dt_max, mixed, stream);
   // the mixed form moves only its FP32 local state: the flagged systems'
   // FP64 copies are refreshed before the cell sort reads them
@@ -778,7 +778,7 @@ bool Handle::run_fire_graph(int iters, double ftol, double dt_max) {
     const bool mixed = prec == PREC_MIXED;
     cudaError_t e = cudaSuccess;
     for (int k = 0; k < iters && e == cudaSuccess; k++) {
-      launch_pass(PASS_FORCE, false, 0);
+      launch_pass(PASS_FORCE, false, 0, true);
       launch_fire_iteration_tail(d, fire, ftol, dt_max, mixed, stream);
       e = capture_rebuild_node(0, [&](cudaStream_t st) {
         if (mixed) launch_mx_materialize(d, d_tab, 0, false, st);

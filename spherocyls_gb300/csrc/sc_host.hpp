@@ -122,7 +122,7 @@ struct Handle {
   bool ensure_se_hist(int nrec);
   bool check_status(const char* where);
   bool rebuild_all();
-  void launch_pass(int mode, bool se, int row);
+  void launch_pass(int mode, bool se, int row, bool fast = false);
   cudaEvent_t next_event();
   void timed(int kind, bool on, const std::function<void()>& f);
   void collect_times();

@@ -176,8 +176,9 @@ enum PassMode {
 
 // ---- kernel launchers (defined in the .cu files) ----
 // tab: device table, row `row` holds nsys StepScalars.
+// fast: the minimiser's force evaluation (FORCE mode only), with fewer FP64 divisions
 void launch_pass_fp64(const Dev& d, int mode, bool se, const StepScalars* tab, int row,
-                      cudaStream_t st);
+                      cudaStream_t st, bool fast = false);
 void launch_pass_mixed(const Dev& d, int mode, bool se, const StepScalars* tab, int row,
                        cudaStream_t st, int block);
 void launch_setback(const Dev& d, const StepScalars* tab, int row, cudaStream_t st);

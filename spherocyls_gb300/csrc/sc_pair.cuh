@@ -26,9 +26,42 @@ struct PairF64 {
   double e, pxx, pyy, pxy, pyx;   // stress/energy contributions (when requested)
 };
 
+// x / y, or, in the minimiser's form (FAST), x times a reciprocal of y shared by
+// several quotients.  The FAST form trades the last bits of the reference's
+// rounding for fewer FP64 divisions (GB300's FP64 rate is a small fraction of its
+// FP32 rate); the force-evaluation and dynamics paths never use it.
+template <bool FAST>
+__device__ __forceinline__ double qdiv(double x, double y, double inv_y) {
+  return FAST ? x * inv_y : x / y;
+}
+
+// Reciprocals of a = |u_A|^2, c = |u_B|^2, delta and sig from one division.
+struct Recip64 {
+  double a, c, delta, sig;
+};
+__device__ __forceinline__ Recip64 recip64(double a, double c, double delta, double sig) {
+  Recip64 r;
+  const double ac = a * c;
+  if (delta > 0) {
+    const double inv = 1.0 / (ac * delta * sig);
+    const double i_ac = delta * sig * inv;
+    r.delta = ac * sig * inv;
+    r.sig = ac * delta * inv;
+    r.a = c * i_ac;
+    r.c = a * i_ac;
+  } else {
+    const double inv = 1.0 / (ac * sig);
+    r.delta = 0.0;
+    r.sig = ac * inv;
+    r.a = c * sig * inv;
+    r.c = a * sig * inv;
+  }
+  return r;
+}
+
 // dX, dY: raw coordinate differences P - Q (no minimum image yet).
 // Returns true when the spherocylinders overlap.
-template <bool SE>
+template <bool SE, bool FAST = false>
 __device__ __forceinline__ bool pair_fp64(double dX, double dY, double nxA, double nyA, double aP,
                                           double nxB, double nyB, double aQ, double sig,
                                           double gamma, double Lx, double Ly, bool virial,
@@ -43,21 +76,34 @@ __device__ __forceinline__ bool pair_fp64(double dX, double dY, double nxA, doub
   double d = nxA * dX + nyA * dY;
   double e = -nxB * dX - nyB * dY;
   double delta = a * c - b * b;
+  Recip64 iv{};
+  if (FAST) iv = recip64(a, c, delta, sig);
 
-  double t = fmin(fmax((b * d - a * e) / delta, -1.), 1.);
-  double s = -(b * t + d) / a;
+  double t = fmin(fmax((FAST && delta > 0) ? (b * d - a * e) * iv.delta
+                                            : (b * d - a * e) / delta,
+                       -1.), 1.);
+  double s = qdiv<FAST>(-(b * t + d), a, iv.a);
   double sarg = fabs(s);
   s = fmin(fmax(s, -1.), 1.);
-  if (sarg > 1) t = fmin(fmax(-(b * s + e) / c, -1.), 1.);
+  if (sarg > 1) t = fmin(fmax(qdiv<FAST>(-(b * s + e), c, iv.c), -1.), 1.);
 
   double dDx = dX + s * nxA - t * nxB;
   double dDy = dY + s * nyA - t * nyB;
   double dsq = dDx * dDx + dDy * dDy;
   if (!(dsq < sig * sig)) return false;
-  double dij = sqrt(dsq);
-  double dvij = (1.0 - dij / sig) / sig;
-  double Fx = dDx * dvij / dij;
-  double Fy = dDy * dvij / dij;
+  double Fx, Fy, dij, dvij;
+  if (FAST) {
+    const double rs = rsqrt(dsq);
+    dij = dsq * rs;
+    dvij = (1.0 - dij * iv.sig) * iv.sig;
+    Fx = dDx * (dvij * rs);
+    Fy = dDy * (dvij * rs);
+  } else {
+    dij = sqrt(dsq);
+    dvij = (1.0 - dij / sig) / sig;
+    Fx = dDx * dvij / dij;
+    Fy = dDy * dvij / dij;
+  }
   o.fx = Fx;
   o.fy = Fy;
   o.tp = s * nxA * Fy - s * nyA * Fx;
@@ -185,65 +231,67 @@ struct Contacts2 {
   bool has2;
 };
 
+template <bool FAST = false>
 __device__ __forceinline__ Contacts2<double> contacts2_fp64(double a, double b, double c, double d,
                                                             double e, double delta, double dX,
                                                             double dY, double nxA, double nyA,
-                                                            double nxB, double nyB) {
+                                                            double nxB, double nyB,
+                                                            const Recip64& iv = Recip64{}) {
   double s1, t1, s2, t2, s3, t3;
   if (delta <= 0) {
-    s1 = fmin(fmax(-(b + d) / a, -1.0), 1.0);
-    s2 = fmin(fmax(-(d - b) / a, -1.0), 1.0);
+    s1 = fmin(fmax(qdiv<FAST>(-(b + d), a, iv.a), -1.0), 1.0);
+    s2 = fmin(fmax(qdiv<FAST>(-(d - b), a, iv.a), -1.0), 1.0);
     if (fabs(s1) == 1)
-      t1 = fmin(fmax(-(b * s1 + e) / c, -1.0), 1.0);
+      t1 = fmin(fmax(qdiv<FAST>(-(b * s1 + e), c, iv.c), -1.0), 1.0);
     else if (b < 0)
-      t1 = fmin(fmax(-(b + e) / c, -1.0), 1.0);
+      t1 = fmin(fmax(qdiv<FAST>(-(b + e), c, iv.c), -1.0), 1.0);
     else
-      t1 = fmin(fmax(-(e - b) / c, -1.0), 1.0);
+      t1 = fmin(fmax(qdiv<FAST>(-(e - b), c, iv.c), -1.0), 1.0);
     if (fabs(s2) == 1)
-      t2 = fmin(fmax(-(b * s2 + e) / c, -1.0), 1.0);
+      t2 = fmin(fmax(qdiv<FAST>(-(b * s2 + e), c, iv.c), -1.0), 1.0);
     else if (b < 0)
-      t2 = fmin(fmax(-(e - b) / c, -1.0), 1.0);
+      t2 = fmin(fmax(qdiv<FAST>(-(e - b), c, iv.c), -1.0), 1.0);
     else
-      t2 = fmin(fmax(-(b + e) / c, -1.0), 1.0);
+      t2 = fmin(fmax(qdiv<FAST>(-(b + e), c, iv.c), -1.0), 1.0);
     s3 = s2;
     t3 = t2;
   } else {
-    t1 = fmin(fmax((b * d - a * e) / delta, -1.), 1.);
-    s1 = -(b * t1 + d) / a;
+    t1 = fmin(fmax(qdiv<FAST>(b * d - a * e, delta, iv.delta), -1.), 1.);
+    s1 = qdiv<FAST>(-(b * t1 + d), a, iv.a);
     double sarg = fabs(s1);
     s1 = fmin(fmax(s1, -1.), 1.);
     if (sarg >= 1) {
-      t1 = fmin(fmax(-(b * s1 + e) / c, -1.), 1.);
+      t1 = fmin(fmax(qdiv<FAST>(-(b * s1 + e), c, iv.c), -1.), 1.);
       s2 = -s1;
-      t2 = -(b * s2 + e) / c;
+      t2 = qdiv<FAST>(-(b * s2 + e), c, iv.c);
       double targ = fabs(t2);
       t2 = fmin(fmax(t2, -1.), 1.);
       if (targ > 1) {
-        s2 = fmin(fmax(-(b * t2 + d) / a, -1.), 1.);
+        s2 = fmin(fmax(qdiv<FAST>(-(b * t2 + d), a, iv.a), -1.), 1.);
         s3 = s2;
         t3 = t2;
       } else {
         t3 = b < 0 ? -s1 : s1;
-        s3 = -(b * t3 + d) / a;
+        s3 = qdiv<FAST>(-(b * t3 + d), a, iv.a);
         sarg = fabs(s3);
         s3 = fmin(fmax(s3, -1.0), 1.0);
-        if (sarg >= 1) t3 = fmin(fmax(-(b * s3 + e) / c, -1.0), 1.0);
+        if (sarg >= 1) t3 = fmin(fmax(qdiv<FAST>(-(b * s3 + e), c, iv.c), -1.0), 1.0);
       }
     } else {
       t2 = -t1;
-      s2 = -(b * t2 + d) / a;
+      s2 = qdiv<FAST>(-(b * t2 + d), a, iv.a);
       sarg = fabs(s2);
       s2 = fmin(fmax(s2, -1.), 1.);
       if (sarg > 1) {
-        t2 = fmin(fmax(-(b * s2 + e) / c, -1.), 1.);
+        t2 = fmin(fmax(qdiv<FAST>(-(b * s2 + e), c, iv.c), -1.), 1.);
         s3 = s2;
         t3 = t2;
       } else {
         s3 = b < 0 ? -t1 : t1;
-        t3 = -(b * s3 + e) / c;
+        t3 = qdiv<FAST>(-(b * s3 + e), c, iv.c);
         double targ = fabs(t3);
         t3 = fmin(fmax(t3, -1.0), 1.0);
-        if (targ >= 1) s3 = fmin(fmax(-(b * t3 + d) / a, -1.0), 1.0);
+        if (targ >= 1) s3 = fmin(fmax(qdiv<FAST>(-(b * t3 + d), a, iv.a), -1.0), 1.0);
       }
     }
   }
@@ -266,18 +314,28 @@ __device__ __forceinline__ Contacts2<double> contacts2_fp64(double a, double b, 
 
 // One harmonic contact at spine parameters (s, t); accumulates into o (no SE arms
 // beyond the virial form: the two-point model is the reference's jamming path).
-template <bool SE>
+template <bool SE, bool FAST = false>
 __device__ __forceinline__ bool contact_fp64(double dX, double dY, double s, double t, double nxA,
                                              double nyA, double nxB, double nyB, double sig,
-                                             double LL, double two_n, PairF64& o) {
+                                             double LL, double two_n, PairF64& o,
+                                             double inv_sig = 0.0) {
   double dDx = dX + s * nxA - t * nxB;
   double dDy = dY + s * nyA - t * nyB;
   double dsq = dDx * dDx + dDy * dDy;
   if (!(dsq < sig * sig)) return false;
-  double dij = sqrt(dsq);
-  double dvij = (1.0 - dij / sig) / sig;
-  double Fx = dDx * dvij / dij;
-  double Fy = dDy * dvij / dij;
+  double dij, dvij, Fx, Fy;
+  if (FAST) {
+    const double rs = rsqrt(dsq);
+    dij = dsq * rs;
+    dvij = (1.0 - dij * inv_sig) * inv_sig;
+    Fx = dDx * (dvij * rs);
+    Fy = dDy * (dvij * rs);
+  } else {
+    dij = sqrt(dsq);
+    dvij = (1.0 - dij / sig) / sig;
+    Fx = dDx * dvij / dij;
+    Fy = dDy * dvij / dij;
+  }
   o.fx += Fx;
   o.fy += Fy;
   o.tp += s * nxA * Fy - s * nyA * Fx;
@@ -296,7 +354,7 @@ __device__ __forceinline__ bool contact_fp64(double dX, double dY, double s, dou
 
 // Two-point contact pair in FP64 (minimum image and Lees-Edwards shift applied
 // here, as in pair_fp64).  Stress uses the virial arms.
-template <bool SE>
+template <bool SE, bool FAST = false>
 __device__ __forceinline__ bool pair2_fp64(double dX, double dY, double nxA, double nyA,
                                            double aP, double nxB, double nyB, double aQ,
                                            double sig, double gamma, double Lx, double Ly,
@@ -310,12 +368,18 @@ __device__ __forceinline__ bool pair2_fp64(double dX, double dY, double nxA, dou
   double d = nxA * dX + nyA * dY;
   double e = -nxB * dX - nyB * dY;
   double delta = a * c - b * b;
-  Contacts2<double> k = contacts2_fp64(a, b, c, d, e, delta, dX, dY, nxA, nyA, nxB, nyB);
+  Recip64 iv{};
+  if (FAST) iv = recip64(a, c, delta, sig);
+  Contacts2<double> k =
+      contacts2_fp64<FAST>(a, b, c, d, e, delta, dX, dY, nxA, nyA, nxB, nyB, iv);
   o.fx = o.fy = o.tp = o.tq = 0.0;
   o.e = o.pxx = o.pyy = o.pxy = o.pyx = 0.0;
   const double LL = Lx * Ly;
-  bool hit = contact_fp64<SE>(dX, dY, k.s1, k.t1, nxA, nyA, nxB, nyB, sig, LL, two_n, o);
-  if (k.has2) hit |= contact_fp64<SE>(dX, dY, k.s2, k.t2, nxA, nyA, nxB, nyB, sig, LL, two_n, o);
+  bool hit = contact_fp64<SE, FAST>(dX, dY, k.s1, k.t1, nxA, nyA, nxB, nyB, sig, LL, two_n, o,
+                                    iv.sig);
+  if (k.has2)
+    hit |= contact_fp64<SE, FAST>(dX, dY, k.s2, k.t2, nxA, nyA, nxB, nyB, sig, LL, two_n, o,
+                                  iv.sig);
   return hit;
 }
 

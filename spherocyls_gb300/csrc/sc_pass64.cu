@@ -90,7 +90,7 @@ __device__ __forceinline__ void flag_moved(const Dev& d, int s, int id, double2 
   }
 }
 
-template <int MODE, bool SE, bool TWO>
+template <int MODE, bool SE, bool TWO, bool FAST = false>
 __global__ void __launch_bounds__(128) k_pass64(Dev d, const StepScalars* __restrict__ tab,
                                                int row) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -151,10 +151,10 @@ __global__ void __launch_bounds__(128) k_pass64(Dev d, const StepScalars* __rest
       const double2 rP = ip ? rai : raj, rQ = ip ? raj : rai;
       PairF64 o;
       const bool hit =
-          two_point ? pair2_fp64<SE>(pP.x - pQ.x, pP.y - pQ.y, nP.x, nP.y, rP.y, nQ.x, nQ.y, rQ.y,
-                                     rP.x + rQ.x, gamma, Lx, Ly, two_n, o)
-                    : pair_fp64<SE>(pP.x - pQ.x, pP.y - pQ.y, nP.x, nP.y, rP.y, nQ.x, nQ.y, rQ.y,
-                                    rP.x + rQ.x, gamma, Lx, Ly, virial, two_n, o);
+          two_point ? pair2_fp64<SE, FAST>(pP.x - pQ.x, pP.y - pQ.y, nP.x, nP.y, rP.y, nQ.x,
+                                           nQ.y, rQ.y, rP.x + rQ.x, gamma, Lx, Ly, two_n, o)
+                    : pair_fp64<SE, FAST>(pP.x - pQ.x, pP.y - pQ.y, nP.x, nP.y, rP.y, nQ.x, nQ.y,
+                                          rQ.y, rP.x + rQ.x, gamma, Lx, Ly, virial, two_n, o);
       if (hit) {
         if (ip) {
           fx += o.fx;
@@ -312,7 +312,16 @@ void launch_one(const Dev& d, const StepScalars* tab, int row, cudaStream_t st) 
 }  // namespace
 
 void launch_pass_fp64(const Dev& d, int mode, bool se, const StepScalars* tab, int row,
-                      cudaStream_t st) {
+                      cudaStream_t st, bool fast) {
+  if (fast && mode == PASS_FORCE && !se) {
+    // the minimiser's force evaluation (shared reciprocals, see qdiv)
+    const int block = 128, grid = (d.ntot + block - 1) / block;
+    if (d.contact_model == 1)
+      k_pass64<PASS_FORCE, false, true, true><<<grid, block, 0, st>>>(d, tab, row);
+    else
+      k_pass64<PASS_FORCE, false, false, true><<<grid, block, 0, st>>>(d, tab, row);
+    return;
+  }
   switch (mode) {
     case PASS_FORCE:
       se ? launch_one<PASS_FORCE, true>(d, tab, row, st) : launch_one<PASS_FORCE, false>(d, tab, row, st);
