@@ -56,6 +56,9 @@ extern "C" {
 
 #define SC_FMT_SP 0 /* src/cpp position file: "N L phi gamma gamma_tot rate dt" */
 #define SC_FMT_SD 1 /* src/cuda position file: "N Lx Ly phi gamma gamma_tot rate dt" */
+#define SC_FMT_BIN 2 /* src/cuda binary position file (save_positions_bin,
+                      * src/cuda/strain_dynamics.cu:845-875): int N, then the sd header's
+                      * seven doubles, then x y phi R A as doubles per particle */
 
 typedef struct sc_handle sc_handle;
 
@@ -137,6 +140,14 @@ int sc_affine_scale(sc_handle *h, int sys, double factor);
  * *n_inc the increments made. */
 int sc_quasistatic_compress(sc_handle *h, double dphi, double ftol, double e_jam,
                             int max_increments, int max_iter, double *phi_jam, int *n_inc);
+/* find_jam_2p / resize_to_energy_2p (src/cuda/2point_dynamics.cu:4582-4606,
+ * 4393-4456): per system, affine length steps of 1 -/+ step (growing by 1.1 per
+ * step, FIRE to ftol after each) towards energy per particle e_jam, reversing with
+ * half the last step each time the energy crosses e_jam, until the step is below
+ * min_step or max_steps resizes were made.  phi_jam[s]: final packing fraction of
+ * system s (negated when max_steps ran out first); *steps: resizes made. */
+int sc_find_jam(sc_handle *h, double e_jam, double step, double min_step, double ftol,
+                int max_iter, int max_steps, double *phi_jam, int *steps);
 
 /* State readers, original particle order, systems concatenated. */
 int sc_get_state(sc_handle *h, double *x, double *y, double *phi);
@@ -175,7 +186,9 @@ int sc_generate_packing(int n, double packing, double a_over_r, double r_small, 
 int sc_read_positions(const char *path, int *n, double *hdr, double *x, double *y, double *phi,
                       double *R, double *A);
 /* save_positions: SC_FMT_SP as src/cpp/spherocyl_box.cpp:410-423 (precision 14),
- * SC_FMT_SD as src/cuda/strain_dynamics.cu:820-843 (%.17g rows). */
+ * SC_FMT_SD as src/cuda/strain_dynamics.cu:820-843 (%.17g rows), SC_FMT_BIN as
+ * src/cuda/strain_dynamics.cu:845-875 (host byte order).  sc_read_positions reads a
+ * path ending in ".bin" as SC_FMT_BIN, any other as text with either header. */
 int sc_save_positions(sc_handle *h, int sys, const char *path, int format);
 
 /* run_strain with output, src/cpp/strain_dynamics.cpp:238-319: t runs from t_start

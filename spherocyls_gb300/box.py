@@ -41,12 +41,13 @@ def generate_packing(n: int, packing: float, a_over_r: float, r_small: float = 0
     return L.value, x, y, p, R, A
 
 
-FMT = {"sp": 0, "sd": 1}
+FMT = {"sp": 0, "sd": 1, "bin": 2}
 
 
 def read_positions(path: str):
-    """Read a position file (src/cpp or src/cuda header); returns (hdr, x, y, phi, R, A)
-    with hdr = dict(Lx, Ly, packing, gamma, gamma_total, rate, dt)."""
+    """Read a position file (src/cpp or src/cuda text header, or the src/cuda binary
+    layout for a path ending in .bin); returns (hdr, x, y, phi, R, A) with
+    hdr = dict(Lx, Ly, packing, gamma, gamma_total, rate, dt)."""
     n = ctypes.c_int(0)
     hdr = np.empty(7)
     L = lib()
@@ -203,6 +204,18 @@ class BoxBatch:
         self._chk(lib().sc_quasistatic_compress(self.h, float(dphi), float(ftol), float(e_jam),
                                                 int(max_increments), int(max_iter), _ptr(pj),
                                                 ctypes.byref(n)))
+        return pj, n.value
+
+    def find_jam(self, e_jam: float, step: float = 1e-3, min_step: float = 1e-12,
+                 ftol: float = 1e-13, max_iter: int = 200000, max_steps: int = 10000):
+        """Bisect each system's packing fraction to energy per particle e_jam
+        (find_jam_2p); returns (phi[nsys], resizes made), phi negated where
+        max_steps ran out first."""
+        pj = np.empty(self.nsys)
+        n = ctypes.c_int()
+        self._chk(lib().sc_find_jam(self.h, float(e_jam), float(step), float(min_step),
+                                    float(ftol), int(max_iter), int(max_steps), _ptr(pj),
+                                    ctypes.byref(n)))
         return pj, n.value
 
     # --- runs with file output (single-system handles) -------------------------

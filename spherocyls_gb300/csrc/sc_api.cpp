@@ -495,6 +495,12 @@ int sc_quasistatic_compress(sc_handle* H, double dphi, double ftol, double e_jam
   return H->h.quasistatic(dphi, ftol, e_jam, max_increments, max_iter, phi_jam, n_inc);
 }
 
+int sc_find_jam(sc_handle* H, double e_jam, double step, double min_step, double ftol,
+                int max_iter, int max_steps, double* phi_jam, int* steps) {
+  if (!H) return SC_E_ARG;
+  return H->h.find_jam(e_jam, step, min_step, ftol, max_iter, max_steps, phi_jam, steps);
+}
+
 int sc_get_counters(sc_handle* H, long long* out) {
   if (!H || !out) return SC_E_ARG;
   out[0] = H->h.steps;

@@ -917,4 +917,77 @@ int Handle::quasistatic(double dphi, double ftol, double e_jam, int max_inc, int
   return SC_OK;
 }
 
+// Jamming point by bisection on the energy (find_jam_2p with resize_to_energy_2p,
+// src/cuda/2point_dynamics.cu:4582-4606, 4393-4456), per system: a phase
+// compresses while E/N < e_jam (expands while E/N > e_jam) by affine length steps
+// of 1 - step (1 + step), minimising after each and growing the step by 1.1 per
+// step; once the energy has crossed e_jam the next phase starts the other way with
+// half the last step, until the step falls below min_step.  The reference compares
+// the total energy; here e_jam is an energy per particle.
+int Handle::find_jam(double e_jam, double step0, double min_step, double ftol, int max_iter,
+                     int max_steps, double* phi_jam, int* steps_out) {
+  if (!(e_jam > 0) || !(step0 > 0) || !(min_step > 0) || max_steps < 0) {
+    fail(SC_E_ARG, "find_jam: need e_jam > 0, step > 0, min_step > 0, max_steps >= 0");
+    return SC_E_ARG;
+  }
+  struct Phase {
+    int dir = 0;          // +1 compress, -1 expand, 0 finished
+    double step = 0;      // step of this phase's first resize
+    double next = 0;      // step of the next resize
+    int k = 0;            // resizes made in this phase
+  };
+  std::vector<Phase> ph(nsys);
+  std::vector<double> se(5 * (size_t)nsys);
+  int rc = fire_minimize(ftol, max_iter, 1e-2, 0.2, nullptr, nullptr, nullptr);
+  if (rc && rc != SC_E_NOCONV) return rc;
+  if ((rc = calc(true, se.data()))) return rc;
+  auto start_phase = [&](int s, double step) {
+    Phase& q = ph[s];
+    const double e = se[5 * s];
+    // an energy exactly at e_jam makes every later phase empty (only the step
+    // shrinks), so the system is finished where it is
+    q.dir = e < e_jam ? 1 : (e > e_jam ? -1 : 0);
+    q.step = q.next = step;
+    q.k = 0;
+  };
+  for (int s = 0; s < nsys; s++) start_phase(s, step0);
+  if (!(step0 > min_step))
+    for (auto& q : ph) q.dir = 0;
+  int steps = 0;
+  for (; steps < max_steps; steps++) {
+    std::vector<double> f(nsys, 1.0);
+    bool any = false;
+    for (int s = 0; s < nsys; s++)
+      if (ph[s].dir != 0) {
+        f[s] = ph[s].dir > 0 ? 1.0 - ph[s].next : 1.0 + ph[s].next;
+        any = true;
+      }
+    if (!any) break;
+    if ((rc = affine_scale(f))) return rc;
+    rc = fire_minimize(ftol, max_iter, 1e-2, 0.2, nullptr, nullptr, nullptr);
+    if (rc && rc != SC_E_NOCONV) return rc;
+    if ((rc = calc(true, se.data()))) return rc;
+    for (int s = 0; s < nsys; s++) {
+      Phase& q = ph[s];
+      if (q.dir == 0) continue;
+      q.k += 1;
+      q.next *= 1.1;
+      const double e = se[5 * s];
+      const bool crossed = q.dir > 0 ? !(e < e_jam) : !(e > e_jam);
+      if (!crossed) continue;
+      // find_jam_2p: dResizeStep * 1.1^(steps in the phase - 1) / 2
+      const double step = q.step * std::pow(1.1, q.k - 1) / 2;
+      if (!(step > min_step)) {
+        q.dir = 0;
+        continue;
+      }
+      start_phase(s, step);
+    }
+  }
+  for (int s = 0; s < nsys; s++)
+    if (phi_jam) phi_jam[s] = ph[s].dir == 0 ? hs[s].packing : -hs[s].packing;
+  if (steps_out) *steps_out = steps;
+  return SC_OK;
+}
+
 }  // namespace sc

@@ -152,6 +152,8 @@ struct Handle {
   int affine_scale(const std::vector<double>& factor);
   int quasistatic(double dphi, double ftol, double e_jam, int max_inc, int max_iter,
                   double* phi_jam, int* n_inc);
+  int find_jam(double e_jam, double step0, double min_step, double ftol, int max_iter,
+               int max_steps, double* phi_jam, int* steps_out);
 };
 
 // last error of calls made without a handle (creation, file reading)

@@ -117,10 +117,51 @@ int check_single(sc_handle* H, const char* what) {
 
 extern "C" {
 
+// Binary position file, save_positions_bin (src/cuda/strain_dynamics.cu:845-875).
+static int read_bin(const char* path, int* n, double* hdr, double* x, double* y, double* phi,
+                    double* R, double* A) {
+  FILE* f = fopen(path, "rb");
+  if (!f) return io_fail(nullptr, SC_E_IO, std::string("cannot open ") + path);
+  int N = 0;
+  double h[7];
+  bool ok = fread(&N, sizeof N, 1, f) == 1 && fread(h, sizeof(double), 7, f) == 7 && N >= 0;
+  if (!ok) {
+    fclose(f);
+    return io_fail(nullptr, SC_E_IO, std::string("short header in ") + path);
+  }
+  if (hdr) memcpy(hdr, h, sizeof h);
+  if (!x) {
+    fclose(f);
+    *n = N;
+    return SC_OK;
+  }
+  if (*n < N) {
+    fclose(f);
+    return io_fail(nullptr, SC_E_ARG, "arrays too short for the file");
+  }
+  for (int k = 0; k < N && ok; k++) {
+    double v[5];
+    ok = fread(v, sizeof(double), 5, f) == 5;
+    if (ok) {
+      x[k] = v[0];
+      y[k] = v[1];
+      phi[k] = v[2];
+      R[k] = v[3];
+      A[k] = v[4];
+    }
+  }
+  fclose(f);
+  if (!ok) return io_fail(nullptr, SC_E_IO, "fewer particles than the header's N");
+  *n = N;
+  return SC_OK;
+}
+
 int sc_read_positions(const char* path, int* n, double* hdr, double* x, double* y, double* phi,
                       double* R, double* A) {
   sc::g_noh_error.clear();
   if (!path || !n) return SC_E_ARG;
+  const size_t plen = strlen(path);
+  if (plen >= 4 && strcmp(path + plen - 4, ".bin") == 0) return read_bin(path, n, hdr, x, y, phi, R, A);
   std::ifstream in(path);
   if (!in) return io_fail(nullptr, SC_E_IO, std::string("cannot open ") + path);
   std::string line;
@@ -176,6 +217,20 @@ int sc_save_positions(sc_handle* H, int sys, const char* path, int format) {
   if (rc) return rc;
   const sc::HostSys& S = h.hs[sys];
   double packing = S.packing * (h.hs[sys].Lx > 0 ? 1.0 : 0.0);
+  if (format == SC_FMT_BIN) {
+    FILE* f = fopen(path, "wb");
+    if (!f) return io_fail(&h, SC_E_IO, std::string("cannot open ") + path);
+    const double head[7] = {S.Lx, S.Ly, packing, S.gamma, S.gamma_total, S.strain_rate, S.step};
+    bool ok = fwrite(&S.n, sizeof S.n, 1, f) == 1 && fwrite(head, sizeof(double), 7, f) == 7;
+    for (int k = 0; k < S.n && ok; k++) {
+      const double v[5] = {x[k], y[k], p[k], h.h_R[S.p0 + k], h.h_A[S.p0 + k]};
+      ok = fwrite(v, sizeof(double), 5, f) == 5;
+    }
+    ok = (fclose(f) == 0) && ok;
+    return ok ? SC_OK : io_fail(&h, SC_E_IO, std::string("write failed: ") + path);
+  }
+  if (format != SC_FMT_SP && format != SC_FMT_SD)
+    return io_fail(&h, SC_E_ARG, "sc_save_positions: unknown format");
   if (format == SC_FMT_SD) {
     FILE* f = fopen(path, "w");
     if (!f) return io_fail(&h, SC_E_IO, std::string("cannot open ") + path);
@@ -207,6 +262,8 @@ int sc_run_strain(sc_handle* H, const char* out_dir, double run_gamma, double po
   sc::HostSys& S = h.hs[0];
   if (!out_dir || !(S.strain_rate != 0) || !(S.step > 0) || !(run_gamma >= 0))
     return io_fail(&h, SC_E_ARG, "sc_run_strain: needs an output directory, rate != 0, dt > 0");
+  if (format != SC_FMT_SP && format != SC_FMT_SD)
+    return io_fail(&h, SC_E_ARG, "sc_run_strain: format must be SC_FMT_SP or SC_FMT_SD");
   const double rate = S.strain_rate, dt = S.step;
   // the drivers' clamps, src/cpp/main.cpp:87-90
   if (se_save < rate * dt) se_save = rate * dt;
@@ -257,6 +314,8 @@ int sc_run_resize(sc_handle* H, const char* out_dir, double final_packing, doubl
   if (!out_dir || !(h.hs[0].resize_rate > 0 && h.hs[0].resize_rate < 1) || !(h.hs[0].step > 0) ||
       !(final_packing > 0))
     return io_fail(&h, SC_E_ARG, "sc_run_resize: needs an output directory, 0 < rate < 1, dt > 0");
+  if (format != SC_FMT_SP && format != SC_FMT_SD)
+    return io_fail(&h, SC_E_ARG, "sc_run_resize: format must be SC_FMT_SP or SC_FMT_SD");
   const double rate = h.hs[0].resize_rate, dt = h.hs[0].step;
   if (se_save < rate * dt) se_save = rate * dt;  // src/cpp/main_resize.cpp:283-286
   if (pos_save < rate) pos_save = rate;

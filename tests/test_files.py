@@ -46,6 +46,33 @@ def test_read_positions_both_headers(library, tmp_path):
     assert np.array_equal(xx, x)
 
 
+def test_read_binary_positions(library, tmp_path):
+    """The src/cuda binary layout (save_positions_bin): int N, the sd header's seven
+    doubles, then x y phi R A per particle, host byte order."""
+    import struct
+
+    from spherocyls_gb300 import ScError, read_positions
+
+    rng = np.random.default_rng(1)
+    n = 7
+    vals = rng.uniform(0, 5, (n, 5))
+    head = (5.0, 6.0, 0.85, 0.25, 3.25, 1e-4, 0.02)
+    path = tmp_path / "sd0000000042.bin"
+    with open(path, "wb") as f:
+        f.write(struct.pack("=i7d", n, *head))
+        for row in vals:
+            f.write(struct.pack("=5d", *row))
+    hdr, x, y, p, R, A = read_positions(str(path))
+    assert [hdr[k] for k in ("Lx", "Ly", "packing", "gamma", "gamma_total", "rate", "dt")] == \
+        list(head)
+    assert np.array_equal(np.stack([x, y, p, R, A], axis=1), vals)
+    short = tmp_path / "short.bin"
+    with open(short, "wb") as f:
+        f.write(struct.pack("=i7d", n, *head) + struct.pack("=5d", *vals[0]))
+    with pytest.raises(ScError):
+        read_positions(str(short))
+
+
 def test_read_positions_errors(library, tmp_path):
     from spherocyls_gb300 import ScError, read_positions
 
@@ -108,6 +135,34 @@ def test_run_strain_files_and_continue(library, tmp_path):
     # the file holds 14 significant digits; two t-units of dynamics later the
     # positions still agree closely with the uninterrupted run
     assert np.max(np.abs(xb - xs)) < 1e-6
+
+
+@pytest.mark.gpu
+def test_save_positions_all_formats_round_trip(library, tmp_path):
+    """sp (precision 14), sd (%.17g) and binary files of the same state read back to
+    the state: the binary and sd files bit for bit."""
+    import spherocyls_gb300 as sc
+
+    L, x, y, p, R, A = sc.generate_packing(64, 0.80, 1.0, seed=5)
+    box = sc.SpherocylBox(L, x, y, p, A, R, 0.1)
+    box.set_strain_rate(1e-3)
+    box.set_step(0.02)
+    box.strain_steps(10)
+    xs, ys, ps = box.state()
+    for fmt, name, exact in (("bin", "sd0000000010.bin", True), ("sd", "sd0000000010.dat", True),
+                             ("sp", "sp0000000010.dat", False)):
+        path = str(tmp_path / name)
+        box.save_positions(path, fmt)
+        hdr, xx, yy, pp, RR, AA = sc.read_positions(path)
+        got = np.stack([xx, yy, pp])
+        want = np.stack([xs, ys, ps])
+        if exact:
+            assert np.array_equal(got, want), fmt
+            assert np.array_equal(AA, A)
+        else:
+            assert np.max(np.abs(got - want)) < 1e-12 * L, fmt
+        assert abs(hdr["gamma"] - box.box()["gamma"]) <= 1e-13
+        assert hdr["dt"] == 0.02
 
 
 @pytest.mark.gpu

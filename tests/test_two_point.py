@@ -176,3 +176,24 @@ def test_quasistatic_two_point_jams(library):
     assert np.all(phi_jam > 0.80) and np.all(phi_jam < 0.95), phi_jam
     se = batch.calc_se()
     assert np.all(se[:, 0] > 1e-10)
+
+
+@pytest.mark.gpu
+def test_find_jam_bisects_to_target_energy(library):
+    """find_jam_2p's bisection: each system ends at a packing fraction whose
+    minimised energy per particle sits at e_jam (the final steps are below 1e-7 in
+    length, where E/N changes by well under a percent of e_jam)."""
+    import spherocyls_gb300 as sc
+
+    packs = [sc.generate_packing(96, 0.80, a, seed=s) for a, s in ((1.0, 81), (0.5, 82))]
+    batch = sc.BoxBatch([96, 96], [pk[0] for pk in packs],
+                        np.concatenate([pk[1] for pk in packs]),
+                        np.concatenate([pk[2] for pk in packs]),
+                        np.concatenate([pk[3] for pk in packs]),
+                        np.concatenate([pk[5] for pk in packs]),
+                        np.concatenate([pk[4] for pk in packs]), 0.1, contacts=2)
+    e_jam = 1e-8
+    phi, steps = batch.find_jam(e_jam, step=1e-3, min_step=1e-7, ftol=1e-11)
+    assert np.all(phi > 0.8) and np.all(phi < 0.95), phi
+    e = batch.calc_se()[:, 0]
+    assert np.all(np.abs(e - e_jam) < 0.05 * e_jam), e
