@@ -175,6 +175,29 @@ int sc_generate_packing(int n, double packing, double a_over_r, double r_small, 
                         uint64_t seed, double min_sep, double *x, double *y, double *phi,
                         double *R, double *A, double *L);
 
+/* The reference's initial configurations (place_spherocyls, place_random_0e_spherocyls,
+ * place_spherocyl_grid, set_shapes, uniformToAngleDist:
+ * src/cuda/spherocyl_box.cpp:1044-1394), seeded and reproducible. */
+#define SC_LAYOUT_RANDOM 0 /* centres uniform in the box */
+#define SC_LAYOUT_GRID 1   /* one particle per grid cell, rows offset at random */
+#define SC_ANGLE_RANDOM 0  /* u uniform in [angle_min, angle_max] */
+#define SC_ANGLE_EVEN 1    /* u = angle_min + (2i+1)(angle_max - angle_min)/(2n) */
+typedef struct sc_gen_options {
+  int layout;         /* SC_LAYOUT_* */
+  int angle_mode;     /* SC_ANGLE_*; angle_min == angle_max gives aligned particles */
+  double angle_min;   /* u range in [0, 1]; the angle is pi u - pi/2, or with     */
+  double angle_max;   /* shear_angles the isolated-rotation steady-shear quantile */
+  int shear_angles;
+  double min_sep;     /* reject spine distances below min_sep (R_i + R_j) */
+  double max_overlap; /* >= 0: also reject d^2 < (1 - max_overlap)(R_i + R_j)^2
+                       * (0 = zero energy); < 0: off */
+  double a_sigma;     /* > 0: a/R Gamma-distributed, mean a_over_r, std a_sigma*a_over_r */
+} sc_gen_options;
+void sc_default_gen_options(sc_gen_options *opt); /* random, u in [0,1], min_sep 0.1 */
+int sc_generate_config(const sc_gen_options *opt, int n, double packing, double a_over_r,
+                       double r_small, double r_ratio, uint64_t seed, double *x, double *y,
+                       double *phi, double *R, double *A, double *L);
+
 /* ---- files and run protocols with output (single-system handles) ---- */
 
 /* Read a position file (DatFileInput with a header row, src/cpp/file_input.h:24-76).

@@ -6,6 +6,7 @@ The work is done by ``libspherocyl`` (C++ host runtime + hand-written CUDA kerne
 C ABI in ``include/spherocyl.h``); this package binds it with ctypes.
 """
 from ._lib import ScError, lib
-from .box import BoxBatch, SpherocylBox, generate_packing, read_positions
+from .box import BoxBatch, SpherocylBox, generate_config, generate_packing, read_positions
 
-__all__ = ["BoxBatch", "SpherocylBox", "generate_packing", "read_positions", "ScError", "lib"]
+__all__ = ["BoxBatch", "SpherocylBox", "generate_config", "generate_packing", "read_positions",
+           "ScError", "lib"]

@@ -45,6 +45,19 @@ class ScOptions(ctypes.Structure):
     ]
 
 
+class ScGenOptions(ctypes.Structure):
+    _fields_ = [
+        ("layout", ctypes.c_int),
+        ("angle_mode", ctypes.c_int),
+        ("angle_min", ctypes.c_double),
+        ("angle_max", ctypes.c_double),
+        ("shear_angles", ctypes.c_int),
+        ("min_sep", ctypes.c_double),
+        ("max_overlap", ctypes.c_double),
+        ("a_sigma", ctypes.c_double),
+    ]
+
+
 # (name, restype, argtypes) of every entry point declared in include/spherocyl.h
 SIGNATURES = [
     ("sc_version", ctypes.c_char_p, []),
@@ -85,6 +98,10 @@ SIGNATURES = [
     ("sc_generate_packing", ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                            ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
                                            ctypes.c_double, _dp, _dp, _dp, _dp, _dp, _dp]),
+    ("sc_default_gen_options", None, [_vp]),
+    ("sc_generate_config", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                          ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
+                                          _dp, _dp, _dp, _dp, _dp, _dp]),
     ("sc_read_positions", ctypes.c_int, [ctypes.c_char_p, _ip, _dp, _dp, _dp, _dp, _dp, _dp]),
     ("sc_save_positions", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_int]),
     ("sc_run_strain", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_double, ctypes.c_double,

@@ -41,6 +41,33 @@ def generate_packing(n: int, packing: float, a_over_r: float, r_small: float = 0
     return L.value, x, y, p, R, A
 
 
+def generate_config(n: int, packing: float, a_over_r: float, *, layout: str = "random",
+                    angles: str = "random", angle_range=(0.0, 1.0), shear_angles: bool = False,
+                    min_sep: float = 0.1, max_overlap: float = -1.0, a_sigma: float = 0.0,
+                    r_small: float = 0.5, r_ratio: float = 1.4, seed: int = 0):
+    """The reference's initial configurations (random / zero-energy / grid layouts;
+    random, evenly spaced or aligned angles; Gamma-distributed a/R), seeded:
+    returns (L, x, y, phi, R, A).  Zero energy: max_overlap=0.  Aligned:
+    angle_range=(u, u)."""
+    from ._lib import ScGenOptions
+
+    o = ScGenOptions()
+    lib().sc_default_gen_options(ctypes.byref(o))
+    o.layout = {"random": 0, "grid": 1}[layout]
+    o.angle_mode = {"random": 0, "even": 1}[angles]
+    o.angle_min, o.angle_max = float(angle_range[0]), float(angle_range[1])
+    o.shear_angles = int(bool(shear_angles))
+    o.min_sep, o.max_overlap, o.a_sigma = float(min_sep), float(max_overlap), float(a_sigma)
+    x, y, p, R, A = (np.empty(n) for _ in range(5))
+    L = ctypes.c_double()
+    st = lib().sc_generate_config(ctypes.byref(o), int(n), float(packing), float(a_over_r),
+                                  float(r_small), float(r_ratio), ctypes.c_uint64(int(seed)),
+                                  _ptr(x), _ptr(y), _ptr(p), _ptr(R), _ptr(A), ctypes.byref(L))
+    if st != 0:
+        raise _lib.ScError(st, "configuration generation failed")
+    return L.value, x, y, p, R, A
+
+
 FMT = {"sp": 0, "sd": 1, "bin": 2}
 
 

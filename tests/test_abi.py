@@ -87,3 +87,50 @@ def test_generator_rejects_bad_arguments(library):
 
     with pytest.raises(ScError):
         generate_packing(10, 1.5, 1.0)
+
+
+def test_generate_config_variants(library, oracle_built):
+    """The reference's initial configurations: zero-energy placement has no overlap
+    (the oracle's energy is exactly zero), aligned and evenly spaced angles, grid
+    layout, Gamma-distributed aspect ratios with the requested mean and spread, the
+    steady-shear angle distribution concentrated along the flow, and the packing
+    fraction exactly as requested in every case."""
+    import spherocyls_gb300 as sc
+
+    def packing(L, R, A):
+        return np.sum(np.pi * R * R + 4 * A * R) / L ** 2
+
+    # random sequential placement without overlap jams near 0.55 at a/R = 1
+    L, x, y, p, R, A = sc.generate_config(400, 0.45, 1.0, max_overlap=0.0, seed=3)
+    assert abs(packing(L, R, A) - 0.45) < 1e-12
+    ob = oracle_built.OracleBox(L, x, y, p, A, R, 0.1)
+    ob.calc_se()
+    assert ob.se()[0] == 0.0
+    ob.close()
+
+    L, x, y, p, R, A = sc.generate_config(300, 0.5, 1.0, angle_range=(0.5, 0.5), seed=4)
+    assert np.all(p == 0.0)
+    L, x, y, p, R, A = sc.generate_config(300, 0.5, 1.0, angles="even", seed=4)
+    d = np.diff(np.sort(p))
+    assert np.allclose(d, np.pi / 300, rtol=1e-9)
+
+    L, x, y, p, R, A = sc.generate_config(256, 0.45, 1.0, layout="grid", seed=5)
+    assert abs(packing(L, R, A) - 0.45) < 1e-12
+    assert np.all((x >= 0) & (x < L) & (y >= 0) & (y < L))
+    ob = oracle_built.OracleBox(L, x, y, p, A, R, 0.1)
+    ob.calc_se()
+    assert np.isfinite(ob.se()[0])
+    ob.close()
+
+    L, x, y, p, R, A = sc.generate_config(4000, 0.5, 1.0, a_sigma=0.3, seed=6)
+    alpha = A / R
+    assert abs(alpha.mean() - 1.0) < 0.03 and abs(alpha.std() - 0.3) < 0.03
+    assert abs(packing(L, R, A) - 0.5) < 1e-12
+
+    L, x, y, p, R, A = sc.generate_config(2000, 0.3, 2.0, shear_angles=True, seed=7)
+    assert np.mean(np.cos(2 * p)) > 0.3
+    L, x, y, p, R, A = sc.generate_config(2000, 0.3, 2.0, seed=7)
+    assert abs(np.mean(np.cos(2 * p))) < 0.1
+
+    with pytest.raises(sc.ScError):
+        sc.generate_config(100, 0.5, 1.0, angle_range=(0.6, 0.4))
