@@ -277,9 +277,11 @@ def max_over_ranks(secs: float, world: int, device: str) -> float:
     return float(t.item())
 
 
-def config_of(args, w, world):
+def config_of(args, w, world, tuned=None):
+    tuned = tuned or {"pad": args.pad, "block": 128}
     return {"workload": args.workload, "N": w["n"], "packing": w["phi"], "a_over_r": w["a"],
             "strain_rate": w["rate"], "dt": w["dt"], "seed": w["seed"], "pad": args.pad,
+            "mixed_pad": tuned["pad"], "mixed_block": tuned["block"],
             "l2": "inputs larger than L2: a mixed step moves 152 + 8 n B per particle "
                   "(about 200 B, 210 MB at N = 2^20) against 129 MB of L2",
             "parallelism": "replicas" if world > 1 else "single"}
@@ -322,6 +324,8 @@ def main():
     ap.add_argument("--pad", type=float, default=0.2, help="neighbour-list padding")
     ap.add_argument("--e2e-steps", type=int, default=1000,
                     help="length of the end-to-end run (1000 steps: the large shear run)")
+    ap.add_argument("--autotune", action=argparse.BooleanOptionalAction, default=True,
+                    help="pick the mixed form's padding and block size with sc_autotune")
     ap.add_argument("--no-minimise", action="store_true",
                     help="skip the minimisation time-to-tolerance leg")
     ap.add_argument("--min-replicas", type=int, default=32)
@@ -359,22 +363,36 @@ def main():
 
     n = w["n"]
 
+    tuned = {"pad": args.pad, "block": 128}
+
     def new_box(precision, profile=False):
+        # the mixed form runs with the autotuned padding and block size
+        pad = tuned["pad"] if precision == "mixed" else args.pad
+        block = tuned["block"] if precision == "mixed" else 0
         if args.workload == "batch512":
             from spherocyls_gb300 import BoxBatch
 
-            b = BoxBatch(w["ns"], w["L"], w["x"], w["y"], w["p"], w["A"], w["R"], args.pad,
+            b = BoxBatch(w["ns"], w["L"], w["x"], w["y"], w["p"], w["A"], w["R"], pad,
                          precision=precision, device=local, profile=profile,
-                         use_graphs=not args.no_graphs)
+                         use_graphs=not args.no_graphs, block=block)
             for k, r in enumerate(w["rates"]):
                 b.set_strain_rate(float(r), sys=k)
         else:
-            b = SpherocylBox(w["L"], w["x"], w["y"], w["p"], w["A"], w["R"], args.pad,
+            b = SpherocylBox(w["L"], w["x"], w["y"], w["p"], w["A"], w["R"], pad,
                              precision=precision, device=local, profile=profile,
-                             use_graphs=not args.no_graphs)
+                             use_graphs=not args.no_graphs, block=block)
             b.set_strain_rate(w["rate"])
         b.set_step(w["dt"])
         return b
+
+    if args.autotune and not args.only:
+        # sc_autotune on the warmed-up workload picks the mixed form's padding and
+        # block size (it times copies; the copies' steps are not timed here)
+        t = new_box("mixed")
+        t.strain_steps(args.warmup)
+        f, blk = t.autotune(30)
+        t.close()
+        tuned = {"pad": args.pad * f, "block": blk}
 
     if args.only:
         b = new_box(args.only)
@@ -466,7 +484,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic (seeded crossing-free packing)",
-            "config": config_of(args, w, world),
+            "config": config_of(args, w, world, tuned),
             "plain_fp64": {"value": value64, "unit": "particle-steps/s",
                            "ms_per_step": 1e3 * secs64 / args.fp64_steps,
                            "steps": args.fp64_steps, "mixed_over_fp64": value / value64},

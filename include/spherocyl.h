@@ -68,7 +68,7 @@ typedef struct sc_options {
   int device;      /* CUDA device ordinal */
   int max_nbrs;    /* FP64 neighbour-list capacity per particle, 0 = default (64) */
   int use_graphs;  /* capture step chunks in CUDA graphs (1) or launch eagerly (0) */
-  int block;       /* threads per block of the mixed force pass, 0 = autotune */
+  int block;       /* threads per block of the mixed force pass (<= 128), 0 = 128 */
   int profile;     /* record per-pass CUDA events inside run calls (sc_get_pass_times) */
   int contact_model; /* SC_CONTACT_* */
 } sc_options;
@@ -148,6 +148,13 @@ int sc_quasistatic_compress(sc_handle *h, double dphi, double ftol, double e_jam
  * system s (negated when max_steps ran out first); *steps: resizes made. */
 int sc_find_jam(sc_handle *h, double e_jam, double step, double min_step, double ftol,
                 int max_iter, int max_steps, double *phi_jam, int *steps);
+
+/* Mixed form: times `steps` shear steps (after as many warm-up steps) of a copy of
+ * the handle for padding factors {0.5, 1, 1.5, 2, 3} x the current padding and
+ * block sizes {64, 128}, and gives the handle the fastest pair (*pad_factor,
+ * *block).  The live state is not advanced.  The FP64 form is left as it is
+ * (factor 1). */
+int sc_autotune(sc_handle *h, int steps, double *pad_factor, int *block);
 
 /* State readers, original particle order, systems concatenated. */
 int sc_get_state(sc_handle *h, double *x, double *y, double *phi);

@@ -233,6 +233,14 @@ class BoxBatch:
                                                 ctypes.byref(n)))
         return pj, n.value
 
+    def autotune(self, steps: int = 50):
+        """Pick the neighbour-list padding and force-pass block size of the mixed
+        form by timing copies of this batch; returns (pad_factor, block)."""
+        f = ctypes.c_double()
+        b = ctypes.c_int()
+        self._chk(lib().sc_autotune(self.h, int(steps), ctypes.byref(f), ctypes.byref(b)))
+        return f.value, b.value
+
     def find_jam(self, e_jam: float, step: float = 1e-3, min_step: float = 1e-12,
                  ftol: float = 1e-13, max_iter: int = 200000, max_steps: int = 10000):
         """Bisect each system's packing fraction to energy per particle e_jam

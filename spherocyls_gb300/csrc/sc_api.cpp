@@ -87,6 +87,10 @@ int sc_create(const sc_options* opt_in, int n_sys, const int* n_per_sys, const d
     g_create_error = "sc_create: unknown precision";
     return SC_E_ARG;
   }
+  if (opt.block < 0 || opt.block > 128 || opt.block % 32 != 0) {
+    g_create_error = "sc_create: block must be 0 or a multiple of 32 up to 128";
+    return SC_E_ARG;
+  }
   if (opt.contact_model != SC_CONTACT_ONE && opt.contact_model != SC_CONTACT_TWO) {
     g_create_error = "sc_create: unknown contact model";
     return SC_E_ARG;
@@ -344,6 +348,91 @@ int sc_set_gamma(sc_handle* h, int sys, double v) {
 }
 int sc_set_total_gamma(sc_handle* h, int sys, double v) {
   return set_scalar(h, sys, v, &sc::HostSys::gamma_total, false, "sc_set_total_gamma");
+}
+
+// Mixed form: time the shear step of a throwaway copy of the handle (same state,
+// scalars and options) for each padding factor and block size, then give the live
+// handle the fastest pair.  The padding only trades list length against rebuild
+// frequency: every pair that can touch stays in the list, so the physics is the
+// same.  The FP64 form keeps the caller's padding (it sets the reference's rebuild
+// timing) and is left alone.
+int sc_autotune(sc_handle* H, int steps, double* pad_factor, int* block) {
+  if (!H || steps < 1) return SC_E_ARG;
+  sc::Handle& h = H->h;
+  cudaSetDevice(h.device);
+  if (pad_factor) *pad_factor = 1.0;
+  if (block) *block = h.block;
+  if (h.prec != sc::PREC_MIXED) return SC_OK;
+  const int n = h.ntot, ns = h.nsys;
+  std::vector<double> x(n), y(n), p(n), L(ns), pad0(ns), pads(ns);
+  std::vector<int> nps(ns);
+  int rc = sc_get_state(H, x.data(), y.data(), p.data());
+  if (rc) return rc;
+  for (int s = 0; s < ns; s++) {
+    nps[s] = h.hs[s].n;
+    L[s] = h.hs[s].Lx;
+    pad0[s] = h.hs[s].pad;
+  }
+  const double factors[] = {0.5, 1.0, 1.5, 2.0, 3.0};
+  const int blocks[] = {64, 128};
+  double best_ms = 1e300, best_f = 1.0;
+  int best_b = h.block;
+  cudaEvent_t e0, e1;
+  if (!h.cuda_ok(cudaEventCreate(&e0), "event") || !h.cuda_ok(cudaEventCreate(&e1), "event"))
+    return h.last_status;
+  for (double f : factors)
+    for (int b : blocks) {
+      sc_options o = h.opt;
+      o.block = b;
+      o.profile = 0;
+      for (int s = 0; s < ns; s++) pads[s] = f * pad0[s];
+      sc_handle* T = nullptr;
+      if (sc_create(&o, ns, nps.data(), L.data(), pads.data(), x.data(), y.data(), p.data(),
+                    h.h_R.data(), h.h_A.data(), &T) != SC_OK)
+        continue;  // e.g. out of memory for the copy: skip the candidate
+      bool ok = true;
+      for (int s = 0; s < ns && ok; s++) {
+        const sc::HostSys& S = h.hs[s];
+        ok = sc_set_strain_rate(T, s, S.strain_rate) == SC_OK &&
+             sc_set_step(T, s, S.step) == SC_OK && sc_set_gamma(T, s, S.gamma) == SC_OK &&
+             sc_set_total_gamma(T, s, S.gamma_total) == SC_OK;
+      }
+      float ms = 0.f;
+      ok = ok && sc_strain_steps(T, steps, 0, nullptr) == SC_OK &&
+           cudaEventRecord(e0, T->h.stream) == cudaSuccess &&
+           sc_strain_steps(T, steps, 0, nullptr) == SC_OK &&
+           cudaEventRecord(e1, T->h.stream) == cudaSuccess &&
+           cudaEventSynchronize(e1) == cudaSuccess &&
+           cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess;
+      sc_destroy(T);
+      if (ok && ms < best_ms) {
+        best_ms = ms;
+        best_f = f;
+        best_b = b;
+      }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaGetLastError();
+  if (best_ms == 1e300) {
+    h.fail(SC_E_CUDA, "sc_autotune: no candidate ran");
+    return SC_E_CUDA;
+  }
+  if (best_f != 1.0) {
+    if (!h.materialize()) return h.last_status;
+    for (int s = 0; s < ns; s++) {
+      h.hs[s].pad = best_f * pad0[s];
+      h.hs[s].configure(false);
+    }
+    if (!h.layout_cells() || !h.rebuild_all() || !h.check_status("sc_autotune"))
+      return h.last_status;
+  }
+  h.block = best_b;
+  h.opt.block = best_b;
+  h.invalidate_graph();
+  if (pad_factor) *pad_factor = best_f;
+  if (block) *block = best_b;
+  return SC_OK;
 }
 
 int sc_find_neighbors(sc_handle* H) {

@@ -257,3 +257,26 @@ def test_graph_and_eager_paths_bitwise_identical(sc, precision):
     assert out[0][2] == out[1][2] and out[0][2] > 1
     assert np.array_equal(out[0][0], out[1][0])
     assert np.array_equal(out[0][1], out[1][1])
+
+
+def test_autotune_keeps_state_and_physics(sc):
+    """The autotuner times copies of the handle: the live state is not advanced, and
+    the tuned run follows an untuned one (same mixed-form tolerance as above)."""
+    L, x, y, p, R, A = sc.generate_packing(4096, 0.85, 1.0, seed=11)
+    boxes = []
+    for tune in (True, False):
+        b = sc.SpherocylBox(L, x, y, p, A, R, 0.1, precision="mixed")
+        b.set_strain_rate(1e-4)
+        b.set_step(0.02)
+        b.strain_steps(50)
+        if tune:
+            s0 = np.concatenate(b.state())
+            f, blk = b.autotune(20)
+            assert f in (0.5, 1.0, 1.5, 2.0, 3.0) and blk in (64, 128)
+            assert np.max(np.abs(np.concatenate(b.state()) - s0)) < 1e-12 * L
+        boxes.append(b)
+    se = [b.strain_steps(200, se_every=200)[-1, 0] for b in boxes]
+    assert abs(se[0][0] - se[1][0]) <= 1e-4 * abs(se[1][0])
+    xa = np.array(boxes[0].state())
+    xb = np.array(boxes[1].state())
+    assert np.max(np.abs(periodic_diff(xa[:2], xb[:2], L))) < 1e-4
