@@ -178,8 +178,9 @@ def test_neighbour_lists_equal_reference_sets_random_states(sc, oracle_built):
 
 
 def test_mixed_precision_against_fp64(sc, oracle_built):
-    """FP32 pair geometry: forces within 1e-4 of the RMS force, energy and stress
-    within 2e-6 relative of the FP64 oracle on the same configuration."""
+    """FP32 pair geometry: forces within 1e-4 of the RMS force, energy within 5e-7
+    relative and stress within 5e-7 of the stress scale (the larger normal stress)
+    of the FP64 oracle on the same configuration (measured: 1.4e-7 and 1.2e-7)."""
     g = load_golden("shear_n1024_phi085")
     L = float(g["L"])
     for prefix in ("s0_", "s100_"):
@@ -189,9 +190,9 @@ def test_mixed_precision_against_fp64(sc, oracle_built):
         se = box.calc_se()
         _assert_forces(box, g, prefix, tol=1e-4)
         sg = g[prefix + "se"]
-        assert abs(se[0] - sg[0]) <= 2e-6 * abs(sg[0])
+        assert abs(se[0] - sg[0]) <= 5e-7 * abs(sg[0])
         for k in (1, 2, 3):
-            assert abs(se[k] - sg[k]) <= 2e-6 * max(abs(sg[1]), abs(sg[2]))
+            assert abs(se[k] - sg[k]) <= 5e-7 * max(abs(sg[1]), abs(sg[2]))
 
 
 def test_mixed_precision_shear_tracks_fp64(sc):
@@ -280,3 +281,30 @@ def test_autotune_keeps_state_and_physics(sc):
     xa = np.array(boxes[0].state())
     xb = np.array(boxes[1].state())
     assert np.max(np.abs(periodic_diff(xa[:2], xb[:2], L))) < 1e-4
+
+
+def test_mixed_and_fp64_ensemble_averages_agree(sc):
+    """Long chaotic runs: the trajectories of the two forms separate after a few
+    hundred steps, but the ensemble-averaged shear stress and energy of 16 sheared
+    replicas agree within their statistical error (3 combined standard errors of
+    the replica means, after a transient of strain 0.2)."""
+    nrep, n = 16, 1024
+    packs = [sc.generate_packing(n, 0.85, 1.0, seed=900 + k) for k in range(nrep)]
+    args = ([n] * nrep, [pk[0] for pk in packs],
+            np.concatenate([pk[1] for pk in packs]), np.concatenate([pk[2] for pk in packs]),
+            np.concatenate([pk[3] for pk in packs]), np.concatenate([pk[5] for pk in packs]),
+            np.concatenate([pk[4] for pk in packs]), 0.1)
+    means = {}
+    for precision in ("fp64", "mixed"):
+        b = sc.BoxBatch(*args, precision=precision, stress="virial")
+        b.set_strain_rate(1e-3)
+        b.set_step(0.02)
+        b.strain_steps(10000)
+        rec = b.strain_steps(10000, se_every=100)  # (100, nrep, 5)
+        means[precision] = rec.mean(axis=0)          # per-replica time averages
+        b.close()
+    for k, name in ((0, "E"), (3, "Pxy")):
+        a, m = means["fp64"][:, k], means["mixed"][:, k]
+        err = np.sqrt(a.var(ddof=1) / nrep + m.var(ddof=1) / nrep)
+        assert abs(a.mean() - m.mean()) <= 3 * err, (name, a.mean(), m.mean(), err)
+        assert abs(a.mean()) > 3 * a.std(ddof=1) / np.sqrt(nrep), name  # a resolved signal
