@@ -20,8 +20,10 @@
 // two cells, so the displacement is rec_i - rec_j - (dc W, dr H) with no box
 // length in the FP32 arithmetic.
 //
-// Force pass: one thread per slot gathers over its list; each pair is computed
-// with the lower particle index as the reference's "p".
+// Force pass: one thread per list position gathers over its particle's list and
+// evaluates each pair from its own side; stress and energy are summed on the
+// lower-index side of each pair, where that evaluation is the reference's (its
+// "p" is the lower index).
 #include "sc_internal.hpp"
 #include "sc_pair.cuh"
 
@@ -99,22 +101,21 @@ __global__ void __launch_bounds__(128, TWO ? 6 : 10) k_pass_mixed(Dev d,
     float dy = ri.y - rj.y + (float)(1 - (int)(e >> 30)) * H;
     if (smallx) dx += Lxf * (float)((dx < -0.5f * Lxf) - (dx > 0.5f * Lxf));
     if (smally) dy += Lyf * (float)((dy < -0.5f * Lyf) - (dy > 0.5f * Lyf));
-    // the lower particle index plays the reference's "p"; select the operands
-    // instead of branching so that the warp runs one copy of the pair code
-    const bool ip = idi < __float_as_int(paj.z);
-    const float sg = ip ? 1.f : -1.f;
+    // Each thread evaluates the pair from its own particle's side (i as "p"):
+    // the forces need no canonical order, the two evaluations of a pair differ
+    // only by FP32 rounding.  Stress and energy, whose compat form is not
+    // symmetric in p and q, are summed on the lower-index side only, where this
+    // evaluation is the reference's.
     PairF32 o;
-    const float nxP = ip ? ri.z : rj.z, nyP = ip ? ri.w : rj.w, aPP = ip ? pai.y : paj.y;
-    const float nxQ = ip ? rj.z : ri.z, nyQ = ip ? rj.w : ri.w, aQQ = ip ? paj.y : pai.y;
-    const float sgm = ip ? pai.x + paj.x : paj.x + pai.x;
     const bool touch =
-        two_point ? pair2_fp32(sg * dx, sg * dy, nxP, nyP, aPP, nxQ, nyQ, aQQ, sgm, gam, o)
-                  : pair_fp32<SE>(sg * dx, sg * dy, nxP, nyP, aPP, nxQ, nyQ, aQQ, sgm, gam, virial,
-                                  o);
+        two_point ? pair2_fp32(dx, dy, ri.z, ri.w, pai.y, rj.z, rj.w, paj.y, pai.x + paj.x, gam, o)
+                  : pair_fp32<SE>(dx, dy, ri.z, ri.w, pai.y, rj.z, rj.w, paj.y, pai.x + paj.x,
+                                  gam, virial, o);
     if (!touch) continue;
-    fx += sg * o.fx;
-    fy += sg * o.fy;
-    tq += ip ? o.tp : o.tq;
+    fx += o.fx;
+    fy += o.fy;
+    tq += o.tp;
+    const bool ip = SE && idi < __float_as_int(paj.z);
     if (SE && ip && two_point) {
       e_acc += (double)o.ov;
       pxx += (double)o.cxa;
