@@ -211,7 +211,7 @@ int sc_create(const sc_options* opt_in, int n_sys, const int* n_per_sys, const d
   if (h.prec == sc::PREC_MIXED)
     ok = ok && h.dalloc(&d.rec, N, "rec") && h.dalloc(&d.rec_t, N, "rec_t") &&
          h.dalloc(&d.mc, N, "mc") && h.dalloc(&d.mv, N, "mv") && h.dalloc(&d.mm, N, "mm") &&
-         h.dalloc(&d.pa, N, "pa") && h.dalloc(&d.rcf, N, "rcf") &&
+         h.dalloc(&d.pa, N, "pa") && h.dalloc(&d.rcf, N, "rcf") && h.dalloc(&d.rf, N, "rf") &&
          h.dalloc(&d.cellp, N, "cellp") && h.dalloc(&d.gbuild, n_sys, "gbuild") &&
          h.dalloc(&d.ord, N, "ord") && h.dalloc(&d.nbr_p, N * d.maxn, "nbr_p") &&
          h.dalloc(&d.nbr_pn, N, "nbr_pn");

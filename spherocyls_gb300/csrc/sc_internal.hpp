@@ -107,6 +107,7 @@ struct Dev {
   float2* mm;     // displacement since the last rebuild
   float4* pa;     // (R, A, particle index as int bits, 1/I)
   float* rcf;     // isolated-rotation coefficient RC
+  float* rf;      // R in FP32: the only per-neighbour constant the force pass gathers
   int* cellp;     // local cell packed as col | row << 16
   float* gbuild;  // [nsys] gamma at which each system's list was built
   // cell lists

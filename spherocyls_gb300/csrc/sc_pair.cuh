@@ -139,15 +139,14 @@ struct PairF32 {
   float cxa, cya, cxb, cyb;      // contact arms (virial or reference form)
 };
 
-// dX, dY: displacement P - Q already reduced to the minimum image (FP32).
+// dX, dY: displacement P - Q already reduced to the minimum image (FP32);
+// a = |u_A|^2 and c = |u_B|^2 are the squared half shaft lengths.
 template <bool SE>
-__device__ __forceinline__ bool pair_fp32(float dX, float dY, float nxA, float nyA, float aP,
-                                          float nxB, float nyB, float aQ, float sig, float gamma,
+__device__ __forceinline__ bool pair_fp32(float dX, float dY, float nxA, float nyA, float a,
+                                          float nxB, float nyB, float c, float sig, float gamma,
                                           bool virial, PairF32& o) {
   dX = fmaf(gamma, dY, dX);
-  float a = aP * aP;
   float b = -(nxA * nxB + nyA * nyB);
-  float c = aQ * aQ;
   float d = nxA * dX + nyA * dY;
   float e = -(nxB * dX + nyB * dY);
   // Unclamped spine parameter of Q.  The reference's (b d - a e)/(a c - b^2) is,
@@ -413,11 +412,10 @@ __device__ __forceinline__ bool contact_fp32(float dX, float dY, float s, float 
 // For the two-point model the PairF32 fields ov, cxa, cya, cxb, cyb hold summed
 // quantities: sum ov^2, and the force-weighted virial terms Pxx, Pyy, Pxy, Pyx (before
 // the division by the box area).
-__device__ __forceinline__ bool pair2_fp32(float dX, float dY, float nxA, float nyA, float aP,
-                                           float nxB, float nyB, float aQ, float sig, float gamma,
+__device__ __forceinline__ bool pair2_fp32(float dX, float dY, float nxA, float nyA, float a,
+                                           float nxB, float nyB, float c, float sig, float gamma,
                                            PairF32& o) {
   dX = fmaf(gamma, dY, dX);
-  float a = aP * aP, c = aQ * aQ;
   float b = -(nxA * nxB + nyA * nyB);
   float d = nxA * dX + nyA * dY;
   float e = -(nxB * dX + nyB * dY);

@@ -82,19 +82,27 @@ __global__ void __launch_bounds__(128, TWO ? 6 : 10) k_pass_mixed(Dev d,
   // are in flight while the current pair is computed
   unsigned e1 = cnt > 0 ? __ldg(Lst) : 0u;
   unsigned e2 = cnt > 1 ? __ldg(Lst + stride) : 0u;
-  float4 r1 = make_float4(0.f, 0.f, 0.f, 0.f), p1 = r1;
+  // the neighbour's record and radius (its A^2 is |shaft|^2 from the record);
+  // its particle index only on the passes that sum stress and energy
+  float4 r1 = make_float4(0.f, 0.f, 0.f, 0.f);
+  float R1 = 0.f;
+  int id1 = 0;
   if (cnt > 0) {
     r1 = REC[e1 & kSlotMask];
-    p1 = d.pa[e1 & kSlotMask];
+    R1 = d.rf[e1 & kSlotMask];
+    if (SE) id1 = __float_as_int(d.pa[e1 & kSlotMask].z);
   }
+  const float ai = pai.y * pai.y;
   for (int k = 0; k < cnt; k++) {
     const unsigned e = e1;
     const float4 rj = r1;
-    const float4 paj = p1;
+    const float Rj = R1;
+    const int idj = id1;
     e1 = e2;
     if (k + 1 < cnt) {
       r1 = REC[e1 & kSlotMask];
-      p1 = d.pa[e1 & kSlotMask];
+      R1 = d.rf[e1 & kSlotMask];
+      if (SE) id1 = __float_as_int(d.pa[e1 & kSlotMask].z);
     }
     if (k + 2 < cnt) e2 = __ldg(Lst + (size_t)(k + 2) * stride);
     float dx = ri.x - rj.x + (float)(1 - (int)((e >> 28) & 3u)) * W;
@@ -107,15 +115,16 @@ __global__ void __launch_bounds__(128, TWO ? 6 : 10) k_pass_mixed(Dev d,
     // symmetric in p and q, are summed on the lower-index side only, where this
     // evaluation is the reference's.
     PairF32 o;
+    const float cj = fmaf(rj.z, rj.z, rj.w * rj.w);
     const bool touch =
-        two_point ? pair2_fp32(dx, dy, ri.z, ri.w, pai.y, rj.z, rj.w, paj.y, pai.x + paj.x, gam, o)
-                  : pair_fp32<SE>(dx, dy, ri.z, ri.w, pai.y, rj.z, rj.w, paj.y, pai.x + paj.x,
-                                  gam, virial, o);
+        two_point ? pair2_fp32(dx, dy, ri.z, ri.w, ai, rj.z, rj.w, cj, pai.x + Rj, gam, o)
+                  : pair_fp32<SE>(dx, dy, ri.z, ri.w, ai, rj.z, rj.w, cj, pai.x + Rj, gam, virial,
+                                  o);
     if (!touch) continue;
     fx += o.fx;
     fy += o.fy;
     tq += o.tp;
-    const bool ip = SE && idi < __float_as_int(paj.z);
+    const bool ip = SE && idi < idj;
     if (SE && ip && two_point) {
       e_acc += (double)o.ov;
       pxx += (double)o.cxa;
@@ -295,6 +304,7 @@ __global__ void k_mx_local(Dev d, const StepScalars* __restrict__ tab, int row, 
   d.mm[i] = make_float2(0.f, 0.f);
   d.pa[i] = make_float4((float)ra.x, A, __int_as_float(d.id[i]), (float)(1.0 / irc.x));
   d.rcf[i] = (float)irc.y;
+  d.rf[i] = (float)ra.x;
 }
 
 // The padded neighbour list in FP32 (see the file comment).
