@@ -132,6 +132,10 @@ int sc_fire_minimize(sc_handle *h, double ftol, int max_iter, double dt0, double
 /* Affine rescale of box and positions by factor (the src/cuda resize_coords,
  * src/cuda/strain_dynamics.cu:1111-1122, as one step); sys = -1 for all. */
 int sc_affine_scale(sc_handle *h, int sys, double factor);
+/* flip_shear_direction (src/cuda/find_neighbors.cu:563-581): reverses the shear of
+ * system sys (-1: all) by reflecting x -> Lx - x, phi -> -phi and gamma -> -gamma;
+ * the cell lists are rebuilt.  Shear then continues with the same strain rate. */
+int sc_flip_shear(sc_handle *h, int sys);
 /* Quasistatic compression to jamming: repeated affine steps raising each system's
  * packing fraction by dphi, each followed by sc_fire_minimize(ftol, max_iter), until
  * the system's energy per particle exceeds e_jam (compress_qs2p / find_jam_2p,

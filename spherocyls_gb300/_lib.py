@@ -89,6 +89,7 @@ SIGNATURES = [
     ("sc_find_jam", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                    ctypes.c_double, ctypes.c_int, ctypes.c_int, _dp, _ip]),
     ("sc_autotune", ctypes.c_int, [_vp, ctypes.c_int, _dp, _ip]),
+    ("sc_flip_shear", ctypes.c_int, [_vp, ctypes.c_int]),
     ("sc_get_state", ctypes.c_int, [_vp, _dp, _dp, _dp]),
     ("sc_get_forces", ctypes.c_int, [_vp, _dp, _dp, _dp]),
     ("sc_get_box", ctypes.c_int, [_vp, ctypes.c_int, _dp]),

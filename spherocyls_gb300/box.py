@@ -220,6 +220,10 @@ class BoxBatch:
             self._chk(st)
         return it.value, fm, dn.astype(bool)
 
+    def flip_shear(self, sys: int = -1):
+        """Reverse the shear direction (x -> Lx - x, phi -> -phi, gamma -> -gamma)."""
+        self._chk(lib().sc_flip_shear(self.h, int(sys)))
+
     def affine_scale(self, factor: float, sys: int = -1):
         self._chk(lib().sc_affine_scale(self.h, int(sys), float(factor)))
 

@@ -59,6 +59,47 @@ inline unsigned long time_from_name(const std::string& f) {
   return std::strtoul(f.substr(f.size() - 14, 10).c_str(), nullptr, 10);
 }
 
+// The optional initial-configuration fields of a random start ('r'): the
+// configuration code 0-8 (random / zero-energy / grid positions, each with random,
+// evenly spaced or aligned angles) or 9 (type, angle range, allowed overlap, angle
+// distribution read explicitly), then the aspect-ratio spread
+// (src/cuda/main.cpp:119-149), mapped onto sc_generate_config.  Without the fields
+// the start is random with random angles.
+inline int random_start(Args& a, int n, double phi, double aspect, double bidisp, double* x,
+                        double* y, double* p, double* R, double* A, double* L) {
+  sc_gen_options o;
+  sc_default_gen_options(&o);
+  if (a.more()) {
+    int config = a.i("Initial configuration (0: random, 1: random-uniform, 2: random-aligned, "
+                     "3: zero-energy, 4: zero-energy-uniform, 5: zero-energy-aligned, 6: grid, "
+                     "7: grid-uniform, 8: grid-aligned, 9: other-specified)");
+    double overlap = 1.0;
+    if (config == 9) {
+      o.layout = a.i("Position configuration type (0: random, 1: grid)") ? SC_LAYOUT_GRID
+                                                                          : SC_LAYOUT_RANDOM;
+      o.angle_min = a.f("Minimum angle");
+      o.angle_max = a.f("Maximum angle");
+      overlap = a.f("Allowed overlap (min 0, max 1)");
+      o.angle_mode = a.i("Angle distribution type (0: random, 1: uniform)") ? SC_ANGLE_EVEN
+                                                                              : SC_ANGLE_RANDOM;
+    } else if (config >= 0 && config < 9) {
+      o.layout = config < 6 ? SC_LAYOUT_RANDOM : SC_LAYOUT_GRID;
+      o.angle_min = 0.0;
+      o.angle_max = config % 3 == 2 ? 0.0 : 1.0;
+      overlap = (config >= 3 && config < 6) ? 0.0 : 1.0;
+      o.angle_mode = config % 3 == 0 ? SC_ANGLE_RANDOM : SC_ANGLE_EVEN;
+    } else {
+      std::cerr << "unknown initial configuration " << config << std::endl;
+      return SC_E_ARG;
+    }
+    // overlap >= 1: only crossing spines are rejected
+    o.max_overlap = overlap < 1.0 ? overlap : -1.0;
+    o.a_sigma = a.f("Aspect ratio distribution width (relative deviation)");
+  }
+  return sc_generate_config(&o, n, phi, aspect, 0.5, bidisp, env_int("SC_SEED", 0), x, y, p, R,
+                            A, L);
+}
+
 inline int fail(const char* what, int rc, sc_handle* h = nullptr) {
   std::cerr << what << ": " << sc_status_string(rc) << ": " << sc_last_error(h) << std::endl;
   return 1;

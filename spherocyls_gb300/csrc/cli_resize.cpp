@@ -3,7 +3,8 @@
 // Arguments as for spherocyl_strain with the substitutions of input/input_key.txt:26-30:
 // resize rate instead of strain rate, final packing fraction instead of run length,
 // and no shear-direction field; for "r": initial packing fraction, aspect ratio
-// A/R (R1 = 0.5), bidispersity R2/R1, configuration type (0).  Position files are
+// A/R (R1 = 0.5), bidispersity R2/R1, optionally the initial configuration code
+// (0-9) and the aspect-ratio spread (see cli::random_start).  Position files are
 // read with the standard header (the src/cpp resize driver's headerless legacy
 // column layout, src/cpp/main_resize.cpp:336-349, is not supported).
 #include <chrono>
@@ -29,14 +30,9 @@ int main(int argc, char** argv) {
     double phi = a.f("Starting Packing Fraction");
     double aspect = a.f("Aspect ratio (A/R)");
     double bidisp = a.f("Bidispersity ratio (R2/R1)");
-    int config = a.more() ? a.i("Initial configuration (0: random)") : 0;
-    if (config != 0) {
-      std::cerr << "only random initial configurations (0) are supported" << std::endl;
-      return 1;
-    }
     x.resize(n), y.resize(n), p.resize(n), R.resize(n), A.resize(n);
-    int rc = sc_generate_packing(n, phi, aspect, 0.5, bidisp, cli::env_int("SC_SEED", 0), 0.1,
-                                 x.data(), y.data(), p.data(), R.data(), A.data(), &L);
+    int rc = cli::random_start(a, n, phi, aspect, bidisp, x.data(), y.data(), p.data(), R.data(),
+                               A.data(), &L);
     if (rc) return cli::fail("packing", rc);
   } else {
     int nf = 0;

@@ -3,9 +3,10 @@
 // Arguments in the order of input/input_key.txt:7-22 (the src/cuda driver's order,
 // src/cuda/main.cpp:63-125): data file or "r", output directory, N, strain rate,
 // step, run length (strain), position save interval (strain), stress save interval
-// (strain), cell padding, shear-direction change (only 0 is supported), and for
-// "r": packing fraction, aspect ratio A/R (R1 = 0.5), bidispersity R2/R1, initial
-// configuration type (only 0, random, is supported).  SC_PRECISION=mixed selects
+// (strain), cell padding, shear-direction change (0: none, 1: reverse; the
+// rotations 2 and 3 are not supported), and for "r": packing fraction, aspect ratio
+// A/R (R1 = 0.5), bidispersity R2/R1, then optionally the initial configuration
+// code (0-9) and the aspect-ratio spread (see cli::random_start).  SC_PRECISION=mixed selects
 // the mixed form, SC_OUTPUT_FORMAT=sd the src/cuda file layout, SC_SEED the seed of
 // the random configuration.
 #include <chrono>
@@ -24,9 +25,9 @@ int main(int argc, char** argv) {
   double pos_save = a.f("Position data save rate");
   double se_save = a.f("Stress data save rate");
   double pad = a.f("Cell padding");
-  int flip = a.i("Change shear direction (0: no)");
-  if (flip != 0) {
-    std::cerr << "shear-direction changes are not supported" << std::endl;
+  int flip = a.i("Change shear direction (0: no, 1: reverse)");
+  if (flip != 0 && flip != 1) {
+    std::cerr << "only shear reversal (1) is supported, not the rotations (2, 3)" << std::endl;
     return 1;
   }
   std::vector<double> x, y, p, R, A;
@@ -36,14 +37,9 @@ int main(int argc, char** argv) {
     double phi = a.f("Packing Fraction");
     double aspect = a.f("Aspect ratio (A/R)");
     double bidisp = a.f("Bidispersity ratio (R2/R1)");
-    int config = a.more() ? a.i("Initial configuration (0: random)") : 0;
-    if (config != 0) {
-      std::cerr << "only random initial configurations (0) are supported" << std::endl;
-      return 1;
-    }
     x.resize(n), y.resize(n), p.resize(n), R.resize(n), A.resize(n);
-    int rc = sc_generate_packing(n, phi, aspect, 0.5, bidisp, cli::env_int("SC_SEED", 0), 0.1,
-                                 x.data(), y.data(), p.data(), R.data(), A.data(), &L);
+    int rc = cli::random_start(a, n, phi, aspect, bidisp, x.data(), y.data(), p.data(), R.data(),
+                               A.data(), &L);
     if (rc) return cli::fail("packing", rc);
   } else {
     int nf = 0;
@@ -72,6 +68,11 @@ int main(int argc, char** argv) {
   if ((rc = sc_set_strain_rate(h, -1, rate)) || (rc = sc_set_step(h, -1, dt)) ||
       (rc = sc_set_gamma(h, -1, gamma)) || (rc = sc_set_total_gamma(h, -1, gamma_total)))
     return cli::fail("setup", rc, h);
+  if (flip == 1) {
+    // main.cpp:258-262: total strain restarts from zero in the reversed direction
+    if ((rc = sc_set_total_gamma(h, -1, 0.0)) || (rc = sc_flip_shear(h, -1)))
+      return cli::fail("flip", rc, h);
+  }
   unsigned long t_end = 0;
   rc = sc_run_strain(h, dir.c_str(), run, pos_save, se_save, t0, cli::out_format(), &t_end);
   if (rc) return cli::fail("run", rc, h);

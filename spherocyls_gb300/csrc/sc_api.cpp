@@ -565,6 +565,18 @@ int sc_fire_minimize(sc_handle* H, double ftol, int max_iter, double dt0, double
   return H->h.fire_minimize(ftol, max_iter, dt0, dt_max, iters, fmax, done);
 }
 
+int sc_flip_shear(sc_handle* H, int sys) {
+  if (!H) return SC_E_ARG;
+  sc::Handle& h = H->h;
+  if (sys < -1 || sys >= h.nsys) {
+    h.fail(SC_E_ARG, "sc_flip_shear: bad system index");
+    return SC_E_ARG;
+  }
+  std::vector<char> sel(h.nsys, 0);
+  for (int s = 0; s < h.nsys; s++) sel[s] = sys < 0 || s == sys;
+  return h.flip_shear(sel);
+}
+
 int sc_affine_scale(sc_handle* H, int sys, double factor) {
   if (!H) return SC_E_ARG;
   sc::Handle& h = H->h;

@@ -219,6 +219,18 @@ __global__ void k_affine(Dev d, const double* factor) {
   d.xy[i] = make_double2(p.x * f, p.y * f);
 }
 
+// flip_shear_direction / reflect_yaxis (src/cuda/find_neighbors.cu:552-581):
+// x -> Lx - x, phi -> -phi in the systems with lx[s] > 0
+__global__ void k_reflect(Dev d, const double* lx) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.ntot) return;
+  const double L = lx[d.psys[i]];
+  if (!(L > 0)) return;
+  double2 p = d.xy[i];
+  d.xy[i] = make_double2(L - p.x, p.y);
+  d.ph[i] = -d.ph[i];
+}
+
 inline int nblk(int n, int b) { return (n + b - 1) / b; }
 
 }  // namespace
@@ -233,6 +245,10 @@ void launch_fire_iteration_tail(const Dev& d, const FireState& f, double ftol, d
   k_fire_chunk<<<d.npchunks, 256, 0, st>>>(d, f);
   k_fire_sys<<<nblk(d.nsys, 128), 128, 0, st>>>(d, f, ftol, dt_max);
   k_fire_update<<<nblk(d.ntot, 256), 256, 0, st>>>(d, f, mixed ? 1 : 0);
+}
+
+void launch_reflect(const Dev& d, const double* lx, cudaStream_t st) {
+  k_reflect<<<nblk(d.ntot, 256), 256, 0, st>>>(d, lx);
 }
 
 void launch_affine(const Dev& d, const double* factor, cudaStream_t st) {

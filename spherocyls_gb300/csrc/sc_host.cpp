@@ -877,6 +877,28 @@ int Handle::affine_scale(const std::vector<double>& factor) {
   return rebuild_all() && check_status("affine scale") ? SC_OK : last_status;
 }
 
+// Reverses the shear direction of the selected systems (flip_shear_direction,
+// src/cuda/find_neighbors.cu:563-581): positions reflected about the box's y axis,
+// angles negated, gamma negated, then the cell lists rebuilt.
+int Handle::flip_shear(const std::vector<char>& sel) {
+  cudaSetDevice(device);
+  if (!materialize()) return last_status;
+  std::vector<double> lx(nsys, 0.0);
+  for (int s = 0; s < nsys; s++)
+    if (sel[s]) lx[s] = hs[s].Lx;
+  double* dl = nullptr;
+  if (!dalloc(&dl, nsys, "flip")) return last_status;
+  bool ok = cuda_ok(cudaMemcpyAsync(dl, lx.data(), nsys * sizeof(double), cudaMemcpyHostToDevice,
+                                    stream), "flip");
+  if (ok) launch_reflect(d, dl, stream);
+  ok = ok && cuda_ok(cudaStreamSynchronize(stream), "flip");
+  dfree(dl);
+  if (!ok) return last_status;
+  for (int s = 0; s < nsys; s++)
+    if (sel[s]) hs[s].gamma = -hs[s].gamma;
+  return rebuild_all() && check_status("flip shear") ? SC_OK : last_status;
+}
+
 // Quasistatic compression to jamming: affine steps of dphi in packing fraction,
 // each followed by a FIRE minimisation; a system stops once its energy per
 // particle after minimisation exceeds e_jam (compress_qs2p / find_jam_2p,

@@ -196,7 +196,7 @@ def test_cli_strain_new_and_continue(library, tmp_path):
     out = tmp_path / "run"
     out.mkdir()
     args = [exe, "r", str(out), "256", "1e-2", "0.02", "0.02", "0.01", "1e-3", "0.1", "0",
-            "0.85", "1.0", "1.4", "0"]
+            "0.85", "1.0", "1.4", "0", "0"]
     r = subprocess.run(args, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     assert (out / "sp0000000002.dat").exists() and (out / "sp_strain_se.dat").exists()
@@ -208,14 +208,30 @@ def test_cli_strain_new_and_continue(library, tmp_path):
     assert (out / "sp0000000003.dat").exists()
     lines = (out / "sp_strain_se.dat").read_text().splitlines()
     assert lines[-1].split()[0] == "3"
+    # reversed shear from a file, and a zero-energy grid start with aligned particles
+    r = subprocess.run([exe, str(out / "sp0000000003.dat"), str(out), "256", "1e-2", "0.02",
+                        "0.01", "0.01", "1e-3", "0.1", "1"], capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert "Change shear direction" in r.stdout
+    grid = tmp_path / "grid"
+    grid.mkdir()
+    r = subprocess.run([exe, "r", str(grid), "256", "1e-2", "0.02", "0.01", "0.01", "1e-3",
+                        "0.1", "0", "0.5", "1.0", "1.4", "8", "0"], capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    from spherocyls_gb300 import read_positions
+
+    hdr, x, y, p, R, A = read_positions(str(grid / "sp0000000000.dat"))
+    assert np.all(p == p[0])
 
 
 @pytest.mark.gpu
 def test_cli_resize_and_minimize(library, tmp_path):
     rz = os.path.join(ROOT, "spherocyls_gb300", "bin", "spherocyl_resize")
     r = subprocess.run([rz, "r", str(tmp_path), "256", "5e-2", "0.02", "0.801", "0.05", "1e-3",
-                        "0.1", "0.80", "1.0", "1.4", "0"], capture_output=True, text=True,
-                       timeout=300)
+                        "0.1", "0.80", "1.0", "1.4", "0", "0"], capture_output=True,
+                       text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     assert (tmp_path / "sp_resize_se.dat").exists()
     mz = os.path.join(ROOT, "spherocyls_gb300", "bin", "spherocyl_minimize")

@@ -308,3 +308,31 @@ def test_mixed_and_fp64_ensemble_averages_agree(sc):
         err = np.sqrt(a.var(ddof=1) / nrep + m.var(ddof=1) / nrep)
         assert abs(a.mean() - m.mean()) <= 3 * err, (name, a.mean(), m.mean(), err)
         assert abs(a.mean()) > 3 * a.std(ddof=1) / np.sqrt(nrep), name  # a resolved signal
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_flip_shear_reverses_the_configuration(sc, precision):
+    """flip_shear_direction: x -> L - x, phi -> -phi, gamma -> -gamma leave the energy
+    and the normal stresses unchanged and negate the shear stress; flipping twice
+    gives the configuration back."""
+    L, x, y, p, R, A = sc.generate_packing(1024, 0.85, 1.0, seed=17)
+    box = sc.SpherocylBox(L, x, y, p, A, R, 0.1, precision=precision, stress="virial")
+    box.set_strain_rate(1e-3)
+    box.set_step(0.02)
+    box.strain_steps(200)
+    se0 = box.calc_se()
+    s0 = np.array(box.state())
+    g0 = box.box()["gamma"]
+    box.flip_shear()
+    se1 = box.calc_se()
+    tol = 1e-12 if precision == "fp64" else 1e-6
+    scale = max(abs(se0[1]), abs(se0[2]))
+    assert abs(se1[0] - se0[0]) <= tol * se0[0]
+    assert abs(se1[1] - se0[1]) <= tol * scale and abs(se1[2] - se0[2]) <= tol * scale
+    assert abs(se1[3] + se0[3]) <= tol * scale
+    assert box.box()["gamma"] == -g0
+    box.flip_shear()
+    s2 = np.array(box.state())
+    assert np.max(np.abs(periodic_diff(s2[:2], s0[:2], L))) < 1e-12 * L
+    dphi = np.remainder(s2[2] - s0[2] + np.pi, 2 * np.pi) - np.pi  # rebuilds wrap phi
+    assert np.max(np.abs(dphi)) < 1e-12
