@@ -85,6 +85,13 @@ void sc_default_options(sc_options *opt);
 int sc_create(const sc_options *opt, int n_sys, const int *n_per_sys, const double *L,
               const double *pad, const double *x, const double *y, const double *phi,
               const double *R, const double *A, sc_handle **out);
+/* As sc_create for rectangular boxes Lx[s] x Ly[s] (the src/cuda box,
+ * src/cuda/spherocyl_box.cpp:529-636): the Lees-Edwards set-back then happens at
+ * gamma >= Lx/(2 Ly) and subtracts Lx/Ly (set_back_coords, src/cuda/find_neighbors.cu:285-330);
+ * for Lx = Ly it is sc_create. */
+int sc_create_rect(const sc_options *opt, int n_sys, const int *n_per_sys, const double *Lx,
+                   const double *Ly, const double *pad, const double *x, const double *y,
+                   const double *phi, const double *R, const double *A, sc_handle **out);
 int sc_destroy(sc_handle *h);
 const char *sc_last_error(const sc_handle *h);
 int sc_set_stream(sc_handle *h, void *cuda_stream);
@@ -136,6 +143,10 @@ int sc_affine_scale(sc_handle *h, int sys, double factor);
  * system sys (-1: all) by reflecting x -> Lx - x, phi -> -phi and gamma -> -gamma;
  * the cell lists are rebuilt.  Shear then continues with the same strain rate. */
 int sc_flip_shear(sc_handle *h, int sys);
+/* rotate_by_gamma (src/cuda/find_neighbors.cu:583-645): turns system sys (-1: all)
+ * to the frame in which its sheared cell is upright, Lx' = Ly sqrt(1 + gamma^2),
+ * Ly' = Lx / sqrt(1 + gamma^2), gamma -> -gamma (the box becomes rectangular). */
+int sc_rotate_shear(sc_handle *h, int sys);
 /* Quasistatic compression to jamming: repeated affine steps raising each system's
  * packing fraction by dphi, each followed by sc_fire_minimize(ftol, max_iter), until
  * the system's energy per particle exceeds e_jam (compress_qs2p / find_jam_2p,

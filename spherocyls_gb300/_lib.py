@@ -90,6 +90,10 @@ SIGNATURES = [
                                    ctypes.c_double, ctypes.c_int, ctypes.c_int, _dp, _ip]),
     ("sc_autotune", ctypes.c_int, [_vp, ctypes.c_int, _dp, _ip]),
     ("sc_flip_shear", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("sc_rotate_shear", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("sc_create_rect", ctypes.c_int, [ctypes.POINTER(ScOptions), ctypes.c_int, _ip, _dp, _dp,
+                                      _dp, _dp, _dp, _dp, _dp, _dp,
+                                      ctypes.POINTER(ctypes.c_void_p)]),
     ("sc_get_state", ctypes.c_int, [_vp, _dp, _dp, _dp]),
     ("sc_get_forces", ctypes.c_int, [_vp, _dp, _dp, _dp]),
     ("sc_get_box", ctypes.c_int, [_vp, ctypes.c_int, _dp]),

@@ -95,7 +95,7 @@ class BoxBatch:
     def __init__(self, n_per_sys, L, x, y, phi, A, R, pad=0.0, *, precision: str = "fp64",
                  stress: str = "compat", device: int = 0, max_nbrs: int = 0,
                  use_graphs: bool = True, block: int = 0, profile: bool = False,
-                 contacts: int = 1):
+                 contacts: int = 1, Ly=None):
         n_per_sys = np.ascontiguousarray(np.atleast_1d(n_per_sys), dtype=np.int32)
         self.nsys = int(n_per_sys.shape[0])
         self.n_per_sys = n_per_sys
@@ -120,10 +120,16 @@ class BoxBatch:
         opt.contact_model = 1 if int(contacts) == 2 else 0
         self.precision = precision
         h = ctypes.c_void_p()
-        st = lib().sc_create(ctypes.byref(opt), self.nsys,
-                             n_per_sys.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _ptr(L),
-                             _ptr(pad), _ptr(x), _ptr(y), _ptr(phi), _ptr(R), _ptr(A),
-                             ctypes.byref(h))
+        nps = n_per_sys.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+        if Ly is None:
+            st = lib().sc_create(ctypes.byref(opt), self.nsys, nps, _ptr(L), _ptr(pad), _ptr(x),
+                                 _ptr(y), _ptr(phi), _ptr(R), _ptr(A), ctypes.byref(h))
+        else:
+            # rectangular boxes Lx = L, Ly (the src/cuda box)
+            Ly = _f64(np.broadcast_to(np.asarray(Ly, dtype=np.float64), (self.nsys,)))
+            st = lib().sc_create_rect(ctypes.byref(opt), self.nsys, nps, _ptr(L), _ptr(Ly),
+                                      _ptr(pad), _ptr(x), _ptr(y), _ptr(phi), _ptr(R), _ptr(A),
+                                      ctypes.byref(h))
         check(st, None)
         self.h = h
 
@@ -219,6 +225,10 @@ class BoxBatch:
         if st not in (0, _lib.SC_E_NOCONV):
             self._chk(st)
         return it.value, fm, dn.astype(bool)
+
+    def rotate_shear(self, sys: int = -1):
+        """Turn to the frame in which the sheared cell is upright (rotate_by_gamma)."""
+        self._chk(lib().sc_rotate_shear(self.h, int(sys)))
 
     def flip_shear(self, sys: int = -1):
         """Reverse the shear direction (x -> Lx - x, phi -> -phi, gamma -> -gamma)."""

@@ -3,8 +3,8 @@
 // Arguments in the order of input/input_key.txt:7-22 (the src/cuda driver's order,
 // src/cuda/main.cpp:63-125): data file or "r", output directory, N, strain rate,
 // step, run length (strain), position save interval (strain), stress save interval
-// (strain), cell padding, shear-direction change (0: none, 1: reverse; the
-// rotations 2 and 3 are not supported), and for "r": packing fraction, aspect ratio
+// (strain), cell padding, shear-direction change (0: none, 1: reverse, 2: rotate;
+// 3, a run before the rotation, is not supported), and for "r": packing fraction, aspect ratio
 // A/R (R1 = 0.5), bidispersity R2/R1, then optionally the initial configuration
 // code (0-9) and the aspect-ratio spread (see cli::random_start).  SC_PRECISION=mixed selects
 // the mixed form, SC_OUTPUT_FORMAT=sd the src/cuda file layout, SC_SEED the seed of
@@ -26,12 +26,12 @@ int main(int argc, char** argv) {
   double se_save = a.f("Stress data save rate");
   double pad = a.f("Cell padding");
   int flip = a.i("Change shear direction (0: no, 1: reverse)");
-  if (flip != 0 && flip != 1) {
-    std::cerr << "only shear reversal (1) is supported, not the rotations (2, 3)" << std::endl;
+  if (flip < 0 || flip > 2) {
+    std::cerr << "shear-direction change must be 0, 1 (reverse) or 2 (rotate)" << std::endl;
     return 1;
   }
   std::vector<double> x, y, p, R, A;
-  double L = 0, gamma = 0, gamma_total = 0;
+  double L = 0, Ly = 0, gamma = 0, gamma_total = 0;
   unsigned long t0 = 0;
   if (file == "r") {
     double phi = a.f("Packing Fraction");
@@ -52,6 +52,7 @@ int main(int argc, char** argv) {
     if (rc) return cli::fail("read", rc);
     n = nf;
     L = hdr[0];
+    Ly = hdr[1];
     gamma = hdr[3];
     gamma_total = hdr[4];
     if (hdr[5] != rate) std::cerr << "Warning: Strain rate in data file does not match the requested rate" << std::endl;
@@ -63,15 +64,18 @@ int main(int argc, char** argv) {
   sc_default_options(&opt);
   opt.precision = cli::precision();
   sc_handle* h = nullptr;
-  int rc = sc_create(&opt, 1, &n, &L, &pad, x.data(), y.data(), p.data(), R.data(), A.data(), &h);
+  if (Ly == 0) Ly = L;
+  int rc = sc_create_rect(&opt, 1, &n, &L, &Ly, &pad, x.data(), y.data(), p.data(), R.data(),
+                          A.data(), &h);
   if (rc) return cli::fail("create", rc);
   if ((rc = sc_set_strain_rate(h, -1, rate)) || (rc = sc_set_step(h, -1, dt)) ||
       (rc = sc_set_gamma(h, -1, gamma)) || (rc = sc_set_total_gamma(h, -1, gamma_total)))
     return cli::fail("setup", rc, h);
-  if (flip == 1) {
-    // main.cpp:258-262: total strain restarts from zero in the reversed direction
-    if ((rc = sc_set_total_gamma(h, -1, 0.0)) || (rc = sc_flip_shear(h, -1)))
-      return cli::fail("flip", rc, h);
+  if (flip == 1 || flip == 2) {
+    // main.cpp:258-267: total strain restarts from zero in the new direction
+    if ((rc = sc_set_total_gamma(h, -1, 0.0)) ||
+        (rc = flip == 1 ? sc_flip_shear(h, -1) : sc_rotate_shear(h, -1)))
+      return cli::fail("shear direction", rc, h);
   }
   unsigned long t_end = 0;
   rc = sc_run_strain(h, dir.c_str(), run, pos_save, se_save, t0, cli::out_format(), &t_end);

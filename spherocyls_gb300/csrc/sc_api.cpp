@@ -71,10 +71,16 @@ const char* sc_last_error(const sc_handle* h) {
 int sc_create(const sc_options* opt_in, int n_sys, const int* n_per_sys, const double* L,
               const double* pad, const double* x, const double* y, const double* phi,
               const double* R, const double* A, sc_handle** out) {
+  return sc_create_rect(opt_in, n_sys, n_per_sys, L, L, pad, x, y, phi, R, A, out);
+}
+
+int sc_create_rect(const sc_options* opt_in, int n_sys, const int* n_per_sys, const double* L,
+                   const double* Ly, const double* pad, const double* x, const double* y,
+                   const double* phi, const double* R, const double* A, sc_handle** out) {
   g_create_error.clear();
   if (!out) return SC_E_ARG;
   *out = nullptr;
-  if (n_sys <= 0 || !n_per_sys || !L || !x || !y || !phi || !R || !A) {
+  if (n_sys <= 0 || !n_per_sys || !L || !Ly || !x || !y || !phi || !R || !A) {
     g_create_error = "sc_create: missing arrays or n_sys <= 0";
     return SC_E_ARG;
   }
@@ -97,7 +103,8 @@ int sc_create(const sc_options* opt_in, int n_sys, const int* n_per_sys, const d
   }
   long long ntot_ll = 0;
   for (int s = 0; s < n_sys; s++) {
-    if (n_per_sys[s] < 2 || !(L[s] > 0) || !std::isfinite(L[s]) || (pad && !(pad[s] >= 0))) {
+    if (n_per_sys[s] < 2 || !(L[s] > 0) || !std::isfinite(L[s]) || !(Ly[s] > 0) ||
+        !std::isfinite(Ly[s]) || (pad && !(pad[s] >= 0))) {
       char buf[160];
       snprintf(buf, sizeof buf, "sc_create: system %d needs n >= 2, L > 0 and pad >= 0", s);
       g_create_error = buf;
@@ -154,7 +161,8 @@ int sc_create(const sc_options* opt_in, int n_sys, const int* n_per_sys, const d
     sc::HostSys& S = h.hs[s];
     S.n = n_per_sys[s];
     S.p0 = p0;
-    S.Lx = S.Ly = L[s];
+    S.Lx = L[s];
+    S.Ly = Ly[s];
     S.pad = pad ? pad[s] : 0.0;
     double filled = 0.0;
     for (int k = 0; k < S.n; k++) {
@@ -364,13 +372,14 @@ int sc_autotune(sc_handle* H, int steps, double* pad_factor, int* block) {
   if (block) *block = h.block;
   if (h.prec != sc::PREC_MIXED) return SC_OK;
   const int n = h.ntot, ns = h.nsys;
-  std::vector<double> x(n), y(n), p(n), L(ns), pad0(ns), pads(ns);
+  std::vector<double> x(n), y(n), p(n), L(ns), Ly(ns), pad0(ns), pads(ns);
   std::vector<int> nps(ns);
   int rc = sc_get_state(H, x.data(), y.data(), p.data());
   if (rc) return rc;
   for (int s = 0; s < ns; s++) {
     nps[s] = h.hs[s].n;
     L[s] = h.hs[s].Lx;
+    Ly[s] = h.hs[s].Ly;
     pad0[s] = h.hs[s].pad;
   }
   const double factors[] = {0.5, 1.0, 1.5, 2.0, 3.0};
@@ -387,8 +396,8 @@ int sc_autotune(sc_handle* H, int steps, double* pad_factor, int* block) {
       o.profile = 0;
       for (int s = 0; s < ns; s++) pads[s] = f * pad0[s];
       sc_handle* T = nullptr;
-      if (sc_create(&o, ns, nps.data(), L.data(), pads.data(), x.data(), y.data(), p.data(),
-                    h.h_R.data(), h.h_A.data(), &T) != SC_OK)
+      if (sc_create_rect(&o, ns, nps.data(), L.data(), Ly.data(), pads.data(), x.data(),
+                         y.data(), p.data(), h.h_R.data(), h.h_A.data(), &T) != SC_OK)
         continue;  // e.g. out of memory for the copy: skip the candidate
       bool ok = true;
       for (int s = 0; s < ns && ok; s++) {
@@ -575,6 +584,18 @@ int sc_flip_shear(sc_handle* H, int sys) {
   std::vector<char> sel(h.nsys, 0);
   for (int s = 0; s < h.nsys; s++) sel[s] = sys < 0 || s == sys;
   return h.flip_shear(sel);
+}
+
+int sc_rotate_shear(sc_handle* H, int sys) {
+  if (!H) return SC_E_ARG;
+  sc::Handle& h = H->h;
+  if (sys < -1 || sys >= h.nsys) {
+    h.fail(SC_E_ARG, "sc_rotate_shear: bad system index");
+    return SC_E_ARG;
+  }
+  std::vector<char> sel(h.nsys, 0);
+  for (int s = 0; s < h.nsys; s++) sel[s] = sys < 0 || s == sys;
+  return h.rotate_shear(sel);
 }
 
 int sc_affine_scale(sc_handle* H, int sys, double factor) {

@@ -311,7 +311,7 @@ __global__ void k_setback(Dev d, const StepScalars* __restrict__ tab, int row) {
     p.y += Ly;
   else if (p.y > Ly)
     p.y -= Ly;
-  p.x += p.y;
+  p.x += (Lx / Ly) * p.y;  // x + y in a square box (Lx / Ly == 1 exactly)
   if (p.x < 0)
     p.x += Lx;
   else

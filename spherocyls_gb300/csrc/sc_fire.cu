@@ -231,6 +231,39 @@ __global__ void k_reflect(Dev d, const double* lx) {
   d.ph[i] = -d.ph[i];
 }
 
+// rotate_by_gamma / gamma_rotate (src/cuda/find_neighbors.cu:583-645) for the
+// systems with q[4s+3] != 0: q[4s..4s+2] = (gamma, new Lx, new Ly).  Positions are
+// mapped to the frame in which the sheared cell is upright (an isometry of the
+// Lees-Edwards system), angles turned by atan(1/gamma), each wrapped once.
+__global__ void k_rotate(Dev d, const double* q) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.ntot) return;
+  const int s = d.psys[i];
+  if (q[4 * s + 3] == 0.0) return;
+  const double g = q[4 * s], Lx = q[4 * s + 1], Ly = q[4 * s + 2];
+  const double pi = 3.14159265358979;  // D_PI of the reference
+  const double2 p = d.xy[i];
+  const double sg = 1 - 2 * (double)signbit(g);
+  const double root = sqrt(1 + g * g);
+  double nx = sg * p.y * root;
+  double ny = -sg * p.x / root;
+  double phi = g != 0.0 ? d.ph[i] - atan(1 / g) : d.ph[i] - pi / 2;
+  if (phi > pi)
+    phi -= 2 * pi;
+  else if (phi < -pi)
+    phi += 2 * pi;
+  if (ny > Ly)
+    ny -= Ly;
+  else if (ny < 0)
+    ny += Ly;
+  if (nx < 0)
+    nx += Lx;
+  else if (nx > Lx)
+    nx -= Lx;
+  d.xy[i] = make_double2(nx, ny);
+  d.ph[i] = phi;
+}
+
 inline int nblk(int n, int b) { return (n + b - 1) / b; }
 
 }  // namespace
@@ -245,6 +278,10 @@ void launch_fire_iteration_tail(const Dev& d, const FireState& f, double ftol, d
   k_fire_chunk<<<d.npchunks, 256, 0, st>>>(d, f);
   k_fire_sys<<<nblk(d.nsys, 128), 128, 0, st>>>(d, f, ftol, dt_max);
   k_fire_update<<<nblk(d.ntot, 256), 256, 0, st>>>(d, f, mixed ? 1 : 0);
+}
+
+void launch_rotate(const Dev& d, const double* q, cudaStream_t st) {
+  k_rotate<<<nblk(d.ntot, 256), 256, 0, st>>>(d, q);
 }
 
 void launch_reflect(const Dev& d, const double* lx, cudaStream_t st) {

@@ -536,8 +536,11 @@ static void advance(HostSys& h, bool resize, int shrink, StepScalars& t) {
   } else {
     h.gamma += h.strain_rate * h.step;
     h.gamma_total += h.strain_rate * h.step;
-    if (h.gamma >= 0.5) {
-      h.gamma -= 1.0;
+    // set_back_gamma at gamma >= 1/2 (src/cpp); for a rectangular box the image
+    // offset Lx/Ly takes the place of 1 (src/cuda/strain_dynamics.cu:712-713)
+    const double r = h.Lx / h.Ly;
+    if (h.gamma >= 0.5 * r) {
+      h.gamma -= r;
       h.gamma_total = static_cast<int>(h.gamma_total + 1) + h.gamma;
       t.setback = 1;
     }
@@ -897,6 +900,38 @@ int Handle::flip_shear(const std::vector<char>& sel) {
   for (int s = 0; s < nsys; s++)
     if (sel[s]) hs[s].gamma = -hs[s].gamma;
   return rebuild_all() && check_status("flip shear") ? SC_OK : last_status;
+}
+
+// Turns the selected systems to the frame in which their sheared cell is upright
+// (rotate_by_gamma, src/cuda/find_neighbors.cu:626-645): Lx' = Ly sqrt(1 + g^2),
+// Ly' = Lx / sqrt(1 + g^2), gamma -> -gamma, positions and angles mapped by
+// k_rotate; the cell grid is configured for the new box and the lists rebuilt.
+int Handle::rotate_shear(const std::vector<char>& sel) {
+  cudaSetDevice(device);
+  if (!materialize()) return last_status;
+  std::vector<double> q(4 * (size_t)nsys, 0.0);
+  for (int s = 0; s < nsys; s++)
+    if (sel[s]) {
+      HostSys& h = hs[s];
+      const double lx = h.Lx, ly = h.Ly;
+      h.Lx = ly * std::sqrt(1 + h.gamma * h.gamma);
+      h.Ly = lx / std::sqrt(1 + h.gamma * h.gamma);
+      q[4 * s] = h.gamma;
+      q[4 * s + 1] = h.Lx;
+      q[4 * s + 2] = h.Ly;
+      q[4 * s + 3] = 1.0;
+      h.gamma = -h.gamma;
+      h.configure(false);
+    }
+  double* dq = nullptr;
+  if (!dalloc(&dq, q.size(), "rotate")) return last_status;
+  bool ok = cuda_ok(cudaMemcpyAsync(dq, q.data(), q.size() * sizeof(double),
+                                    cudaMemcpyHostToDevice, stream), "rotate");
+  if (ok) launch_rotate(d, dq, stream);
+  ok = ok && cuda_ok(cudaStreamSynchronize(stream), "rotate");
+  dfree(dq);
+  if (!ok) return last_status;
+  return layout_cells() && rebuild_all() && check_status("rotate shear") ? SC_OK : last_status;
 }
 
 // Quasistatic compression to jamming: affine steps of dphi in packing fraction,

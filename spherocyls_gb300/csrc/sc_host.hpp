@@ -151,6 +151,7 @@ struct Handle {
                     double* fmax_out, int* done_out);
   int affine_scale(const std::vector<double>& factor);
   int flip_shear(const std::vector<char>& sel);
+  int rotate_shear(const std::vector<char>& sel);
   int quasistatic(double dphi, double ftol, double e_jam, int max_inc, int max_iter,
                   double* phi_jam, int* n_inc);
   int find_jam(double e_jam, double step0, double min_step, double ftol, int max_iter,

@@ -203,6 +203,7 @@ void launch_fire_iteration_tail(const Dev& d, const FireState& f, double ftol, d
                                 bool mixed, cudaStream_t st);
 void launch_affine(const Dev& d, const double* factor, cudaStream_t st);
 void launch_reflect(const Dev& d, const double* lx, cudaStream_t st);
+void launch_rotate(const Dev& d, const double* q, cudaStream_t st);
 // mixed form
 void launch_mx_materialize(const Dev& d, const StepScalars* tab, int row, bool all,
                            cudaStream_t st);

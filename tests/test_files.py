@@ -227,6 +227,34 @@ def test_cli_strain_new_and_continue(library, tmp_path):
 
 
 @pytest.mark.gpu
+def test_cli_strain_rectangular_sd_file(library, tmp_path):
+    """An sd file with Lx != Ly (the src/cuda header) runs in a rectangular box and
+    the box survives into the output files."""
+    import spherocyls_gb300 as sc
+
+    exe = os.path.join(ROOT, "spherocyls_gb300", "bin", "spherocyl_strain")
+    L, x, y, p, R, A = sc.generate_packing(128, 0.80, 1.0, seed=9)
+    n = 2 * len(x)
+    src = tmp_path / "sd0000000000.dat"
+    with open(src, "w") as f:
+        f.write(f"{n} {float(2 * L)!r} {float(L)!r} 0.8 0 0 0.001 0.02\n")
+        for xx, yy, pp, RR, AA in zip(np.concatenate([x, x + L]), np.concatenate([y, y]),
+                                      np.concatenate([p, p]), np.concatenate([R, R]),
+                                      np.concatenate([A, A])):
+            f.write(f"{float(xx)!r} {float(yy)!r} {float(pp)!r} {float(RR)} {float(AA)!r}\n")
+    out = tmp_path / "out"
+    out.mkdir()
+    env = dict(os.environ, SC_OUTPUT_FORMAT="sd")
+    r = subprocess.run([exe, str(src), str(out), str(n), "1e-3", "0.02", "0.02", "0.01", "1e-3",
+                        "0.1", "0"], capture_output=True, text=True, timeout=300, env=env)
+    assert r.returncode == 0, r.stderr
+    last = sorted(f for f in os.listdir(out) if f.startswith("sd0") and f.endswith(".dat"))[-1]
+    assert last != "sd0000000000.dat"
+    hdr, *_ = sc.read_positions(str(out / last))
+    assert hdr["Lx"] == 2 * L and hdr["Ly"] == L
+
+
+@pytest.mark.gpu
 def test_cli_resize_and_minimize(library, tmp_path):
     rz = os.path.join(ROOT, "spherocyls_gb300", "bin", "spherocyl_resize")
     r = subprocess.run([rz, "r", str(tmp_path), "256", "5e-2", "0.02", "0.801", "0.05", "1e-3",

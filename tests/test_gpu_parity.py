@@ -336,3 +336,49 @@ def test_flip_shear_reverses_the_configuration(sc, precision):
     assert np.max(np.abs(periodic_diff(s2[:2], s0[:2], L))) < 1e-12 * L
     dphi = np.remainder(s2[2] - s0[2] + np.pi, 2 * np.pi) - np.pi  # rebuilds wrap phi
     assert np.max(np.abs(dphi)) < 1e-12
+
+
+def test_rectangular_box_tiles_the_square_one(sc):
+    """A rectangular box of two copies of a square packing side by side (Lx = 2L,
+    Ly = L) is the same Lees-Edwards system: under shear it keeps the square box's
+    energy per particle and stresses, through set-backs at gamma = 1/2 in the square
+    box and gamma = 1 in the rectangular one (set_back_coords' Lx/Ly)."""
+    # virial stress: the reference's compat Pxy keeps only the lower-index particle's
+    # arm, and the copies change which particle of a pair has the lower index
+    L, x, y, p, R, A = sc.generate_packing(512, 0.85, 1.0, seed=41)
+    sq = sc.SpherocylBox(L, x, y, p, A, R, 0.1, stress="virial")
+    rect = sc.SpherocylBox(2 * L, np.concatenate([x, x + L]), np.concatenate([y, y]),
+                           np.concatenate([p, p]), np.concatenate([A, A]),
+                           np.concatenate([R, R]), 0.1, Ly=L, stress="virial")
+    for b in (sq, rect):
+        b.set_strain_rate(0.5)
+        b.set_step(0.02)
+    a = sq.strain_steps(150, se_every=10)[:, 0]
+    b = rect.strain_steps(150, se_every=10)[:, 0]
+    assert rect.box()["Lx"] == 2 * L and rect.box()["Ly"] == L
+    scale = np.max(np.abs(a[:, 1:3]), axis=1)
+    assert np.all(np.abs(a[:, 0] - b[:, 0]) <= 1e-9 * a[:, 0])
+    assert np.all(np.abs(a[:, 3] - b[:, 3]) <= 1e-9 * scale)
+
+
+def test_rotate_shear_is_an_isometry(sc):
+    """rotate_by_gamma turns the sheared cell upright: the energy and the normal
+    stress sum are unchanged, the box becomes Ly sqrt(1+g^2) x Lx/sqrt(1+g^2) with
+    gamma -> -gamma, and shearing continues in the rectangular box."""
+    L, x, y, p, R, A = sc.generate_packing(1024, 0.85, 1.0, seed=43)
+    box = sc.SpherocylBox(L, x, y, p, A, R, 0.1, stress="virial")
+    box.set_strain_rate(1e-2)
+    box.set_step(0.02)
+    box.strain_steps(500)
+    g = box.box()["gamma"]
+    se0 = box.calc_se()
+    box.rotate_shear()
+    bx = box.box()
+    se1 = box.calc_se()
+    assert abs(bx["Lx"] - L * np.sqrt(1 + g * g)) <= 1e-12 * L
+    assert abs(bx["Ly"] - L / np.sqrt(1 + g * g)) <= 1e-12 * L
+    assert bx["gamma"] == -g
+    assert abs(se1[0] - se0[0]) <= 1e-10 * se0[0]
+    assert abs((se1[1] + se1[2]) - (se0[1] + se0[2])) <= 1e-10 * abs(se0[1] + se0[2])
+    rec = box.strain_steps(200, se_every=50)
+    assert np.all(np.isfinite(rec)) and np.all(rec[:, 0, 0] > 0)
