@@ -236,7 +236,9 @@ int sc_create_rect(const sc_options* opt_in, int n_sys, const int* n_per_sys, co
   ok = ok && h.dalloc(&pcs, d.npchunks, "pchunk") && h.dalloc(&pcp, d.npchunks, "pchunk") &&
        h.dalloc(&pcn, d.npchunks, "pchunk");
   ok = ok && h.dalloc(&d.flags, n_sys, "flags") && h.dalloc(&d.istar, n_sys, "istar") &&
-       h.dalloc(&d.any, 1, "any") &&
+       h.dalloc(&d.any, 1, "any") && h.dalloc(&d.work, n_sys, "work") &&
+       h.dalloc(&d.woff, n_sys + 1, "woff") && h.dalloc(&d.wcoff, n_sys + 1, "wcoff") &&
+       h.dalloc(&d.nwork, 3, "nwork") &&
        h.dalloc(&d.status, 2, "status");
   if (!ok) return bail(h.last_status ? h.last_status : SC_E_NOMEM);
   d.geom = geom;
@@ -282,6 +284,7 @@ int sc_create_rect(const sc_options* opt_in, int n_sys, const int* n_per_sys, co
        h.cuda_ok(cudaMemsetAsync(d.flags, 0, n_sys * sizeof(int), st), "memset") &&
        h.cuda_ok(cudaMemsetAsync(d.istar, 0x7f, n_sys * sizeof(int), st), "memset") &&
        h.cuda_ok(cudaMemsetAsync(d.any, 0, sizeof(int), st), "memset") &&
+       h.cuda_ok(cudaMemsetAsync(d.nwork, 0, 3 * sizeof(int), st), "memset") &&
        h.cuda_ok(cudaMemsetAsync(d.status, 0, 2 * sizeof(int), st), "memset") &&
        h.cuda_ok(cudaMemsetAsync(d.nbr_n, 0, N * sizeof(int), st), "memset") &&
        h.cuda_ok(cudaMemsetAsync(d.fx, 0, N * sizeof(double), st), "memset") &&

@@ -46,11 +46,69 @@ __device__ __forceinline__ double wrap_bounded(double v, double lo, double hi, d
   return v;
 }
 
+// block-wide exclusive scan of one int per thread (blockDim.x a multiple of 32);
+// returns the exclusive prefix, *total the block's sum
+__device__ __forceinline__ int block_excl_scan(int v, int* sh, int* total) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sh[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    int t = lane < nw ? sh[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    sh[lane] = t;  // inclusive warp totals
+  }
+  __syncthreads();
+  const int excl = x - v + (w > 0 ? sh[w - 1] : 0);
+  *total = sh[nw - 1];
+  __syncthreads();
+  return excl;
+}
+
+// The rebuild worklist (one block): the flagged systems in increasing order with
+// the exclusive prefix sums of their slot and cell counts.
+__global__ void __launch_bounds__(1024) k_rb_worklist(Dev d) {
+  __shared__ int sh[32];
+  if (*d.any == 0) {
+    if (threadIdx.x == 0) d.nwork[0] = d.nwork[1] = d.nwork[2] = 0;
+    return;
+  }
+  int ba = 0, bb = 0, bc = 0;  // running totals (identical in every thread)
+  for (int s0 = 0; s0 < d.nsys; s0 += blockDim.x) {
+    const int s = s0 + threadIdx.x;
+    const bool f = s < d.nsys && d.flags[s] != 0;
+    int ta, tb, tc;
+    const int ea = block_excl_scan(f ? 1 : 0, sh, &ta);
+    const int eb = block_excl_scan(f ? d.geom[s].n : 0, sh, &tb);
+    const int ec = block_excl_scan(f ? d.geom[s].cols * d.geom[s].rows : 0, sh, &tc);
+    if (f) {
+      d.work[ba + ea] = s;
+      d.woff[ba + ea] = bb + eb;
+      d.wcoff[ba + ea] = bc + ec;
+    }
+    ba += ta;
+    bb += tb;
+    bc += tc;
+  }
+  if (threadIdx.x == 0) {
+    d.nwork[0] = ba;
+    d.nwork[1] = bb;
+    d.nwork[2] = bc;
+    d.woff[ba] = bb;
+    d.wcoff[ba] = bc;
+  }
+}
+
 __global__ void k_rb_zero(Dev d) {
   if (*d.any == 0) return;
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= d.ncells) return;
-  if (d.flags[d.cell_sys[c]]) d.cell_count[c] = 0;
+  for_listed_cells(d, [&](int c, int) { d.cell_count[c] = 0; });
 }
 
 // find_cells, spherocyl_box.cpp:270-301: wrap, then hash.
@@ -65,50 +123,48 @@ __global__ void k_rb_zero(Dev d) {
 // particle sits at.  Forced rebuilds and set-back steps wrap every particle.
 __global__ void k_rb_hash(Dev d, const StepScalars* __restrict__ tab, int row, int mixed) {
   if (*d.any == 0) return;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= d.ntot) return;
-  int s = d.psys[i];
-  if (d.flags[s] == 0) return;
-  const SysGeom& g = d.geom[s];
-  const StepScalars& ts = tab[row * d.nsys + s];
-  const double Lx = ts.Lx_c, Ly = ts.Ly_c;
-  double2 p = d.xy[i];
-  double phi = d.ph[i];
-  double2 mv = make_double2(0.0, 0.0);
-  const int istar = d.istar[s];
-  if (!mixed && istar != kNoTrigger && !ts.setback && d.id[i] > istar) {
-    double2 p0 = d.s_xy[i];
-    p0.x = wrap_bounded(p0.x, 0.0, Lx, Lx, d.status);
-    p0.y = wrap_bounded(p0.y, 0.0, Ly, Ly, d.status);
-    double ph0 = wrap_bounded(d.s_ph[i], -kRefPi, kRefPi, 2 * kRefPi, d.status);
-    p = make_double2(p0.x + d.v0x[i], p0.y + d.v0y[i]);
-    phi = ph0 + d.v0p[i];
-    if (ts.mode == 1) {
-      p.x *= ts.scale;
-      p.y *= ts.scale;
-    } else if (ts.mode == 2) {
-      p.x /= ts.scale;
-      p.y /= ts.scale;
+  for_listed_slots(d, [&](int i, int s) {
+    const SysGeom& g = d.geom[s];
+    const StepScalars& ts = tab[row * d.nsys + s];
+    const double Lx = ts.Lx_c, Ly = ts.Ly_c;
+    double2 p = d.xy[i];
+    double phi = d.ph[i];
+    double2 mv = make_double2(0.0, 0.0);
+    const int istar = d.istar[s];
+    if (!mixed && istar != kNoTrigger && !ts.setback && d.id[i] > istar) {
+      double2 p0 = d.s_xy[i];
+      p0.x = wrap_bounded(p0.x, 0.0, Lx, Lx, d.status);
+      p0.y = wrap_bounded(p0.y, 0.0, Ly, Ly, d.status);
+      double ph0 = wrap_bounded(d.s_ph[i], -kRefPi, kRefPi, 2 * kRefPi, d.status);
+      p = make_double2(p0.x + d.v0x[i], p0.y + d.v0y[i]);
+      phi = ph0 + d.v0p[i];
+      if (ts.mode == 1) {
+        p.x *= ts.scale;
+        p.y *= ts.scale;
+      } else if (ts.mode == 2) {
+        p.x /= ts.scale;
+        p.y /= ts.scale;
+      }
+      mv = make_double2(p.x - p0.x, p.y - p0.y);
+    } else {
+      p.x = wrap_bounded(p.x, 0.0, Lx, Lx, d.status);
+      p.y = wrap_bounded(p.y, 0.0, Ly, Ly, d.status);
+      phi = wrap_bounded(phi, -kRefPi, kRefPi, 2 * kRefPi, d.status);
     }
-    mv = make_double2(p.x - p0.x, p.y - p0.y);
-  } else {
-    p.x = wrap_bounded(p.x, 0.0, Lx, Lx, d.status);
-    p.y = wrap_bounded(p.y, 0.0, Ly, Ly, d.status);
-    phi = wrap_bounded(phi, -kRefPi, kRefPi, 2 * kRefPi, d.status);
-  }
-  d.xy[i] = p;
-  d.ph[i] = phi;
-  d.nxy_t[i] = mv;  // displacement counter to carry into the new slot
-  int col = (int)(p.x / ts.W_p);
-  int rw = (int)(p.y / ts.H_p);
-  // a coordinate at (or, after a resize, just past) the box edge stays on the grid
-  if (col >= g.cols) col = g.cols - 1;
-  if (rw >= g.rows) rw = g.rows - 1;
-  if (col < 0) col = 0;
-  if (rw < 0) rw = 0;
-  int c = g.c0 + col + rw * g.cols;
-  d.cell_tmp[i] = c;
-  d.rank[i] = atomicAdd(&d.cell_count[c], 1);
+    d.xy[i] = p;
+    d.ph[i] = phi;
+    d.nxy_t[i] = mv;  // displacement counter to carry into the new slot
+    int col = (int)(p.x / ts.W_p);
+    int rw = (int)(p.y / ts.H_p);
+    // a coordinate at (or, after a resize, just past) the box edge stays on the grid
+    if (col >= g.cols) col = g.cols - 1;
+    if (rw >= g.rows) rw = g.rows - 1;
+    if (col < 0) col = 0;
+    if (rw < 0) rw = 0;
+    int c = g.c0 + col + rw * g.cols;
+    d.cell_tmp[i] = c;
+    d.rank[i] = atomicAdd(&d.cell_count[c], 1);
+  });
 }
 
 __device__ __forceinline__ int block_sum_int(int v, int* sh) {
@@ -184,99 +240,92 @@ __global__ void __launch_bounds__(1024) k_rb_cellscan(Dev d) {
 
 __global__ void k_rb_scatter(Dev d) {
   if (*d.any == 0) return;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= d.ntot) return;
-  if (d.flags[d.psys[i]] == 0) return;
-  d.perm[d.cell_start[d.cell_tmp[i]] + d.rank[i]] = i;
+  for_listed_slots(d, [&](int i, int) { d.perm[d.cell_start[d.cell_tmp[i]] + d.rank[i]] = i; });
 }
 
 // Order each cell's slots by particle index: the reference's cell lists are
 // filled in particle order (spherocyl_box.cpp:277-298).
 __global__ void k_rb_cellsort(Dev d) {
   if (*d.any == 0) return;
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= d.ncells) return;
-  if (d.flags[d.cell_sys[c]] == 0) return;
-  int st = d.cell_start[c], n = d.cell_count[c];
-  if (n <= 1) return;
-  int* P = d.perm + st;
-  if (n <= kMaxCellSort) {
-    int key[kMaxCellSort], val[kMaxCellSort];
-    for (int k = 0; k < n; k++) {
-      val[k] = P[k];
-      key[k] = d.id[val[k]];
-    }
-    for (int k = 1; k < n; k++) {
-      int kk = key[k], vv = val[k], m = k - 1;
-      while (m >= 0 && key[m] > kk) {
-        key[m + 1] = key[m];
-        val[m + 1] = val[m];
-        m--;
+  for_listed_cells(d, [&](int c, int) {
+    int st = d.cell_start[c], n = d.cell_count[c];
+    if (n <= 1) return;
+    int* P = d.perm + st;
+    if (n <= kMaxCellSort) {
+      int key[kMaxCellSort], val[kMaxCellSort];
+      for (int k = 0; k < n; k++) {
+        val[k] = P[k];
+        key[k] = d.id[val[k]];
       }
-      key[m + 1] = kk;
-      val[m + 1] = vv;
-    }
-    for (int k = 0; k < n; k++) P[k] = val[k];
-  } else {
-    for (int k = 1; k < n; k++) {
-      int vv = P[k], kk = d.id[vv], m = k - 1;
-      while (m >= 0 && d.id[P[m]] > kk) {
-        P[m + 1] = P[m];
-        m--;
+      for (int k = 1; k < n; k++) {
+        int kk = key[k], vv = val[k], m = k - 1;
+        while (m >= 0 && key[m] > kk) {
+          key[m + 1] = key[m];
+          val[m + 1] = val[m];
+          m--;
+        }
+        key[m + 1] = kk;
+        val[m + 1] = vv;
       }
-      P[m + 1] = vv;
+      for (int k = 0; k < n; k++) P[k] = val[k];
+    } else {
+      for (int k = 1; k < n; k++) {
+        int vv = P[k], kk = d.id[vv], m = k - 1;
+        while (m >= 0 && d.id[P[m]] > kk) {
+          P[m + 1] = P[m];
+          m--;
+        }
+        P[m + 1] = vv;
+      }
     }
-  }
+  });
 }
 
 __global__ void k_rb_gather(Dev d) {
   if (*d.any == 0) return;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= d.ntot) return;
-  if (d.flags[d.psys[i]] == 0) return;
-  int src = d.perm[i];
-  d.s_xy[i] = d.xy[src];
-  d.s_ph[i] = d.ph[src];
-  d.s_ra[i] = d.ra[src];
-  d.s_irc[i] = d.irc[src];
-  d.s_id[i] = d.id[src];
-  d.s_cell[i] = d.cell_tmp[src];
-  double2 mv = d.nxy_t[src];
-  d.v0x[i] = mv.x;
-  d.v0y[i] = mv.y;
-  if (d.fvx) {  // minimiser velocities travel with their particles (predictor copy is dead here)
-    d.xy_t[i] = make_double2(d.fvx[src], d.fvy[src]);
-    d.ph_t[i] = d.fvp[src];
-  }
+  for_listed_slots(d, [&](int i, int) {
+    int src = d.perm[i];
+    d.s_xy[i] = d.xy[src];
+    d.s_ph[i] = d.ph[src];
+    d.s_ra[i] = d.ra[src];
+    d.s_irc[i] = d.irc[src];
+    d.s_id[i] = d.id[src];
+    d.s_cell[i] = d.cell_tmp[src];
+    double2 mv = d.nxy_t[src];
+    d.v0x[i] = mv.x;
+    d.v0y[i] = mv.y;
+    if (d.fvx) {  // minimiser velocities travel with their particles (predictor copy is dead here)
+      d.xy_t[i] = make_double2(d.fvx[src], d.fvy[src]);
+      d.ph_t[i] = d.fvp[src];
+    }
+  });
 }
 
 __global__ void k_rb_commit(Dev d, const StepScalars* __restrict__ tab, int row, int mixed) {
   if (*d.any == 0) return;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= d.ntot) return;
-  int s = d.psys[i];
-  if (d.flags[s] == 0) return;
-  double2 p = d.s_xy[i];
-  double phi = d.s_ph[i];
-  double2 ra = d.s_ra[i];
-  d.xy[i] = p;
-  d.ph[i] = phi;
-  d.ra[i] = ra;
-  d.irc[i] = d.s_irc[i];
-  d.id[i] = d.s_id[i];
-  d.cell[i] = d.s_cell[i];
-  d.moved[i] = make_double2(d.v0x[i], d.v0y[i]);
-  if (d.fvx) {
-    double2 v = d.xy_t[i];
-    d.fvx[i] = v.x;
-    d.fvy[i] = v.y;
-    d.fvp[i] = d.ph_t[i];
-  }
-  if (!mixed) {
-    double sn, cs;
-    sincos(phi, &sn, &cs);
-    d.nxy[i] = make_double2(ra.y * cs, ra.y * sn);
-  }
+  for_listed_slots(d, [&](int i, int) {
+    double2 p = d.s_xy[i];
+    double phi = d.s_ph[i];
+    double2 ra = d.s_ra[i];
+    d.xy[i] = p;
+    d.ph[i] = phi;
+    d.ra[i] = ra;
+    d.irc[i] = d.s_irc[i];
+    d.id[i] = d.s_id[i];
+    d.cell[i] = d.s_cell[i];
+    d.moved[i] = make_double2(d.v0x[i], d.v0y[i]);
+    if (d.fvx) {
+      double2 v = d.xy_t[i];
+      d.fvx[i] = v.x;
+      d.fvy[i] = v.y;
+      d.fvp[i] = d.ph_t[i];
+    }
+    if (!mixed) {
+      double sn, cs;
+      sincos(phi, &sn, &cs);
+      d.nxy[i] = make_double2(ra.y * cs, ra.y * sn);
+    }
+  });
 }
 
 __global__ void k_rb_clear(Dev d) {
@@ -441,15 +490,17 @@ inline int nblk(int n, int b) { return (n + b - 1) / b; }
 
 void launch_rebuild(const Dev& d, bool mixed, const StepScalars* tab, int row, cudaStream_t st) {
   const int B = 256;
-  k_rb_zero<<<nblk(d.ncells, B), B, 0, st>>>(d);
-  k_rb_hash<<<nblk(d.ntot, B), B, 0, st>>>(d, tab, row, mixed ? 1 : 0);
+  // the slot and cell kernels walk the worklist with a fixed grid
+  k_rb_worklist<<<1, 1024, 0, st>>>(d);
+  k_rb_zero<<<kWalkBlocks, B, 0, st>>>(d);
+  k_rb_hash<<<kWalkBlocks, B, 0, st>>>(d, tab, row, mixed ? 1 : 0);
   k_rb_chunksum<<<d.nchunks, 256, 0, st>>>(d);
   k_rb_sysscan<<<nblk(d.nsys, 128), 128, 0, st>>>(d);
   k_rb_cellscan<<<d.nchunks, 1024, 0, st>>>(d);
-  k_rb_scatter<<<nblk(d.ntot, B), B, 0, st>>>(d);
-  k_rb_cellsort<<<nblk(d.ncells, 128), 128, 0, st>>>(d);
-  k_rb_gather<<<nblk(d.ntot, B), B, 0, st>>>(d);
-  k_rb_commit<<<nblk(d.ntot, B), B, 0, st>>>(d, tab, row, mixed ? 1 : 0);
+  k_rb_scatter<<<kWalkBlocks, B, 0, st>>>(d);
+  k_rb_cellsort<<<2 * kWalkBlocks, 128, 0, st>>>(d);
+  k_rb_gather<<<kWalkBlocks, B, 0, st>>>(d);
+  k_rb_commit<<<kWalkBlocks, B, 0, st>>>(d, tab, row, mixed ? 1 : 0);
   if (mixed) {
     launch_mx_local(d, tab, row, false, st);
     launch_mx_build_list(d, tab, row, false, st);

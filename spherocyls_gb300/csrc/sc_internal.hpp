@@ -151,6 +151,10 @@ struct Dev {
   int* flags;               // [nsys] bit0 moved-rebuild, bit1 forced rebuild
   int* istar;               // [nsys] lowest particle index that triggered a rebuild
   int* any;                 // [1] set when any system needs a rebuild
+  int* work;                // [nsys] rebuild worklist: the flagged systems, ascending
+  int* woff;                // [nsys + 1] first work item (slot) of each listed system
+  int* wcoff;               // [nsys + 1] first work item (cell) of each listed system
+  int* nwork;               // [3] listed systems, their slots, their cells
   int* status;              // [2] sticky error bits (ST_*), rebuild-chain count
 };
 
@@ -211,5 +215,55 @@ void launch_mx_local(const Dev& d, const StepScalars* tab, int row, bool all, cu
 void launch_mx_order(const Dev& d, bool all, cudaStream_t st);
 void launch_mx_build_list(const Dev& d, const StepScalars* tab, int row, bool all,
                           cudaStream_t st);
+
+constexpr int kWalkBlocks = 152 * 8;  // fixed grid of the worklist kernels
+
+#ifdef __CUDACC__
+// Grid-stride walks over the slots / cells of the systems on the rebuild worklist
+// (k_rb_worklist), so that a rebuild of a few systems of a large batch costs in
+// proportion to those systems.  f(slot or cell, system).
+// the listed system that work item g belongs to (off: exclusive prefix sums)
+__device__ __forceinline__ int listed_system(const int* __restrict__ off, int nw, int g) {
+  int lo = 0, hi = nw - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (off[mid] <= g)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+template <class F>
+__device__ __forceinline__ void for_listed_slots(const Dev& d, F&& f) {
+  const int nw = d.nwork[0], W = d.nwork[1];
+  const int t = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+  for (int g = t; g < W; g += stride) {
+    const int w = listed_system(d.woff, nw, g);
+    const int s = d.work[w];
+    f(d.geom[s].p0 + (g - d.woff[w]), s);
+  }
+}
+template <class F>
+__device__ __forceinline__ void for_listed_cells(const Dev& d, F&& f) {
+  const int nw = d.nwork[0], W = d.nwork[2];
+  const int t = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+  for (int g = t; g < W; g += stride) {
+    const int w = listed_system(d.wcoff, nw, g);
+    const int s = d.work[w];
+    f(d.geom[s].c0 + (g - d.wcoff[w]), s);
+  }
+}
+// all: every slot of every system (forced refreshes), else the worklist
+template <class F>
+__device__ __forceinline__ void for_slots(const Dev& d, bool all, F&& f) {
+  if (!all) {
+    for_listed_slots(d, f);
+    return;
+  }
+  const int t = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+  for (int i = t; i < d.ntot; i += stride) f(i, d.psys[i]);
+}
+#endif
 
 }  // namespace sc

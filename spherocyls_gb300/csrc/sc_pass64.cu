@@ -36,46 +36,44 @@ __device__ __forceinline__ bool nbr_criterion(double2 pp, double2 pq, double sig
 __global__ void __launch_bounds__(128) k_build_nbrs(Dev d, const StepScalars* __restrict__ tab,
                                                    int row) {
   if (*d.any == 0) return;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= d.ntot) return;
-  int s = d.psys[i];
-  if (d.flags[s] == 0) return;
-  const SysGeom g = d.geom[s];
-  const StepScalars ts = tab[row * d.nsys + s];
-  double2 pi = d.xy[i];
-  double2 rai = d.ra[i];
-  int idi = d.id[i];
-  int c = d.cell[i] - g.c0;
-  int col = c % g.cols, rw = c / g.cols;
-  // 3x3 block of cells; a dimension with fewer than three cells is scanned once
-  // per distinct cell (the reference would list such cells twice).
-  int ncx = g.cols < 3 ? g.cols : 3, ncy = g.rows < 3 ? g.rows : 3;
-  int cnt = 0;
-  for (int a = 0; a < ncy; a++) {
-    int r2 = ncy == 3 ? wrap_index(rw + a - 1, g.rows) : a;
-    for (int b = 0; b < ncx; b++) {
-      int c2 = ncx == 3 ? wrap_index(col + b - 1, g.cols) : b;
-      int cc = g.c0 + r2 * g.cols + c2;
-      int st = d.cell_start[cc], nn = d.cell_count[cc];
-      for (int j = st; j < st + nn; j++) {
-        if (j == i) continue;
-        int idj = d.id[j];
-        double2 pj = d.xy[j];
-        double2 raj = d.ra[j];
-        bool ip = idi < idj;
-        // S = R_p + A_p + R_q + A_q summed in the reference's order
-        double sig = ip ? rai.x + rai.y + raj.x + raj.y : raj.x + raj.y + rai.x + rai.y;
-        bool hit = ip ? nbr_criterion(pi, pj, sig, g.pad, ts.gamma_p, ts.Lx_p, ts.Ly_p)
-                      : nbr_criterion(pj, pi, sig, g.pad, ts.gamma_p, ts.Lx_p, ts.Ly_p);
-        if (hit) {
-          if (cnt < d.maxn) d.nbr[(size_t)cnt * d.ntot + i] = j;
-          cnt++;
+  for_listed_slots(d, [&](int i, int s) {
+    const SysGeom g = d.geom[s];
+    const StepScalars ts = tab[row * d.nsys + s];
+    double2 pi = d.xy[i];
+    double2 rai = d.ra[i];
+    int idi = d.id[i];
+    int c = d.cell[i] - g.c0;
+    int col = c % g.cols, rw = c / g.cols;
+    // 3x3 block of cells; a dimension with fewer than three cells is scanned once
+    // per distinct cell (the reference would list such cells twice).
+    int ncx = g.cols < 3 ? g.cols : 3, ncy = g.rows < 3 ? g.rows : 3;
+    int cnt = 0;
+    for (int a = 0; a < ncy; a++) {
+      int r2 = ncy == 3 ? wrap_index(rw + a - 1, g.rows) : a;
+      for (int b = 0; b < ncx; b++) {
+        int c2 = ncx == 3 ? wrap_index(col + b - 1, g.cols) : b;
+        int cc = g.c0 + r2 * g.cols + c2;
+        int st = d.cell_start[cc], nn = d.cell_count[cc];
+        for (int j = st; j < st + nn; j++) {
+          if (j == i) continue;
+          int idj = d.id[j];
+          double2 pj = d.xy[j];
+          double2 raj = d.ra[j];
+          bool ip = idi < idj;
+          // S = R_p + A_p + R_q + A_q summed in the reference's order
+          double sig = ip ? rai.x + rai.y + raj.x + raj.y : raj.x + raj.y + rai.x + rai.y;
+          bool hit = ip ? nbr_criterion(pi, pj, sig, g.pad, ts.gamma_p, ts.Lx_p, ts.Ly_p)
+                        : nbr_criterion(pj, pi, sig, g.pad, ts.gamma_p, ts.Lx_p, ts.Ly_p);
+          if (hit) {
+            if (cnt < d.maxn) d.nbr[(size_t)cnt * d.ntot + i] = j;
+            cnt++;
+          }
         }
       }
     }
-  }
-  d.nbr_n[i] = cnt;
-  if (cnt > d.maxn) atomicOr(d.status, ST_NBR_OVERFLOW);
+    d.nbr_n[i] = cnt;
+    if (cnt > d.maxn) atomicOr(d.status, ST_NBR_OVERFLOW);
+  });
 }
 
 // The reference rebuilds inside its corrector loop as soon as particle i has
@@ -340,9 +338,7 @@ void launch_pass_fp64(const Dev& d, int mode, bool se, const StepScalars* tab, i
 }
 
 void launch_build_nbrs(const Dev& d, const StepScalars* tab, int row, cudaStream_t st) {
-  int block = 128;
-  int grid = (d.ntot + block - 1) / block;
-  k_build_nbrs<<<grid, block, 0, st>>>(d, tab, row);
+  k_build_nbrs<<<2 * kWalkBlocks, 128, 0, st>>>(d, tab, row);
 }
 
 }  // namespace sc

@@ -280,81 +280,77 @@ __global__ void k_mx_materialize(Dev d, const StepScalars* __restrict__ tab, int
 // Compensated local state from the FP64 state after a cell sort.
 __global__ void k_mx_local(Dev d, const StepScalars* __restrict__ tab, int row, int all) {
   if (!all && *d.any == 0) return;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= d.ntot) return;
-  int s = d.psys[i];
-  if (!all && d.flags[s] == 0) return;
-  const SysGeom& g = d.geom[s];
-  const StepScalars& ts = tab[row * d.nsys + s];
-  int lc = d.cell[i] - g.c0;
-  int col = lc % g.cols, rw = lc / g.cols;
-  d.cellp[i] = col | (rw << 16);
-  double2 p = d.xy[i];
-  double lx = p.x - (col + 0.5) * ts.W_p;
-  double ly = p.y - (rw + 0.5) * ts.H_p;
-  double phi = d.ph[i];
-  float xl = (float)lx, yl = (float)ly, pf = (float)phi;
-  double2 ra = d.ra[i];
-  double2 irc = d.irc[i];
-  float A = (float)ra.y;
-  float sn, cs;
-  sincosf(pf, &sn, &cs);
-  d.rec[i] = make_float4(xl, yl, A * cs, A * sn);
-  d.mc[i] = make_float4((float)(lx - xl), (float)(ly - yl), pf, (float)(phi - pf));
-  d.mm[i] = make_float2(0.f, 0.f);
-  d.pa[i] = make_float4((float)ra.x, A, __int_as_float(d.id[i]), (float)(1.0 / irc.x));
-  d.rcf[i] = (float)irc.y;
-  d.rf[i] = (float)ra.x;
+  for_slots(d, all != 0, [&](int i, int s) {
+    const SysGeom& g = d.geom[s];
+    const StepScalars& ts = tab[row * d.nsys + s];
+    int lc = d.cell[i] - g.c0;
+    int col = lc % g.cols, rw = lc / g.cols;
+    d.cellp[i] = col | (rw << 16);
+    double2 p = d.xy[i];
+    double lx = p.x - (col + 0.5) * ts.W_p;
+    double ly = p.y - (rw + 0.5) * ts.H_p;
+    double phi = d.ph[i];
+    float xl = (float)lx, yl = (float)ly, pf = (float)phi;
+    double2 ra = d.ra[i];
+    double2 irc = d.irc[i];
+    float A = (float)ra.y;
+    float sn, cs;
+    sincosf(pf, &sn, &cs);
+    d.rec[i] = make_float4(xl, yl, A * cs, A * sn);
+    d.mc[i] = make_float4((float)(lx - xl), (float)(ly - yl), pf, (float)(phi - pf));
+    d.mm[i] = make_float2(0.f, 0.f);
+    d.pa[i] = make_float4((float)ra.x, A, __int_as_float(d.id[i]), (float)(1.0 / irc.x));
+    d.rcf[i] = (float)irc.y;
+    d.rf[i] = (float)ra.x;
+  });
 }
 
 // The padded neighbour list in FP32 (see the file comment).
 __global__ void __launch_bounds__(128) k_mx_build_list(Dev d, const StepScalars* __restrict__ tab,
                                                       int row, int all) {
   if (!all && *d.any == 0) return;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= d.ntot) return;
-  int s = d.psys[i];
-  if (!all && d.flags[s] == 0) return;
-  const SysGeom& g = d.geom[s];
-  const StepScalars& ts = tab[row * d.nsys + s];
-  const float W = ts.f_Wp, H = ts.f_Hp, gam = ts.f_gamma_p, pad = (float)g.pad;
-  const float Lxf = W * g.cols, Lyf = H * g.rows;
-  const int cp = d.cellp[i];
-  const int col = cp & 0xffff, rw = cp >> 16;
-  const float4 ri = d.rec[i];
-  const float4 pai = d.pa[i];
-  const int ncx = g.cols < 3 ? g.cols : 3, ncy = g.rows < 3 ? g.rows : 3;
-  const bool smallx = ncx < 3, smally = ncy < 3;
-  int cnt = 0;
-  for (int a = 0; a < ncy; a++) {
-    int dr = smally ? a - rw : a - 1;
-    int r2 = smally ? a : wrap_index(rw + dr, g.rows);
-    for (int b = 0; b < ncx; b++) {
-      int dc = smallx ? b - col : b - 1;
-      int c2 = smallx ? b : wrap_index(col + dc, g.cols);
-      int cc = g.c0 + r2 * g.cols + c2;
-      int st = d.cell_start[cc], en = st + d.cell_count[cc];
-      unsigned code = ((unsigned)(dc + 1) << 28) | ((unsigned)(dr + 1) << 30);
-      for (int j = st; j < en; j++) {
-        if (j == i) continue;
-        float4 rj = d.rec[j];
-        float4 paj = d.pa[j];
-        float dx = ri.x - rj.x - (float)dc * W;
-        float dy = ri.y - rj.y - (float)dr * H;
-        if (smallx) dx += Lxf * (float)((dx < -0.5f * Lxf) - (dx > 0.5f * Lxf));
-        if (smally) dy += Lyf * (float)((dy < -0.5f * Lyf) - (dy > 0.5f * Lyf));
-        float lim = (pai.x + pai.y + paj.x + paj.y + pad) * 1.00002f + 1e-6f;
-        float dxl = fmaf(gam, dy, dx);
-        if (dxl * dxl + dy * dy < lim * lim) {
-          if (cnt < d.maxn) d.nbr[(size_t)cnt * d.ntot + i] = (int)((unsigned)j | code);
-          cnt++;
+  for_slots(d, all != 0, [&](int i, int s) {
+    const SysGeom& g = d.geom[s];
+    const StepScalars& ts = tab[row * d.nsys + s];
+    const float W = ts.f_Wp, H = ts.f_Hp, gam = ts.f_gamma_p, pad = (float)g.pad;
+    const float Lxf = W * g.cols, Lyf = H * g.rows;
+    const int cp = d.cellp[i];
+    const int col = cp & 0xffff, rw = cp >> 16;
+    const float4 ri = d.rec[i];
+    const float4 pai = d.pa[i];
+    const int ncx = g.cols < 3 ? g.cols : 3, ncy = g.rows < 3 ? g.rows : 3;
+    const bool smallx = ncx < 3, smally = ncy < 3;
+    int cnt = 0;
+    for (int a = 0; a < ncy; a++) {
+      int dr = smally ? a - rw : a - 1;
+      int r2 = smally ? a : wrap_index(rw + dr, g.rows);
+      for (int b = 0; b < ncx; b++) {
+        int dc = smallx ? b - col : b - 1;
+        int c2 = smallx ? b : wrap_index(col + dc, g.cols);
+        int cc = g.c0 + r2 * g.cols + c2;
+        int st = d.cell_start[cc], en = st + d.cell_count[cc];
+        unsigned code = ((unsigned)(dc + 1) << 28) | ((unsigned)(dr + 1) << 30);
+        for (int j = st; j < en; j++) {
+          if (j == i) continue;
+          float4 rj = d.rec[j];
+          float4 paj = d.pa[j];
+          float dx = ri.x - rj.x - (float)dc * W;
+          float dy = ri.y - rj.y - (float)dr * H;
+          if (smallx) dx += Lxf * (float)((dx < -0.5f * Lxf) - (dx > 0.5f * Lxf));
+          if (smally) dy += Lyf * (float)((dy < -0.5f * Lyf) - (dy > 0.5f * Lyf));
+          float lim = (pai.x + pai.y + paj.x + paj.y + pad) * 1.00002f + 1e-6f;
+          float dxl = fmaf(gam, dy, dx);
+          if (dxl * dxl + dy * dy < lim * lim) {
+            if (cnt < d.maxn) d.nbr[(size_t)cnt * d.ntot + i] = (int)((unsigned)j | code);
+            cnt++;
+          }
         }
       }
     }
-  }
-  d.nbr_n[i] = cnt;
-  if (cnt > d.maxn) atomicOr(d.status, ST_NBR_OVERFLOW);
-  if (i == g.p0) d.gbuild[s] = gam;
+    d.nbr_n[i] = cnt;
+    if (cnt > d.maxn) atomicOr(d.status, ST_NBR_OVERFLOW);
+    if (i == g.p0) d.gbuild[s] = gam;
+  });
 }
 
 // Force-pass ordering: within each window of kOrderWindow slots, a stable sort
@@ -420,12 +416,12 @@ void launch_mx_materialize(const Dev& d, const StepScalars* tab, int row, bool a
 }
 
 void launch_mx_local(const Dev& d, const StepScalars* tab, int row, bool all, cudaStream_t st) {
-  k_mx_local<<<nblk(d.ntot, 256), 256, 0, st>>>(d, tab, row, all ? 1 : 0);
+  k_mx_local<<<kWalkBlocks, 256, 0, st>>>(d, tab, row, all ? 1 : 0);
 }
 
 void launch_mx_build_list(const Dev& d, const StepScalars* tab, int row, bool all,
                           cudaStream_t st) {
-  k_mx_build_list<<<nblk(d.ntot, 128), 128, 0, st>>>(d, tab, row, all ? 1 : 0);
+  k_mx_build_list<<<2 * kWalkBlocks, 128, 0, st>>>(d, tab, row, all ? 1 : 0);
 }
 
 }  // namespace sc
