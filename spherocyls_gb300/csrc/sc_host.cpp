@@ -593,7 +593,10 @@ int Handle::run_steps(bool resize, int shrink, int nsteps, int se_every, double*
       }
     }
     if (nk == 0) {
-      // the grid changes before the next step: re-grid, rebuild, continue
+      // the grid changes before the next step: re-grid, rebuild, continue.  The
+      // mixed form's positions are relative to the old grid's cell centres, so the
+      // FP64 state is brought up to date before the grid changes.
+      if (!materialize()) return last_status;
       for (int s = 0; s < nsys; s++) hs[s].configure(false);
       if (!layout_cells() || !rebuild_all()) return last_status;
       continue;
@@ -654,6 +657,8 @@ int Handle::run_steps(bool resize, int shrink, int nsteps, int se_every, double*
     done += nk;
     steps += nk;
     if (regrid) {
+      // mixed form: positions relative to the old grid's cell centres first
+      if (!materialize()) return last_status;
       for (int s = 0; s < nsys; s++) hs[s].configure(false);
       if (!layout_cells() || !rebuild_all()) return last_status;
     }
