@@ -411,3 +411,24 @@ def test_mixed_resize_tracks_reference(sc, name):
         assert np.max(np.abs(periodic_diff(y, g[f"s{cp}_y"], bx[1]))) < 1e-4 * bx[1]
         e = box.calc_se()[0]
         assert abs(e - g[f"s{cp}_se"][0]) <= 1e-3 * abs(g[f"s{cp}_se"][0])
+
+
+def test_mixed_setback_tracks_fp64(sc):
+    """Mixed and FP64 shear through Lees-Edwards set-backs (gamma reaching 1/2 twice):
+    energy and shear stress per record within 1e-4 of the FP64 run's, the same gamma,
+    and positions within 1e-3 of the box at the end (well before chaos separates the
+    trajectories at this strain rate)."""
+    L, x, y, p, R, A = sc.generate_packing(1024, 0.85, 1.0, seed=51)
+    runs = []
+    for prec in ("fp64", "mixed"):
+        b = sc.SpherocylBox(L, x, y, p, A, R, 0.1, precision=prec, stress="virial")
+        b.set_strain_rate(0.1)
+        b.set_step(0.02)
+        rec = b.strain_steps(600, se_every=20)[:, 0]
+        runs.append((rec, np.array(b.state()), b.box()["gamma"], b.box()["gamma_total"]))
+    (ra, sa, ga, ta), (rb, sb, gb, tb) = runs
+    assert ta > 1.0 and abs(ga - gb) < 1e-12 and abs(ta - tb) < 1e-12
+    scale = np.max(np.abs(ra[:, 1:3]), axis=1)
+    assert np.all(np.abs(ra[:, 0] - rb[:, 0]) <= 1e-4 * ra[:, 0])
+    assert np.all(np.abs(ra[:, 3] - rb[:, 3]) <= 1e-4 * scale)
+    assert np.max(np.abs(periodic_diff(sa[:2], sb[:2], L))) < 1e-3 * L
