@@ -213,13 +213,14 @@ def test_mixed_precision_shear_tracks_fp64(sc):
     assert np.all(np.abs(sa[:, 0, 0] - sb[:, 0, 0]) <= 1e-4 * np.abs(sa[:, 0, 0]))
 
 
-def test_batched_systems_match_single_runs(sc):
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batched_systems_match_single_runs(sc, precision):
     """Several systems of different size in one handle advance exactly as alone."""
     specs = [(256, 0.85, 1.0, 1e-3, 21), (400, 0.80, 0.5, 5e-4, 22), (300, 0.88, 2.0, 2e-3, 23)]
     packs = [sc.generate_packing(n, phi, a, seed=s) for n, phi, a, _, s in specs]
     singles = []
     for (n, phi, a, rate, s), (L, x, y, p, R, A) in zip(specs, packs):
-        box = sc.SpherocylBox(L, x, y, p, A, R, 0.1)
+        box = sc.SpherocylBox(L, x, y, p, A, R, 0.1, precision=precision)
         box.set_strain_rate(rate)
         box.set_step(0.02)
         box.strain_steps(150)
@@ -229,7 +230,7 @@ def test_batched_systems_match_single_runs(sc):
                         np.concatenate([pk[2] for pk in packs]),
                         np.concatenate([pk[3] for pk in packs]),
                         np.concatenate([pk[5] for pk in packs]),
-                        np.concatenate([pk[4] for pk in packs]), 0.1)
+                        np.concatenate([pk[4] for pk in packs]), 0.1, precision=precision)
     for i, sp in enumerate(specs):
         batch.set_strain_rate(sp[3], sys=i)
     batch.set_step(0.02)
@@ -432,3 +433,23 @@ def test_mixed_setback_tracks_fp64(sc):
     assert np.all(np.abs(ra[:, 0] - rb[:, 0]) <= 1e-4 * ra[:, 0])
     assert np.all(np.abs(ra[:, 3] - rb[:, 3]) <= 1e-4 * scale)
     assert np.max(np.abs(periodic_diff(sa[:2], sb[:2], L))) < 1e-3 * L
+
+
+def test_fp64_two_point_shear_matches_restatement(sc, oracle_built):
+    """Shear steps with the two-point contact rule: the FP64 form against the oracle's
+    restatement of it over 50 Heun steps with a rebuild inside."""
+    L, x, y, p, R, A = sc.generate_packing(512, 0.80, 1.0, seed=61)
+    f = np.sqrt(0.80 / 0.87)
+    L, x, y = L * f, x * f, y * f
+    box = sc.SpherocylBox(L, x, y, p, A, R, 0.1, contacts=2)
+    ob = oracle_built.OracleBox(L, x, y, p, A, R, 0.1, strain_rate=1e-2, step=0.02,
+                                two_point=True)
+    box.set_strain_rate(1e-2)
+    box.set_step(0.02)
+    box.strain_steps(50)
+    ob.run_strain_steps(50)
+    xs, ys, ps = box.state()
+    xo, yo, po = ob.state()
+    assert np.max(np.abs(periodic_diff(xs, xo, L))) < 1e-10 * L
+    assert np.max(np.abs(periodic_diff(ys, yo, L))) < 1e-10 * L
+    assert np.max(np.abs(ps - po)) < 1e-10
