@@ -195,7 +195,8 @@ def cpu_baseline(w, sample_n, steps, threads, pad):
 METRIC = "particle-steps/s (Lees-Edwards shear, Heun step)"
 
 
-def minimise_leg(replicas=32, n=4096, max_iter=20000, ftol=1e-14, device=0):
+def minimise_leg(replicas=32, n=4096, max_iter=20000, ftol=1e-14, device=0, e_jam=1e-12,
+                 dt_max=0.2):
     """Minimisation time to tolerance on the jamming workload's shape: replicas of
     N = 4096 with a/R in {0.25, 0.5, 1, 2} (a quarter each), seeds 100 + k, from
     packing 0.70.  Untimed preparation: the mixed form compresses every replica to
@@ -219,7 +220,7 @@ def minimise_leg(replicas=32, n=4096, max_iter=20000, ftol=1e-14, device=0):
                     **kw)
     t0 = time.perf_counter()
     prep.fire_minimize(1e-6, 100000)
-    phi_j, n_inc = prep.quasistatic_compress(2e-3, 1e-6, 1e-12, 1000, 100000)
+    phi_j, n_inc = prep.quasistatic_compress(2e-3, 1e-6, e_jam, 1000, 100000)
     t_prep = time.perf_counter() - t0
     Lj = np.array([prep.box(s)["Lx"] for s in range(replicas)])
     xs, ys, ps = prep.state()
@@ -230,7 +231,7 @@ def minimise_leg(replicas=32, n=4096, max_iter=20000, ftol=1e-14, device=0):
 
     def run(b, tol, cap):
         t = time.perf_counter()
-        it, fmax, done = b.fire_minimize(tol, cap)
+        it, fmax, done = b.fire_minimize(tol, cap, dt_max=dt_max)
         return time.perf_counter() - t, it, fmax, done
 
     m = BoxBatch([n] * replicas, L1, x1, y1, ps, A, R, 0.1, precision="mixed", **kw)
