@@ -154,14 +154,16 @@ __global__ void k_fire_update(Dev d, FireState f, int mixed) {
     r.w = A * sn;
     d.rec[i] = r;
     d.mc[i] = c;
-    float2 m = d.mm[i];
+    float4 m = d.mm[i];
     m.x += (float)ddx;
     m.y += (float)ddy;
     d.mm[i] = m;
-    // the mixed list criterion (fixed gamma): displacement plus the next step's
-    // allowance within half the padding
-    float dd = (float)sqrt(ddx * ddx + ddy * ddy);
-    if (!(sqrtf(m.x * m.x + m.y * m.y) + dd < 0.5f * g.fpad)) {
+    // the mixed list criterion (fixed gamma): spine movement since the build
+    // (centre plus A times the rotation) and the next step's allowance within half
+    // the padding
+    float dd = (float)sqrt(ddx * ddx + ddy * ddy) + A * (float)fabs(ddp);
+    float moved = sqrtf(m.x * m.x + m.y * m.y) + A * fabsf((c.z + c.w) - m.z);
+    if (!(moved + dd < 0.5f * g.fpad)) {
       if (d.flags[s] == 0) atomicOr(&d.flags[s], 1);
       if (*d.any == 0) atomicExch(d.any, 1);
     }

@@ -104,7 +104,7 @@ struct Dev {
   float4* rec_t;  // the same for the predictor copy
   float4* mc;     // (x compensation, y compensation, phi, phi compensation)
   float4* mv;     // (v0x, v0y, v0phi, predicted phi)
-  float2* mm;     // displacement since the last rebuild
+  float4* mm;     // (x, y displacement since the last rebuild, angle at it, unused)
   float4* pa;     // (R, A, particle index as int bits, 1/I)
   float* rcf;     // isolated-rotation coefficient RC
   float* rf;      // R in FP32: the only per-neighbour constant the force pass gathers

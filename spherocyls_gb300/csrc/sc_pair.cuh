@@ -215,6 +215,29 @@ __device__ __forceinline__ bool may_touch_fp32(float dX, float dY, float nxA, fl
   return dDx * dDx + dDy * dDy < lim * lim;
 }
 
+// Spines P + s u_A and Q + t u_B (P - Q = D, lab frame) closer than lim: the
+// closest points in FP32 with the cross-product form of the parameter (an error in
+// it only moves the evaluated pair along the spines, raising the distance by the
+// misalignment angle times the spine length, far below the caller's margin).
+__device__ __forceinline__ bool capsules_within(float dX, float dY, float nxA, float nyA,
+                                                float nxB, float nyB, float lim) {
+  const float a = fmaf(nxA, nxA, nyA * nyA), c = fmaf(nxB, nxB, nyB * nyB);
+  const float b = -(nxA * nxB + nyA * nyB);
+  const float d = nxA * dX + nyA * dY;
+  const float e = -(nxB * dX + nyB * dY);
+  const float w = nyA * nxB;
+  const float uxv = fmaf(nxA, nyB, -w) + fmaf(-nyA, nxB, w);
+  const float w2 = nyA * dX;
+  const float uxD = fmaf(nxA, dY, -w2) + fmaf(-nyA, dX, w2);
+  float t = uxv == 0.f ? -1.f : fminf(fmaxf(__fdividef(uxD, uxv), -1.f), 1.f);
+  float s = a > 0.f ? -__fdividef(b * t + d, a) : 0.f;
+  const float sarg = fabsf(s);
+  s = fminf(fmaxf(s, -1.f), 1.f);
+  if (sarg > 1.f && c > 0.f) t = fminf(fmaxf(-__fdividef(b * s + e, c), -1.f), 1.f);
+  const float x = dX + s * nxA - t * nxB, y = dY + s * nyA - t * nyB;
+  return x * x + y * y < lim * lim;
+}
+
 // ---- two-point contacts (src/cuda/2point_dynamics.cu:385-546, euler_est_2p) ----
 //
 // For nearly parallel overlapping spines the single closest-point pair jumps from

@@ -8,14 +8,15 @@
 // FP64 instruction runs in the force passes except the stress/energy sums on the
 // steps that record them.
 //
-// Neighbour list: every pair whose centres, in the Lees-Edwards frame of the
-// build, are closer than R_i+A_i+R_j+A_j+pad (the reach of a contact plus the
-// padding; FP32, bound inflated by 2e-5 relative).  It is rebuilt when a particle's
-// displacement since the build, plus this step's displacement as an allowance for
-// the next predictor excursion, exceeds half of what is left of the padding once
-// the shear accumulated since the build, |gamma - gamma_build| (S_max + pad), is
-// taken off.  Then no pair outside the list can come into contact, so the set of
-// interacting pairs is exactly the reference's (whose own padded list is larger).
+// Neighbour list: every pair whose spines, in the Lees-Edwards frame of the build,
+// are closer than R_i + R_j + pad (the capsule distance; FP32, bound inflated by
+// 2e-5 relative plus 1e-5).  It is rebuilt when a particle's spine has moved since
+// the build (centre displacement plus A times the rotation), plus this step's move
+// as an allowance for the next predictor excursion, by half of what is left of the
+// padding once the shear accumulated since the build, |gamma - gamma_build|
+// (S_max + pad), is taken off.  Then no pair outside the list can come into
+// contact, so the set of interacting pairs is exactly the reference's (whose own
+// padded list is larger).
 // Each entry packs the neighbour's slot with the cell offset (dc, dr) between the
 // two cells, so the displacement is rec_i - rec_j - (dc W, dr H) with no box
 // length in the FP32 arithmetic.
@@ -211,7 +212,7 @@ __global__ void __launch_bounds__(128, TWO ? 6 : 10) k_pass_mixed(Dev d,
       ddy = 0.5f * dt * (v0.y + fy);
       ddp = 0.5f * dt * (v0.z + tq * invI);
     }
-    float2 m = d.mm[i];
+    float4 m = d.mm[i];
     if (MODE == PASS_CORR_RESIZE) {
       const float f = ts.f_factor;
       const int cp = d.cellp[i];
@@ -241,7 +242,10 @@ __global__ void __launch_bounds__(128, TWO ? 6 : 10) k_pass_mixed(Dev d,
     // padding left after the shear since the list was built (next corrector's gamma)
     float dg = fabsf(ts.f_gamma_p - d.gbuild[s]) + 2.f * fabsf(ts.f_rate * dt);
     float h = 0.5f * (g.fpad - dg * (g.smax + g.fpad));
-    float reach = sqrtf(m.x * m.x + m.y * m.y) + sqrtf(ddx * ddx + ddy * ddy);
+    // a spine end moves by at most the centre's displacement plus A times the
+    // rotation; the next step's move is allowed for as well
+    float reach = sqrtf(m.x * m.x + m.y * m.y) + A * fabsf((c.z + c.w) - m.z) +
+                  sqrtf(ddx * ddx + ddy * ddy) + A * fabsf(ddp);
     if (!(reach < h)) {
       if (d.flags[s] == 0) atomicOr(&d.flags[s], 1);
       if (*d.any == 0) atomicExch(d.any, 1);
@@ -298,7 +302,7 @@ __global__ void k_mx_local(Dev d, const StepScalars* __restrict__ tab, int row, 
     sincosf(pf, &sn, &cs);
     d.rec[i] = make_float4(xl, yl, A * cs, A * sn);
     d.mc[i] = make_float4((float)(lx - xl), (float)(ly - yl), pf, (float)(phi - pf));
-    d.mm[i] = make_float2(0.f, 0.f);
+    d.mm[i] = make_float4(0.f, 0.f, pf + (float)(phi - pf), 0.f);
     d.pa[i] = make_float4((float)ra.x, A, __int_as_float(d.id[i]), (float)(1.0 / irc.x));
     d.rcf[i] = (float)irc.y;
     d.rf[i] = (float)ra.x;
@@ -340,7 +344,9 @@ __global__ void __launch_bounds__(128) k_mx_build_list(Dev d, const StepScalars*
           if (smally) dy += Lyf * (float)((dy < -0.5f * Lyf) - (dy > 0.5f * Lyf));
           float lim = (pai.x + pai.y + paj.x + paj.y + pad) * 1.00002f + 1e-6f;
           float dxl = fmaf(gam, dy, dx);
-          if (dxl * dxl + dy * dy < lim * lim) {
+          if (dxl * dxl + dy * dy < lim * lim &&
+              capsules_within(dxl, dy, ri.z, ri.w, rj.z, rj.w,
+                              (pai.x + paj.x + pad) * 1.00002f + 1e-5f)) {
             if (cnt < d.maxn) d.nbr[(size_t)cnt * d.ntot + i] = (int)((unsigned)j | code);
             cnt++;
           }
