@@ -61,8 +61,8 @@ def bytes_per_pass(precision: str, nbar: float) -> float:
 
 # DRAM bytes (read + write) per particle of one mixed force pass, the mean of the
 # predictor and corrector launches in one ncu capture of the default workload
-# (profiles/k_pass_mixed_n1048576.md: 115.9 and 161.6 MB per launch at N = 2^20).
-PASS_DRAM_BYTES_PER_PARTICLE = {"shear_n1048576_phi084": 138.75e6 / (1 << 20)}
+# (profiles/k_pass_mixed_n1048576.md: 107.7 and 166.6 MB per launch at N = 2^20).
+PASS_DRAM_BYTES_PER_PARTICLE = {"shear_n1048576_phi084": 137.15e6 / (1 << 20)}
 
 
 def _peaks():
@@ -391,7 +391,7 @@ def main():
         # block size (it times copies; the copies' steps are not timed here)
         t = new_box("mixed")
         t.strain_steps(args.warmup)
-        f, blk = t.autotune(30)
+        f, blk = t.autotune(100)  # long enough to include rebuilds
         t.close()
         tuned = {"pad": args.pad * f, "block": blk}
 
