@@ -121,6 +121,15 @@ int sc_strain_steps(sc_handle *h, int nsteps, int se_every, double *se_out);
 /* nsteps Heun steps with affine resize by (1-rate)^dt per step (shrink != 0) or its
  * inverse (resize_step + calc_forces, src/cpp/resize_dynamics.cpp:164-243, :297-307). */
 int sc_resize_steps(sc_handle *h, int nsteps, int shrink, int se_every, double *se_out);
+/* nsteps pure-shear steps at each system's strain rate e (pure_strain_step_2p,
+ * src/cuda/2point_dynamics.cu:1664-2283): the predictor adds the flow (+e x/2,
+ * -e y/2) and the isolated rotation -e RC sin(2 phi)/2 to the contact motion, the
+ * corrector adds dt/2 times the change of the contact forces evaluated in the
+ * predicted box Lx(1 + dt e/2) x Ly(1 - dt e/2); then Lx += dt e Lx/2,
+ * Ly -= dt e Ly/2, gamma_total += dt e (gamma is unchanged).  Unit drag and the
+ * torque over I, as in the other steps; the contact model is the handle's.
+ * Records as sc_strain_steps.  Replaces Spherocyl_Box::pure_strain_step_2p. */
+int sc_pure_strain_steps(sc_handle *h, int nsteps, int se_every, double *se_out);
 /* Fixed-step gradient descent (gradient_descent_minimize's loop,
  * src/cpp/relaxation_dynamics.cpp:11-85): calc_se, stop when every system's
  * E <= e_min, else x += dt F.  *steps_taken receives the iterations done. */
@@ -219,6 +228,13 @@ void sc_default_gen_options(sc_gen_options *opt); /* random, u in [0,1], min_sep
 int sc_generate_config(const sc_gen_options *opt, int n, double packing, double a_over_r,
                        double r_small, double r_ratio, uint64_t seed, double *x, double *y,
                        double *phi, double *R, double *A, double *L);
+/* The same in a rectangle of aspect box_aspect = Lx/Ly and area L^2 (the
+ * pure-shear driver starts at Lx/Ly = 1/stop_aspect, src/cuda/main_pure_shear.cpp:
+ * 168-170); box_aspect = 1 gives sc_generate_config's packing. */
+int sc_generate_config_rect(const sc_gen_options *opt, int n, double packing, double a_over_r,
+                            double r_small, double r_ratio, double box_aspect, uint64_t seed,
+                            double *x, double *y, double *phi, double *R, double *A, double *Lx,
+                            double *Ly);
 
 /* ---- files and run protocols with output (single-system handles) ---- */
 
@@ -248,6 +264,14 @@ int sc_run_strain(sc_handle *h, const char *out_dir, double run_gamma, double po
  * sp_resize_se.dat with the packing fraction as second column). */
 int sc_run_resize(sc_handle *h, const char *out_dir, double final_packing, double pos_save,
                   double se_save, unsigned long t_start, int format, unsigned long *t_end);
+/* run_pure_strain_2p with output, src/cuda/2point_dynamics.cu:2286-2391: pure
+ * shear until Lx/Ly >= stop_aspect, in time units of 1/dt steps; SE lines (format
+ * and file as sc_run_strain) for the states after every multiple of se_save/(e dt)
+ * steps and at each position save; position files every pos_save/e time units and
+ * of the final state.  t_start > 0 continues as sc_run_strain.  A negative rate is
+ * used as its magnitude.  *t_end receives the final time. */
+int sc_run_pure_strain(sc_handle *h, const char *out_dir, double stop_aspect, double pos_save,
+                       double se_save, unsigned long t_start, int format, unsigned long *t_end);
 /* gradient_descent_minimize with output, src/cpp/relaxation_dynamics.cpp:33-85 (SE
  * file sr_strain_se.dat, position files sr%010lu.dat every pos_save_n steps). */
 int sc_run_minimize(sc_handle *h, const char *out_dir, int max_steps, double e_min,

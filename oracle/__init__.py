@@ -89,6 +89,11 @@ class _Lib:
                                    [handle, ctypes.c_int, ctypes.c_int, _dp])
         self.run_gd_steps = fn("run_gd_steps", ctypes.c_int,
                                [handle, ctypes.c_int, ctypes.c_double, _dp])
+        if prefix == "orc_":
+            self.create_rect = fn("create_rect", handle,
+                                  [ctypes.c_int, ctypes.c_double, ctypes.c_double, _dp, _dp, _dp,
+                                   _dp, _dp, ctypes.c_double])
+            self.run_pure_steps = fn("run_pure_steps", ctypes.c_int, [handle, ctypes.c_int, _dp])
         self.n = fn("n", ctypes.c_int, [handle])
         self.get_state = fn("get_state", None, [handle, _dp, _dp, _dp])
         self.get_forces = fn("get_forces", None, [handle, _dp, _dp, _dp])
@@ -129,14 +134,20 @@ class _BoxBase:
     kind = "orc"
 
     def __init__(self, L, x, y, phi, A, R, pad=0.0, *, strain_rate=0.0, resize_rate=0.0,
-                 step=0.05, gamma=0.0, total_gamma=0.0, two_point=False):
+                 step=0.05, gamma=0.0, total_gamma=0.0, two_point=False, Ly=None):
         if two_point and self.kind != "orc":
             raise ValueError("the two-point contact rule exists only in the restatement")
+        if Ly is not None and self.kind != "orc":
+            raise ValueError("the reference's src/cpp box is square")
         self._L = _lib(self.kind)
         x, y, phi, A, R = (_f64(v) for v in (x, y, phi, A, R))
         self.n = int(x.shape[0])
-        self.h = self._L.create(self.n, float(L), _ptr(x), _ptr(y), _ptr(phi), _ptr(A), _ptr(R),
-                                float(pad))
+        if Ly is None:
+            self.h = self._L.create(self.n, float(L), _ptr(x), _ptr(y), _ptr(phi), _ptr(A),
+                                    _ptr(R), float(pad))
+        else:
+            self.h = self._L.create_rect(self.n, float(L), float(Ly), _ptr(x), _ptr(y), _ptr(phi),
+                                         _ptr(A), _ptr(R), float(pad))
         if not self.h:
             raise RuntimeError("oracle box creation failed")
         self.set_params(strain_rate=strain_rate, resize_rate=resize_rate, step=step, gamma=gamma,
@@ -202,6 +213,13 @@ class _BoxBase:
                                       _ptr(out) if out is not None else None)
         if rc != 0:
             raise RuntimeError("oracle resize run failed")
+        return out
+
+    def run_pure_steps(self, nsteps: int, record_se: bool = False):
+        out = np.zeros((nsteps, 5)) if record_se else None
+        rc = self._L.run_pure_steps(self.h, int(nsteps), _ptr(out) if out is not None else None)
+        if rc != 0:
+            raise RuntimeError("oracle pure-shear run failed")
         return out
 
     def run_gd_steps(self, nsteps: int, emin: float = 0.0):

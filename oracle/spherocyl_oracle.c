@@ -581,6 +581,85 @@ int orc_resize_step(orc_box *b, int shrink) {
   return b->err ? -1 : 0;
 }
 
+/* pure_strain_step_2p, src/cuda/2point_dynamics.cu:2180-2283: predictor
+ * pure_euler_est_2p :1872-1891 (the flow +x/2, -y/2 and the isolated rotation
+ * -RC sin(2 phi)/2 at the strain rate, with the contact motion, by an Euler step),
+ * corrector pure_heun_corr_2p :2140-2173 (forces at the predicted state in the
+ * predicted box Lx(1 + dt rate/2) x Ly(1 - dt rate/2), gamma unchanged; the state
+ * becomes the prediction plus dt/2 times the change of the contact motion), then
+ * the box update :2255-2256, the total strain :2278, the grid check
+ * (reconfigure_cells(0.0), src/cuda/spherocyl_box.cpp:46-67) and the rebuild.
+ * Drag and rotation follow the src/cpp path: unit drag and the torque over I
+ * (the src/cuda code divides by Kd times the area); the rebuild rule is the src/cpp
+ * per-axis one, applied after the step as the src/cuda code does. */
+int orc_pure_step(orc_box *b) {
+  int n = b->n;
+  double *f0 = (double *)malloc(3 * (size_t)n * sizeof(double));
+  if (!f0) return -1;
+  double *fx0 = f0, *fy0 = f0 + n, *tau0 = f0 + 2 * (size_t)n;
+  const double e = b->strain_rate, dt = b->step;
+  for (int i = 0; i < n; i++) {
+    fx0[i] = b->fx[i];
+    fy0[i] = b->fy[i];
+    tau0[i] = b->tau[i];
+    b->tx[i] = b->x[i] + dt * (b->fx[i] + 0.5 * e * b->x[i]);
+    b->ty[i] = b->y[i] + dt * (b->fy[i] - 0.5 * e * b->y[i]);
+    b->tphi[i] = b->phi[i] + dt * (b->tau[i] / b->I[i] + e * (-0.5 * b->RC[i] * sin(2 * b->phi[i])));
+  }
+  {
+    pview v = {b->tx, b->ty, b->tphi, b->tfx, b->tfy, b->ttau};
+    zero3(b->tfx, b->tfy, b->ttau, b->n);
+    loop_pairs(b, &v, b->gamma, b->Lx * (1 + 0.5 * dt * e), b->Ly * (1 - 0.5 * dt * e), 0);
+  }
+  int rebuild = 0;
+  for (int i = 0; i < n; i++) {
+    double ddx = 0.5 * dt * (b->tfx[i] - fx0[i]);
+    double ddy = 0.5 * dt * (b->tfy[i] - fy0[i]);
+    double ddp = 0.5 * dt * (b->ttau[i] / b->I[i] - tau0[i] / b->I[i]);
+    double x0 = b->x[i], y0 = b->y[i];
+    b->x[i] = b->tx[i] + ddx;
+    b->y[i] = b->ty[i] + ddy;
+    b->phi[i] = b->tphi[i] + ddp;
+    b->xm[i] += b->x[i] - x0;
+    b->ym[i] += b->y[i] - y0;
+    if (moved_too_far(b, i)) rebuild = 1;
+  }
+  free(f0);
+  b->Lx += 0.5 * dt * e * b->Lx;
+  b->Ly -= 0.5 * dt * e * b->Ly;
+  b->gamma_total += dt * e;
+  {
+    double wmin = 2.24 * (b->Rmax + b->Amax) + b->pad;
+    double hmin = 2 * (b->Rmax + b->Amax) + b->pad;
+    int rows = (int)(b->Ly / hmin), cols = (int)(b->Lx / wmin);
+    if (rows < 1) rows = 1;
+    if (cols < 1) cols = 1;
+    if (rows != b->rows || cols != b->cols) {
+      if (configure_cells(b)) b->err = 1;
+      rebuild = 1;
+    } else {
+      b->W = b->Lx / b->cols;
+      b->H = b->Ly / b->rows;
+    }
+  }
+  if (rebuild) find_neighbors(b);
+  return b->err ? -1 : 0;
+}
+
+/* pure-shear steps, each followed by calc_forces (or calc_se when se_out) */
+int orc_run_pure_steps(orc_box *b, int nsteps, double *se_out) {
+  for (int k = 0; k < nsteps; k++) {
+    if (orc_pure_step(b)) return -1;
+    if (se_out) {
+      orc_calc_se(b);
+      orc_get_se(b, se_out + 5 * (size_t)k);
+    } else {
+      orc_calc_forces(b);
+    }
+  }
+  return 0;
+}
+
 /* gradient_relax_step, relaxation_dynamics.cpp:11-31 */
 int orc_gd_step(orc_box *b) {
   for (int i = 0; i < b->n; i++) {
@@ -600,12 +679,19 @@ int orc_gd_step(orc_box *b) {
  * spherocyl_box.cpp:152-173 ---- */
 orc_box *orc_create(int n, double L, const double *x, const double *y, const double *phi,
                     const double *A, const double *R, double pad) {
-  if (n <= 0 || !(L > 0)) return NULL;
+  return orc_create_rect(n, L, L, x, y, phi, A, R, pad);
+}
+
+/* The src/cuda box takes Lx and Ly (src/cuda/spherocyl_box.cpp:529-560); the
+ * src/cpp routines used here already keep the two lengths apart. */
+orc_box *orc_create_rect(int n, double Lx, double Ly, const double *x, const double *y,
+                         const double *phi, const double *A, const double *R, double pad) {
+  if (n <= 0 || !(Lx > 0) || !(Ly > 0)) return NULL;
   orc_box *b = (orc_box *)calloc(1, sizeof(orc_box));
   if (!b) return NULL;
   b->n = n;
-  b->Lx = L;
-  b->Ly = L;
+  b->Lx = Lx;
+  b->Ly = Ly;
   b->step = 0.05; /* set_defaults, spherocyl_box.cpp:16-53 */
   size_t nd = (size_t)n;
   double **arrs[] = {&b->x,  &b->y,   &b->phi, &b->R,  &b->A,  &b->I,   &b->RC, &b->fx, &b->fy,

@@ -16,6 +16,8 @@ typedef struct orc_box orc_box;
 
 orc_box *orc_create(int n, double L, const double *x, const double *y, const double *phi,
                     const double *A, const double *R, double pad);
+orc_box *orc_create_rect(int n, double Lx, double Ly, const double *x, const double *y,
+                         const double *phi, const double *A, const double *R, double pad);
 void orc_destroy(orc_box *b);
 
 void orc_set_strain_rate(orc_box *b, double v);
@@ -32,10 +34,12 @@ void orc_calc_se(orc_box *b);
 int orc_strain_step(orc_box *b);
 int orc_resize_step(orc_box *b, int shrink);
 int orc_gd_step(orc_box *b);
+int orc_pure_step(orc_box *b);
 
 int orc_run_strain_steps(orc_box *b, int nsteps, double *se_out);
 int orc_run_resize_steps(orc_box *b, int nsteps, int shrink, double *se_out);
 int orc_run_gd_steps(orc_box *b, int nsteps, double emin, double *e_out);
+int orc_run_pure_steps(orc_box *b, int nsteps, double *se_out);
 
 int orc_n(const orc_box *b);
 void orc_get_state(const orc_box *b, double *x, double *y, double *phi);

@@ -79,6 +79,7 @@ SIGNATURES = [
     ("sc_calc_se", ctypes.c_int, [_vp, _dp]),
     ("sc_strain_steps", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp]),
     ("sc_resize_steps", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp]),
+    ("sc_pure_strain_steps", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp]),
     ("sc_gd_minimize", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double, _ip, _dp]),
     ("sc_fire_minimize", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_int, ctypes.c_double,
                                         ctypes.c_double, _ip, _dp, _ip]),
@@ -108,6 +109,10 @@ SIGNATURES = [
     ("sc_generate_config", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                           ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
                                           _dp, _dp, _dp, _dp, _dp, _dp]),
+    ("sc_generate_config_rect", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double,
+                                               ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                               ctypes.c_double, ctypes.c_uint64, _dp, _dp, _dp,
+                                               _dp, _dp, _dp, _dp]),
     ("sc_read_positions", ctypes.c_int, [ctypes.c_char_p, _ip, _dp, _dp, _dp, _dp, _dp, _dp]),
     ("sc_save_positions", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_int]),
     ("sc_run_strain", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_double, ctypes.c_double,
@@ -116,6 +121,9 @@ SIGNATURES = [
     ("sc_run_resize", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_double, ctypes.c_double,
                                      ctypes.c_double, ctypes.c_ulong, ctypes.c_int,
                                      ctypes.POINTER(ctypes.c_ulong)]),
+    ("sc_run_pure_strain", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_double,
+                                          ctypes.c_double, ctypes.c_double, ctypes.c_ulong,
+                                          ctypes.c_int, ctypes.POINTER(ctypes.c_ulong)]),
     ("sc_run_minimize", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_double,
                                        ctypes.c_int, _ip]),
     ("sc_forces_noalloc", ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.c_double,

@@ -49,6 +49,23 @@ def generate_config(n: int, packing: float, a_over_r: float, *, layout: str = "r
     random, evenly spaced or aligned angles; Gamma-distributed a/R), seeded:
     returns (L, x, y, phi, R, A).  Zero energy: max_overlap=0.  Aligned:
     angle_range=(u, u)."""
+    return _generate(n, packing, a_over_r, layout, angles, angle_range, shear_angles, min_sep,
+                     max_overlap, a_sigma, r_small, r_ratio, seed, None)
+
+
+def generate_config_rect(n: int, packing: float, a_over_r: float, box_aspect: float, *,
+                         layout: str = "random", angles: str = "random", angle_range=(0.0, 1.0),
+                         shear_angles: bool = False, min_sep: float = 0.1,
+                         max_overlap: float = -1.0, a_sigma: float = 0.0, r_small: float = 0.5,
+                         r_ratio: float = 1.4, seed: int = 0):
+    """generate_config in a box of aspect Lx/Ly = box_aspect (the pure-shear start,
+    src/cuda/main_pure_shear.cpp:168-170): returns (Lx, Ly, x, y, phi, R, A)."""
+    return _generate(n, packing, a_over_r, layout, angles, angle_range, shear_angles, min_sep,
+                     max_overlap, a_sigma, r_small, r_ratio, seed, float(box_aspect))
+
+
+def _generate(n, packing, a_over_r, layout, angles, angle_range, shear_angles, min_sep,
+              max_overlap, a_sigma, r_small, r_ratio, seed, box_aspect):
     from ._lib import ScGenOptions
 
     o = ScGenOptions()
@@ -60,12 +77,23 @@ def generate_config(n: int, packing: float, a_over_r: float, *, layout: str = "r
     o.min_sep, o.max_overlap, o.a_sigma = float(min_sep), float(max_overlap), float(a_sigma)
     x, y, p, R, A = (np.empty(n) for _ in range(5))
     L = ctypes.c_double()
-    st = lib().sc_generate_config(ctypes.byref(o), int(n), float(packing), float(a_over_r),
-                                  float(r_small), float(r_ratio), ctypes.c_uint64(int(seed)),
-                                  _ptr(x), _ptr(y), _ptr(p), _ptr(R), _ptr(A), ctypes.byref(L))
+    Ly = ctypes.c_double()
+    if box_aspect is None:
+        st = lib().sc_generate_config(ctypes.byref(o), int(n), float(packing), float(a_over_r),
+                                      float(r_small), float(r_ratio), ctypes.c_uint64(int(seed)),
+                                      _ptr(x), _ptr(y), _ptr(p), _ptr(R), _ptr(A),
+                                      ctypes.byref(L))
+    else:
+        st = lib().sc_generate_config_rect(ctypes.byref(o), int(n), float(packing),
+                                           float(a_over_r), float(r_small), float(r_ratio),
+                                           box_aspect, ctypes.c_uint64(int(seed)), _ptr(x),
+                                           _ptr(y), _ptr(p), _ptr(R), _ptr(A), ctypes.byref(L),
+                                           ctypes.byref(Ly))
     if st != 0:
         raise _lib.ScError(st, "configuration generation failed")
-    return L.value, x, y, p, R, A
+    if box_aspect is None:
+        return L.value, x, y, p, R, A
+    return L.value, Ly.value, x, y, p, R, A
 
 
 FMT = {"sp": 0, "sd": 1, "bin": 2}
@@ -205,6 +233,16 @@ class BoxBatch:
                                         _ptr(out) if out is not None else None))
         return out
 
+    def pure_strain_steps(self, nsteps: int, se_every: int = 0):
+        """Pure shear at each system's strain rate (pure_strain_step_2p,
+        src/cuda/2point_dynamics.cu:2180-2283): x stretched, y compressed."""
+        out = None
+        if se_every > 0 and nsteps // se_every > 0:
+            out = np.empty((nsteps // se_every, self.nsys, 5))
+        self._chk(lib().sc_pure_strain_steps(self.h, int(nsteps), int(se_every),
+                                             _ptr(out) if out is not None else None))
+        return out
+
     def gd_minimize(self, max_steps: int, e_min: float = 0.0):
         steps = ctypes.c_int()
         ef = ctypes.c_double()
@@ -284,6 +322,14 @@ class BoxBatch:
         self._chk(lib().sc_run_resize(self.h, out_dir.encode(), float(final_packing),
                                       float(pos_save), float(se_save), int(t_start), FMT[fmt],
                                       ctypes.byref(t)))
+        return t.value
+
+    def run_pure_strain(self, out_dir: str, stop_aspect: float, pos_save: float, se_save: float,
+                        t_start: int = 0, fmt: str = "sd") -> int:
+        t = ctypes.c_ulong()
+        self._chk(lib().sc_run_pure_strain(self.h, out_dir.encode(), float(stop_aspect),
+                                           float(pos_save), float(se_save), int(t_start),
+                                           FMT[fmt], ctypes.byref(t)))
         return t.value
 
     def run_minimize(self, out_dir: str, max_steps: int, e_min: float = 0.0,

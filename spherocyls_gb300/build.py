@@ -35,6 +35,7 @@ CLI_UNITS = {
     "spherocyl_strain": "cli_strain.cpp",
     "spherocyl_resize": "cli_resize.cpp",
     "spherocyl_minimize": "cli_minimize.cpp",
+    "spherocyl_pure_shear": "cli_pure_shear.cpp",
 }
 
 

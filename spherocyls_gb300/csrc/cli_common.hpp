@@ -47,9 +47,10 @@ inline int precision() {
   const char* v = std::getenv("SC_PRECISION");
   return (v && std::string(v) == "mixed") ? SC_PREC_MIXED : SC_PREC_FP64;
 }
-inline int out_format() {
+inline int out_format(int dflt = SC_FMT_SP) {
   const char* v = std::getenv("SC_OUTPUT_FORMAT");
-  return (v && std::string(v) == "sd") ? SC_FMT_SD : SC_FMT_SP;
+  if (!v) return dflt;
+  return std::string(v) == "sd" ? SC_FMT_SD : (std::string(v) == "sp" ? SC_FMT_SP : dflt);
 }
 
 // time of a continued run: the last 14 characters of the file name are
@@ -65,8 +66,10 @@ inline unsigned long time_from_name(const std::string& f) {
 // distribution read explicitly), then the aspect-ratio spread
 // (src/cuda/main.cpp:119-149), mapped onto sc_generate_config.  Without the fields
 // the start is random with random angles.
+// box_aspect = Lx/Ly of the start box (L receives Lx, Ly the height).
 inline int random_start(Args& a, int n, double phi, double aspect, double bidisp, double* x,
-                        double* y, double* p, double* R, double* A, double* L) {
+                        double* y, double* p, double* R, double* A, double* L,
+                        double box_aspect = 1.0, double* Ly = nullptr) {
   sc_gen_options o;
   sc_default_gen_options(&o);
   if (a.more()) {
@@ -96,8 +99,11 @@ inline int random_start(Args& a, int n, double phi, double aspect, double bidisp
     o.max_overlap = overlap < 1.0 ? overlap : -1.0;
     o.a_sigma = a.f("Aspect ratio distribution width (relative deviation)");
   }
-  return sc_generate_config(&o, n, phi, aspect, 0.5, bidisp, env_int("SC_SEED", 0), x, y, p, R,
-                            A, L);
+  double ly = 0;
+  int rc = sc_generate_config_rect(&o, n, phi, aspect, 0.5, bidisp, box_aspect,
+                                   env_int("SC_SEED", 0), x, y, p, R, A, L, &ly);
+  if (Ly) *Ly = ly;
+  return rc;
 }
 
 inline int fail(const char* what, int rc, sc_handle* h = nullptr) {

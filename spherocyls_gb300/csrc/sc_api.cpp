@@ -467,12 +467,17 @@ int sc_calc_se(sc_handle* H, double* se_out) {
 
 int sc_strain_steps(sc_handle* H, int nsteps, int se_every, double* se_out) {
   if (!H) return SC_E_ARG;
-  return H->h.run_steps(false, 0, nsteps, se_every, se_out);
+  return H->h.run_steps(sc::KIND_STRAIN, 0, nsteps, se_every, se_out);
 }
 
 int sc_resize_steps(sc_handle* H, int nsteps, int shrink, int se_every, double* se_out) {
   if (!H) return SC_E_ARG;
-  return H->h.run_steps(true, shrink ? 1 : 0, nsteps, se_every, se_out);
+  return H->h.run_steps(sc::KIND_RESIZE, shrink ? 1 : 0, nsteps, se_every, se_out);
+}
+
+int sc_pure_strain_steps(sc_handle* H, int nsteps, int se_every, double* se_out) {
+  if (!H) return SC_E_ARG;
+  return H->h.run_steps(sc::KIND_PURE, 0, nsteps, se_every, se_out);
 }
 
 int sc_gd_minimize(sc_handle* H, int max_steps, double e_min, int* steps_taken, double* e_final) {

@@ -126,12 +126,14 @@ __global__ void k_rb_hash(Dev d, const StepScalars* __restrict__ tab, int row, i
   for_listed_slots(d, [&](int i, int s) {
     const SysGeom& g = d.geom[s];
     const StepScalars& ts = tab[row * d.nsys + s];
-    const double Lx = ts.Lx_c, Ly = ts.Ly_c;
+    // pure shear rebuilds after the box update (pure_strain_step_2p,
+    // src/cuda/2point_dynamics.cu:2255-2282), so it wraps with the new box
+    const double Lx = ts.mode == 3 ? ts.Lx_p : ts.Lx_c, Ly = ts.mode == 3 ? ts.Ly_p : ts.Ly_c;
     double2 p = d.xy[i];
     double phi = d.ph[i];
     double2 mv = make_double2(0.0, 0.0);
     const int istar = d.istar[s];
-    if (!mixed && istar != kNoTrigger && !ts.setback && d.id[i] > istar) {
+    if (!mixed && istar != kNoTrigger && !ts.setback && ts.mode != 3 && d.id[i] > istar) {
       double2 p0 = d.s_xy[i];
       p0.x = wrap_bounded(p0.x, 0.0, Lx, Lx, d.status);
       p0.y = wrap_bounded(p0.y, 0.0, Ly, Ly, d.status);

@@ -120,10 +120,13 @@ extern "C" void sc_default_gen_options(sc_gen_options* o) {
   o->a_sigma = 0.0;
 }
 
-extern "C" int sc_generate_config(const sc_gen_options* opt, int n, double packing,
-                                  double a_over_r, double r_small, double r_ratio, uint64_t seed,
-                                  double* x, double* y, double* phi, double* R, double* A,
-                                  double* L_out) {
+// box_aspect = Lx/Ly; the area Lx*Ly is the square box's L^2
+// (the pure-shear driver's start box, src/cuda/main_pure_shear.cpp:168-170)
+extern "C" int sc_generate_config_rect(const sc_gen_options* opt, int n, double packing,
+                                       double a_over_r, double r_small, double r_ratio,
+                                       double box_aspect, uint64_t seed, double* x, double* y,
+                                       double* phi, double* R, double* A, double* Lx_out,
+                                       double* Ly_out) {
   sc_gen_options o;
   if (opt)
     o = *opt;
@@ -134,7 +137,8 @@ extern "C" int sc_generate_config(const sc_gen_options* opt, int n, double packi
       !(o.angle_min >= 0 && o.angle_max <= 1 && o.angle_min <= o.angle_max) ||
       (o.layout != SC_LAYOUT_RANDOM && o.layout != SC_LAYOUT_GRID) ||
       (o.angle_mode != SC_ANGLE_RANDOM && o.angle_mode != SC_ANGLE_EVEN) || !(o.max_overlap < 1) ||
-      !x || !y || !phi || !R || !A || !L_out)
+      !(box_aspect > 0 && box_aspect < 1e6 && 1.0 / box_aspect < 1e6) || !x || !y || !phi ||
+      !R || !A || !Lx_out || !Ly_out)
     return SC_E_ARG;
   const double pi = 3.14159265358979323846;
   SplitMix64 rng{seed * 0x2545F4914F6CDD1Dull + 0x9876543ull};
@@ -152,7 +156,9 @@ extern "C" int sc_generate_config(const sc_gen_options* opt, int n, double packi
     amax = std::fmax(amax, A[i]);
   }
   const double L = std::sqrt(filled / packing);
-  *L_out = L;
+  const double Lx = L * std::sqrt(box_aspect), Ly = L / std::sqrt(box_aspect);
+  *Lx_out = Lx;
+  *Ly_out = Ly;
   // rotation coefficient of the largest shape (place_spherocyls' dC)
   const double al = rmax > 0 ? amax / rmax : 0.0;
   const double C = al * (8 + 6 * pi * al + 8 * al * al) /
@@ -162,23 +168,24 @@ extern "C" int sc_generate_config(const sc_gen_options* opt, int n, double packi
   const double sep = o.max_overlap >= 0 ? std::fmax(o.min_sep, std::sqrt(1.0 - o.max_overlap))
                                         : o.min_sep;
   const double reach = 2.0 * amax + 2.0 * sep * rmax;
-  int ng = (int)(L / std::fmax(reach, 1e-300));
-  if (ng > 2048) ng = 2048;
-  const bool gridded = ng >= 3;
-  if (!gridded) ng = 1;
-  const double gw = L / ng;
-  std::vector<std::vector<int>> grid((size_t)ng * ng);
+  int ngx = (int)(Lx / std::fmax(reach, 1e-300)), ngy = (int)(Ly / std::fmax(reach, 1e-300));
+  if (ngx > 2048) ngx = 2048;
+  if (ngy > 2048) ngy = 2048;
+  const bool gridded = ngx >= 3 && ngy >= 3;
+  if (!gridded) ngx = ngy = 1;
+  const double gwx = Lx / ngx, gwy = Ly / ngy;
+  std::vector<std::vector<int>> grid((size_t)ngx * ngy);
   // grid layout (place_spherocyl_grid): cells of W x H, one particle each, rows
   // shifted by a random offset of up to +-(R + A)
   int ncols = 1, nrows = 1;
-  double W = L, H = L;
+  double W = Lx, H = Ly;
   std::vector<double> row_off;
   if (o.layout == SC_LAYOUT_GRID) {
     const double aspect = (amax + rmax) / rmax;
-    ncols = std::max(1, (int)std::sqrt(n / aspect));
+    ncols = std::max(1, (int)std::sqrt(n / aspect * box_aspect));
     nrows = (n + ncols - 1) / ncols;
-    W = L / ncols;
-    H = L / nrows;
+    W = Lx / ncols;
+    H = Ly / nrows;
     if (W < 2 * (amax + rmax) || H < 2 * rmax) return SC_E_ARG;  // does not fit
     row_off.assign(nrows, 0.0);
     for (int r = 1; r < nrows; r++) row_off[r] = (rmax + amax) * (1.0 - 2.0 * rng.uniform());
@@ -193,11 +200,11 @@ extern "C" int sc_generate_config(const sc_gen_options* opt, int n, double packi
         const int r = i / ncols, c = i % ncols;
         xi = c * W + (amax + rmax) + row_off[r] + (W - 2 * (amax + rmax)) * rng.uniform();
         yi = r * H + rmax + (H - 2 * rmax) * rng.uniform();
-        xi -= L * std::floor(xi / L);
-        yi -= L * std::floor(yi / L);
+        xi -= Lx * std::floor(xi / Lx);
+        yi -= Ly * std::floor(yi / Ly);
       } else {
-        xi = L * rng.uniform();
-        yi = L * rng.uniform();
+        xi = Lx * rng.uniform();
+        yi = Ly * rng.uniform();
       }
       double u;
       if (o.angle_mode == SC_ANGLE_EVEN)
@@ -206,17 +213,17 @@ extern "C" int sc_generate_config(const sc_gen_options* opt, int n, double packi
         u = o.angle_min + (o.angle_max - o.angle_min) * rng.uniform();
       const double pi_ = angle_of(u, C, o.shear_angles != 0);
       double ux = A[i] * std::cos(pi_), uy = A[i] * std::sin(pi_);
-      int gx = gridded ? std::min((int)(xi / gw), ng - 1) : 0;
-      int gy = gridded ? std::min((int)(yi / gw), ng - 1) : 0;
+      int gx = gridded ? std::min((int)(xi / gwx), ngx - 1) : 0;
+      int gy = gridded ? std::min((int)(yi / gwy), ngy - 1) : 0;
       bool ok = true;
       int span = gridded ? 1 : 0;
       for (int a = -span; a <= span && ok; a++)
         for (int b = -span; b <= span && ok; b++) {
-          int cx = (gx + b + ng) % ng, cy = (gy + a + ng) % ng;
-          for (int j : grid[(size_t)cy * ng + cx]) {
+          int cx = (gx + b + ngx) % ngx, cy = (gy + a + ngy) % ngy;
+          for (int j : grid[(size_t)cy * ngx + cx]) {
             double dx = xi - x[j], dy = yi - y[j];
-            dx -= L * std::round(dx / L);
-            dy -= L * std::round(dy / L);
+            dx -= Lx * std::round(dx / Lx);
+            dy -= Ly * std::round(dy / Ly);
             double vx = A[j] * std::cos(phi[j]), vy = A[j] * std::sin(phi[j]);
             double dd = seg_seg(dx, dy, ux, uy, 0.0, 0.0, vx, vy);
             if (dd < sep * (R[i] + R[j])) {
@@ -229,11 +236,20 @@ extern "C" int sc_generate_config(const sc_gen_options* opt, int n, double packi
       x[i] = xi;
       y[i] = yi;
       phi[i] = pi_;
-      grid[(size_t)gy * ng + gx].push_back(i);
+      grid[(size_t)gy * ngx + gx].push_back(i);
       break;
     }
   }
   return SC_OK;
+}
+
+extern "C" int sc_generate_config(const sc_gen_options* opt, int n, double packing,
+                                  double a_over_r, double r_small, double r_ratio, uint64_t seed,
+                                  double* x, double* y, double* phi, double* R, double* A,
+                                  double* L_out) {
+  double Ly = 0;
+  return sc_generate_config_rect(opt, n, packing, a_over_r, r_small, r_ratio, 1.0, seed, x, y,
+                                 phi, R, A, L_out, &Ly);
 }
 
 extern "C" int sc_generate_packing(int n, double packing, double a_over_r, double r_small,

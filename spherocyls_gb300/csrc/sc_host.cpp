@@ -82,6 +82,17 @@ bool HostSys::grid_changes(double Lx_now, double Ly_now) const {
   return r != rows || c != cols;
 }
 
+// The same test with rows from Ly and columns from Lx (configure_cells' own
+// orientation), for boxes whose two sides change differently
+// (reconfigure_cells(0.0) in pure_strain_step_2p, src/cuda/spherocyl_box.cpp:46-67).
+bool HostSys::grid_changes_xy(double Lx_now, double Ly_now) const {
+  double wmin = 2.24 * (Rmax + Amax) + pad;
+  double hmin = 2 * (Rmax + Amax) + pad;
+  int r = std::max(static_cast<int>(Ly_now / hmin), 1);
+  int c = std::max(static_cast<int>(Lx_now / wmin), 1);
+  return r != rows || c != cols;
+}
+
 // FP32 copies of a row, for the mixed form
 static void fill_f32(StepScalars& t) {
   t.f_gamma_c = (float)t.gamma_c;
@@ -92,7 +103,14 @@ static void fill_f32(StepScalars& t) {
   t.f_Hp = (float)t.H_p;
   t.f_rate = (float)t.rate;
   t.f_step = (float)t.step;
-  t.f_factor = t.mode == 1 ? (float)t.scale : (t.mode == 2 ? (float)(1.0 / t.scale) : 1.0f);
+  if (t.mode == 1 || t.mode == 2) {
+    t.f_gx = t.f_gy = (float)(t.mode == 1 ? t.scale - 1.0 : 1.0 / t.scale - 1.0);
+  } else if (t.mode == 3) {
+    t.f_gx = (float)(0.5 * t.step * t.rate);
+    t.f_gy = (float)(-0.5 * t.step * t.rate);
+  } else {
+    t.f_gx = t.f_gy = 0.0f;
+  }
 }
 
 StepScalars Handle::row_current(int s) const {
@@ -512,8 +530,9 @@ void Handle::enqueue_se_record(int rec) {
 
 // Advance one system's host mirror by one step and fill its table row
 // (strain_step, strain_dynamics.cpp:231-234 with set_back_gamma,
-// spherocyl_box.cpp:542-543; resize_step, resize_dynamics.cpp:230-238).
-static void advance(HostSys& h, bool resize, int shrink, StepScalars& t) {
+// spherocyl_box.cpp:542-543; resize_step, resize_dynamics.cpp:230-238;
+// pure_strain_step_2p, src/cuda/2point_dynamics.cu:2233-2278).
+static void advance(HostSys& h, int kind, int shrink, StepScalars& t) {
   std::memset(&t, 0, sizeof t);
   t.rate = h.strain_rate;
   t.step = h.step;
@@ -523,7 +542,19 @@ static void advance(HostSys& h, bool resize, int shrink, StepScalars& t) {
   t.W_c = h.Lx / h.cols;
   t.H_c = h.Ly / h.rows;
   t.scale = 1.0;
-  if (resize) {
+  if (kind == KIND_PURE) {
+    // the corrector pass sees the predicted box; gamma stays, the box follows the
+    // flow after the step
+    t.mode = 3;
+    t.gamma_c = h.gamma;
+    t.Lx_c = h.Lx * (1 + 0.5 * h.step * h.strain_rate);
+    t.Ly_c = h.Ly * (1 - 0.5 * h.step * h.strain_rate);
+    t.W_c = t.Lx_c / h.cols;
+    t.H_c = t.Ly_c / h.rows;
+    h.Lx += 0.5 * h.step * h.strain_rate * h.Lx;
+    h.Ly -= 0.5 * h.step * h.strain_rate * h.Ly;
+    h.gamma_total += h.step * h.strain_rate;
+  } else if (kind == KIND_RESIZE) {
     t.scale = std::pow(1.0 - h.resize_rate, h.step);
     t.mode = shrink ? 1 : 2;
     if (shrink) {
@@ -552,16 +583,26 @@ static void advance(HostSys& h, bool resize, int shrink, StepScalars& t) {
   t.H_p = h.Ly / h.rows;
 }
 
-int Handle::run_steps(bool resize, int shrink, int nsteps, int se_every, double* se_out) {
+int Handle::run_steps(int kind, int shrink, int nsteps, int se_every, double* se_out) {
   if (nsteps < 0 || se_every < 0) {
     fail(SC_E_ARG, "nsteps and se_every must be >= 0");
     return SC_E_ARG;
   }
   if (nsteps == 0) return SC_OK;
-  if (resize) {
+  // resize and pure shear share the affine pass modes (the row's mode tells them
+  // apart); only simple shear sets gamma back
+  const bool resize = kind != KIND_STRAIN;
+  if (kind == KIND_RESIZE) {
     for (int s = 0; s < nsys; s++)
       if (!(hs[s].resize_rate > 0 && hs[s].resize_rate < 1)) {
         fail(SC_E_ARG, "resize rate of system %d must be in (0, 1)", s);
+        return SC_E_ARG;
+      }
+  }
+  if (kind == KIND_PURE) {
+    for (int s = 0; s < nsys; s++)
+      if (!(hs[s].strain_rate != 0) || !(std::fabs(hs[s].strain_rate * hs[s].step) < 1)) {
+        fail(SC_E_ARG, "pure shear of system %d needs 0 < |strain rate| < 1/dt", s);
         return SC_E_ARG;
       }
   }
@@ -572,7 +613,8 @@ int Handle::run_steps(bool resize, int shrink, int nsteps, int se_every, double*
   while (done < nsteps) {
     // chunk length: at most kChunk steps, a multiple of the recording period when
     // possible, and ending before any system's cell grid would change
-    // (reconfigure_cells, resize_dynamics.cpp:106-121)
+    // (reconfigure_cells, resize_dynamics.cpp:106-121; for pure shear
+    // src/cuda/spherocyl_box.cpp:46-67)
     int want = std::min(nsteps - done, kChunk);
     if (se_every > 0 && want >= se_every) want = (want / se_every) * se_every;
     int nk = want;
@@ -583,13 +625,15 @@ int Handle::run_steps(bool resize, int shrink, int nsteps, int se_every, double*
       for (int k = 0; k < want; k++) {
         bool change = false;
         for (int s = 0; s < nsys; s++)
-          if (sim[s].grid_changes(sim[s].Lx, sim[s].Ly)) change = true;
+          if (kind == KIND_PURE ? sim[s].grid_changes_xy(sim[s].Lx, sim[s].Ly)
+                                : sim[s].grid_changes(sim[s].Lx, sim[s].Ly))
+            change = true;
         if (change) {
           nk = k;
           regrid = true;
           break;
         }
-        for (int s = 0; s < nsys; s++) advance(sim[s], resize, shrink, tmp);
+        for (int s = 0; s < nsys; s++) advance(sim[s], kind, shrink, tmp);
       }
     }
     if (nk == 0) {
@@ -606,13 +650,15 @@ int Handle::run_steps(bool resize, int shrink, int nsteps, int se_every, double*
     for (int s = 0; s < nsys; s++) {
       // row 0 primes the predictor of the first step, which scales like any step
       rows[s] = row_current(s);
-      if (resize) {
+      if (kind == KIND_RESIZE) {
         rows[s].scale = std::pow(1.0 - hs[s].resize_rate, hs[s].step);
         rows[s].mode = shrink ? 1 : 2;
+      } else if (kind == KIND_PURE) {
+        rows[s].mode = 3;
       }
     }
     for (int k = 1; k <= nk; k++)
-      for (int s = 0; s < nsys; s++) advance(sim[s], resize, shrink, rows[(size_t)k * nsys + s]);
+      for (int s = 0; s < nsys; s++) advance(sim[s], kind, shrink, rows[(size_t)k * nsys + s]);
     if (!upload_table(rows)) return last_status;
     // records of this chunk: steps done+k with (done+k) % se_every == 0
     int first_rec = rec_done;
@@ -620,11 +666,11 @@ int Handle::run_steps(bool resize, int shrink, int nsteps, int se_every, double*
     for (int k = 1; k <= nk; k++)
       if (se_every > 0 && (done + k) % se_every == 0) nrec++;
     if (nrec > 0 && !ensure_se_hist(nrec)) return last_status;
-    const int kind = resize ? (shrink ? 2 : 3) : 1;
-    if (!pred_valid || pred_kind != kind) {
+    const int pkind = kind == KIND_PURE ? 4 : (resize ? (shrink ? 2 : 3) : 1);
+    if (!pred_valid || pred_kind != pkind) {
       launch_pass(resize ? PASS_PRED_RESIZE : PASS_PRED_STRAIN, false, 0);
       pred_valid = true;
-      pred_kind = kind;
+      pred_kind = pkind;
     }
     bool aligned = se_every == 0 || done % se_every == 0;
     bool use_graph = opt.use_graphs && !opt.profile && nk >= 16 && aligned;
@@ -648,7 +694,9 @@ int Handle::run_steps(bool resize, int shrink, int nsteps, int se_every, double*
     }
     collect_times();
     long long rb0 = dev_rebuilds;
-    if (!check_status(resize ? "resize steps" : "strain steps")) return last_status;
+    if (!check_status(kind == KIND_PURE ? "pure shear steps"
+                                        : (resize ? "resize steps" : "strain steps")))
+      return last_status;
     if (use_graph && graph_conditional) kernels += (dev_rebuilds - rb0) * body_kernels;
     fp64_valid = prec != PREC_MIXED;
     forces_valid = false;

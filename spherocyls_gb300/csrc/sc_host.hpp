@@ -28,7 +28,11 @@ struct HostSys {
 
   void configure(bool set_pad);
   bool grid_changes(double Lx_now, double Ly_now) const;
+  bool grid_changes_xy(double Lx_now, double Ly_now) const;
 };
+
+// kinds of Heun step the step table describes
+enum StepKind { KIND_STRAIN = 0, KIND_RESIZE = 1, KIND_PURE = 2 };
 
 struct GraphKey {
   bool resize = false;
@@ -63,7 +67,7 @@ struct Handle {
   int se_hist_cap = 0;
   int* h_pinned = nullptr;  // status word + scratch for small reads
   bool pred_valid = false;  // predictor copy consistent with the state
-  int pred_kind = 0;        // 1 strain, 2 shrink, 3 grow
+  int pred_kind = 0;        // 1 strain, 2 shrink, 3 grow, 4 pure shear
   bool fp64_valid = true;   // mixed form: FP64 copy of the state is current
   bool forces_valid = false;// mixed form: fx/fy/tau hold the forces of the state
   long long steps = 0, rebuilds = 0;
@@ -136,7 +140,7 @@ struct Handle {
   void invalidate_graph();
   bool run_graph(bool resize, int nsteps, int se_every);
 
-  int run_steps(bool resize, int shrink, int nsteps, int se_every, double* se_out);
+  int run_steps(int kind, int shrink, int nsteps, int se_every, double* se_out);
   int calc(bool se, double* se_out);
   bool materialize();
   bool read_unsorted(bool forces, double* a, double* b, double* c);

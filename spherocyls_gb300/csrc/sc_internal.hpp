@@ -46,12 +46,15 @@ struct StepScalars {
   double rate;       // strain rate
   double step;       // integration step
   double scale;      // resize factor pow(1-rate, dt)
-  int mode;          // 0 none, 1 multiply by scale (shrink), 2 divide by scale (grow)
+  int mode;          // 0 none, 1 multiply by scale (shrink), 2 divide by scale (grow),
+                     // 3 pure shear (x stretched and y compressed at the strain rate)
   int setback;       // set back gamma at the end of this step
   // FP32 copies for the mixed form (no FP64 arithmetic in its passes)
   float f_gamma_c, f_gamma_p, f_Wc, f_Hc, f_Wp, f_Hp, f_rate, f_step;
-  float f_factor;    // scale (mode 1), 1/scale (mode 2), 1 (mode 0)
-  float f_pad_;
+  // affine increment of one step, x <- x + g x: scale - 1 (mode 1) or 1/scale - 1
+  // (mode 2) on both axes, +dt rate/2 on x and -dt rate/2 on y (mode 3), else 0.
+  // Held as the increment, not as 1 + g, so that FP32 keeps its relative precision.
+  float f_gx, f_gy;
 };
 
 // FIRE minimiser state of one system
@@ -175,8 +178,9 @@ enum PassMode {
   PASS_FORCE = 0,        // forces at the state positions
   PASS_CORR_STRAIN = 1,  // forces at the predictor copy + Heun corrector (shear)
   PASS_PRED_STRAIN = 2,  // forces at the state + predictor for the next step (shear)
-  PASS_CORR_RESIZE = 3,  // forces at the predictor copy + corrector (affine resize)
-  PASS_PRED_RESIZE = 4   // forces at the state + predictor (affine resize)
+  PASS_CORR_RESIZE = 3,  // forces at the predictor copy + corrector (affine resize,
+                         // or pure shear when the row's mode is 3)
+  PASS_PRED_RESIZE = 4   // forces at the state + predictor (affine resize or pure shear)
 };
 
 // ---- kernel launchers (defined in the .cu files) ----

@@ -287,7 +287,7 @@ int sc_run_strain(sc_handle* H, const char* out_dir, double run_gamma, double po
   }
   std::vector<double> rec((size_t)(nInt / nSE + 1) * 5);
   for (unsigned long t = t_start + 1; t <= t_start + (unsigned long)nT; t++) {
-    rc = h.run_steps(false, 0, nInt, nSE, rec.data());
+    rc = h.run_steps(sc::KIND_STRAIN, 0, nInt, nSE, rec.data());
     if (rc) return rc;
     for (int k = 0; k < nInt / nSE; k++) {
       memcpy(se, &rec[5 * (size_t)k], sizeof se);
@@ -348,7 +348,7 @@ int sc_run_resize(sc_handle* H, const char* out_dir, double final_packing, doubl
       int seg = std::min(nSE - (done % nSE), nInt - done);
       bool rec_here = (done + seg) % nSE == 0;
       double r5[5];
-      rc = h.run_steps(true, shrink ? 1 : 0, seg, rec_here ? seg : 0, rec_here ? r5 : nullptr);
+      rc = h.run_steps(sc::KIND_RESIZE, shrink ? 1 : 0, seg, rec_here ? seg : 0, rec_here ? r5 : nullptr);
       if (rc) return rc;
       done += seg;
       if (rec_here) {
@@ -363,6 +363,97 @@ int sc_run_resize(sc_handle* H, const char* out_dir, double final_packing, doubl
       if ((rc = sc_save_positions(H, 0, pos_name(dir, prefix, t).c_str(), format))) return rc;
     }
   }
+  se_out.close();
+  if ((rc = sc_save_positions(H, 0, pos_name(dir, prefix, t).c_str(), format))) return rc;
+  if (t_end) *t_end = t;
+  return SC_OK;
+}
+
+// run_pure_strain_2p, src/cuda/2point_dynamics.cu:2286-2391: pure shear in whole
+// time units (1/dt steps) until Lx/Ly reaches stop_aspect.  A negative rate is
+// taken as its magnitude.  Stress/energy lines describe the state after N steps for
+// every N that is a multiple of the stress interval, labelled with the time unit
+// that N falls in; at each position save the line and the position file describe
+// the state at the start of the unit.  The run ends with a line and a position file
+// of the final state (the reference takes one more simple-shear step to write
+// them, :2389).
+int sc_run_pure_strain(sc_handle* H, const char* out_dir, double stop_aspect, double pos_save,
+                       double se_save, unsigned long t_start, int format, unsigned long* t_end) {
+  int rc = check_single(H, "sc_run_pure_strain");
+  if (rc) return rc;
+  sc::Handle& h = H->h;
+  // h.hs is reassigned by every run_steps call: read it afresh each time
+  auto box_aspect = [&]() { return h.hs[0].Lx / h.hs[0].Ly; };
+  if (!out_dir || !(h.hs[0].strain_rate != 0) || !(h.hs[0].step > 0) || !(stop_aspect > 0))
+    return io_fail(&h, SC_E_ARG,
+                   "sc_run_pure_strain: needs an output directory, a non-zero rate, dt > 0");
+  if (format != SC_FMT_SP && format != SC_FMT_SD)
+    return io_fail(&h, SC_E_ARG, "sc_run_pure_strain: format must be SC_FMT_SP or SC_FMT_SD");
+  if (h.hs[0].strain_rate < 0) {  // :2294-2297
+    h.hs[0].strain_rate = -h.hs[0].strain_rate;
+    h.pred_valid = false;
+  }
+  if (box_aspect() > stop_aspect)
+    return io_fail(&h, SC_E_ARG,
+                   "sc_run_pure_strain: the box aspect is already beyond the stop aspect");
+  const double rate = h.hs[0].strain_rate, dt = h.hs[0].step;
+  if (se_save < rate * dt) se_save = rate * dt;  // :2306-2309
+  if (pos_save < rate) pos_save = rate;
+  const unsigned long nInt = (unsigned long)(1.0 / dt + 0.5);
+  const unsigned long nSE = std::max(1UL, (unsigned long)(se_save / (rate * dt) + 0.5));
+  const unsigned long nPos = std::max(1UL, (unsigned long)(pos_save / rate + 0.5));
+  const std::string dir(out_dir);
+  const char* prefix = format == SC_FMT_SD ? "sd" : "sp";
+  const std::string se_path = dir + (format == SC_FMT_SD ? "/sd_stress_energy.dat" : "/sp_strain_se.dat");
+  std::ofstream se_out;
+  if ((rc = open_se(h, se_path, t_start, se_out))) return rc;
+  double se[5] = {0, 0, 0, 0, 0};
+  bool have_top = false;  // se holds the record of the state at the unit's start
+  unsigned long t = t_start;
+  std::vector<double> rec;
+  while (box_aspect() < stop_aspect) {
+    const unsigned long N0 = t * nInt;
+    const bool pos_here = t % nPos == 0;
+    if (!(t == t_start && t_start > 0) && (pos_here || N0 % nSE == 0)) {
+      // the continued line and position file of t_start are already written
+      if (!have_top && (rc = sc_calc_se(H, se))) return rc;
+      se_line(se_out, format, t, se, false, 0);
+      if (pos_here) {
+        se_out.flush();
+        if ((rc = sc_save_positions(H, 0, pos_name(dir, prefix, t).c_str(), format))) return rc;
+      }
+    }
+    have_top = false;
+    unsigned long done = 0;
+    while (done < nInt) {
+      const unsigned long N = N0 + done;
+      unsigned long seg, every;
+      if (N % nSE == 0 && nSE <= nInt - done) {
+        seg = ((nInt - done) / nSE) * nSE;  // whole record intervals in one call
+        every = nSE;
+      } else {
+        seg = std::min(nSE - N % nSE, nInt - done);  // up to the next record (or unit end)
+        every = (N + seg) % nSE == 0 ? seg : 0;
+      }
+      const unsigned long nrec = every ? seg / every : 0;
+      rec.assign(nrec * 5 + 5, 0.0);
+      rc = h.run_steps(sc::KIND_PURE, 0, (int)seg, (int)every, nrec ? rec.data() : nullptr);
+      if (rc) return rc;
+      for (unsigned long k = 0; k < nrec; k++) {
+        const unsigned long Nk = N + (k + 1) * every;
+        if (Nk == N0 + nInt) {
+          memcpy(se, &rec[5 * k], sizeof se);  // the next unit's opening record
+          have_top = true;
+        } else {
+          se_line(se_out, format, t, &rec[5 * k], false, 0);
+        }
+      }
+      done += seg;
+    }
+    t += 1;
+  }
+  if (!have_top && (rc = sc_calc_se(H, se))) return rc;
+  se_line(se_out, format, t, se, false, 0);
   se_out.close();
   if ((rc = sc_save_positions(H, 0, pos_name(dir, prefix, t).c_str(), format))) return rc;
   if (t_end) *t_end = t;

@@ -248,14 +248,26 @@ __global__ void __launch_bounds__(128) k_pass64(Dev d, const StepScalars* __rest
     d.v0y[i] = fy;
     d.v0p[i] = tq;
     double2 p = d.xy[i];
-    double2 pt = make_double2(p.x + dt * fx, p.y + dt * fy);
-    double pht = d.ph[i] + dt * tq / irc.x;
-    if (ts.mode == 1) {
-      pt.x *= ts.scale;
-      pt.y *= ts.scale;
-    } else if (ts.mode == 2) {
-      pt.x /= ts.scale;
-      pt.y /= ts.scale;
+    double2 pt;
+    double pht;
+    if (ts.mode == 3) {
+      // pure-shear predictor (pure_euler_est_2p, src/cuda/2point_dynamics.cu:1882-1891,
+      // with unit drag and the torque over I): the affine flow (+x/2, -y/2) times the
+      // strain rate, and the isolated rotation -RC sin(2 phi)/2, by an Euler step
+      const double phi = d.ph[i];
+      pt = make_double2(p.x + dt * (fx + 0.5 * ts.rate * p.x),
+                        p.y + dt * (fy - 0.5 * ts.rate * p.y));
+      pht = phi + dt * (tq / irc.x + ts.rate * (-0.5 * irc.y * sin(2 * phi)));
+    } else {
+      pt = make_double2(p.x + dt * fx, p.y + dt * fy);
+      pht = d.ph[i] + dt * tq / irc.x;
+      if (ts.mode == 1) {
+        pt.x *= ts.scale;
+        pt.y *= ts.scale;
+      } else if (ts.mode == 2) {
+        pt.x /= ts.scale;
+        pt.y /= ts.scale;
+      }
     }
     d.xy_t[i] = pt;
     d.ph_t[i] = pht;
@@ -263,20 +275,33 @@ __global__ void __launch_bounds__(128) k_pass64(Dev d, const StepScalars* __rest
     sincos(pht, &sn, &cs);
     d.nxy_t[i] = make_double2(rai.y * cs, rai.y * sn);
   } else if (MODE == PASS_CORR_RESIZE) {
-    // resize_step corrector, resize_dynamics.cpp:194-218
-    double ddx = 0.5 * dt * (d.v0x[i] + fx);
-    double ddy = 0.5 * dt * (d.v0y[i] + fy);
-    double ddp = 0.5 * dt * (d.v0p[i] + tq) / irc.x;
     double2 p0 = d.xy[i];
     const double phi0 = d.ph[i];
-    double2 p = make_double2(p0.x + ddx, p0.y + ddy);
-    double phi = phi0 + ddp;
-    if (ts.mode == 1) {
-      p.x *= ts.scale;
-      p.y *= ts.scale;
-    } else if (ts.mode == 2) {
-      p.x /= ts.scale;
-      p.y /= ts.scale;
+    double2 p;
+    double phi, ddx, ddy, ddp;
+    if (ts.mode == 3) {
+      // pure-shear corrector (pure_heun_corr_2p, src/cuda/2point_dynamics.cu:2140-2173):
+      // the predicted state plus dt/2 times the change of the contact forces
+      ddx = 0.5 * dt * (fx - d.v0x[i]);
+      ddy = 0.5 * dt * (fy - d.v0y[i]);
+      ddp = 0.5 * dt * (tq / irc.x - d.v0p[i] / irc.x);
+      const double2 pt = d.xy_t[i];
+      p = make_double2(pt.x + ddx, pt.y + ddy);
+      phi = d.ph_t[i] + ddp;
+    } else {
+      // resize_step corrector, resize_dynamics.cpp:194-218
+      ddx = 0.5 * dt * (d.v0x[i] + fx);
+      ddy = 0.5 * dt * (d.v0y[i] + fy);
+      ddp = 0.5 * dt * (d.v0p[i] + tq) / irc.x;
+      p = make_double2(p0.x + ddx, p0.y + ddy);
+      phi = phi0 + ddp;
+      if (ts.mode == 1) {
+        p.x *= ts.scale;
+        p.y *= ts.scale;
+      } else if (ts.mode == 2) {
+        p.x /= ts.scale;
+        p.y /= ts.scale;
+      }
     }
     d.xy[i] = p;
     d.ph[i] = phi;

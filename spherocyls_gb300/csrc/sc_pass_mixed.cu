@@ -39,15 +39,18 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
   s = t;
 }
 
-// (s + c) <- (s + c + v) * f, keeping the rounding error of the product in c
-__device__ __forceinline__ void kahan_add_scale(float& s, float& c, float v, float f) {
+// Affine step of a compensated coordinate, with g the increment of the scale
+// (the factor is 1 + g): (s + c) <- (s + c + v)(1 + g) when the increment v is
+// scaled too (resize), (s + c)(1 + g) + v when it is not (pure shear).  The
+// affine part (s + c + v) g is small, so it is added to the increment before the
+// compensated sum and the FP32 factor's rounding never touches s itself.
+template <bool SCALE_V>
+__device__ __forceinline__ void kahan_affine(float& s, float& c, float v, float g) {
   float y = v + c;
+  y = fmaf(SCALE_V ? s + y : s + c, g, y);
   float t = s + y;
-  float e = y - (t - s);
-  float p = t * f;
-  float pe = fmaf(t, f, -p) + e * f;
-  s = p;
-  c = pe;
+  c = y - (t - s);
+  s = t;
 }
 
 template <int MODE, bool SE, bool TWO>
@@ -181,17 +184,29 @@ __global__ void __launch_bounds__(128, TWO ? 6 : 10) k_pass_mixed(Dev d,
       v0y = fy;
       v0p = tq * invI;
     }
+    // pure shear: isolated rotation in the flow (+x/2, -y/2) at the strain rate
+    // (pure_euler_est_2p, src/cuda/2point_dynamics.cu:1889-1891)
+    const float rot = (MODE == PASS_PRED_RESIZE && ts.mode == 3)
+                          ? ts.f_rate * (-0.5f * d.rcf[i] * __sinf(2.f * (c.z + c.w)))
+                          : 0.f;
     float xt = ri.x + (c.x + dt * v0x);
     float yt = ri.y + (c.y + dt * v0y);
-    float pt = c.z + (c.w + dt * v0p);
+    float pt = c.z + (c.w + dt * (v0p + rot));
     if (MODE == PASS_PRED_RESIZE) {
-      xt *= ts.f_factor;  // about the (equally scaled) cell centre
-      yt *= ts.f_factor;
+      // about the cell centre, which moves with the same affine map
+      if (ts.mode == 3) {
+        xt = fmaf(ri.x + c.x, ts.f_gx, xt);  // the flow acts on the pre-step position
+        yt = fmaf(ri.y + c.y, ts.f_gy, yt);
+      } else {
+        xt = fmaf(xt, ts.f_gx, xt);  // resize scales the moved position
+        yt = fmaf(yt, ts.f_gy, yt);
+      }
     }
     float sn, cs;
     sincosf(pt, &sn, &cs);
     d.rec_t[i] = make_float4(xt, yt, A * cs, A * sn);
-    d.mv[i] = make_float4(v0x, v0y, v0p, pt);
+    // pure shear keeps the rotation rate of the flow in place of the predicted angle
+    d.mv[i] = make_float4(v0x, v0y, v0p, (MODE == PASS_PRED_RESIZE && ts.mode == 3) ? rot : pt);
   } else {
     const float4 v0 = d.mv[i];
     float4 c = d.mc[i];
@@ -207,23 +222,34 @@ __global__ void __launch_bounds__(128, TWO ? 6 : 10) k_pass_mixed(Dev d,
       ddy = 0.5f * dt * (v0.y + v1y);
       ddp = 0.5f * dt * (v0.z + v1p);
     } else {
-      // resize_step corrector, resize_dynamics.cpp:194-218
+      // resize_step corrector, resize_dynamics.cpp:194-218.  Pure shear
+      // (pure_heun_corr_2p, src/cuda/2point_dynamics.cu:2140-2173) ends at the
+      // predicted state plus dt/2 (F~ - F0): the same Heun mean of the contact
+      // forces, with the flow's displacement and rotation taken by Euler.
       ddx = 0.5f * dt * (v0.x + fx);
       ddy = 0.5f * dt * (v0.y + fy);
       ddp = 0.5f * dt * (v0.z + tq * invI);
+      if (ts.mode == 3) ddp = fmaf(dt, v0.w, ddp);
     }
     float4 m = d.mm[i];
+    float aff = 0.f;  // the next step's affine displacement, for the rebuild test
     if (MODE == PASS_CORR_RESIZE) {
-      const float f = ts.f_factor;
+      const float gx = ts.f_gx, gy = ts.f_gy;
       const int cp = d.cellp[i];
-      // the cell centre moves with the affine scale as well
+      // the cell centre moves with the affine map as well
       float cx = ((float)(cp & 0xffff) + 0.5f) * ts.f_Wc;
       float cy = ((float)(cp >> 16) + 0.5f) * ts.f_Hc;
       float x0 = r.x, y0 = r.y;
-      kahan_add_scale(r.x, c.x, ddx, f);
-      kahan_add_scale(r.y, c.y, ddy, f);
-      m.x += (r.x - x0) + cx * (f - 1.f);
-      m.y += (r.y - y0) + cy * (f - 1.f);
+      if (ts.mode == 3) {
+        kahan_affine<false>(r.x, c.x, ddx, gx);
+        kahan_affine<false>(r.y, c.y, ddy, gy);
+      } else {
+        kahan_affine<true>(r.x, c.x, ddx, gx);
+        kahan_affine<true>(r.y, c.y, ddy, gy);
+      }
+      m.x += (r.x - x0) + cx * gx;
+      m.y += (r.y - y0) + cy * gy;
+      aff = fabsf((cx + r.x) * gx) + fabsf((cy + r.y) * gy);
     } else {
       kahan_add(r.x, c.x, ddx);
       kahan_add(r.y, c.y, ddy);
@@ -245,7 +271,7 @@ __global__ void __launch_bounds__(128, TWO ? 6 : 10) k_pass_mixed(Dev d,
     // a spine end moves by at most the centre's displacement plus A times the
     // rotation; the next step's move is allowed for as well
     float reach = sqrtf(m.x * m.x + m.y * m.y) + A * fabsf((c.z + c.w) - m.z) +
-                  sqrtf(ddx * ddx + ddy * ddy) + A * fabsf(ddp);
+                  sqrtf(ddx * ddx + ddy * ddy) + aff + A * fabsf(ddp);
     if (!(reach < h)) {
       if (d.flags[s] == 0) atomicOr(&d.flags[s], 1);
       if (*d.any == 0) atomicExch(d.any, 1);
