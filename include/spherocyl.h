@@ -249,7 +249,9 @@ int sc_read_positions(const char *path, int *n, double *hdr, double *x, double *
 /* save_positions: SC_FMT_SP as src/cpp/spherocyl_box.cpp:410-423 (precision 14),
  * SC_FMT_SD as src/cuda/strain_dynamics.cu:820-843 (%.17g rows), SC_FMT_BIN as
  * src/cuda/strain_dynamics.cu:845-875 (host byte order).  sc_read_positions reads a
- * path ending in ".bin" as SC_FMT_BIN, any other as text with either header. */
+ * path ending in ".bin" as SC_FMT_BIN, one ending in ".gz" as gzip-compressed text
+ * (GzFileInput, src/cpp/gz_file_input.cpp; needs libz.so.1 at run time), any other
+ * as text with either header. */
 int sc_save_positions(sc_handle *h, int sys, const char *path, int format);
 
 /* run_strain with output, src/cpp/strain_dynamics.cpp:238-319: t runs from t_start

@@ -55,7 +55,8 @@ inline int out_format(int dflt = SC_FMT_SP) {
 
 // time of a continued run: the last 14 characters of the file name are
 // "##########.dat" (src/cpp/main.cpp:154-157)
-inline unsigned long time_from_name(const std::string& f) {
+inline unsigned long time_from_name(std::string f) {
+  if (f.size() > 3 && f.compare(f.size() - 3, 3, ".gz") == 0) f.resize(f.size() - 3);
   if (f.size() < 14) return 0;
   return std::strtoul(f.substr(f.size() - 14, 10).c_str(), nullptr, 10);
 }

@@ -13,7 +13,10 @@
 //    (t E Pxx Pyy P Pxy Pyx, strain_dynamics.cu:697).
 // The reader is the reference's DatFileInput with a header row
 // (src/cpp/file_input.h:24-76): whitespace-separated columns, header length 7
-// (one box length) or 8 (Lx, Ly; src/cuda/main.cpp:201).
+// (one box length) or 8 (Lx, Ly; src/cuda/main.cpp:201), plain or gzip-compressed
+// (GzFileInput, src/cpp/gz_file_input.cpp).
+#include <dlfcn.h>
+
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
@@ -156,14 +159,54 @@ static int read_bin(const char* path, int* n, double* hdr, double* x, double* y,
   return SC_OK;
 }
 
+// Whole content of a gzip-compressed file.  The reference's GzFileInput pipes the
+// file through zcat (src/cpp/gz_file_input.cpp:76-78); here zlib is loaded at run
+// time (libz.so.1, present wherever Python is), so neither a shell nor zlib's
+// headers are needed to build.
+static int read_gz(const char* path, std::string& out) {
+  typedef void* (*open_fn)(const char*, const char*);
+  typedef int (*read_fn)(void*, void*, unsigned);
+  typedef int (*close_fn)(void*);
+  static void* lib = dlopen("libz.so.1", RTLD_NOW | RTLD_LOCAL);
+  if (!lib) return io_fail(nullptr, SC_E_IO, "reading .gz files needs libz.so.1");
+  auto gz_open = reinterpret_cast<open_fn>(dlsym(lib, "gzopen"));
+  auto gz_read = reinterpret_cast<read_fn>(dlsym(lib, "gzread"));
+  auto gz_close = reinterpret_cast<close_fn>(dlsym(lib, "gzclose"));
+  if (!gz_open || !gz_read || !gz_close) return io_fail(nullptr, SC_E_IO, "libz.so.1 lacks gzopen");
+  void* f = gz_open(path, "rb");
+  if (!f) return io_fail(nullptr, SC_E_IO, std::string("cannot open ") + path);
+  std::vector<char> buf(1 << 20);
+  int got;
+  while ((got = gz_read(f, buf.data(), (unsigned)buf.size())) > 0) out.append(buf.data(), got);
+  gz_close(f);
+  if (got < 0) return io_fail(nullptr, SC_E_IO, std::string("corrupt gzip data in ") + path);
+  return SC_OK;
+}
+
+static int read_text(std::istream& in, const char* path, int* n, double* hdr, double* x,
+                     double* y, double* phi, double* R, double* A);
+
 int sc_read_positions(const char* path, int* n, double* hdr, double* x, double* y, double* phi,
                       double* R, double* A) {
   sc::g_noh_error.clear();
   if (!path || !n) return SC_E_ARG;
   const size_t plen = strlen(path);
   if (plen >= 4 && strcmp(path + plen - 4, ".bin") == 0) return read_bin(path, n, hdr, x, y, phi, R, A);
+  if (plen >= 3 && strcmp(path + plen - 3, ".gz") == 0) {
+    std::string text;
+    int rc = read_gz(path, text);
+    if (rc) return rc;
+    std::istringstream in(text);
+    return read_text(in, path, n, hdr, x, y, phi, R, A);
+  }
   std::ifstream in(path);
   if (!in) return io_fail(nullptr, SC_E_IO, std::string("cannot open ") + path);
+  return read_text(in, path, n, hdr, x, y, phi, R, A);
+}
+
+// DatFileInput with a header row (src/cpp/file_input.h:24-76) on either header layout
+static int read_text(std::istream& in, const char* path, int* n, double* hdr, double* x,
+                     double* y, double* phi, double* R, double* A) {
   std::string line;
   if (!std::getline(in, line)) return io_fail(nullptr, SC_E_IO, std::string("empty file ") + path);
   std::vector<double> head;

@@ -73,6 +73,34 @@ def test_read_binary_positions(library, tmp_path):
         read_positions(str(short))
 
 
+def test_read_gzip_positions(library, tmp_path):
+    """A gzip-compressed position file (GzFileInput, src/cpp/gz_file_input.cpp) reads
+    as the plain one; corrupt data is an error, not a short read."""
+    import gzip
+
+    from spherocyls_gb300 import ScError, read_positions
+
+    rng = np.random.default_rng(2)
+    n = 1000
+    x, y, p = rng.uniform(0, 5, (3, n))
+    R = np.full(n, 0.5)
+    A = np.full(n, 0.25)
+    sp = tmp_path / "sp0000000050.dat"
+    _write_sp(sp, n, 5.0, x, y, p, R, A, gamma=0.3, gt=2.5)
+    gz = tmp_path / "sp0000000050.dat.gz"
+    gz.write_bytes(gzip.compress(sp.read_bytes()))
+    plain = read_positions(str(sp))
+    packed = read_positions(str(gz))
+    assert plain[0] == packed[0]
+    for a, b in zip(plain[1:], packed[1:]):
+        assert np.array_equal(a, b)
+    bad = tmp_path / "bad.dat.gz"
+    data = gzip.compress(sp.read_bytes())
+    bad.write_bytes(data[: len(data) // 2])
+    with pytest.raises(ScError):
+        read_positions(str(bad))
+
+
 def test_read_positions_errors(library, tmp_path):
     from spherocyls_gb300 import ScError, read_positions
 
