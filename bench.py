@@ -61,8 +61,9 @@ def bytes_per_pass(precision: str, nbar: float) -> float:
 
 # DRAM bytes (read + write) per particle of one mixed force pass, the mean of the
 # predictor and corrector launches in one ncu capture of the default workload
-# (profiles/k_pass_mixed_n1048576.md: 107.7 and 166.6 MB per launch at N = 2^20).
-PASS_DRAM_BYTES_PER_PARTICLE = {"shear_n1048576_phi084": 137.15e6 / (1 << 20)}
+# (profiles/k_pass_mixed_n1048576.md: 108.7 and 167.6 MB per launch at N = 2^20,
+# padding 0.4).
+PASS_DRAM_BYTES_PER_PARTICLE = {"shear_n1048576_phi084": 138.17e6 / (1 << 20)}
 
 
 def _peaks():
@@ -436,6 +437,13 @@ def main():
     nbar = mean_list_length(prof)
     bpp = bytes_per_pass("mixed", nbar)
     achieved = bpp * n / (pass_ms / 1e3) / 1e9
+    # a forced rebuild of every system (cell sort + list build + ordering), host-timed
+    # with a synchronisation per call, so it includes the launches of the chain
+    prof.find_neighbors()
+    t0 = time.perf_counter()
+    for _ in range(10):
+        prof.find_neighbors()
+    full_rebuild_ms = 1e3 * (time.perf_counter() - t0) / 10
     prof.close()
 
     # ---- plain FP64 form on the same workload ----
@@ -497,7 +505,8 @@ def main():
                          "traffic_unit": "bytes per launch (ncu capture)",
                          "kernel": "k_pass_mixed (corrector/predictor force passes)",
                          "pass_ms": pass_ms, "bytes_per_particle_pass": bpp, "mean_list_length": nbar,
-                         "rebuild_ms_mean": pt["rebuild_ms"]},
+                         "rebuild_body_ms_mean_eager": pt["rebuild_ms"],
+                         "full_rebuild_ms": full_rebuild_ms},
             "cpu_baseline": base,
             "minimise": mini,
             "e2e": e2e,

@@ -54,7 +54,7 @@ __device__ __forceinline__ void kahan_affine(float& s, float& c, float v, float 
 }
 
 template <int MODE, bool SE, bool TWO>
-__global__ void __launch_bounds__(128, TWO ? 6 : 10) k_pass_mixed(Dev d,
+__global__ void __launch_bounds__(128, TWO ? 6 : (SE ? 10 : 12)) k_pass_mixed(Dev d,
                                                        const StepScalars* __restrict__ tab,
                                                        int row) {
   const int pos = blockIdx.x * blockDim.x + threadIdx.x;
@@ -77,15 +77,18 @@ __global__ void __launch_bounds__(128, TWO ? 6 : 10) k_pass_mixed(Dev d,
   const float4 pai = d.pa[i];  // (R, A, index bits, 1/I)
   const int idi = __float_as_int(pai.z);
   const int cnt = d.nbr_pn[pos];
+  // the list is column-major: entry k of this slot sits k * ntot words further on;
+  // Lst walks it, two entries ahead of the pair being computed
   const unsigned* __restrict__ Lst = reinterpret_cast<const unsigned*>(d.nbr_p) + pos;
-  const size_t stride = d.ntot;
+  const int stride = d.ntot;
 
   float fx = 0.f, fy = 0.f, tq = 0.f;
   double e_acc = 0.0, pxx = 0.0, pyy = 0.0, pxy = 0.0, pyx = 0.0;
   // software pipeline: the list entry two ahead and the neighbour data one ahead
   // are in flight while the current pair is computed
   unsigned e1 = cnt > 0 ? __ldg(Lst) : 0u;
-  unsigned e2 = cnt > 1 ? __ldg(Lst + stride) : 0u;
+  Lst += stride;
+  unsigned e2 = cnt > 1 ? __ldg(Lst) : 0u;
   // the neighbour's record and radius (its A^2 is |shaft|^2 from the record);
   // its particle index only on the passes that sum stress and energy
   float4 r1 = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -108,7 +111,8 @@ __global__ void __launch_bounds__(128, TWO ? 6 : 10) k_pass_mixed(Dev d,
       R1 = d.rf[e1 & kSlotMask];
       if (SE) id1 = __float_as_int(d.pa[e1 & kSlotMask].z);
     }
-    if (k + 2 < cnt) e2 = __ldg(Lst + (size_t)(k + 2) * stride);
+    Lst += stride;
+    if (k + 2 < cnt) e2 = __ldg(Lst);
     float dx = ri.x - rj.x + (float)(1 - (int)((e >> 28) & 3u)) * W;
     float dy = ri.y - rj.y + (float)(1 - (int)(e >> 30)) * H;
     if (smallx) dx += Lxf * (float)((dx < -0.5f * Lxf) - (dx > 0.5f * Lxf));
