@@ -71,6 +71,8 @@ typedef struct sc_options {
   int block;       /* threads per block of the mixed force pass (<= 128), 0 = 128 */
   int profile;     /* record per-pass CUDA events inside run calls (sc_get_pass_times) */
   int contact_model; /* SC_CONTACT_* */
+  int stage_inputs;  /* 1: copy the input arrays to the device before building the state,
+                      * also where the GPU reads pageable host memory in place (0) */
 } sc_options;
 
 const char *sc_version(void);
@@ -93,6 +95,11 @@ int sc_create_rect(const sc_options *opt, int n_sys, const int *n_per_sys, const
                    const double *Ly, const double *pad, const double *x, const double *y,
                    const double *phi, const double *R, const double *A, sc_handle **out);
 int sc_destroy(sc_handle *h);
+/* Device memory of all handles on a device comes from one stream-ordered pool that
+ * keeps the blocks of destroyed handles for the next one (creating a handle of a
+ * size seen before then allocates nothing).  sc_trim_memory returns the unused
+ * blocks to the driver. */
+int sc_trim_memory(int device);
 const char *sc_last_error(const sc_handle *h);
 int sc_set_stream(sc_handle *h, void *cuda_stream);
 int sc_synchronize(sc_handle *h);

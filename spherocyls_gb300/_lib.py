@@ -42,6 +42,7 @@ class ScOptions(ctypes.Structure):
         ("block", ctypes.c_int),
         ("profile", ctypes.c_int),
         ("contact_model", ctypes.c_int),
+        ("stage_inputs", ctypes.c_int),
     ]
 
 
@@ -80,6 +81,7 @@ SIGNATURES = [
     ("sc_strain_steps", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp]),
     ("sc_resize_steps", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp]),
     ("sc_pure_strain_steps", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp]),
+    ("sc_trim_memory", ctypes.c_int, [ctypes.c_int]),
     ("sc_gd_minimize", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double, _ip, _dp]),
     ("sc_fire_minimize", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_int, ctypes.c_double,
                                         ctypes.c_double, _ip, _dp, _ip]),

@@ -99,6 +99,11 @@ def _generate(n, packing, a_over_r, layout, angles, angle_range, shear_angles, m
 FMT = {"sp": 0, "sd": 1, "bin": 2}
 
 
+def trim_memory(device: int = 0) -> None:
+    """Return the device memory cached from destroyed handles to the driver."""
+    check(lib().sc_trim_memory(int(device)), None)
+
+
 def read_positions(path: str):
     """Read a position file (src/cpp or src/cuda text header, or the src/cuda binary
     layout for a path ending in .bin); returns (hdr, x, y, phi, R, A) with
@@ -123,7 +128,7 @@ class BoxBatch:
     def __init__(self, n_per_sys, L, x, y, phi, A, R, pad=0.0, *, precision: str = "fp64",
                  stress: str = "compat", device: int = 0, max_nbrs: int = 0,
                  use_graphs: bool = True, block: int = 0, profile: bool = False,
-                 contacts: int = 1, Ly=None):
+                 contacts: int = 1, Ly=None, stage_inputs: bool = False):
         n_per_sys = np.ascontiguousarray(np.atleast_1d(n_per_sys), dtype=np.int32)
         self.nsys = int(n_per_sys.shape[0])
         self.n_per_sys = n_per_sys
@@ -146,6 +151,7 @@ class BoxBatch:
         if int(contacts) not in (1, 2):
             raise ValueError("contacts must be 1 (one contact per pair) or 2")
         opt.contact_model = 1 if int(contacts) == 2 else 0
+        opt.stage_inputs = int(bool(stage_inputs))
         self.precision = precision
         h = ctypes.c_void_p()
         nps = n_per_sys.ctypes.data_as(ctypes.POINTER(ctypes.c_int))

@@ -22,12 +22,6 @@ namespace {
 const double kRefPi = 3.14159265358979;  // src/cpp/spherocyl_box.cpp:12
 std::string& g_create_error = sc::g_noh_error;
 
-bool finite_all(const double* a, size_t n) {
-  for (size_t i = 0; i < n; i++)
-    if (!std::isfinite(a[i])) return false;
-  return true;
-}
-
 }  // namespace
 
 extern "C" {
@@ -61,6 +55,7 @@ void sc_default_options(sc_options* opt) {
   opt->block = 0;
   opt->profile = 0;
   opt->contact_model = SC_CONTACT_ONE;
+  opt->stage_inputs = 0;
 }
 
 const char* sc_last_error(const sc_handle* h) {
@@ -117,16 +112,37 @@ int sc_create_rect(const sc_options* opt_in, int n_sys, const int* n_per_sys, co
     return SC_E_ARG;
   }
   const int ntot = (int)ntot_ll;
-  if (!finite_all(x, ntot) || !finite_all(y, ntot) || !finite_all(phi, ntot) ||
-      !finite_all(R, ntot) || !finite_all(A, ntot)) {
-    g_create_error = "sc_create: non-finite input";
-    return SC_E_NAN;
-  }
-  for (int i = 0; i < ntot; i++)
-    if (!(R[i] > 0) || !(A[i] >= 0)) {
+  // One pass over the caller's arrays: the input checks, and per system the largest
+  // R and A and the filled area (set_particle, src/cpp/spherocyl_box.cpp:216-219;
+  // calculate_packing_fraction :357-366, summed in particle order).
+  std::vector<double> rmax(n_sys, 0.0), amax(n_sys, 0.0), filled(n_sys, 0.0);
+  {
+    bool finite = true, shapes = true;
+    int i = 0;
+    for (int s = 0; s < n_sys; s++) {
+      double rm = 0.0, am = 0.0, f = 0.0;
+      for (int k = 0; k < n_per_sys[s]; k++, i++) {
+        const double r = R[i], a = A[i];
+        finite = finite && std::isfinite(x[i]) && std::isfinite(y[i]) &&
+                 std::isfinite(phi[i]) && std::isfinite(r) && std::isfinite(a);
+        shapes = shapes && r > 0 && a >= 0;
+        if (a > am) am = a;
+        if (r > rm) rm = r;
+        f += (kRefPi * r + 4.0 * a) * r;
+      }
+      rmax[s] = rm;
+      amax[s] = am;
+      filled[s] = f;
+    }
+    if (!finite) {
+      g_create_error = "sc_create: non-finite input";
+      return SC_E_NAN;
+    }
+    if (!shapes) {
       g_create_error = "sc_create: every R must be > 0 and every A >= 0";
       return SC_E_ARG;
     }
+  }
 
   sc_handle* H = new (std::nothrow) sc_handle;
   if (!H) return SC_E_NOMEM;
@@ -148,13 +164,12 @@ int sc_create_rect(const sc_options* opt_in, int n_sys, const int* n_per_sys, co
   if (!h.cuda_ok(cudaStreamCreateWithFlags(&h.stream, cudaStreamNonBlocking), "stream"))
     return bail(SC_E_CUDA);
   h.own_stream = true;
+  h.use_pool = sc::device_pool(h.device) != nullptr;
   if (!h.cuda_ok(cudaMallocHost((void**)&h.h_pinned, (16 + 12 * (size_t)n_sys) * sizeof(int)),
                  "pinned"))
     return bail(SC_E_NOMEM);
 
-  // host-side particle constants: set_particle, src/cpp/spherocyl_box.cpp:188-221
-  std::vector<double> hx(x, x + ntot), hy(y, y + ntot), hp(phi, phi + ntot);
-  std::vector<double> hI(ntot), hRC(ntot);
+  // per-system scalars; the per-particle constants are computed on the device
   h.hs.resize(n_sys);
   int p0 = 0;
   for (int s = 0; s < n_sys; s++) {
@@ -164,25 +179,10 @@ int sc_create_rect(const sc_options* opt_in, int n_sys, const int* n_per_sys, co
     S.Lx = L[s];
     S.Ly = Ly[s];
     S.pad = pad ? pad[s] : 0.0;
-    double filled = 0.0;
-    for (int k = 0; k < S.n; k++) {
-      int i = p0 + k;
-      double al = A[i] / R[i];
-      double C = (3 * kRefPi + 24 * al + 6 * kRefPi * al * al + 8 * al * al * al);
-      double area = R[i] * (kRefPi * R[i] + 4 * A[i]);
-      hI[i] = R[i] * R[i] * R[i] * R[i] * C / (6 * area);
-      hRC[i] = (8 * al + 6 * kRefPi * al * al + 8 * al * al * al) / C;
-      while (hx[i] > S.Lx) hx[i] -= S.Lx;
-      while (hx[i] < 0.0) hx[i] += S.Lx;
-      while (hy[i] > S.Ly) hy[i] -= S.Ly;
-      while (hy[i] < 0.0) hy[i] += S.Ly;
-      while (hp[i] > kRefPi) hp[i] -= 2 * kRefPi;
-      while (hp[i] < -kRefPi) hp[i] += 2 * kRefPi;
-      if (A[i] > S.Amax) S.Amax = A[i];
-      if (R[i] > S.Rmax) S.Rmax = R[i];
-      filled += (kRefPi * R[i] + 4.0 * A[i]) * R[i];
-    }
-    S.packing = filled / (S.Lx * S.Ly);
+    S.Amax = amax[s];
+    S.Rmax = rmax[s];
+    const double filled_s = filled[s];
+    S.packing = filled_s / (S.Lx * S.Ly);
     S.configure(true);
     p0 += S.n;
   }
@@ -247,33 +247,43 @@ int sc_create_rect(const sc_options* opt_in, int n_sys, const int* n_per_sys, co
   d.pchunk_p0 = pcp;
   d.pchunk_np = pcn;
 
-  // initial slots: the input order
-  std::vector<double2> xy(N), ra(N), irc(N);
-  std::vector<int> id(N), ps(N);
+  // initial slots: the input order.  The ingest kernel reads the caller's arrays in
+  // place where the GPU addresses pageable host memory (Grace's coherent link), else
+  // from device copies staged in the stress-partials buffer (5 N doubles, unused
+  // until the first pass).
+  cudaStream_t st = h.stream;
+  std::vector<int> sys_p0(n_sys + 1);
+  std::vector<double> sys_L(2 * (size_t)n_sys);
   for (int s = 0; s < n_sys; s++) {
-    const sc::HostSys& S = h.hs[s];
-    for (int k = 0; k < S.n; k++) {
-      int i = S.p0 + k;
-      xy[i] = make_double2(hx[i], hy[i]);
-      ra[i] = make_double2(R[i], A[i]);
-      irc[i] = make_double2(hI[i], hRC[i]);
-      id[i] = k;
-      ps[i] = s;
+    sys_p0[s] = h.hs[s].p0;
+    sys_L[2 * s] = h.hs[s].Lx;
+    sys_L[2 * s + 1] = h.hs[s].Ly;
+  }
+  sys_p0[n_sys] = ntot;
+  int* d_sys_p0 = nullptr;
+  double* d_sys_L = nullptr;
+  ok = h.dalloc(&d_sys_p0, n_sys + 1, "systems") && h.dalloc(&d_sys_L, 2 * (size_t)n_sys, "systems");
+  if (!ok) return bail(h.last_status ? h.last_status : SC_E_NOMEM);
+  int pageable = 0;
+  cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, h.device);
+  const double* src[5] = {x, y, phi, R, A};
+  if (!pageable || opt.stage_inputs) {
+    for (int k = 0; k < 5 && ok; k++) {
+      ok = h.cuda_ok(cudaMemcpyAsync(d.se_part + (size_t)k * N, src[k], N * sizeof(double),
+                                     cudaMemcpyDefault, st), "upload");
+      src[k] = d.se_part + (size_t)k * N;
     }
   }
-  cudaStream_t st = h.stream;
-  ok = h.cuda_ok(cudaMemcpyAsync(d.xy, xy.data(), N * sizeof(double2), cudaMemcpyHostToDevice, st),
-                 "upload") &&
-       h.cuda_ok(cudaMemcpyAsync(d.ph, hp.data(), N * sizeof(double), cudaMemcpyHostToDevice, st),
-                 "upload") &&
-       h.cuda_ok(cudaMemcpyAsync(d.ra, ra.data(), N * sizeof(double2), cudaMemcpyHostToDevice, st),
-                 "upload") &&
-       h.cuda_ok(cudaMemcpyAsync(d.irc, irc.data(), N * sizeof(double2), cudaMemcpyHostToDevice,
-                                 st), "upload") &&
-       h.cuda_ok(cudaMemcpyAsync(d.id, id.data(), N * sizeof(int), cudaMemcpyHostToDevice, st),
-                 "upload") &&
-       h.cuda_ok(cudaMemcpyAsync(psys, ps.data(), N * sizeof(int), cudaMemcpyHostToDevice, st),
-                 "upload") &&
+  ok = ok &&
+       h.cuda_ok(cudaMemcpyAsync(d_sys_p0, sys_p0.data(), (n_sys + 1) * sizeof(int),
+                                 cudaMemcpyHostToDevice, st), "upload") &&
+       h.cuda_ok(cudaMemcpyAsync(d_sys_L, sys_L.data(), 2 * (size_t)n_sys * sizeof(double),
+                                 cudaMemcpyHostToDevice, st), "upload");
+  if (ok) {
+    sc::launch_ingest(d, src[0], src[1], src[2], src[3], src[4], d_sys_p0, d_sys_L, psys, st);
+    ok = h.cuda_ok(cudaGetLastError(), "ingest launch");
+  }
+  ok = ok &&
        h.cuda_ok(cudaMemcpyAsync(pcs, pchunk_sys.data(), d.npchunks * sizeof(int),
                                  cudaMemcpyHostToDevice, st), "upload") &&
        h.cuda_ok(cudaMemcpyAsync(pcp, pchunk_p0.data(), d.npchunks * sizeof(int),
@@ -292,6 +302,8 @@ int sc_create_rect(const sc_options* opt_in, int n_sys, const int* n_per_sys, co
        h.cuda_ok(cudaMemsetAsync(d.tau, 0, N * sizeof(double), st), "memset") &&
        h.cuda_ok(cudaStreamSynchronize(st), "upload sync");
   if (!ok) return bail(h.last_status);
+  h.dfree(d_sys_p0);
+  h.dfree(d_sys_L);
   if (!h.layout_cells() || !h.rebuild_all() || !h.check_status("create"))
     return bail(h.last_status);
   *out = H;
@@ -300,6 +312,17 @@ int sc_create_rect(const sc_options* opt_in, int n_sys, const int* n_per_sys, co
 
 int sc_destroy(sc_handle* h) {
   delete h;
+  return SC_OK;
+}
+
+int sc_trim_memory(int device) {
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) {
+    cudaGetLastError();
+    return SC_E_ARG;
+  }
+  cudaMemPool_t pool = sc::device_pool(device);
+  if (pool && cudaMemPoolTrimTo(pool, 0) != cudaSuccess) return SC_E_CUDA;
   return SC_OK;
 }
 

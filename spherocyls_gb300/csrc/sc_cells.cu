@@ -467,6 +467,59 @@ __global__ void k_se_store(Dev d, double* dst) {
 
 // Output in the caller's particle order: slot i holds particle p0 + id[i] of its
 // system, so each value goes to out[k * ntot + p0 + id[i]].
+// set_particle's wrap loop (src/cpp/spherocyl_box.cpp:204-215) for the input state:
+// the reference's repeated subtraction, finished by a floor for a value more than
+// 64 periods out (where the loop would take that long; not an error here).
+__device__ __forceinline__ double wrap_input(double v, double lo, double hi, double period) {
+  int it = 0;
+  while (v > hi && it < 64) {
+    v -= period;
+    it++;
+  }
+  while (v < lo && it < 64) {
+    v += period;
+    it++;
+  }
+  if (it >= 64) v -= period * floor((v - lo) / period);
+  return v;
+}
+
+// Per-particle state of a new handle (set_particle, src/cpp/spherocyl_box.cpp:188-221):
+// the wrapped position and angle, (R, A), the moment of inertia I and the rotation
+// coefficient RC in the reference's operation order, the particle index and system
+// of each slot.  x..A are the caller's arrays: host memory that the GPU reads in
+// place where it can address pageable memory, else a device copy.  sys_p0 holds the
+// first slot of each system and ntot at [nsys]; sys_L the (Lx, Ly) pairs.
+__global__ void k_ingest(Dev d, const double* __restrict__ x, const double* __restrict__ y,
+                         const double* __restrict__ phi, const double* __restrict__ R,
+                         const double* __restrict__ A, const int* __restrict__ sys_p0,
+                         const double* __restrict__ sys_L, int* __restrict__ psys) {
+  const int stride = gridDim.x * blockDim.x;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.ntot; i += stride) {
+    int lo = 0, hi = d.nsys - 1;  // the system whose slot range holds i
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (sys_p0[mid] <= i)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    const int s = lo;
+    const double Lx = sys_L[2 * s], Ly = sys_L[2 * s + 1];
+    const double r = R[i], a = A[i];
+    const double al = a / r;
+    const double C = (3 * kRefPi + 24 * al + 6 * kRefPi * al * al + 8 * al * al * al);
+    const double area = r * (kRefPi * r + 4 * a);
+    d.irc[i] = make_double2(r * r * r * r * C / (6 * area),
+                            (8 * al + 6 * kRefPi * al * al + 8 * al * al * al) / C);
+    d.ra[i] = make_double2(r, a);
+    d.xy[i] = make_double2(wrap_input(x[i], 0.0, Lx, Lx), wrap_input(y[i], 0.0, Ly, Ly));
+    d.ph[i] = wrap_input(phi[i], -kRefPi, kRefPi, 2 * kRefPi);
+    d.id[i] = i - sys_p0[s];
+    psys[i] = s;
+  }
+}
+
 __global__ void k_unsort_state(Dev d, double* __restrict__ out) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.ntot) return;
@@ -556,6 +609,13 @@ void launch_refresh_geometry(const Dev& d, bool mixed, const StepScalars* tab, i
 void launch_gd_update(const Dev& d, bool mixed, const StepScalars* tab, int row, cudaStream_t st) {
   (void)mixed;  // the CPU-compatible gradient descent is a plain FP64 protocol
   k_gd_update<<<nblk(d.ntot, 256), 256, 0, st>>>(d, tab, row);
+}
+
+void launch_ingest(const Dev& d, const double* x, const double* y, const double* phi,
+                   const double* R, const double* A, const int* sys_p0, const double* sys_L,
+                   int* psys, cudaStream_t st) {
+  const int blocks = nblk(d.ntot, 256) < 152 * 8 ? nblk(d.ntot, 256) : 152 * 8;
+  k_ingest<<<blocks, 256, 0, st>>>(d, x, y, phi, R, A, sys_p0, sys_L, psys);
 }
 
 void launch_unsort_state(const Dev& d, double* out, cudaStream_t st) {

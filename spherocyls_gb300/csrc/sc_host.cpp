@@ -15,8 +15,11 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdint>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -48,15 +51,53 @@ void Handle::dfree(void* p) {
   if (!p) return;
   auto it = std::find(allocs.begin(), allocs.end(), p);
   if (it != allocs.end()) allocs.erase(it);
-  cudaFree(p);
+  if (use_pool)
+    cudaFreeAsync(p, stream);  // after the work already queued on the handle's stream
+  else
+    cudaFree(p);
+}
+
+cudaMemPool_t device_pool(int device) {
+  static std::mutex mu;
+  static std::map<int, cudaMemPool_t> pools;
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = pools.find(device);
+  if (it != pools.end()) return it->second;
+  cudaMemPool_t pool = nullptr;
+  int supported = 0;
+  if (cudaDeviceGetAttribute(&supported, cudaDevAttrMemoryPoolsSupported, device) ==
+          cudaSuccess &&
+      supported) {
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    if (cudaMemPoolCreate(&pool, &props) == cudaSuccess) {
+      // keep freed blocks: a handle created after another of the same size (a new
+      // run, a copy for tuning) then costs no device allocation
+      uint64_t keep = UINT64_MAX;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    } else {
+      pool = nullptr;
+    }
+  }
+  cudaGetLastError();  // a device without pools leaves no sticky error behind
+  pools[device] = pool;
+  return pool;
 }
 
 Handle::~Handle() {
   if (device >= 0) cudaSetDevice(device);
   if (graph_exec) cudaGraphExecDestroy(graph_exec);
+  for (auto& c : sub_graphs) cudaGraphExecDestroy(c.exec);
   if (stream2) cudaStreamDestroy(stream2);
   for (auto& e : ev_pool) cudaEventDestroy(e);
-  for (void* p : allocs) cudaFree(p);
+  if (use_pool) {
+    for (void* p : allocs) cudaFreeAsync(p, stream);
+    cudaStreamSynchronize(stream);
+  } else {
+    for (void* p : allocs) cudaFree(p);
+  }
   if (h_pinned) cudaFreeHost(h_pinned);
   if (own_stream && stream) cudaStreamDestroy(stream);
 }
@@ -391,6 +432,8 @@ void Handle::invalidate_graph() {
   if (graph_exec) cudaGraphExecDestroy(graph_exec);
   graph_exec = nullptr;
   graph_key = GraphKey{};
+  for (auto& c : sub_graphs) cudaGraphExecDestroy(c.exec);
+  sub_graphs.clear();
   if (fire_exec) cudaGraphExecDestroy(fire_exec);
   fire_exec = nullptr;
   fire_key_iters = 0;
@@ -436,7 +479,8 @@ cudaError_t Handle::capture_rebuild_node(int row, const std::function<int(cudaSt
 // Capture the per-step sequence with the rebuild body inside a conditional graph
 // node (skipped when no system needs a rebuild).  Returns false, with the capture
 // ended, when any capture step fails.
-bool Handle::capture_conditional(bool resize, int nsteps, int se_every, cudaGraph_t* out) {
+bool Handle::capture_conditional(bool resize, int nsteps, const std::vector<char>& se,
+                                 cudaGraph_t* out) {
   if (!stream2 && !cuda_ok(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking), "stream"))
     return false;
   if (!cuda_ok(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture"))
@@ -445,14 +489,13 @@ bool Handle::capture_conditional(bool resize, int nsteps, int se_every, cudaGrap
   int r = 0;
   long long fixed = 0;
   for (int k = 1; k <= nsteps && e == cudaSuccess; k++) {
-    bool se = se_every > 0 && k % se_every == 0;
     enqueue_corr(resize, k, false);
     e = capture_rebuild_node(
         k, [&](cudaStream_t st) { return enqueue_rebuild_body(resize, k, false, st); });
     if (e != cudaSuccess) break;
-    enqueue_pred(resize, k, se, false);
+    enqueue_pred(resize, k, se[k] != 0, false);
     fixed += 3;
-    if (se) {
+    if (se[k]) {
       enqueue_se_record(r++);
       fixed += 3;
     }
@@ -469,43 +512,110 @@ bool Handle::capture_conditional(bool resize, int nsteps, int se_every, cudaGrap
   return true;
 }
 
+// Capture `nsteps` steps (rows 1..nsteps of the current table pointer; se[k]: step k
+// records stress/energy) and instantiate them.  With conditional nodes the rebuild
+// bodies run only when needed, else every step carries the (early-exiting) chain.
+bool Handle::instantiate_steps(bool resize, int nsteps, const std::vector<char>& se,
+                               cudaGraphExec_t* exec, long long* nkernels) {
+  cudaGraph_t g = nullptr;
+  long long k0 = kernels;
+  graph_conditional = use_conditional && capture_conditional(resize, nsteps, se, &g);
+  kernels = k0;
+  if (!graph_conditional) {
+    use_conditional = false;  // plain capture: the rebuild kernels exit early
+    if (!cuda_ok(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal),
+                 "begin capture"))
+      return false;
+    int r = 0;
+    for (int k = 1; k <= nsteps; k++) {
+      enqueue_step(resize, k, se[k] != 0, false);
+      if (se[k]) enqueue_se_record(r++);
+    }
+    graph_kernels = kernels - k0;
+    kernels = k0;
+    body_kernels = 0;
+    if (!cuda_ok(cudaStreamEndCapture(stream, &g), "end capture")) return false;
+  }
+  cudaError_t e = cudaGraphInstantiate(exec, g, 0);
+  cudaGraphDestroy(g);
+  if (!cuda_ok(e, "graph instantiate")) {
+    *exec = nullptr;
+    return false;
+  }
+  *nkernels = graph_kernels;
+  return true;
+}
+
 // Capture `nsteps` steps (rows 1..nsteps) as one graph; reused while the table
 // pointer, the shapes and the step kind stay the same (the table contents change
 // from call to call, the graph reads them from device memory).
 bool Handle::run_graph(bool resize, int nsteps, int se_every) {
+  if (nsteps % kGraphSteps == 0) return run_subgraphs(resize, nsteps, se_every);
   GraphKey key{resize, nsteps, se_every, prec};
   if (!graph_exec || !(key == graph_key)) {
-    invalidate_graph();
-    cudaGraph_t g = nullptr;
-    long long k0 = kernels;
-    graph_conditional = use_conditional && capture_conditional(resize, nsteps, se_every, &g);
-    kernels = k0;
-    if (!graph_conditional) {
-      use_conditional = false;  // plain capture: the rebuild kernels exit early
-      if (!cuda_ok(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal),
-                   "begin capture"))
-        return false;
-      int r = 0;
-      for (int k = 1; k <= nsteps; k++) {
-        bool se = se_every > 0 && k % se_every == 0;
-        enqueue_step(resize, k, se, false);
-        if (se) enqueue_se_record(r++);
-      }
-      graph_kernels = kernels - k0;
-      kernels = k0;
-      body_kernels = 0;
-      if (!cuda_ok(cudaStreamEndCapture(stream, &g), "end capture")) return false;
-    }
-    cudaError_t e = cudaGraphInstantiate(&graph_exec, g, 0);
-    cudaGraphDestroy(g);
-    if (!cuda_ok(e, "graph instantiate")) {
-      graph_exec = nullptr;
-      return false;
-    }
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    graph_exec = nullptr;
+    graph_key = GraphKey{};
+    std::vector<char> se(nsteps + 1, 0);
+    for (int k = 1; k <= nsteps; k++) se[k] = se_every > 0 && k % se_every == 0;
+    long long nk = 0;
+    if (!instantiate_steps(resize, nsteps, se, &graph_exec, &nk)) return false;
     graph_key = key;
+    chunk_kernels = nk;
   }
-  kernels += graph_kernels;
+  kernels += chunk_kernels;
   return cuda_ok(cudaGraphLaunch(graph_exec, stream), "graph launch");
+}
+
+// The chunk (rows 1..nsteps of the table, records of steps that are multiples of
+// se_every) as nsteps / kGraphSteps launches of sub-chunk graphs.
+bool Handle::run_subgraphs(bool resize, int nsteps, int se_every) {
+  const int G = kGraphSteps;
+  if (!d_win && (!dalloc(&d_win, (size_t)(G + 1) * nsys, "step window") ||
+                 !dalloc(&d_win_se, (size_t)G * nsys * 5, "record window")))
+    return false;
+  int rec = 0;
+  for (int j = 0; j < nsteps / G; j++) {
+    unsigned mask = 0;
+    for (int k = 1; k <= G; k++)
+      if (se_every > 0 && (j * G + k) % se_every == 0) mask |= 1u << (k - 1);
+    SubGraph* sg = nullptr;
+    for (auto& c : sub_graphs)
+      if (c.resize == resize && c.se_mask == mask && c.prec == prec) sg = &c;
+    if (!sg) {
+      // capture against the windows: swap them in for the table and record buffer
+      std::vector<char> se(G + 1, 0);
+      for (int k = 1; k <= G; k++) se[k] = (mask >> (k - 1)) & 1u;
+      StepScalars* tab_keep = d_tab;
+      double* rec_keep = d_se_hist;
+      d_tab = d_win;
+      d_se_hist = d_win_se;
+      SubGraph c{resize, mask, prec, nullptr, 0};
+      bool ok = instantiate_steps(resize, G, se, &c.exec, &c.kernels);
+      d_tab = tab_keep;
+      d_se_hist = rec_keep;
+      if (!ok) return false;
+      sub_graphs.push_back(c);
+      sg = &sub_graphs.back();
+    }
+    const int nrec = __builtin_popcount(mask);
+    if (!cuda_ok(cudaMemcpyAsync(d_win, d_tab + (size_t)j * G * nsys,
+                                 (size_t)(G + 1) * nsys * sizeof(StepScalars),
+                                 cudaMemcpyDeviceToDevice, stream),
+                 "step window") ||
+        !cuda_ok(cudaGraphLaunch(sg->exec, stream), "graph launch"))
+      return false;
+    kernels += sg->kernels;
+    if (nrec > 0) {
+      if (!cuda_ok(cudaMemcpyAsync(d_se_hist + (size_t)rec * nsys * 5, d_win_se,
+                                   (size_t)nrec * nsys * 5 * sizeof(double),
+                                   cudaMemcpyDeviceToDevice, stream),
+                   "record window"))
+        return false;
+      rec += nrec;
+    }
+  }
+  return true;
 }
 
 bool Handle::ensure_se_hist(int nrec) {

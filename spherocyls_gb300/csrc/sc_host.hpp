@@ -43,6 +43,11 @@ struct GraphKey {
   }
 };
 
+// The memory pool of a device that all handles on it allocate from (nullptr where
+// the device has no stream-ordered pools).  Freed blocks stay in the pool for the
+// next handle until sc_trim_memory releases them.
+cudaMemPool_t device_pool(int device);
+
 struct Handle {
   static constexpr int kChunk = 100;  // steps per table upload / captured graph
   static constexpr int kFireChunk = 50;  // FIRE iterations between host checks
@@ -74,12 +79,29 @@ struct Handle {
   int dev_status = 0;
   long long dev_rebuilds = 0;  // rebuild chains the device executed
   long long kernels = 0;       // kernels launched (eagerly or inside graphs)
-  long long graph_kernels = 0; // kernels in the captured chunk graph
+  long long graph_kernels = 0; // kernels in the last captured graph
+  long long chunk_kernels = 0; // kernels in the chunk graph (graph_exec)
   int last_status = SC_OK;
   std::string err;
   // CUDA graph of one chunk of steps
   cudaGraphExec_t graph_exec = nullptr;
   GraphKey graph_key{};
+  // Chunks whose length is a multiple of kGraphSteps run as sub-chunk graphs of
+  // kGraphSteps steps, which read their rows from a window of the step table (d_win,
+  // refilled before each launch) and leave their records in d_win_se: a graph 5x
+  // shorter to capture and instantiate, reused for every sub-chunk with the same step
+  // kind and the same steps recording stress/energy (se_mask).
+  static constexpr int kGraphSteps = 20;
+  struct SubGraph {
+    bool resize;
+    unsigned se_mask;
+    int prec;
+    cudaGraphExec_t exec;
+    long long kernels;
+  };
+  std::vector<SubGraph> sub_graphs;
+  StepScalars* d_win = nullptr;
+  double* d_win_se = nullptr;
   cudaStream_t stream2 = nullptr;  // captures the conditional rebuild bodies
   bool use_conditional = true;     // conditional graph nodes available
   bool graph_conditional = false;  // the current graph uses them
@@ -103,11 +125,14 @@ struct Handle {
   ~Handle();
   void fail(int code, const char* fmt, ...);
   bool cuda_ok(cudaError_t e, const char* what);
+  bool use_pool = false;  // device memory comes from the device's cached pool
   template <class T>
   bool dalloc(T** p, size_t count, const char* what) {
     *p = nullptr;
     if (count == 0) count = 1;
-    cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+    cudaError_t e = use_pool ? cudaMallocFromPoolAsync((void**)p, count * sizeof(T),
+                                                       device_pool(device), stream)
+                             : cudaMalloc((void**)p, count * sizeof(T));
     if (e != cudaSuccess) {
       fail(SC_E_NOMEM, "cudaMalloc %s (%zu bytes): %s", what, count * sizeof(T),
            cudaGetErrorString(e));
@@ -135,7 +160,11 @@ struct Handle {
   int enqueue_rebuild_body(bool resize, int k, bool prof, cudaStream_t st);
   void enqueue_pred(bool resize, int k, bool se, bool prof);
   cudaError_t capture_rebuild_node(int row, const std::function<int(cudaStream_t)>& body);
-  bool capture_conditional(bool resize, int nsteps, int se_every, cudaGraph_t* out);
+  bool capture_conditional(bool resize, int nsteps, const std::vector<char>& se,
+                           cudaGraph_t* out);
+  bool instantiate_steps(bool resize, int nsteps, const std::vector<char>& se,
+                         cudaGraphExec_t* exec, long long* nkernels);
+  bool run_subgraphs(bool resize, int nsteps, int se_every);
   void enqueue_se_record(int rec);
   void invalidate_graph();
   bool run_graph(bool resize, int nsteps, int se_every);

@@ -201,6 +201,9 @@ void launch_gd_update(const Dev& d, bool mixed, const StepScalars* tab, int row,
 void launch_se_store(const Dev& d, double* dst, cudaStream_t st);
 // per-slot values back to input order: out[k * ntot + input index] (k = 0, 1, 2)
 void launch_unsort_state(const Dev& d, double* out, cudaStream_t st);
+void launch_ingest(const Dev& d, const double* x, const double* y, const double* phi,
+                   const double* R, const double* A, const int* sys_p0, const double* sys_L,
+                   int* psys, cudaStream_t st);
 void launch_unsort_forces(const Dev& d, double* out, cudaStream_t st);
 void launch_refresh_geometry(const Dev& d, bool mixed, const StepScalars* tab, int row,
                              cudaStream_t st);
