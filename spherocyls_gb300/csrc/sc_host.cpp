@@ -352,10 +352,12 @@ bool Handle::rebuild_all() {
 
 void Handle::launch_pass(int mode, bool se, int row, bool fast) {
   kernels += 1;
+  Dev dd = d;
+  dd.cond = (mode == PASS_CORR_STRAIN || mode == PASS_CORR_RESIZE) ? step_cond : 0;
   if (prec == PREC_MIXED)
-    launch_pass_mixed(d, mode, se, d_tab, row, stream, block);
+    launch_pass_mixed(dd, mode, se, d_tab, row, stream, block);
   else
-    launch_pass_fp64(d, mode, se, d_tab, row, stream, fast);
+    launch_pass_fp64(dd, mode, se, d_tab, row, stream, fast);
 }
 
 cudaEvent_t Handle::next_event() {
@@ -442,18 +444,25 @@ void Handle::invalidate_graph() {
 // Inside a capture on `stream`: k_pre_rebuild for table row `row`, then a
 // conditional IF node it switches on when any system needs a rebuild; `body`
 // enqueues the node's contents on stream2 and returns its kernel count.
-cudaError_t Handle::capture_rebuild_node(int row, const std::function<int(cudaStream_t)>& body) {
+// A conditional handle on the graph being captured on `stream`, reset to 0 at
+// every launch of the graph.
+cudaError_t Handle::new_cond_handle(cudaGraphConditionalHandle* h) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t gcap = nullptr;
+  cudaError_t e = cudaStreamGetCaptureInfo(stream, &cs, nullptr, &gcap, nullptr, nullptr, nullptr);
+  if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(h, gcap, 0, cudaGraphCondAssignDefault);
+  return e;
+}
+
+// Inside a capture on `stream`: an IF node on `hcond` after the work captured so far,
+// whose body `body` records on stream2.
+cudaError_t Handle::add_cond_body(cudaGraphConditionalHandle hcond,
+                                  const std::function<int(cudaStream_t)>& body) {
   cudaStreamCaptureStatus cs;
   cudaGraph_t gcap = nullptr;
   const cudaGraphNode_t* deps = nullptr;
   size_t nd = 0;
   cudaError_t e = cudaStreamGetCaptureInfo(stream, &cs, nullptr, &gcap, &deps, nullptr, &nd);
-  cudaGraphConditionalHandle hcond;
-  if (e == cudaSuccess)
-    e = cudaGraphConditionalHandleCreate(&hcond, gcap, 0, cudaGraphCondAssignDefault);
-  if (e != cudaSuccess) return e;
-  launch_pre_rebuild(d, d_tab, row, hcond, stream);
-  e = cudaStreamGetCaptureInfo(stream, &cs, nullptr, &gcap, &deps, nullptr, &nd);
   if (e != cudaSuccess) return e;
   // zeroed raw storage: the struct's union has no default constructor in C++
   alignas(cudaGraphNodeParams) unsigned char cp_buf[sizeof(cudaGraphNodeParams)] = {};
@@ -476,6 +485,16 @@ cudaError_t Handle::capture_rebuild_node(int row, const std::function<int(cudaSt
   return cudaStreamEndCapture(stream2, &bg);
 }
 
+// Inside a capture on `stream`: k_pre_rebuild for table row `row` (systems that set
+// gamma back, or a pending rebuild), then the conditional node it switches on.
+cudaError_t Handle::capture_rebuild_node(int row, const std::function<int(cudaStream_t)>& body) {
+  cudaGraphConditionalHandle hcond;
+  cudaError_t e = new_cond_handle(&hcond);
+  if (e != cudaSuccess) return e;
+  launch_pre_rebuild(d, d_tab, row, hcond, stream);
+  return add_cond_body(hcond, body);
+}
+
 // Capture the per-step sequence with the rebuild body inside a conditional graph
 // node (skipped when no system needs a rebuild).  Returns false, with the capture
 // ended, when any capture step fails.
@@ -489,12 +508,18 @@ bool Handle::capture_conditional(bool resize, int nsteps, const std::vector<char
   int r = 0;
   long long fixed = 0;
   for (int k = 1; k <= nsteps && e == cudaSuccess; k++) {
+    // the corrector pass itself switches the step's rebuild node on
+    cudaGraphConditionalHandle hcond;
+    e = new_cond_handle(&hcond);
+    if (e != cudaSuccess) break;
+    step_cond = hcond;
     enqueue_corr(resize, k, false);
-    e = capture_rebuild_node(
-        k, [&](cudaStream_t st) { return enqueue_rebuild_body(resize, k, false, st); });
+    step_cond = 0;
+    e = add_cond_body(hcond,
+                      [&](cudaStream_t st) { return enqueue_rebuild_body(resize, k, false, st); });
     if (e != cudaSuccess) break;
     enqueue_pred(resize, k, se[k] != 0, false);
-    fixed += 3;
+    fixed += 2;
     if (se[k]) {
       enqueue_se_record(r++);
       fixed += 3;

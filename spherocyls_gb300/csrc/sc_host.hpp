@@ -160,6 +160,10 @@ struct Handle {
   int enqueue_rebuild_body(bool resize, int k, bool prof, cudaStream_t st);
   void enqueue_pred(bool resize, int k, bool se, bool prof);
   cudaError_t capture_rebuild_node(int row, const std::function<int(cudaStream_t)>& body);
+  cudaError_t new_cond_handle(cudaGraphConditionalHandle* h);
+  cudaError_t add_cond_body(cudaGraphConditionalHandle h,
+                            const std::function<int(cudaStream_t)>& body);
+  unsigned long long step_cond = 0;  // rebuild node of the step being captured
   bool capture_conditional(bool resize, int nsteps, const std::vector<char>& se,
                            cudaGraph_t* out);
   bool instantiate_steps(bool resize, int nsteps, const std::vector<char>& se,

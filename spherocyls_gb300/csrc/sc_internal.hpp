@@ -159,6 +159,9 @@ struct Dev {
   int* wcoff;               // [nsys + 1] first work item (cell) of each listed system
   int* nwork;               // [3] listed systems, their slots, their cells
   int* status;              // [2] sticky error bits (ST_*), rebuild-chain count
+  // the conditional rebuild node of the step a corrector pass belongs to, inside a
+  // captured chunk (0 elsewhere): the pass switches it on when a rebuild is due
+  unsigned long long cond;
 };
 
 // sticky device status bits
@@ -260,6 +263,28 @@ __device__ __forceinline__ void for_listed_cells(const Dev& d, F&& f) {
     const int s = d.work[w];
     f(d.geom[s].c0 + (g - d.wcoff[w]), s);
   }
+}
+// Corrector passes inside a captured step (d.cond != 0), block 0 before any early
+// exit: mark the systems that set gamma back at this step (their rows say so) and
+// switch the step's rebuild node on for them, or for a rebuild still pending.
+__device__ __forceinline__ void mark_pending_rebuilds(const Dev& d,
+                                                      const StepScalars* __restrict__ tab,
+                                                      int row) {
+  if (!d.cond || blockIdx.x != 0) return;
+  bool setback = false;
+  for (int s = threadIdx.x; s < d.nsys; s += blockDim.x)
+    if (tab[row * d.nsys + s].setback) {
+      atomicOr(&d.flags[s], 2);
+      setback = true;
+    }
+  if (setback) atomicExch(d.any, 1);
+  if (setback || (threadIdx.x == 0 && *d.any != 0)) cudaGraphSetConditional(d.cond, 1u);
+}
+// A particle of system s needs its list rebuilt: flag the system, raise the pending
+// word, and (the thread that raises it) switch the step's rebuild node on.
+__device__ __forceinline__ void request_rebuild(const Dev& d, int s) {
+  if (d.flags[s] == 0) atomicOr(&d.flags[s], 1);
+  if (*d.any == 0 && atomicExch(d.any, 1) == 0 && d.cond) cudaGraphSetConditional(d.cond, 1u);
 }
 // all: every slot of every system (forced refreshes), else the worklist
 template <class F>

@@ -82,18 +82,18 @@ __global__ void __launch_bounds__(128) k_build_nbrs(Dev d, const StepScalars* __
 // particles the reference wrapped before, and which after, their update.
 __device__ __forceinline__ void flag_moved(const Dev& d, int s, int id, double2 m, double pad) {
   if (m.x > 0.5 * pad || m.x < -0.5 * pad || m.y > 0.5 * pad || m.y < -0.5 * pad) {
-    if (d.flags[s] == 0) atomicOr(&d.flags[s], 1);
     atomicMin(&d.istar[s], id);
-    if (*d.any == 0) atomicExch(d.any, 1);
+    request_rebuild(d, s);
   }
 }
 
 template <int MODE, bool SE, bool TWO, bool FAST = false>
 __global__ void __launch_bounds__(128) k_pass64(Dev d, const StepScalars* __restrict__ tab,
                                                int row) {
+  constexpr bool kPred = (MODE == PASS_CORR_STRAIN || MODE == PASS_CORR_RESIZE);
+  if (kPred) mark_pending_rebuilds(d, tab, row);
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.ntot) return;
-  constexpr bool kPred = (MODE == PASS_CORR_STRAIN || MODE == PASS_CORR_RESIZE);
   int s = d.psys[i];
   const SysGeom& g = d.geom[s];
   const StepScalars ts = tab[row * d.nsys + s];

@@ -57,10 +57,11 @@ template <int MODE, bool SE, bool TWO>
 __global__ void __launch_bounds__(128, TWO ? 6 : (SE ? 10 : 12)) k_pass_mixed(Dev d,
                                                        const StepScalars* __restrict__ tab,
                                                        int row) {
+  constexpr bool kPred = (MODE == PASS_CORR_STRAIN || MODE == PASS_CORR_RESIZE);
+  if (kPred) mark_pending_rebuilds(d, tab, row);
   const int pos = blockIdx.x * blockDim.x + threadIdx.x;
   if (pos >= d.ntot) return;
   const int i = d.ord[pos];  // the slot this thread works on (lists ordered by length)
-  constexpr bool kPred = (MODE == PASS_CORR_STRAIN || MODE == PASS_CORR_RESIZE);
   const int s = d.psys[i];
   const SysGeom& g = d.geom[s];
   const StepScalars& ts = tab[row * d.nsys + s];
@@ -276,10 +277,7 @@ __global__ void __launch_bounds__(128, TWO ? 6 : (SE ? 10 : 12)) k_pass_mixed(De
     // rotation; the next step's move is allowed for as well
     float reach = sqrtf(m.x * m.x + m.y * m.y) + A * fabsf((c.z + c.w) - m.z) +
                   sqrtf(ddx * ddx + ddy * ddy) + aff + A * fabsf(ddp);
-    if (!(reach < h)) {
-      if (d.flags[s] == 0) atomicOr(&d.flags[s], 1);
-      if (*d.any == 0) atomicExch(d.any, 1);
-    }
+    if (!(reach < h)) request_rebuild(d, s);
   }
 }
 
