@@ -143,6 +143,24 @@ int sc_pure_strain_steps(sc_handle *h, int nsteps, int se_every, double *se_out)
 int sc_gd_minimize(sc_handle *h, int max_steps, double e_min, int *steps_taken,
                    double *e_final);
 
+/* Polak-Ribiere conjugate gradient with the reference's line search
+ * (cjpr_relax_2p / cjpr_relax_step_2p / line_search_2p,
+ * src/cuda/2point_dynamics.cu:3609-3780, 3886-4020, 4233-4296), FP64 form, every
+ * system at once and entirely on the device.  Per iteration: D = F + beta D with
+ * beta = max(0, (F.F - F.F0)/F0.F0) (restarted every 3N iterations); a line search
+ * from 2e-6/|F|_rms, doubling while the energy falls and halving while it rises
+ * (within [1e-18, 2]/|F|_rms), then the minimum of the parabola through E(0), E(s),
+ * E(2s); on failure steepest descent, then F/sqrt|F|.  A system stops at zero force
+ * (reason SC_CG_ZERO_FORCE), three equal iteration energies (SC_CG_STALLED), no
+ * lower energy in any direction (SC_CG_STEP) or max_iter iterations
+ * (SC_CG_MAX_ITER).  iters, energy (the calc_se energy at the end) and reason take
+ * n_sys entries each and may be NULL.  Returns SC_E_NOCONV when a system reached
+ * max_iter. */
+#define SC_CG_ZERO_FORCE 1
+#define SC_CG_STALLED 2
+#define SC_CG_STEP 3
+#define SC_CG_MAX_ITER 4
+int sc_cg_minimize(sc_handle *h, int max_iter, int *iters, double *energy, int *reason);
 /* Production minimiser: FIRE on every system of the handle, on the device, until
  * every |F_i| and |tau_i|/sqrt(I_i) is below ftol, or max_iter iterations.  Replaces
  * the reference's conjugate-gradient relaxation (cjpr_relax_2p,

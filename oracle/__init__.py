@@ -94,6 +94,8 @@ class _Lib:
                                   [ctypes.c_int, ctypes.c_double, ctypes.c_double, _dp, _dp, _dp,
                                    _dp, _dp, ctypes.c_double])
             self.run_pure_steps = fn("run_pure_steps", ctypes.c_int, [handle, ctypes.c_int, _dp])
+            self.cg_minimize = fn("cg_minimize", ctypes.c_int,
+                                  [handle, ctypes.c_int, _ip, _dp, _ip])
         self.n = fn("n", ctypes.c_int, [handle])
         self.get_state = fn("get_state", None, [handle, _dp, _dp, _dp])
         self.get_forces = fn("get_forces", None, [handle, _dp, _dp, _dp])
@@ -221,6 +223,16 @@ class _BoxBase:
         if rc != 0:
             raise RuntimeError("oracle pure-shear run failed")
         return out
+
+    def cg_minimize(self, max_iter: int):
+        """(iterations, energy, stop reason) of the conjugate-gradient restatement."""
+        it = ctypes.c_int()
+        e = ctypes.c_double()
+        why = ctypes.c_int()
+        if self._L.cg_minimize(self.h, int(max_iter), ctypes.byref(it), ctypes.byref(e),
+                               ctypes.byref(why)) != 0:
+            raise RuntimeError("oracle cg failed")
+        return it.value, e.value, why.value
 
     def run_gd_steps(self, nsteps: int, emin: float = 0.0):
         out = np.zeros(nsteps)

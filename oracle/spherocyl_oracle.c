@@ -660,6 +660,177 @@ int orc_run_pure_steps(orc_box *b, int nsteps, double *se_out) {
   return 0;
 }
 
+/* ---- Polak-Ribiere conjugate gradient: cjpr_relax_2p / cjpr_relax_step_2p /
+ * line_search_2p, src/cuda/2point_dynamics.cu:3609-3780, 3886-4020, 4233-4296.
+ * PARITY UNPINNED against the reference itself (its CG exists only in CUDA); the
+ * GPU form is checked against this restatement.  The reference's norms are FP32
+ * sums; here they are FP64.  Its line search is a recursion; this is the same
+ * sequence of probes written as a loop, except that the reference's outer frame,
+ * after a successful halving chain, also probes from the moved position: here a
+ * line search ends with its move. ---- */
+
+/* energy (calc_se's E) at x + t D */
+static double probe_energy(orc_box *b, double t, const double *dx, const double *dy,
+                           const double *dp) {
+  for (int i = 0; i < b->n; i++) {
+    b->tx[i] = b->x[i] + t * dx[i];
+    b->ty[i] = b->y[i] + t * dy[i];
+    b->tphi[i] = b->phi[i] + t * dp[i];
+  }
+  pview v = {b->tx, b->ty, b->tphi, b->tfx, b->tfy, b->ttau};
+  zero3(b->tfx, b->tfy, b->ttau, b->n);
+  b->E = 0.0;
+  loop_pairs(b, &v, b->gamma, b->Lx, b->Ly, 1);
+  return b->E;
+}
+
+enum { CG_TOP = 1, CG_SECOND, CG_HALVE, CG_DOUBLE, CG_FINAL, CG_MOVE, CG_FAIL };
+
+/* line_search_2p from step0 in the current direction: 1 = moved, 0 = no lower
+ * energy found (E0 is the energy at x) */
+static int line_search(orc_box *b, double E0, double step, double min_step, double max_step,
+                       const double *dx, const double *dy, const double *dp) {
+  double E1 = 0, E2 = 0, tmin = 1;
+  int phase = CG_TOP;
+  double t = step;
+  while (phase != CG_MOVE && phase != CG_FAIL) {
+    double E = probe_energy(b, t, dx, dy, dp);
+    int findmin = 0;
+    switch (phase) {
+      case CG_TOP:
+        E1 = E;
+        if (E1 > E0 && step > min_step) {
+          step /= 2;
+          E2 = E1;
+          t = step;
+          phase = CG_HALVE;
+        } else {
+          t = 2 * step;
+          phase = CG_SECOND;
+        }
+        break;
+      case CG_HALVE:
+        E1 = E;
+        if (E1 > E0 && step > min_step) {
+          step /= 2;
+          E2 = E1;
+          t = step;
+        } else {
+          findmin = 1;
+        }
+        break;
+      case CG_SECOND:
+      case CG_DOUBLE:
+        E2 = E;
+        if (E2 <= E1 && step < max_step) {
+          step *= 2;
+          E1 = E2;
+          t = 2 * step;
+          phase = CG_DOUBLE;
+        } else {
+          findmin = 1;
+        }
+        break;
+      case CG_FINAL:
+        if (E > E1) tmin = 1;
+        phase = CG_MOVE;
+        break;
+    }
+    if (findmin) {
+      if (E1 > E0) {
+        phase = CG_FAIL;
+      } else {
+        tmin = (3 * E0 - 4 * E1 + E2) / (2 * E0 - 4 * E1 + 2 * E2);
+        if (tmin > 2)
+          tmin = 2;
+        else if (E1 == E0)
+          tmin = 1;
+        t = tmin * step;
+        phase = CG_FINAL;
+      }
+    }
+  }
+  if (phase == CG_FAIL) return 0;
+  int rebuild = 0;
+  const double h = tmin * step;
+  for (int i = 0; i < b->n; i++) {
+    double ddx = h * dx[i], ddy = h * dy[i];
+    b->x[i] += ddx;
+    b->y[i] += ddy;
+    b->phi[i] += h * dp[i];
+    b->xm[i] += ddx;
+    b->ym[i] += ddy;
+    if (moved_too_far(b, i)) rebuild = 1;
+  }
+  if (rebuild) find_neighbors(b);
+  return 1;
+}
+
+/* Runs until a stop rule of cjpr_relax_step_2p holds or max_iter iterations; *iters,
+ * *e_out (the calc_se energy at the last evaluation) and *reason (1 zero force,
+ * 2 three equal energies, 3 no lower energy in any direction, 4 max_iter). */
+int orc_cg_minimize(orc_box *b, int max_iter, int *iters, double *e_out, int *reason) {
+  const int n = b->n;
+  double *buf = (double *)calloc(6 * (size_t)n, sizeof(double));
+  if (!buf) return -1;
+  double *dx = buf, *dy = buf + n, *dp = buf + 2 * (size_t)n;
+  double *f0x = buf + 3 * (size_t)n, *f0y = buf + 4 * (size_t)n, *f0p = buf + 5 * (size_t)n;
+  double E0 = 0, Eh1 = 0, Eh2 = 0;
+  int it = 0, why = 0;
+  for (;;) {
+    orc_calc_se(b);
+    double F2 = 0, FF0 = 0, F02 = 0;
+    for (int i = 0; i < n; i++) {
+      F2 += b->fx[i] * b->fx[i] + b->fy[i] * b->fy[i] + b->tau[i] * b->tau[i];
+      FF0 += b->fx[i] * f0x[i] + b->fy[i] * f0y[i] + b->tau[i] * f0p[i];
+      F02 += f0x[i] * f0x[i] + f0y[i] * f0y[i] + f0p[i] * f0p[i];
+    }
+    Eh2 = Eh1;
+    Eh1 = E0;
+    E0 = b->E;
+    if (F2 == 0) { why = 1; break; }
+    if (Eh1 == E0 && Eh2 == Eh1) { why = 2; break; }
+    if (it >= max_iter) { why = 4; break; }
+    it++;
+    int restart = (it - 1) % (3 * n) == 0;
+    double beta = (restart || !(F02 > 0)) ? 0.0 : fmax(0.0, (F2 - FF0) / F02);
+    for (int i = 0; i < n; i++) {
+      dx[i] = b->fx[i] + beta * dx[i];
+      dy[i] = b->fy[i] + beta * dy[i];
+      dp[i] = b->tau[i] + beta * dp[i];
+      f0x[i] = b->fx[i];
+      f0y[i] = b->fy[i];
+      f0p[i] = b->tau[i];
+    }
+    double norm = sqrt(F2 / (3 * n));
+    double min_step = 1e-18 / norm, max_step = 2 / norm;
+    if (line_search(b, E0, 2e-6 / norm, min_step, max_step, dx, dy, dp)) continue;
+    /* steepest descent */
+    for (int i = 0; i < n; i++) {
+      dx[i] = b->fx[i];
+      dy[i] = b->fy[i];
+      dp[i] = b->tau[i];
+    }
+    if (line_search(b, E0, 1e-6 / norm, min_step, max_step, dx, dy, dp)) continue;
+    /* F / sqrt|F| per particle (sqrt_grad_dir_2p, :3293-3340) */
+    for (int i = 0; i < n; i++) {
+      double fm = sqrt(b->fx[i] * b->fx[i] + b->fy[i] * b->fy[i]), tm = fabs(b->tau[i]);
+      dx[i] = fm == 0 ? 0.0 : b->fx[i] / sqrt(fm);
+      dy[i] = fm == 0 ? 0.0 : b->fy[i] / sqrt(fm);
+      dp[i] = tm == 0 ? 0.0 : b->tau[i] / sqrt(tm);
+    }
+    double rn = sqrt(norm);
+    if (line_search(b, E0, 2e-6 / rn, 1e-18 / rn, 2 / rn, dx, dy, dp)) continue;
+    why = 3;
+    break;
+  }
+  free(buf);
+  if (iters) *iters = it;
+  if (e_out) *e_out = E0;
+  if (reason) *reason = why;
+  return b->err ? -1 : 0;
+}
+
 /* gradient_relax_step, relaxation_dynamics.cpp:11-31 */
 int orc_gd_step(orc_box *b) {
   for (int i = 0; i < b->n; i++) {

@@ -40,6 +40,7 @@ int orc_run_strain_steps(orc_box *b, int nsteps, double *se_out);
 int orc_run_resize_steps(orc_box *b, int nsteps, int shrink, double *se_out);
 int orc_run_gd_steps(orc_box *b, int nsteps, double emin, double *e_out);
 int orc_run_pure_steps(orc_box *b, int nsteps, double *se_out);
+int orc_cg_minimize(orc_box *b, int max_iter, int *iters, double *e_out, int *reason);
 
 int orc_n(const orc_box *b);
 void orc_get_state(const orc_box *b, double *x, double *y, double *phi);

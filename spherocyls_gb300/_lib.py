@@ -83,6 +83,7 @@ SIGNATURES = [
     ("sc_pure_strain_steps", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp]),
     ("sc_trim_memory", ctypes.c_int, [ctypes.c_int]),
     ("sc_gd_minimize", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double, _ip, _dp]),
+    ("sc_cg_minimize", ctypes.c_int, [_vp, ctypes.c_int, _ip, _dp, _ip]),
     ("sc_fire_minimize", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_int, ctypes.c_double,
                                         ctypes.c_double, _ip, _dp, _ip]),
     ("sc_affine_scale", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double]),

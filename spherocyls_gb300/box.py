@@ -257,6 +257,21 @@ class BoxBatch:
         return steps.value, ef.value
 
     # --- minimisation and quasistatic compression -------------------------------
+    def cg_minimize(self, max_iter: int = 100000):
+        """The reference's Polak-Ribiere conjugate gradient (cjpr_relax_2p,
+        src/cuda/2point_dynamics.cu:4233-4296) on every system: returns per-system
+        (iterations, energy, stop reason) with reason 1 zero force, 2 three equal
+        energies, 3 no lower energy along any direction, 4 max_iter."""
+        it = np.zeros(self.nsys, dtype=np.int32)
+        e = np.zeros(self.nsys)
+        why = np.zeros(self.nsys, dtype=np.int32)
+        ip = ctypes.POINTER(ctypes.c_int)
+        st = lib().sc_cg_minimize(self.h, int(max_iter), it.ctypes.data_as(ip), _ptr(e),
+                                  why.ctypes.data_as(ip))
+        if st not in (0, _lib.SC_E_NOCONV):
+            self._chk(st)
+        return it, e, why
+
     def fire_minimize(self, ftol: float, max_iter: int = 100000, dt0: float = 1e-2,
                       dt_max: float = 0.2):
         """FIRE until max|F| < ftol per system; returns (iters, fmax[nsys], done[nsys])."""

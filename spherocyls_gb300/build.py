@@ -29,6 +29,7 @@ CU_UNITS = {
     "sc_pass_mixed.cu": True,
     "sc_noalloc.cu": False,
     "sc_fire.cu": True,
+    "sc_cg.cu": False,
 }
 CPP_UNITS = ["sc_host.cpp", "sc_api.cpp", "sc_generate.cpp", "sc_io.cpp"]
 CLI_UNITS = {

@@ -300,6 +300,11 @@ __global__ void k_rb_gather(Dev d) {
       d.xy_t[i] = make_double2(d.fvx[src], d.fvy[src]);
       d.ph_t[i] = d.fvp[src];
     }
+    if (d.cg0x) {  // and the minimiser's previous forces (stress partials are dead here)
+      d.se_part[i] = d.cg0x[src];
+      d.se_part[(size_t)d.ntot + i] = d.cg0y[src];
+      d.se_part[2 * (size_t)d.ntot + i] = d.cg0p[src];
+    }
   });
 }
 
@@ -321,6 +326,11 @@ __global__ void k_rb_commit(Dev d, const StepScalars* __restrict__ tab, int row,
       d.fvx[i] = v.x;
       d.fvy[i] = v.y;
       d.fvp[i] = d.ph_t[i];
+    }
+    if (d.cg0x) {
+      d.cg0x[i] = d.se_part[i];
+      d.cg0y[i] = d.se_part[(size_t)d.ntot + i];
+      d.cg0p[i] = d.se_part[2 * (size_t)d.ntot + i];
     }
     if (!mixed) {
       double sn, cs;
@@ -465,8 +475,6 @@ __global__ void k_se_store(Dev d, double* dst) {
   for (int k = 0; k < 5; k++) dst[5 * s + k] = d.se_sys[(size_t)k * d.nsys + s];
 }
 
-// Output in the caller's particle order: slot i holds particle p0 + id[i] of its
-// system, so each value goes to out[k * ntot + p0 + id[i]].
 // set_particle's wrap loop (src/cpp/spherocyl_box.cpp:204-215) for the input state:
 // the reference's repeated subtraction, finished by a floor for a value more than
 // 64 periods out (where the loop would take that long; not an error here).
@@ -520,6 +528,8 @@ __global__ void k_ingest(Dev d, const double* __restrict__ x, const double* __re
   }
 }
 
+// Output in the caller's particle order: slot i holds particle p0 + id[i] of its
+// system, so each value goes to out[k * ntot + p0 + id[i]].
 __global__ void k_unsort_state(Dev d, double* __restrict__ out) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.ntot) return;

@@ -90,6 +90,7 @@ Handle::~Handle() {
   if (device >= 0) cudaSetDevice(device);
   if (graph_exec) cudaGraphExecDestroy(graph_exec);
   for (auto& c : sub_graphs) cudaGraphExecDestroy(c.exec);
+  if (cg_exec) cudaGraphExecDestroy(cg_exec);
   if (stream2) cudaStreamDestroy(stream2);
   for (auto& e : ev_pool) cudaEventDestroy(e);
   if (use_pool) {
@@ -436,6 +437,9 @@ void Handle::invalidate_graph() {
   graph_key = GraphKey{};
   for (auto& c : sub_graphs) cudaGraphExecDestroy(c.exec);
   sub_graphs.clear();
+  if (cg_exec) cudaGraphExecDestroy(cg_exec);
+  cg_exec = nullptr;
+  cg_key_iter = -1;
   if (fire_exec) cudaGraphExecDestroy(fire_exec);
   fire_exec = nullptr;
   fire_key_iters = 0;
@@ -447,17 +451,23 @@ void Handle::invalidate_graph() {
 // A conditional handle on the graph being captured on `stream`, reset to 0 at
 // every launch of the graph.
 cudaError_t Handle::new_cond_handle(cudaGraphConditionalHandle* h) {
+  return new_cond_handle(h, 0);
+}
+
+cudaError_t Handle::new_cond_handle(cudaGraphConditionalHandle* h, unsigned int dflt) {
   cudaStreamCaptureStatus cs;
   cudaGraph_t gcap = nullptr;
   cudaError_t e = cudaStreamGetCaptureInfo(stream, &cs, nullptr, &gcap, nullptr, nullptr, nullptr);
-  if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(h, gcap, 0, cudaGraphCondAssignDefault);
+  if (e == cudaSuccess)
+    e = cudaGraphConditionalHandleCreate(h, gcap, dflt, cudaGraphCondAssignDefault);
   return e;
 }
 
-// Inside a capture on `stream`: an IF node on `hcond` after the work captured so far,
-// whose body `body` records on stream2.
+// Inside a capture on `stream`: an IF (or WHILE) node on `hcond` after the work
+// captured so far, whose body `body` records on stream2.
 cudaError_t Handle::add_cond_body(cudaGraphConditionalHandle hcond,
-                                  const std::function<int(cudaStream_t)>& body) {
+                                  const std::function<int(cudaStream_t)>& body,
+                                  cudaGraphConditionalNodeType type) {
   cudaStreamCaptureStatus cs;
   cudaGraph_t gcap = nullptr;
   const cudaGraphNode_t* deps = nullptr;
@@ -469,7 +479,7 @@ cudaError_t Handle::add_cond_body(cudaGraphConditionalHandle hcond,
   cudaGraphNodeParams& cp = *reinterpret_cast<cudaGraphNodeParams*>(cp_buf);
   cp.type = cudaGraphNodeTypeConditional;
   cp.conditional.handle = hcond;
-  cp.conditional.type = cudaGraphCondTypeIf;
+  cp.conditional.type = type;
   cp.conditional.size = 1;
   cudaGraphNode_t cn;
   e = cudaGraphAddNode(&cn, gcap, deps, nullptr, nd, &cp);
@@ -1038,6 +1048,186 @@ int Handle::fire_minimize(double ftol, int max_iter, double dt0, double dt_max, 
   }
   if (iters) *iters = max_it;
   return all_done ? SC_OK : SC_E_NOCONV;
+}
+
+// ---- conjugate gradient (cjpr_relax_2p, src/cuda/2point_dynamics.cu:4233-4296) ----
+
+bool Handle::ensure_cg() {
+  if (!ensure_fire()) return false;  // the search direction lives in the minimiser arrays
+  if (cg.sys) return true;
+  double *x0 = nullptr, *y0 = nullptr, *p0 = nullptr, *part = nullptr;
+  CgSys* sys = nullptr;
+  int* searching = nullptr;
+  if (!dalloc(&x0, ntot, "cg f0x") || !dalloc(&y0, ntot, "cg f0y") ||
+      !dalloc(&p0, ntot, "cg f0p") || !dalloc(&sys, nsys, "cg sys") ||
+      !dalloc(&part, 3 * (size_t)d.npchunks, "cg partials") ||
+      !dalloc(&searching, 1, "cg flag"))
+    return false;
+  cg.sys = sys;
+  cg.part = part;
+  cg.searching = searching;
+  d.cg0x = x0;  // the rebuild permutes the previous forces from now on
+  d.cg0y = y0;
+  d.cg0p = p0;
+  invalidate_graph();
+  return true;
+}
+
+// forces and energy at the state, then the start of each system's iteration
+void Handle::enqueue_cg_head(int max_iter, unsigned long long search, cudaStream_t st) {
+  cudaStream_t keep = stream;
+  stream = st;
+  launch_pass(PASS_FORCE, true, 0);
+  launch_se_reduce(d, st);
+  launch_cg_begin(d, cg, max_iter, search, st);
+  kernels += 5;
+  stream = keep;
+}
+
+// one line-search probe of every searching system: x_t, E(x_t), the next transition
+void Handle::enqueue_cg_probe(unsigned long long search, cudaStream_t st) {
+  cudaStream_t keep = stream;
+  stream = st;
+  launch_cg_probe(d, cg, st);
+  launch_pass(PASS_ENERGY_T, true, 0);
+  launch_se_reduce(d, st);
+  launch_cg_search(d, cg, search, st);
+  kernels += 4;
+  stream = keep;
+}
+
+// the chosen move (with the rebuild request through `cond` inside a graph)
+void Handle::enqueue_cg_move(unsigned long long cond, cudaStream_t st) {
+  Dev dd = d;
+  dd.cond = cond;
+  launch_cg_move(dd, cg, st);
+  kernels += 2;
+}
+
+// kCgChunk iterations as one graph: per iteration the head, the line search in a
+// WHILE node (switched on by the head, off by the search when no system probes
+// again), the move, and the rebuild chain in an IF node the move switches on.
+bool Handle::run_cg_graph(int max_iter) {
+  if (!use_conditional) return false;
+  if (!cg_exec || cg_key_iter != max_iter) {
+    if (cg_exec) cudaGraphExecDestroy(cg_exec);
+    cg_exec = nullptr;
+    cg_key_iter = -1;
+    if (!stream2 && !cuda_ok(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking), "stream"))
+      return false;
+    if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    long long k0 = kernels;
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < kCgChunk && e == cudaSuccess; k++) {
+      cudaGraphConditionalHandle hs, hr;
+      e = new_cond_handle(&hs, 0);
+      if (e != cudaSuccess) break;
+      enqueue_cg_head(max_iter, hs, stream);
+      e = add_cond_body(
+          hs, [&](cudaStream_t st2) { enqueue_cg_probe(hs, st2); return 4; },
+          cudaGraphCondTypeWhile);
+      if (e != cudaSuccess) break;
+      e = new_cond_handle(&hr, 0);
+      if (e != cudaSuccess) break;
+      enqueue_cg_move(hr, stream);
+      e = add_cond_body(hr, [&](cudaStream_t st2) {
+        launch_rebuild(d, false, d_tab, 0, st2);
+        return 12;
+      });
+    }
+    kernels = k0;
+    cudaGraph_t g = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(stream, &g);
+    cudaGraphExec_t ex = nullptr;
+    if (e == cudaSuccess && e2 == cudaSuccess) e = cudaGraphInstantiate(&ex, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    cg_exec = ex;
+    cg_key_iter = max_iter;
+  }
+  kernels += 7LL * kCgChunk;
+  return cuda_ok(cudaGraphLaunch(cg_exec, stream), "cg graph launch");
+}
+
+// The same iterations launched from the host, which reads the "searching" word
+// after every probe (the reference's host-driven line search).
+bool Handle::run_cg_eager(int max_iter) {
+  for (int k = 0; k < kCgChunk; k++) {
+    if (!cuda_ok(cudaMemsetAsync(cg.searching, 0, sizeof(int), stream), "cg flag")) return false;
+    enqueue_cg_head(max_iter, 0, stream);
+    for (;;) {
+      int searching = 0;
+      if (!cuda_ok(cudaMemcpyAsync(h_pinned + 2, cg.searching, sizeof(int),
+                                   cudaMemcpyDeviceToHost, stream), "cg flag") ||
+          !cuda_ok(cudaStreamSynchronize(stream), "cg flag"))
+        return false;
+      searching = h_pinned[2];
+      if (!searching) break;
+      enqueue_cg_probe(0, stream);
+    }
+    enqueue_cg_move(0, stream);
+    launch_rebuild(d, false, d_tab, 0, stream);
+    kernels += 12;
+  }
+  return cuda_ok(cudaGetLastError(), "cg launch");
+}
+
+// Conjugate gradient on every system until each stops by the reference's rules
+// (zero force, three equal energies, no lower energy along any direction) or has
+// taken max_iter iterations; the host reads the per-system state between chunks.
+int Handle::cg_minimize(int max_iter, int* iters, double* energy, int* reason) {
+  if (max_iter < 0) {
+    fail(SC_E_ARG, "cg: max_iter must be >= 0");
+    return SC_E_ARG;
+  }
+  if (prec != PREC_FP64) {
+    fail(SC_E_STATE, "cg: the conjugate-gradient minimiser runs in the FP64 form");
+    return SC_E_STATE;
+  }
+  cudaSetDevice(device);
+  if (!ensure_cg()) return last_status;
+  // rows at fixed gamma and box; the probes' energy pass reads the corrector fields
+  std::vector<StepScalars> rows(nsys);
+  for (int s = 0; s < nsys; s++) {
+    StepScalars t = row_current(s);
+    t.gamma_c = t.gamma_p;
+    t.Lx_c = t.Lx_p;
+    t.Ly_c = t.Ly_p;
+    t.W_c = t.W_p;
+    t.H_c = t.H_p;
+    rows[s] = t;
+  }
+  if (!upload_table(rows)) return last_status;
+  launch_cg_reset(d, cg, stream);
+  std::vector<CgSys> hsys(nsys);
+  bool all_done = false;
+  while (!all_done) {
+    if (!(opt.use_graphs && run_cg_graph(max_iter)) && !run_cg_eager(max_iter))
+      return last_status;
+    if (!cuda_ok(cudaGetLastError(), "cg launch") ||
+        !cuda_ok(cudaMemcpyAsync(hsys.data(), cg.sys, nsys * sizeof(CgSys),
+                                 cudaMemcpyDeviceToHost, stream), "cg state") ||
+        !check_status("cg"))
+      return last_status;
+    all_done = true;
+    for (auto& q : hsys) all_done = all_done && q.done;
+  }
+  pred_valid = false;
+  forces_valid = false;
+  bool capped = false;
+  for (int s = 0; s < nsys; s++) {
+    if (iters) iters[s] = hsys[s].iters;
+    if (energy) energy[s] = hsys[s].E0;
+    if (reason) reason[s] = hsys[s].reason;
+    capped = capped || hsys[s].reason == CG_MAX_ITER;
+  }
+  return capped ? SC_E_NOCONV : SC_OK;
 }
 
 // Box and positions of each system scaled by factor[s] (1 leaves it alone).

@@ -162,7 +162,9 @@ struct Handle {
   cudaError_t capture_rebuild_node(int row, const std::function<int(cudaStream_t)>& body);
   cudaError_t new_cond_handle(cudaGraphConditionalHandle* h);
   cudaError_t add_cond_body(cudaGraphConditionalHandle h,
-                            const std::function<int(cudaStream_t)>& body);
+                            const std::function<int(cudaStream_t)>& body,
+                            cudaGraphConditionalNodeType type = cudaGraphCondTypeIf);
+  cudaError_t new_cond_handle(cudaGraphConditionalHandle* h, unsigned int dflt);
   unsigned long long step_cond = 0;  // rebuild node of the step being captured
   bool capture_conditional(bool resize, int nsteps, const std::vector<char>& se,
                            cudaGraph_t* out);
@@ -187,6 +189,18 @@ struct Handle {
   int fire_minimize(double ftol, int max_iter, double dt0, double dt_max, int* iters,
                     double* fmax_out, int* done_out);
   int affine_scale(const std::vector<double>& factor);
+  // Polak-Ribiere conjugate gradient with the reference's line search
+  CgState cg{};
+  static constexpr int kCgChunk = 10;  // iterations per captured graph
+  cudaGraphExec_t cg_exec = nullptr;
+  int cg_key_iter = -1;
+  bool ensure_cg();
+  void enqueue_cg_head(int max_iter, unsigned long long search, cudaStream_t st);
+  void enqueue_cg_probe(unsigned long long search, cudaStream_t st);
+  void enqueue_cg_move(unsigned long long cond, cudaStream_t st);
+  bool run_cg_graph(int max_iter);
+  bool run_cg_eager(int max_iter);
+  int cg_minimize(int max_iter, int* iters, double* energy, int* reason);
   int flip_shear(const std::vector<char>& sel);
   int rotate_shear(const std::vector<char>& sel);
   int quasistatic(double dphi, double ftol, double e_jam, int max_inc, int max_iter,

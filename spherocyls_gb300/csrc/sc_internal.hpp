@@ -73,6 +73,30 @@ struct FireState {
   double* part;   // [4 * npchunks] chunk partials
 };
 
+// Conjugate-gradient minimiser state of one system (the reference's line-search
+// energies h_pdLineEnergy[0..4], step bounds and the search position as data)
+enum CgPhase { CG_IDLE = 0, CG_TOP = 1, CG_SECOND = 2, CG_HALVE = 3, CG_DOUBLE = 4,
+               CG_FINAL = 5, CG_MOVE = 6 };
+enum CgReason { CG_RUNNING = 0, CG_ZERO_FORCE = 1, CG_STALLED = 2, CG_STEP = 3,
+                CG_MAX_ITER = 4 };
+struct CgSys {
+  double E0, E1, E2;     // energies at 0, one step and two steps along D
+  double Eh1, Eh2;       // iteration-start energies of the two iterations before
+  double F2, beta;       // |F|^2 and the Polak-Ribiere beta of this iteration
+  double norm;           // |F|_rms = sqrt(|F|^2 / 3N)
+  double step, min_step, max_step;
+  double t, tmin;        // position of the next probe; the chosen multiple of step
+  int phase, attempt;    // CgPhase; 0 PR direction, 1 steepest descent, 2 sqrt-scaled
+  int redirect;          // the next probe first sets D (1: F, 2: F/sqrt|F|)
+  int done, reason, iters;
+};
+
+struct CgState {
+  CgSys* sys;      // [nsys]
+  double* part;    // [3 * npchunks] chunk partials of |F|^2, F.F0, |F0|^2
+  int* searching;  // any system probing (for the host-driven loop)
+};
+
 // Device pointers handed to every kernel by value.
 struct Dev {
   int ntot, nsys, ncells, nchunks, npchunks;
@@ -148,9 +172,12 @@ struct Dev {
   const int* pchunk_p0;
   const int* pchunk_np;
   // flags
-  double* fvx;              // FIRE velocities (null until the minimiser is used);
-  double* fvy;              // permuted with the particles by the rebuild
-  double* fvp;
+  double* fvx;              // FIRE velocities or CG directions (null until a
+  double* fvy;              // minimiser is used); permuted with the particles by
+  double* fvp;              // the rebuild
+  double* cg0x;             // CG: the previous iteration's forces (null until CG is
+  double* cg0y;             // used), permuted with the particles by the rebuild
+  double* cg0p;
   int* flags;               // [nsys] bit0 moved-rebuild, bit1 forced rebuild
   int* istar;               // [nsys] lowest particle index that triggered a rebuild
   int* any;                 // [1] set when any system needs a rebuild
@@ -183,7 +210,9 @@ enum PassMode {
   PASS_PRED_STRAIN = 2,  // forces at the state + predictor for the next step (shear)
   PASS_CORR_RESIZE = 3,  // forces at the predictor copy + corrector (affine resize,
                          // or pure shear when the row's mode is 3)
-  PASS_PRED_RESIZE = 4   // forces at the state + predictor (affine resize or pure shear)
+  PASS_PRED_RESIZE = 4,  // forces at the state + predictor (affine resize or pure shear)
+  PASS_ENERGY_T = 5      // energy (stress partials) at the predictor copy, nothing stored
+                         // else (line-search probes of the conjugate-gradient minimiser)
 };
 
 // ---- kernel launchers (defined in the .cu files) ----
@@ -204,6 +233,13 @@ void launch_gd_update(const Dev& d, bool mixed, const StepScalars* tab, int row,
 void launch_se_store(const Dev& d, double* dst, cudaStream_t st);
 // per-slot values back to input order: out[k * ntot + input index] (k = 0, 1, 2)
 void launch_unsort_state(const Dev& d, double* out, cudaStream_t st);
+void launch_cg_reset(const Dev& d, const CgState& c, cudaStream_t st);
+void launch_cg_begin(const Dev& d, const CgState& c, int max_iter, unsigned long long search,
+                     cudaStream_t st);
+void launch_cg_probe(const Dev& d, const CgState& c, cudaStream_t st);
+void launch_cg_search(const Dev& d, const CgState& c, unsigned long long search,
+                      cudaStream_t st);
+void launch_cg_move(const Dev& d, const CgState& c, cudaStream_t st);
 void launch_ingest(const Dev& d, const double* x, const double* y, const double* phi,
                    const double* R, const double* A, const int* sys_p0, const double* sys_L,
                    int* psys, cudaStream_t st);

@@ -90,8 +90,9 @@ __device__ __forceinline__ void flag_moved(const Dev& d, int s, int id, double2 
 template <int MODE, bool SE, bool TWO, bool FAST = false>
 __global__ void __launch_bounds__(128) k_pass64(Dev d, const StepScalars* __restrict__ tab,
                                                int row) {
-  constexpr bool kPred = (MODE == PASS_CORR_STRAIN || MODE == PASS_CORR_RESIZE);
-  if (kPred) mark_pending_rebuilds(d, tab, row);
+  constexpr bool kPred =
+      (MODE == PASS_CORR_STRAIN || MODE == PASS_CORR_RESIZE || MODE == PASS_ENERGY_T);
+  if (MODE == PASS_CORR_STRAIN || MODE == PASS_CORR_RESIZE) mark_pending_rebuilds(d, tab, row);
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.ntot) return;
   int s = d.psys[i];
@@ -359,6 +360,7 @@ void launch_pass_fp64(const Dev& d, int mode, bool se, const StepScalars* tab, i
       se ? launch_one<PASS_PRED_RESIZE, true>(d, tab, row, st)
          : launch_one<PASS_PRED_RESIZE, false>(d, tab, row, st);
       break;
+    case PASS_ENERGY_T: launch_one<PASS_ENERGY_T, true>(d, tab, row, st); break;
   }
 }
 
