@@ -63,6 +63,8 @@ def bytes_per_pass(precision: str, nbar: float) -> float:
 # predictor and corrector launches in one ncu capture of the default workload
 # (profiles/k_pass_mixed_n1048576.md: 108.7 and 167.6 MB per launch at N = 2^20,
 # padding 0.4).
+REF_PI = 3.14159265358979  # the reference's pi (src/cpp/spherocyl_box.cpp:12)
+
 PASS_DRAM_BYTES_PER_PARTICLE = {"shear_n1048576_phi084": 138.17e6 / (1 << 20)}
 
 
@@ -207,7 +209,9 @@ def minimise_leg(replicas=32, n=4096, max_iter=20000, ftol=1e-14, device=0, e_ja
     compressed by one more
     1e-4 increment.  From that same state the two timed arms minimise to
     max|F_i|, |tau_i|/sqrt(I_i) < ftol: (a) mixed FIRE to 1e-6, then FP64 FIRE;
-    (b) FP64 FIRE alone.  Each FP64 stage stops after max_iter iterations."""
+    (b) FP64 FIRE alone; (c) the reference's conjugate gradient (FP64) on one replica
+    of each aspect ratio, stopped by the reference's rules.  Each FP64 stage stops
+    after max_iter iterations."""
     from spherocyls_gb300 import BoxBatch, generate_packing
 
     aors = [0.25, 0.5, 1.0, 2.0]
@@ -247,6 +251,25 @@ def minimise_leg(replicas=32, n=4096, max_iter=20000, ftol=1e-14, device=0, e_ja
     tc, ic, fc, dc = run(p, ftol, max_iter)
     e_c = p.calc_se()[:, 0]
     p.close()
+    # (c) the reference's conjugate gradient (FP64, on the device) from the same start
+    # on one replica of each aspect ratio (its line search evaluates the energy some
+    # tens of times per iteration), stopped by its own rules; residual as for FIRE
+    sub = sorted({(k * replicas) // 4 for k in range(4)})
+    sel = np.concatenate([np.arange(k * n, (k + 1) * n) for k in sub])
+    q = BoxBatch([n] * len(sub), L1[sub], x1[sel], y1[sel], ps[sel], A[sel], R[sel], 0.1,
+                 precision="fp64", **kw)
+    t = time.perf_counter()
+    cit, ce, cwhy = q.cg_minimize(max_iter)
+    tcg = time.perf_counter() - t
+    q.calc_forces()
+    qfx, qfy, qtq = q.forces()
+    q.close()
+    Rs, As = R[sel], A[sel]
+    al = As / Rs
+    C = 3 * REF_PI + 24 * al + 6 * REF_PI * al ** 2 + 8 * al ** 3
+    inertia = Rs ** 4 * C / (6 * Rs * (REF_PI * Rs + 4 * As))
+    res = np.maximum(np.hypot(qfx, qfy), np.abs(qtq) / np.sqrt(inertia)).reshape(len(sub), n)
+    cres = res.max(axis=1)
     # jammed replicas (E/N > 1e-16 at the FP64 minimum) that both arms converged
     both = da & db & dc & (e_c > 1e-16) & (e_a > 1e-16)
     return {
@@ -258,6 +281,13 @@ def minimise_leg(replicas=32, n=4096, max_iter=20000, ftol=1e-14, device=0, e_ja
                             "max_residual": float(fb.max())},
         "fp64": {"seconds": tc, "iters": ic, "converged": int(dc.sum()),
                  "max_residual": float(fc.max())},
+        "cg_fp64": {"replicas": len(sub), "seconds": tcg, "iters_max": int(cit.max()),
+                    "iters_mean": float(cit.mean()),
+                    "stop_reasons": {str(k): int((cwhy == k).sum()) for k in (1, 2, 3, 4)},
+                    "below_ftol": int((cres < ftol).sum()), "max_residual": float(cres.max()),
+                    "note": "the reference's Polak-Ribiere CG and line search, stopped by its "
+                            "rules (1 zero force, 2 three equal energies, 3 no lower energy, "
+                            "4 max_iter)"},
         "speedup": tc / (ta + tb),
         "energy_rel_diff_max": (float(np.max(np.abs(e_a[both] - e_c[both]) / e_c[both]))
                                 if both.any() else None),
