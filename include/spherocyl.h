@@ -238,6 +238,18 @@ int sc_generate_packing(int n, double packing, double a_over_r, double r_small, 
 #define SC_LAYOUT_GRID 1   /* one particle per grid cell, rows offset at random */
 #define SC_ANGLE_RANDOM 0  /* u uniform in [angle_min, angle_max] */
 #define SC_ANGLE_EVEN 1    /* u = angle_min + (2i+1)(angle_max - angle_min)/(2n) */
+/* sc_generate_packing's packing (same shapes, box and rejection rule) placed on GPU
+ * `device` in rounds: every particle still to place draws from a counter-based hash
+ * of (seed, particle, round), and is redrawn while its spine comes closer than
+ * min_sep (R_i + R_j) to that of a lower-numbered particle (for large N; the host
+ * placement is sequential).  Deterministic for a seed, but not the host's sequence.
+ * min_sep = 1 gives zero-energy (contact-free) placement.  SC_E_ARG for a box of
+ * fewer than 3 reach-wide cells, SC_E_NOCONV past the placement's saturation. */
+int sc_generate_packing_device(int device, int n, double packing, double a_over_r,
+                               double r_small, double r_ratio, uint64_t seed, double min_sep,
+                               double *x, double *y, double *phi, double *R, double *A,
+                               double *L);
+
 typedef struct sc_gen_options {
   int layout;         /* SC_LAYOUT_* */
   int angle_mode;     /* SC_ANGLE_*; angle_min == angle_max gives aligned particles */

@@ -112,6 +112,10 @@ SIGNATURES = [
     ("sc_generate_config", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                           ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
                                           _dp, _dp, _dp, _dp, _dp, _dp]),
+    ("sc_generate_packing_device", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                                  ctypes.c_double, ctypes.c_double,
+                                                  ctypes.c_double, ctypes.c_uint64,
+                                                  ctypes.c_double, _dp, _dp, _dp, _dp, _dp, _dp]),
     ("sc_generate_config_rect", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double,
                                                ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                                ctypes.c_double, ctypes.c_uint64, _dp, _dp, _dp,

@@ -41,6 +41,22 @@ def generate_packing(n: int, packing: float, a_over_r: float, r_small: float = 0
     return L.value, x, y, p, R, A
 
 
+def generate_packing_device(n: int, packing: float, a_over_r: float, r_small: float = 0.5,
+                            r_ratio: float = 1.4, seed: int = 0, min_sep: float = 0.1,
+                            device: int = 0):
+    """generate_packing's packing placed on the GPU (for large N): returns
+    (L, x, y, phi, R, A); deterministic for a seed, a different sequence."""
+    x, y, p, R, A = (np.empty(n) for _ in range(5))
+    L = ctypes.c_double()
+    st = lib().sc_generate_packing_device(int(device), int(n), float(packing), float(a_over_r),
+                                          float(r_small), float(r_ratio),
+                                          ctypes.c_uint64(int(seed)), float(min_sep), _ptr(x),
+                                          _ptr(y), _ptr(p), _ptr(R), _ptr(A), ctypes.byref(L))
+    if st != 0:
+        raise _lib.ScError(st, "device packing generation failed")
+    return L.value, x, y, p, R, A
+
+
 def generate_config(n: int, packing: float, a_over_r: float, *, layout: str = "random",
                     angles: str = "random", angle_range=(0.0, 1.0), shear_angles: bool = False,
                     min_sep: float = 0.1, max_overlap: float = -1.0, a_sigma: float = 0.0,

@@ -30,6 +30,7 @@ CU_UNITS = {
     "sc_noalloc.cu": False,
     "sc_fire.cu": True,
     "sc_cg.cu": False,
+    "sc_gen_device.cu": False,
 }
 CPP_UNITS = ["sc_host.cpp", "sc_api.cpp", "sc_generate.cpp", "sc_io.cpp"]
 CLI_UNITS = {
