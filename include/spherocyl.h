@@ -125,6 +125,12 @@ int sc_calc_se(sc_handle *h, double *se_out);
  * src/cpp/strain_dynamics.cpp:179-235 and :285-296).  When se_every > 0 and
  * se_out != NULL, se_out receives (nsteps/se_every) records of 5*n_sys values. */
 int sc_strain_steps(sc_handle *h, int nsteps, int se_every, double *se_out);
+/* Shear without setting gamma back until gamma >= gamma_max (run_strain(dGammaMax),
+ * src/cuda/strain_dynamics.cu:1097-1108, the strain driver's shear-direction change
+ * 3 before rotate_by_gamma), on cells 2 sqrt(1 + gamma_max^2)(R_max + A_max) + pad
+ * wide, which the handle keeps.  One system per handle; *steps receives the steps
+ * taken. */
+int sc_strain_to_gamma(sc_handle *h, double gamma_max, long *steps);
 /* nsteps Heun steps with affine resize by (1-rate)^dt per step (shrink != 0) or its
  * inverse (resize_step + calc_forces, src/cpp/resize_dynamics.cpp:164-243, :297-307). */
 int sc_resize_steps(sc_handle *h, int nsteps, int shrink, int se_every, double *se_out);
@@ -283,7 +289,8 @@ int sc_generate_config_rect(const sc_gen_options *opt, int n, double packing, do
  * hdr[0..6] = Lx Ly packing gamma gamma_total rate dt. */
 int sc_read_positions(const char *path, int *n, double *hdr, double *x, double *y, double *phi,
                       double *R, double *A);
-/* save_positions: SC_FMT_SP as src/cpp/spherocyl_box.cpp:410-423 (precision 14),
+/* save_positions: SC_FMT_SP as src/cpp/spherocyl_box.cpp:410-423 (precision 14; a
+ * rectangular box gets the src/cuda header's Lx and Ly),
  * SC_FMT_SD as src/cuda/strain_dynamics.cu:820-843 (%.17g rows), SC_FMT_BIN as
  * src/cuda/strain_dynamics.cu:845-875 (host byte order).  sc_read_positions reads a
  * path ending in ".bin" as SC_FMT_BIN, one ending in ".gz" as gzip-compressed text

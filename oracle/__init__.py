@@ -96,6 +96,7 @@ class _Lib:
             self.run_pure_steps = fn("run_pure_steps", ctypes.c_int, [handle, ctypes.c_int, _dp])
             self.cg_minimize = fn("cg_minimize", ctypes.c_int,
                                   [handle, ctypes.c_int, _ip, _dp, _ip])
+            self.strain_to_gamma = fn("strain_to_gamma", ctypes.c_long, [handle, ctypes.c_double])
         self.n = fn("n", ctypes.c_int, [handle])
         self.get_state = fn("get_state", None, [handle, _dp, _dp, _dp])
         self.get_forces = fn("get_forces", None, [handle, _dp, _dp, _dp])
@@ -223,6 +224,12 @@ class _BoxBase:
         if rc != 0:
             raise RuntimeError("oracle pure-shear run failed")
         return out
+
+    def strain_to_gamma(self, gamma_max: float) -> int:
+        k = self._L.strain_to_gamma(self.h, float(gamma_max))
+        if k < 0:
+            raise RuntimeError("oracle strain_to_gamma failed")
+        return k
 
     def cg_minimize(self, max_iter: int):
         """(iterations, energy, stop reason) of the conjugate-gradient restatement."""

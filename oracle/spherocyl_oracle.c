@@ -69,6 +69,9 @@ struct orc_box {
   long n_rebuilds;
   int err;
   int two_point; /* contact model: 0 one point (src/cpp), 1 two points (src/cuda 2p) */
+  double wfac;   /* cell width over Rmax + Amax: 2.24 (src/cpp), 2 sqrt(1 + g^2) for a run
+                  * to gamma g (src/cuda/spherocyl_box.cpp:132-144) */
+  int no_setback; /* shear past gamma = 1/2 (run_strain(dGammaMax)) */
 };
 
 /* ---- per-particle constants and wrap: set_particle, spherocyl_box.cpp:188-221 ---- */
@@ -107,7 +110,7 @@ static double packing_fraction(const orc_box *b) {
 
 /* ---- cell grid: configure_cells, spherocyl_box.cpp:223-268 ---- */
 static int configure_cells(orc_box *b) {
-  double wmin = 2.24 * (b->Rmax + b->Amax) + b->pad;
+  double wmin = (b->wfac > 0 ? b->wfac : 2.24) * (b->Rmax + b->Amax) + b->pad;
   double hmin = 2 * (b->Rmax + b->Amax) + b->pad;
   int rows = (int)(b->Ly / hmin);
   int cols = (int)(b->Lx / wmin);
@@ -504,8 +507,29 @@ int orc_strain_step(orc_box *b) {
   free(fx0);
   b->gamma += b->strain_rate * b->step;
   b->gamma_total += b->strain_rate * b->step;
-  if (b->gamma >= 0.5) set_back_gamma(b);
+  if (b->gamma >= 0.5 && !b->no_setback) set_back_gamma(b);
   return b->err ? -1 : 0;
+}
+
+/* run_strain(dGammaMax), src/cuda/strain_dynamics.cu:1097-1108: cells for gamma up
+ * to gamma_max, then strain steps (each followed by calc_forces) without set-back
+ * until gamma >= gamma_max.  Returns the steps taken. */
+long orc_strain_to_gamma(orc_box *b, double gamma_max) {
+  double w = 2 * sqrt(gamma_max * gamma_max + 1);
+  if (w > (b->wfac > 0 ? b->wfac : 2.24)) {
+    b->wfac = w;
+    if (configure_cells(b)) return -1;
+    find_neighbors(b);
+  }
+  b->no_setback = 1;
+  long k = 0;
+  while (b->gamma < gamma_max) {
+    if (orc_strain_step(b)) break;
+    orc_calc_forces(b);
+    k++;
+  }
+  b->no_setback = 0;
+  return b->err ? -1 : k;
 }
 
 /* reconfigure_cells, resize_dynamics.cpp:106-121 (note the reference pairs the

@@ -32,6 +32,7 @@ void orc_find_neighbors(orc_box *b);
 void orc_calc_forces(orc_box *b);
 void orc_calc_se(orc_box *b);
 int orc_strain_step(orc_box *b);
+long orc_strain_to_gamma(orc_box *b, double gamma_max);
 int orc_resize_step(orc_box *b, int shrink);
 int orc_gd_step(orc_box *b);
 int orc_pure_step(orc_box *b);

@@ -81,6 +81,7 @@ SIGNATURES = [
     ("sc_strain_steps", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp]),
     ("sc_resize_steps", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp]),
     ("sc_pure_strain_steps", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp]),
+    ("sc_strain_to_gamma", ctypes.c_int, [_vp, ctypes.c_double, ctypes.POINTER(ctypes.c_long)]),
     ("sc_trim_memory", ctypes.c_int, [ctypes.c_int]),
     ("sc_gd_minimize", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double, _ip, _dp]),
     ("sc_cg_minimize", ctypes.c_int, [_vp, ctypes.c_int, _ip, _dp, _ip]),

@@ -255,6 +255,13 @@ class BoxBatch:
                                         _ptr(out) if out is not None else None))
         return out
 
+    def strain_to_gamma(self, gamma_max: float) -> int:
+        """Shear without setting gamma back until gamma >= gamma_max (run_strain
+        (dGammaMax), src/cuda/strain_dynamics.cu:1097-1108); returns the steps."""
+        k = ctypes.c_long()
+        self._chk(lib().sc_strain_to_gamma(self.h, float(gamma_max), ctypes.byref(k)))
+        return k.value
+
     def pure_strain_steps(self, nsteps: int, se_every: int = 0):
         """Pure shear at each system's strain rate (pure_strain_step_2p,
         src/cuda/2point_dynamics.cu:2180-2283): x stretched, y compressed."""

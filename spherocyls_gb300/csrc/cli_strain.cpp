@@ -3,12 +3,13 @@
 // Arguments in the order of input/input_key.txt:7-22 (the src/cuda driver's order,
 // src/cuda/main.cpp:63-125): data file or "r", output directory, N, strain rate,
 // step, run length (strain), position save interval (strain), stress save interval
-// (strain), cell padding, shear-direction change (0: none, 1: reverse, 2: rotate;
-// 3, a run before the rotation, is not supported), and for "r": packing fraction, aspect ratio
-// A/R (R1 = 0.5), bidispersity R2/R1, then optionally the initial configuration
-// code (0-9) and the aspect-ratio spread (see cli::random_start).  SC_PRECISION=mixed selects
-// the mixed form, SC_OUTPUT_FORMAT=sd the src/cuda file layout, SC_SEED the seed of
-// the random configuration.
+// (strain), cell padding, shear-direction change (0: none, 1: reverse, 2: rotate, 3:
+// shear to a maximum gamma without set-back, then rotate), and for "r": packing
+// fraction, aspect ratio A/R (R1 = 0.5), bidispersity R2/R1, then optionally the
+// initial configuration code (0-9) and the aspect-ratio spread (see
+// cli::random_start); for change 3 the maximum gamma comes last (main.cpp:269-275).
+// SC_PRECISION=mixed selects the mixed form, SC_OUTPUT_FORMAT=sd the src/cuda file
+// layout, SC_SEED the seed of the random configuration.
 #include <chrono>
 #include <vector>
 
@@ -25,9 +26,10 @@ int main(int argc, char** argv) {
   double pos_save = a.f("Position data save rate");
   double se_save = a.f("Stress data save rate");
   double pad = a.f("Cell padding");
-  int flip = a.i("Change shear direction (0: no, 1: reverse)");
-  if (flip < 0 || flip > 2) {
-    std::cerr << "shear-direction change must be 0, 1 (reverse) or 2 (rotate)" << std::endl;
+  int flip = a.i("Change shear direction (1 to reverse, 2 to rotate by gamma, 3 to increase "
+                  "gamma and rotate)");
+  if (flip < 0 || flip > 3) {
+    std::cerr << "shear-direction change must be 0, 1 (reverse), 2 (rotate) or 3" << std::endl;
     return 1;
   }
   std::vector<double> x, y, p, R, A;
@@ -71,8 +73,14 @@ int main(int argc, char** argv) {
   if ((rc = sc_set_strain_rate(h, -1, rate)) || (rc = sc_set_step(h, -1, dt)) ||
       (rc = sc_set_gamma(h, -1, gamma)) || (rc = sc_set_total_gamma(h, -1, gamma_total)))
     return cli::fail("setup", rc, h);
-  if (flip == 1 || flip == 2) {
-    // main.cpp:258-267: total strain restarts from zero in the new direction
+  if (flip == 3) {
+    // main.cpp:269-275: shear to the maximum gamma first
+    double gmax = a.f("Max gamma to shear before rotation");
+    long k = 0;
+    if ((rc = sc_strain_to_gamma(h, gmax, &k))) return cli::fail("shear to gamma", rc, h);
+  }
+  if (flip >= 1) {
+    // main.cpp:258-275: total strain restarts from zero in the new direction
     if ((rc = sc_set_total_gamma(h, -1, 0.0)) ||
         (rc = flip == 1 ? sc_flip_shear(h, -1) : sc_rotate_shear(h, -1)))
       return cli::fail("shear direction", rc, h);

@@ -605,6 +605,11 @@ int sc_fire_minimize(sc_handle* H, double ftol, int max_iter, double dt0, double
   return H->h.fire_minimize(ftol, max_iter, dt0, dt_max, iters, fmax, done);
 }
 
+int sc_strain_to_gamma(sc_handle* H, double gamma_max, long* steps) {
+  if (!H) return SC_E_ARG;
+  return H->h.strain_to_gamma(gamma_max, steps);
+}
+
 int sc_cg_minimize(sc_handle* H, int max_iter, int* iters, double* energy, int* reason) {
   if (!H) return SC_E_ARG;
   return H->h.cg_minimize(max_iter, iters, energy, reason);

@@ -107,7 +107,7 @@ Handle::~Handle() {
 
 // configure_cells, src/cpp/spherocyl_box.cpp:223-241
 void HostSys::configure(bool set_pad) {
-  double wmin = 2.24 * (Rmax + Amax) + pad;
+  double wmin = wfac * (Rmax + Amax) + pad;
   double hmin = 2 * (Rmax + Amax) + pad;
   rows = std::max(static_cast<int>(Ly / hmin), 1);
   cols = std::max(static_cast<int>(Lx / wmin), 1);
@@ -117,7 +117,7 @@ void HostSys::configure(bool set_pad) {
 // reconfigure_cells' test, src/cpp/resize_dynamics.cpp:106-121 (rows from Lx,
 // columns from Ly, as written there)
 bool HostSys::grid_changes(double Lx_now, double Ly_now) const {
-  double wmin = 2.24 * (Rmax + Amax) + pad;
+  double wmin = wfac * (Rmax + Amax) + pad;
   double hmin = 2 * (Rmax + Amax) + pad;
   int r = std::max(static_cast<int>(Lx_now / hmin), 1);
   int c = std::max(static_cast<int>(Ly_now / wmin), 1);
@@ -128,7 +128,7 @@ bool HostSys::grid_changes(double Lx_now, double Ly_now) const {
 // orientation), for boxes whose two sides change differently
 // (reconfigure_cells(0.0) in pure_strain_step_2p, src/cuda/spherocyl_box.cpp:46-67).
 bool HostSys::grid_changes_xy(double Lx_now, double Ly_now) const {
-  double wmin = 2.24 * (Rmax + Amax) + pad;
+  double wmin = wfac * (Rmax + Amax) + pad;
   double hmin = 2 * (Rmax + Amax) + pad;
   int r = std::max(static_cast<int>(Ly_now / hmin), 1);
   int c = std::max(static_cast<int>(Lx_now / wmin), 1);
@@ -715,7 +715,7 @@ static void advance(HostSys& h, int kind, int shrink, StepScalars& t) {
     // set_back_gamma at gamma >= 1/2 (src/cpp); for a rectangular box the image
     // offset Lx/Ly takes the place of 1 (src/cuda/strain_dynamics.cu:712-713)
     const double r = h.Lx / h.Ly;
-    if (h.gamma >= 0.5 * r) {
+    if (h.setback && h.gamma >= 0.5 * r) {
       h.gamma -= r;
       h.gamma_total = static_cast<int>(h.gamma_total + 1) + h.gamma;
       t.setback = 1;
@@ -1310,6 +1310,48 @@ int Handle::rotate_shear(const std::vector<char>& sel) {
   dfree(dq);
   if (!ok) return last_status;
   return layout_cells() && rebuild_all() && check_status("rotate shear") ? SC_OK : last_status;
+}
+
+// run_strain(dGammaMax), src/cuda/strain_dynamics.cu:1097-1108: shear without
+// setting gamma back until gamma >= gamma_max (no output), on a cell grid wide
+// enough for that gamma (reconfigure_cells(dGammaMax), src/cuda/spherocyl_box.cpp:
+// 46-67); the grid keeps that width afterwards.  One system per handle.
+int Handle::strain_to_gamma(double gamma_max, long* steps_out) {
+  if (nsys != 1) {
+    fail(SC_E_ARG, "sc_strain_to_gamma: one system per handle");
+    return SC_E_ARG;
+  }
+  HostSys& S = hs[0];
+  if (!(S.strain_rate > 0) || !(S.step > 0) || !std::isfinite(gamma_max)) {
+    fail(SC_E_ARG, "sc_strain_to_gamma: needs a positive strain rate and step");
+    return SC_E_ARG;
+  }
+  // the steps the loop takes, with the host mirror's own accumulation
+  long k = 0;
+  for (double g = S.gamma; g < gamma_max; g += S.strain_rate * S.step)
+    if (++k > (1L << 31)) {
+      fail(SC_E_ARG, "sc_strain_to_gamma: too many steps");
+      return SC_E_ARG;
+    }
+  if (steps_out) *steps_out = k;
+  if (k == 0) return SC_OK;
+  cudaSetDevice(device);
+  const double w = 2 * std::sqrt(gamma_max * gamma_max + 1);
+  if (w > S.wfac) {
+    if (!materialize()) return last_status;
+    S.wfac = w;
+    S.configure(false);
+    if (!layout_cells() || !rebuild_all()) return last_status;
+  }
+  S.setback = false;
+  int rc = SC_OK;
+  for (long done = 0; done < k && rc == SC_OK;) {
+    const int chunk = (int)std::min<long>(k - done, 1L << 20);
+    rc = run_steps(KIND_STRAIN, 0, chunk, 0, nullptr);
+    done += chunk;
+  }
+  hs[0].setback = true;
+  return rc;
 }
 
 // Quasistatic compression to jamming: affine steps of dphi in packing fraction,

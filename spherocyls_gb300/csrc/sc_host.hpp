@@ -25,6 +25,11 @@ struct HostSys {
   double packing = 0;
   int rows = 1, cols = 1;
   int c0 = 0, chunk0 = 0, nchunks = 0;
+  // cell width over R_max + A_max (configure_cells, src/cpp/spherocyl_box.cpp:225:
+  // 2.24, enough for |gamma| <= 1/2; 2 sqrt(1 + gamma^2) for a run to larger gamma,
+  // src/cuda/spherocyl_box.cpp:132-144) and whether gamma is set back at 1/2
+  double wfac = 2.24;
+  bool setback = true;
 
   void configure(bool set_pad);
   bool grid_changes(double Lx_now, double Ly_now) const;
@@ -203,6 +208,7 @@ struct Handle {
   int cg_minimize(int max_iter, int* iters, double* energy, int* reason);
   int flip_shear(const std::vector<char>& sel);
   int rotate_shear(const std::vector<char>& sel);
+  int strain_to_gamma(double gamma_max, long* steps);
   int quasistatic(double dphi, double ftol, double e_jam, int max_inc, int max_iter,
                   double* phi_jam, int* n_inc);
   int find_jam(double e_jam, double step0, double min_step, double ftol, int max_iter,

@@ -288,8 +288,12 @@ int sc_save_positions(sc_handle* H, int sys, const char* path, int format) {
   std::ofstream o(path);
   if (!o) return io_fail(&h, SC_E_IO, std::string("cannot open ") + path);
   o.precision(14);
-  o << S.n << " " << S.Lx << " " << packing << " " << S.gamma << " " << S.gamma_total << " "
-    << S.strain_rate << " " << S.step << std::endl;
+  // the src/cpp header has one box length; a rectangular box (after a rotation or
+  // pure shear) takes the src/cuda header's two, which the reader tells by its length
+  o << S.n << " " << S.Lx << " ";
+  if (S.Ly != S.Lx) o << S.Ly << " ";
+  o << packing << " " << S.gamma << " " << S.gamma_total << " " << S.strain_rate << " " << S.step
+    << std::endl;
   for (int k = 0; k < S.n; k++)
     o << x[k] << " " << y[k] << " " << p[k] << " " << h.h_R[S.p0 + k] << " " << h.h_A[S.p0 + k]
       << std::endl;
