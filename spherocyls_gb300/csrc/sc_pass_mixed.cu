@@ -338,7 +338,7 @@ __global__ void k_mx_local(Dev d, const StepScalars* __restrict__ tab, int row, 
 }
 
 // The padded neighbour list in FP32 (see the file comment).
-__global__ void __launch_bounds__(128) k_mx_build_list(Dev d, const StepScalars* __restrict__ tab,
+__global__ void __launch_bounds__(128, 12) k_mx_build_list(Dev d, const StepScalars* __restrict__ tab,
                                                       int row, int all) {
   if (!all && *d.any == 0) return;
   for_slots(d, all != 0, [&](int i, int s) {
