@@ -96,7 +96,7 @@ struct Handle {
   // refilled before each launch) and leave their records in d_win_se: a graph 5x
   // shorter to capture and instantiate, reused for every sub-chunk with the same step
   // kind and the same steps recording stress/energy (se_mask).
-  static constexpr int kGraphSteps = 20;
+  static constexpr int kGraphSteps = 10;
   struct SubGraph {
     bool resize;
     unsigned se_mask;
