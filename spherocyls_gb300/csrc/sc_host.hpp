@@ -93,7 +93,7 @@ struct Handle {
   GraphKey graph_key{};
   // Chunks whose length is a multiple of kGraphSteps run as sub-chunk graphs of
   // kGraphSteps steps, which read their rows from a window of the step table (d_win,
-  // refilled before each launch) and leave their records in d_win_se: a graph 5x
+  // refilled before each launch) and leave their records in d_win_se: a graph 10x
   // shorter to capture and instantiate, reused for every sub-chunk with the same step
   // kind and the same steps recording stress/energy (se_mask).
   static constexpr int kGraphSteps = 10;
