@@ -114,19 +114,12 @@ void HostSys::configure(bool set_pad) {
   if (set_pad && pad == 0) pad = std::max(Lx / cols - wmin, Ly / rows - hmin);
 }
 
-// reconfigure_cells' test, src/cpp/resize_dynamics.cpp:106-121 (rows from Lx,
-// columns from Ly, as written there)
-bool HostSys::grid_changes(double Lx_now, double Ly_now) const {
-  double wmin = wfac * (Rmax + Amax) + pad;
-  double hmin = 2 * (Rmax + Amax) + pad;
-  int r = std::max(static_cast<int>(Lx_now / hmin), 1);
-  int c = std::max(static_cast<int>(Ly_now / wmin), 1);
-  return r != rows || c != cols;
-}
-
-// The same test with rows from Ly and columns from Lx (configure_cells' own
-// orientation), for boxes whose two sides change differently
-// (reconfigure_cells(0.0) in pure_strain_step_2p, src/cuda/spherocyl_box.cpp:46-67).
+// Whether the cell grid of the box (Lx_now, Ly_now) differs from the current one:
+// reconfigure_cells' test (src/cpp/resize_dynamics.cpp:106-121, which takes the rows
+// from Lx and the columns from Ly; the same for its square boxes) with rows from Ly
+// and columns from Lx, the orientation configure() builds, so that the test is
+// false right after a re-grid for rectangular boxes too (reconfigure_cells(0.0) of
+// pure_strain_step_2p, src/cuda/spherocyl_box.cpp:46-67, uses that orientation).
 bool HostSys::grid_changes_xy(double Lx_now, double Ly_now) const {
   double wmin = wfac * (Rmax + Amax) + pad;
   double hmin = 2 * (Rmax + Amax) + pad;
@@ -755,6 +748,7 @@ int Handle::run_steps(int kind, int shrink, int nsteps, int se_every, double* se
   int nrec_total = (se_every > 0) ? nsteps / se_every : 0;
   std::vector<double> se_host((size_t)nrec_total * nsys * 5);
   int done = 0, rec_done = 0;
+  bool regridded = false;  // the last pass of the loop re-gridded without stepping
   while (done < nsteps) {
     // chunk length: at most kChunk steps, a multiple of the recording period when
     // possible, and ending before any system's cell grid would change
@@ -770,9 +764,7 @@ int Handle::run_steps(int kind, int shrink, int nsteps, int se_every, double* se
       for (int k = 0; k < want; k++) {
         bool change = false;
         for (int s = 0; s < nsys; s++)
-          if (kind == KIND_PURE ? sim[s].grid_changes_xy(sim[s].Lx, sim[s].Ly)
-                                : sim[s].grid_changes(sim[s].Lx, sim[s].Ly))
-            change = true;
+          if (sim[s].grid_changes_xy(sim[s].Lx, sim[s].Ly)) change = true;
         if (change) {
           nk = k;
           regrid = true;
@@ -785,11 +777,19 @@ int Handle::run_steps(int kind, int shrink, int nsteps, int se_every, double* se
       // the grid changes before the next step: re-grid, rebuild, continue.  The
       // mixed form's positions are relative to the old grid's cell centres, so the
       // FP64 state is brought up to date before the grid changes.
+      if (regridded) {
+        // the new grid already matched the box: a second change means the test and
+        // the grid disagree, which would repeat for ever
+        fail(SC_E_STATE, "cell grid does not settle after a re-grid");
+        return SC_E_STATE;
+      }
       if (!materialize()) return last_status;
       for (int s = 0; s < nsys; s++) hs[s].configure(false);
       if (!layout_cells() || !rebuild_all()) return last_status;
+      regridded = true;
       continue;
     }
+    regridded = false;
     std::vector<HostSys> sim = hs;
     std::vector<StepScalars> rows((size_t)(nk + 1) * nsys);
     for (int s = 0; s < nsys; s++) {

@@ -32,7 +32,6 @@ struct HostSys {
   bool setback = true;
 
   void configure(bool set_pad);
-  bool grid_changes(double Lx_now, double Ly_now) const;
   bool grid_changes_xy(double Lx_now, double Ly_now) const;
 };
 
