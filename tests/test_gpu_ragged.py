@@ -65,3 +65,31 @@ def test_ragged_batch_matches_single_runs(sc, precision, kind):
         box = bb.box(s)
         assert box["Lx"] == sbox["Lx"] and box["Ly"] == sbox["Ly"] and box["gamma"] == sbox["gamma"]
         off += n
+
+
+@pytest.mark.parametrize("shrink", [True, False])
+def test_rectangular_resize_through_a_regrid(sc, shrink):
+    """A 1 x 2 box shrinks (or grows) through a change of its cell grid: the run ends,
+    the grid follows the box, the box lengths are the product of the step factors,
+    and the mixed form tracks the FP64 form."""
+    Lx, Ly, x, y, p, R, A = sc.generate_config_rect(3000, 0.70, 1.0, 0.5, seed=76)
+    rate, dt, steps = 1e-2, 0.02, 400  # lengths change by 8%: several row changes
+    out = []
+    for prec in ("fp64", "mixed"):
+        with sc.SpherocylBox(Lx, x, y, p, A, R, 0.1, Ly=Ly, precision=prec) as b:
+            g0 = b.box()
+            b.set_resize_rate(rate)
+            b.set_step(dt)
+            b.resize_steps(steps, shrink=shrink)
+            g1 = b.box()
+            out.append((np.array(b.state()), g0, g1, b.calc_se()[0]))
+    (sa, g0, ga, ea), (sb, _, gb, eb) = out
+    f = (1 - rate) ** dt
+    lx, ly = Lx, Ly
+    for _ in range(steps):
+        lx, ly = (lx * f, ly * f) if shrink else (lx / f, ly / f)
+    assert ga["Lx"] == gb["Lx"] == lx and ga["Ly"] == gb["Ly"] == ly
+    assert (ga["rows"], ga["cols"]) != (g0["rows"], g0["cols"])
+    hmin = 2 * (R.max() + A.max()) + ga["pad"]
+    assert ga["rows"] == max(int(ga["Ly"] / hmin), 1)
+    assert abs(ea - eb) <= 1e-3 * max(abs(ea), 1e-12)
