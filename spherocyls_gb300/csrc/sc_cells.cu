@@ -580,8 +580,9 @@ void launch_force_rebuild_all(const Dev& d, cudaStream_t st) { k_force_all<<<1, 
 
 void launch_clear_flags(const Dev& d, cudaStream_t st) { k_rb_clear<<<1, 256, 0, st>>>(d); }
 
-// Inside a captured step: mark the systems that set back gamma at this step and
-// switch the graph's conditional rebuild body on when any system needs a rebuild.
+// Inside a captured FIRE iteration: mark the systems that set back gamma at this row
+// and switch the graph's conditional rebuild body on when any system needs a
+// rebuild.  (The captured shear steps switch theirs from the corrector pass.)
 __global__ void k_pre_rebuild(Dev d, const StepScalars* __restrict__ tab, int row,
                               cudaGraphConditionalHandle cond) {
   __shared__ int need;

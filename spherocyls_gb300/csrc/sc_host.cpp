@@ -438,9 +438,6 @@ void Handle::invalidate_graph() {
   fire_key_iters = 0;
 }
 
-// Inside a capture on `stream`: k_pre_rebuild for table row `row`, then a
-// conditional IF node it switches on when any system needs a rebuild; `body`
-// enqueues the node's contents on stream2 and returns its kernel count.
 // A conditional handle on the graph being captured on `stream`, reset to 0 at
 // every launch of the graph.
 cudaError_t Handle::new_cond_handle(cudaGraphConditionalHandle* h) {
@@ -488,8 +485,10 @@ cudaError_t Handle::add_cond_body(cudaGraphConditionalHandle hcond,
   return cudaStreamEndCapture(stream2, &bg);
 }
 
-// Inside a capture on `stream`: k_pre_rebuild for table row `row` (systems that set
-// gamma back, or a pending rebuild), then the conditional node it switches on.
+// Inside a capture on `stream` (the FIRE iterations, whose update kernel does not
+// switch the node itself): k_pre_rebuild for table row `row` (systems that set gamma
+// back, or a pending rebuild), then the conditional node it switches on; `body`
+// enqueues the node's contents on stream2 and returns its kernel count.
 cudaError_t Handle::capture_rebuild_node(int row, const std::function<int(cudaStream_t)>& body) {
   cudaGraphConditionalHandle hcond;
   cudaError_t e = new_cond_handle(&hcond);
