@@ -196,8 +196,9 @@ int sc_rotate_shear(sc_handle *h, int sys);
 int sc_quasistatic_compress(sc_handle *h, double dphi, double ftol, double e_jam,
                             int max_increments, int max_iter, double *phi_jam, int *n_inc);
 /* find_jam_2p / resize_to_energy_2p (src/cuda/2point_dynamics.cu:4582-4606,
- * 4393-4456): per system, affine length steps of 1 -/+ step (growing by 1.1 per
- * step, FIRE to ftol after each) towards energy per particle e_jam, reversing with
+ * 4393-4456): per system, affine length factors 1 - step to compress and
+ * 1/(1 - step) to expand (resize_step_2p), the step growing by 1.1 per resize and
+ * FIRE to ftol after each, towards energy per particle e_jam, reversing with
  * half the last step each time the energy crosses e_jam, until the step is below
  * min_step or max_steps resizes were made.  phi_jam[s]: final packing fraction of
  * system s (negated when max_steps ran out first); *steps: resizes made. */
@@ -318,6 +319,16 @@ int sc_run_resize(sc_handle *h, const char *out_dir, double final_packing, doubl
  * used as its magnitude.  *t_end receives the final time. */
 int sc_run_pure_strain(sc_handle *h, const char *out_dir, double stop_aspect, double pos_save,
                        double se_save, unsigned long t_start, int format, unsigned long *t_end);
+/* find_jam_2p with output, src/cuda/2point_dynamics.cu:4393-4456, 4582-4606, for a
+ * one-system handle: the bisection of sc_find_jam (min_step 1e-15) towards e_jam
+ * given, as there, as calc_fe_2p's energy per unit area (E/N x N / 2LxLy); each
+ * resize relaxes with sc_cg_minimize(max_iter) in the FP64 form (cjpr_relax_2p) and
+ * FIRE to ftol in the mixed form.  Writes sd0000000000.dat, then per resize t a line
+ * "t packing E Pxx Pyy Pxy Pyx" (E per unit area) in sd_stress_energy.dat and
+ * sd%010d.dat, and the final state as sd%010d.bin.  *steps: resizes made; *phi_jam:
+ * final packing fraction (negated if the step limit of 10^6 resizes ran out). */
+int sc_run_find_jam(sc_handle *h, const char *out_dir, double e_jam, double step,
+                    double ftol, int max_iter, int *steps, double *phi_jam);
 /* gradient_descent_minimize with output, src/cpp/relaxation_dynamics.cpp:33-85 (SE
  * file sr_strain_se.dat, position files sr%010lu.dat every pos_save_n steps). */
 int sc_run_minimize(sc_handle *h, const char *out_dir, int max_steps, double e_min,

@@ -134,6 +134,8 @@ SIGNATURES = [
                                           ctypes.c_int, ctypes.POINTER(ctypes.c_ulong)]),
     ("sc_run_minimize", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_int, ctypes.c_double,
                                        ctypes.c_int, _ip]),
+    ("sc_run_find_jam", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_double, ctypes.c_double,
+                                       ctypes.c_double, ctypes.c_int, _ip, _dp]),
     ("sc_forces_noalloc", ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                          ctypes.c_double, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                          _vp]),

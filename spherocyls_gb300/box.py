@@ -383,6 +383,17 @@ class BoxBatch:
                                         int(pos_save_n), ctypes.byref(s)))
         return s.value
 
+    def run_find_jam(self, out_dir: str, e_jam: float, step: float, ftol: float = 1e-13,
+                     max_iter: int = 200000):
+        """find_jam_2p with its files; e_jam per unit area as there.  Returns
+        (packing fraction, resizes made)."""
+        s = ctypes.c_int()
+        phi = ctypes.c_double()
+        self._chk(lib().sc_run_find_jam(self.h, out_dir.encode(), float(e_jam), float(step),
+                                        float(ftol), int(max_iter), ctypes.byref(s),
+                                        ctypes.byref(phi)))
+        return phi.value, s.value
+
     # --- state ------------------------------------------------------------
     def state(self):
         x, y, p = (np.empty(self.ntot) for _ in range(3))

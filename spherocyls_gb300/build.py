@@ -38,6 +38,7 @@ CLI_UNITS = {
     "spherocyl_resize": "cli_resize.cpp",
     "spherocyl_minimize": "cli_minimize.cpp",
     "spherocyl_pure_shear": "cli_pure_shear.cpp",
+    "spherocyl_find_jam": "cli_find_jam.cpp",
 }
 
 

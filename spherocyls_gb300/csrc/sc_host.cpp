@@ -1396,12 +1396,16 @@ int Handle::quasistatic(double dphi, double ftol, double e_jam, int max_inc, int
 // Jamming point by bisection on the energy (find_jam_2p with resize_to_energy_2p,
 // src/cuda/2point_dynamics.cu:4582-4606, 4393-4456), per system: a phase
 // compresses while E/N < e_jam (expands while E/N > e_jam) by affine length steps
-// of 1 - step (1 + step), minimising after each and growing the step by 1.1 per
+// of 1 - step (1 / (1 - step)), minimising after each and growing the step by 1.1 per
 // step; once the energy has crossed e_jam the next phase starts the other way with
-// half the last step, until the step falls below min_step.  The reference compares
-// the total energy; here e_jam is an energy per particle.
+// half the last step, until the step falls below min_step.  e_jam is an energy per
+// particle, or with per_area the reference's measure (calc_fe_2p's energy per unit
+// area, E/N x N / 2LxLy); on_step sees each resize's stress/energy; cg_relax relaxes
+// with the conjugate gradient (cjpr_relax_2p) instead of FIRE.
 int Handle::find_jam(double e_jam, double step0, double min_step, double ftol, int max_iter,
-                     int max_steps, double* phi_jam, int* steps_out) {
+                     int max_steps, double* phi_jam, int* steps_out,
+                     const std::function<int(int, const double*)>& on_step, bool cg_relax,
+                     bool per_area) {
   if (!(e_jam > 0) || !(step0 > 0) || !(min_step > 0) || max_steps < 0) {
     fail(SC_E_ARG, "find_jam: need e_jam > 0, step > 0, min_step > 0, max_steps >= 0");
     return SC_E_ARG;
@@ -1414,12 +1418,23 @@ int Handle::find_jam(double e_jam, double step0, double min_step, double ftol, i
   };
   std::vector<Phase> ph(nsys);
   std::vector<double> se(5 * (size_t)nsys);
-  int rc = fire_minimize(ftol, max_iter, 1e-2, 0.2, nullptr, nullptr, nullptr);
+  // cjpr_relax_2p (the reference's relaxation here) or FIRE to ftol
+  auto relax = [&]() {
+    return cg_relax ? cg_minimize(max_iter, nullptr, nullptr, nullptr)
+                    : fire_minimize(ftol, max_iter, 1e-2, 0.2, nullptr, nullptr, nullptr);
+  };
+  // the compared energy: per particle, or calc_fe_2p's energy per unit area, which
+  // sums (1 - d/sigma)^2 / (4 Lx Ly) per contact side against (1 - d/sigma)^2 / 2N
+  auto energy = [&](int s) {
+    const HostSys& h = hs[s];
+    return per_area ? se[5 * s] * (double)h.n / (2.0 * h.Lx * h.Ly) : se[5 * s];
+  };
+  int rc = relax();
   if (rc && rc != SC_E_NOCONV) return rc;
   if ((rc = calc(true, se.data()))) return rc;
   auto start_phase = [&](int s, double step) {
     Phase& q = ph[s];
-    const double e = se[5 * s];
+    const double e = energy(s);
     // an energy exactly at e_jam makes every later phase empty (only the step
     // shrinks), so the system is finished where it is
     q.dir = e < e_jam ? 1 : (e > e_jam ? -1 : 0);
@@ -1435,20 +1450,24 @@ int Handle::find_jam(double e_jam, double step0, double min_step, double ftol, i
     bool any = false;
     for (int s = 0; s < nsys; s++)
       if (ph[s].dir != 0) {
-        f[s] = ph[s].dir > 0 ? 1.0 - ph[s].next : 1.0 + ph[s].next;
+        // resize_step_2p (src/cuda/2point_dynamics.cu:1187-1195): lengths x (1 - step)
+        // to compress, / (1 - step) to expand
+        f[s] = ph[s].dir > 0 ? 1.0 - ph[s].next : 1.0 / (1.0 - ph[s].next);
         any = true;
       }
     if (!any) break;
     if ((rc = affine_scale(f))) return rc;
-    rc = fire_minimize(ftol, max_iter, 1e-2, 0.2, nullptr, nullptr, nullptr);
+    rc = relax();
     if (rc && rc != SC_E_NOCONV) return rc;
     if ((rc = calc(true, se.data()))) return rc;
+    // each resize's output (resize_to_energy_2p writes a line and a file per step)
+    if (on_step && (rc = on_step(steps + 1, se.data()))) return rc;
     for (int s = 0; s < nsys; s++) {
       Phase& q = ph[s];
       if (q.dir == 0) continue;
       q.k += 1;
       q.next *= 1.1;
-      const double e = se[5 * s];
+      const double e = energy(s);
       const bool crossed = q.dir > 0 ? !(e < e_jam) : !(e > e_jam);
       if (!crossed) continue;
       // find_jam_2p: dResizeStep * 1.1^(steps in the phase - 1) / 2

@@ -211,7 +211,9 @@ struct Handle {
   int quasistatic(double dphi, double ftol, double e_jam, int max_inc, int max_iter,
                   double* phi_jam, int* n_inc);
   int find_jam(double e_jam, double step0, double min_step, double ftol, int max_iter,
-               int max_steps, double* phi_jam, int* steps_out);
+               int max_steps, double* phi_jam, int* steps_out,
+               const std::function<int(int, const double*)>& on_step = nullptr,
+               bool cg_relax = false, bool per_area = false);
 };
 
 // last error of calls made without a handle (creation, file reading)

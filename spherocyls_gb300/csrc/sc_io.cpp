@@ -507,6 +507,47 @@ int sc_run_pure_strain(sc_handle* H, const char* out_dir, double stop_aspect, do
   return SC_OK;
 }
 
+// find_jam_2p with its output (src/cuda/2point_dynamics.cu:4393-4456, 4582-4606): the
+// start's position file, then per resize a stress/energy line "t packing E Pxx Pyy
+// Pxy Pyx" in sd_stress_energy.dat and a position file, and the final state as a
+// binary file.  One system per handle.  As there, e_jam and the lines' energy column
+// are calc_fe_2p's energy per unit area, and each resize relaxes with the conjugate gradient (cjpr_relax_2p, up to
+// max_iter iterations) in the FP64 form; the mixed form relaxes with FIRE to ftol.
+int sc_run_find_jam(sc_handle* H, const char* out_dir, double e_jam, double step,
+                    double ftol, int max_iter, int* steps_out, double* phi_jam) {
+  int rc = check_single(H, "sc_run_find_jam");
+  if (rc) return rc;
+  sc::Handle& h = H->h;
+  if (!out_dir) return io_fail(&h, SC_E_ARG, "sc_run_find_jam: needs an output directory");
+  const std::string dir(out_dir);
+  std::ofstream se_out(dir + "/sd_stress_energy.dat");
+  if (!se_out) return io_fail(&h, SC_E_IO, "cannot open " + dir + "/sd_stress_energy.dat");
+  if ((rc = sc_save_positions(H, 0, pos_name(dir, "sd", 0).c_str(), SC_FMT_SD))) return rc;
+  auto each = [&](int t, const double* se) -> int {
+    const sc::HostSys& q = h.hs[0];
+    // the energy column in e_jam's units (per unit area), the stresses as calc_se
+    const double e_area = se[0] * (double)q.n / (2.0 * q.Lx * q.Ly);
+    char buf[256];
+    snprintf(buf, sizeof buf, "%d %.10f %.9g %.9g %.9g %.9g %.9g\n", t, q.packing, e_area, se[1],
+             se[2], se[3], se[4]);
+    se_out << buf;
+    se_out.flush();
+    return sc_save_positions(H, 0, pos_name(dir, "sd", (unsigned long)t).c_str(), SC_FMT_SD);
+  };
+  int steps = 0;
+  double phi = 0;
+  rc = h.find_jam(e_jam, step, 1e-15, ftol, max_iter, 1000000, &phi, &steps, each,
+                  h.prec == sc::PREC_FP64, true);
+  if (rc) return rc;
+  se_out.close();
+  char bin[32];
+  snprintf(bin, sizeof bin, "/sd%010d.bin", steps);
+  if ((rc = sc_save_positions(H, 0, (dir + bin).c_str(), SC_FMT_BIN))) return rc;
+  if (steps_out) *steps_out = steps;
+  if (phi_jam) *phi_jam = phi;
+  return SC_OK;
+}
+
 int sc_run_minimize(sc_handle* H, const char* out_dir, int max_steps, double e_min,
                     int pos_save_n, int* steps_taken) {
   int rc = check_single(H, "sc_run_minimize");
