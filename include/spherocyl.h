@@ -329,6 +329,16 @@ int sc_run_pure_strain(sc_handle *h, const char *out_dir, double stop_aspect, do
  * final packing fraction (negated if the step limit of 10^6 resizes ran out). */
 int sc_run_find_jam(sc_handle *h, const char *out_dir, double e_jam, double step,
                     double ftol, int max_iter, int *steps, double *phi_jam);
+/* compress_qs2p / expand_qs2p with output, src/cuda/2point_dynamics.cu:4296-4391,
+ * for a one-system handle: relaxation, then affine resizes by the length factor
+ * 1 - |step| (compression, final_packing above the current packing fraction) or
+ * 1/(1 - |step|) (expansion), each followed by a relaxation -- sc_cg_minimize(max_iter)
+ * in the FP64 form (cjpr_relax_2p), FIRE to ftol in the mixed form -- until the
+ * packing fraction reaches final_packing.  The start and each resize t write a line
+ * "t packing E Pxx Pyy Pxy Pyx" (E per unit area, as sc_run_find_jam) in
+ * sd_stress_energy.dat and sd%010d.dat.  *steps: resizes made. */
+int sc_run_qs_compress(sc_handle *h, const char *out_dir, double final_packing, double step,
+                       double ftol, int max_iter, int *steps);
 /* gradient_descent_minimize with output, src/cpp/relaxation_dynamics.cpp:33-85 (SE
  * file sr_strain_se.dat, position files sr%010lu.dat every pos_save_n steps). */
 int sc_run_minimize(sc_handle *h, const char *out_dir, int max_steps, double e_min,

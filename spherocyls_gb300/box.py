@@ -394,6 +394,16 @@ class BoxBatch:
                                         ctypes.byref(phi)))
         return phi.value, s.value
 
+    def run_qs_compress(self, out_dir: str, final_packing: float, step: float,
+                        ftol: float = 1e-13, max_iter: int = 1000000) -> int:
+        """compress_qs2p (expand_qs2p below the current packing fraction) with its
+        files; returns the resizes made."""
+        s = ctypes.c_int()
+        self._chk(lib().sc_run_qs_compress(self.h, out_dir.encode(), float(final_packing),
+                                           float(step), float(ftol), int(max_iter),
+                                           ctypes.byref(s)))
+        return s.value
+
     # --- state ------------------------------------------------------------
     def state(self):
         x, y, p = (np.empty(self.ntot) for _ in range(3))

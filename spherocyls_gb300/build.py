@@ -39,6 +39,7 @@ CLI_UNITS = {
     "spherocyl_minimize": "cli_minimize.cpp",
     "spherocyl_pure_shear": "cli_pure_shear.cpp",
     "spherocyl_find_jam": "cli_find_jam.cpp",
+    "spherocyl_qs_compress": "cli_qs_compress.cpp",
 }
 
 

@@ -1,0 +1,84 @@
+// spherocyl_qs_compress -- quasistatic compression to a packing fraction.
+//
+// Arguments of the src/cuda quasistatic-compression driver
+// (src/cuda/main_2point_qscompress.cpp:63-261): data file or "r", output directory, N,
+// resize step (the driver's "resize rate", the relative length step per resize),
+// integration step, final packing fraction, position and stress save rates (read
+// and, as there, not used: every resize is saved), cell padding, and for "r":
+// packing fraction, aspect ratio A/R (R1 = 0.5), bidispersity R2/R1, then optionally
+// the initial configuration code (0-9) and the aspect-ratio spread (see
+// cli::random_start).  A final packing fraction below the start's expands
+// (expand_qs2p).  Contacts are the two-point model of the src/cuda 2p code unless
+// SC_CONTACTS=1; each resize relaxes with the conjugate gradient in the default FP64
+// form (SC_PRECISION=mixed: FIRE); SC_SEED seeds the random configuration.  Files:
+// sd_stress_energy.dat and sd%010d.dat for the start and every resize.
+#include <chrono>
+#include <cstdio>
+#include <vector>
+
+#include "cli_common.hpp"
+
+int main(int argc, char** argv) {
+  cli::Args a{argc, argv};
+  std::string file = a.s("Data file ('r' for random)");
+  std::string dir = a.s("Output data directory");
+  int n = a.i("Number of particles");
+  double step = a.f("Resize rate (epsilon)");
+  double dt = a.f("Integration step size");
+  double final_packing = a.f("Final packing fraction");
+  (void)a.f("Position data save rate");
+  (void)a.f("Stress data save rate");
+  double pad = a.f("Cell padding");
+  if (!(step != 0) || !(final_packing > 0)) {
+    std::cerr << "need a non-zero resize step and a positive final packing fraction" << std::endl;
+    return 1;
+  }
+  std::vector<double> x, y, p, R, A;
+  double L = 0, Ly = 0, gamma = 0, gamma_total = 0;
+  if (file == "r") {
+    double phi = a.f("Packing Fraction");
+    double aspect = a.f("Aspect ratio (A/R)");
+    double bidisp = a.f("Bidispersity ratio (R2/R1)");
+    x.resize(n), y.resize(n), p.resize(n), R.resize(n), A.resize(n);
+    int rc = cli::random_start(a, n, phi, aspect, bidisp, x.data(), y.data(), p.data(), R.data(),
+                               A.data(), &L);
+    if (rc) return cli::fail("packing", rc);
+  } else {
+    int nf = 0;
+    double hdr[7];
+    int rc = sc_read_positions(file.c_str(), &nf, hdr, nullptr, nullptr, nullptr, nullptr, nullptr);
+    if (rc) return cli::fail("read", rc);
+    if (nf != n) std::cerr << "Warning: Number of particles in data file may not match requested number" << std::endl;
+    x.resize(nf), y.resize(nf), p.resize(nf), R.resize(nf), A.resize(nf);
+    rc = sc_read_positions(file.c_str(), &nf, hdr, x.data(), y.data(), p.data(), R.data(), A.data());
+    if (rc) return cli::fail("read", rc);
+    n = nf;
+    L = hdr[0];
+    Ly = hdr[1];
+    gamma = hdr[3];
+    gamma_total = hdr[4];
+  }
+  auto start = std::chrono::steady_clock::now();
+  sc_options opt;
+  sc_default_options(&opt);
+  opt.precision = cli::precision();
+  opt.contact_model = cli::env_int("SC_CONTACTS", 2) == 1 ? SC_CONTACT_ONE : SC_CONTACT_TWO;
+  sc_handle* h = nullptr;
+  if (Ly == 0) Ly = L;
+  int rc = sc_create_rect(&opt, 1, &n, &L, &Ly, &pad, x.data(), y.data(), p.data(), R.data(),
+                          A.data(), &h);
+  if (rc) return cli::fail("create", rc);
+  if ((rc = sc_set_step(h, -1, dt)) || (rc = sc_set_gamma(h, -1, gamma)) ||
+      (rc = sc_set_total_gamma(h, -1, gamma_total)))
+    return cli::fail("setup", rc, h);
+  int steps = 0;
+  // compress_qs2p: a million conjugate-gradient iterations at most per relaxation
+  rc = sc_run_qs_compress(h, dir.c_str(), final_packing, step, 1e-13, 1000000, &steps);
+  if (rc) return cli::fail("compress", rc, h);
+  double box[10];
+  if ((rc = sc_get_box(h, 0, box))) return cli::fail("box", rc, h);
+  double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - start).count();
+  std::printf("\nResizes: %d\nPacking fraction: %.10f\nRun Time: %g\n", steps, box[7], secs);
+  sc_destroy(h);
+  return 0;
+}

@@ -18,6 +18,7 @@
 #include <dlfcn.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -545,6 +546,59 @@ int sc_run_find_jam(sc_handle* H, const char* out_dir, double e_jam, double step
   if ((rc = sc_save_positions(H, 0, (dir + bin).c_str(), SC_FMT_BIN))) return rc;
   if (steps_out) *steps_out = steps;
   if (phi_jam) *phi_jam = phi;
+  return SC_OK;
+}
+
+// compress_qs2p / expand_qs2p (src/cuda/2point_dynamics.cu:4296-4391): relaxation,
+// then affine resizes by the length factor 1 - step (1/(1 - step) to expand, as
+// resize_step_2p) each followed by a relaxation, until the packing fraction reaches
+// final_packing; the start and every resize give a line "t packing E Pxx Pyy Pxy
+// Pyx" in sd_stress_energy.dat (E per unit area, as the find-jam run) and sd%010d.dat.
+// Relaxation: the conjugate gradient (cjpr_relax_2p, max_iter iterations) in the
+// FP64 form, FIRE to ftol in the mixed form.
+int sc_run_qs_compress(sc_handle* H, const char* out_dir, double final_packing, double step,
+                       double ftol, int max_iter, int* steps_out) {
+  int rc = check_single(H, "sc_run_qs_compress");
+  if (rc) return rc;
+  sc::Handle& h = H->h;
+  if (!out_dir) return io_fail(&h, SC_E_ARG, "sc_run_qs_compress: needs an output directory");
+  step = std::fabs(step);
+  if (!(step > 0 && step < 1) || !(final_packing > 0))
+    return io_fail(&h, SC_E_ARG, "sc_run_qs_compress: need 0 < |step| < 1 and final_packing > 0");
+  const std::string dir(out_dir);
+  std::ofstream se_out(dir + "/sd_stress_energy.dat");
+  if (!se_out) return io_fail(&h, SC_E_IO, "cannot open " + dir + "/sd_stress_energy.dat");
+  const bool fp64 = h.prec == sc::PREC_FP64;
+  auto relax = [&]() {
+    int r = fp64 ? h.cg_minimize(max_iter, nullptr, nullptr, nullptr)
+                 : h.fire_minimize(ftol, max_iter, 1e-2, 0.2, nullptr, nullptr, nullptr);
+    return r == SC_E_NOCONV ? SC_OK : r;
+  };
+  double se[5];
+  auto record = [&](int t) -> int {
+    int r = h.calc(true, se);
+    if (r) return r;
+    if ((r = sc_save_positions(H, 0, pos_name(dir, "sd", (unsigned long)t).c_str(), SC_FMT_SD)))
+      return r;
+    const sc::HostSys& q = h.hs[0];
+    char buf[256];
+    // the start's line prints the packing with %f, the resizes' with %.9f
+    snprintf(buf, sizeof buf, t == 0 ? "%d %f %g %g %g %g %g\n" : "%d %.9f %g %g %g %g %g\n", t,
+             q.packing, se[0] * (double)q.n / (2.0 * q.Lx * q.Ly), se[1], se[2], se[3], se[4]);
+    se_out << buf;
+    se_out.flush();
+    return SC_OK;
+  };
+  if ((rc = relax()) || (rc = record(0))) return rc;
+  const bool compress = final_packing >= h.hs[0].packing;
+  const double f = compress ? 1.0 - step : 1.0 / (1.0 - step);
+  int t = 0;
+  while (compress ? h.hs[0].packing < final_packing : h.hs[0].packing > final_packing) {
+    t += 1;
+    if ((rc = h.affine_scale(std::vector<double>{f})) || (rc = relax()) || (rc = record(t)))
+      return rc;
+  }
+  if (steps_out) *steps_out = t;
   return SC_OK;
 }
 

@@ -1,4 +1,5 @@
-"""find_jam_2p as a run with output (sc_run_find_jam) and its command-line driver.
+"""The quasistatic jamming runs with output: find_jam_2p (sc_run_find_jam) and
+compress_qs2p / expand_qs2p (sc_run_qs_compress), and their command-line drivers.
 
 The run writes the reference's files (the start's position file, a stress/energy
 line and a position file per resize, the final state as a binary file).  The lines
@@ -99,3 +100,50 @@ def test_cli_find_jam_random_start(library, tmp_path):
     assert (tmp_path / f"sd{steps:010d}.bin").exists()
     assert abs(rows[-1][2] - 1e-6) < 0.05e-6
     assert 0.80 < rows[-1][1] < 0.95
+
+
+def test_run_qs_compress_and_expand(library, tmp_path):
+    """compress_qs2p: the start and every resize give a line and a position file; the
+    packing fraction grows by 1/(1 - step)^2 per resize and the run stops at the first
+    resize at or above the target; expand_qs2p (a target below) shrinks it by
+    (1 - step)^2 per resize.  Energies per unit area, as the find-jam run."""
+    import spherocyls_gb300 as sc
+
+    L, x, y, p, R, A = sc.generate_packing(128, 0.80, 1.0, seed=92)
+    step = 5e-3
+    with sc.SpherocylBox(L, x, y, p, A, R, 0.1, contacts=2, precision="fp64") as b:
+        phi0 = b.box()["packing"]
+        up = tmp_path / "up"
+        up.mkdir()
+        n_up = b.run_qs_compress(str(up), 0.93, step)
+        box = b.box()
+        e_end = b.calc_se()[0] * 128 / (2 * box["Lx"] * box["Ly"])
+        down = tmp_path / "down"
+        down.mkdir()
+        n_down = b.run_qs_compress(str(down), 0.90, -step)
+        phi_end = b.box()["packing"]
+    rows = _lines(up / "sd_stress_energy.dat")
+    assert [r[0] for r in rows] == list(range(n_up + 1))
+    for t in range(n_up + 1):
+        assert (up / f"sd{t:010d}.dat").exists()
+    want = phi0 / (1 - step) ** (2 * np.arange(n_up + 1))
+    got = np.array([r[1] for r in rows])
+    assert abs(got[0] - want[0]) < 1e-6 and np.allclose(got[1:], want[1:], rtol=0, atol=2e-9)
+    assert want[-1] >= 0.93 > want[-2]
+    assert e_end > 0 and abs(rows[-1][2] - e_end) <= 1e-5 * e_end
+    rows = _lines(down / "sd_stress_energy.dat")
+    assert [r[0] for r in rows] == list(range(n_down + 1))
+    want = rows[0][1] * (1 - step) ** (2 * np.arange(n_down + 1))
+    assert np.allclose([r[1] for r in rows[1:]], want[1:], rtol=0, atol=2e-6)
+    assert phi_end <= 0.90 < phi_end / (1 - step) ** 2
+
+
+def test_cli_qs_compress_random_start(library, tmp_path):
+    exe = os.path.join(ROOT, "spherocyls_gb300", "bin", "spherocyl_qs_compress")
+    r = subprocess.run([exe, "r", str(tmp_path), "64", "5e-3", "0.01", "0.85", "0.01", "0.01",
+                        "0.1", "0.80", "1.0", "1.4", "0", "0"], capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stderr
+    rows = _lines(tmp_path / "sd_stress_energy.dat")
+    assert rows[0][0] == 0 and rows[-1][1] >= 0.85 > rows[-2][1]
+    assert (tmp_path / f"sd{rows[-1][0]:010d}.dat").exists()
