@@ -7,7 +7,8 @@
 // there, not used by the bisection), cell padding, and for "r": packing fraction,
 // aspect ratio A/R (R1 = 0.5), bidispersity R2/R1, then optionally the initial
 // configuration code (0-9) and the aspect-ratio spread (see cli::random_start).
-// Contacts are the two-point model of the src/cuda 2p code unless SC_CONTACTS=1;
+// Contacts are the two-point model of the src/cuda 2p code unless SC_CONTACTS=1 (the
+// one-point rule of the src/cuda 1p find-jam driver, main_1point_findjam.cpp);
 // each resize relaxes with the conjugate gradient in the default FP64 form
 // (SC_PRECISION=mixed: FIRE); SC_SEED seeds the random configuration.  Files:
 // sd_stress_energy.dat, sd%010d.dat per resize, the final state as sd%010d.bin.

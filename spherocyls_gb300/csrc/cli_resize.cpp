@@ -6,7 +6,9 @@
 // A/R (R1 = 0.5), bidispersity R2/R1, optionally the initial configuration code
 // (0-9) and the aspect-ratio spread (see cli::random_start).  Position files are
 // read with the standard header (the src/cpp resize driver's headerless legacy
-// column layout, src/cpp/main_resize.cpp:336-349, is not supported).
+// column layout, src/cpp/main_resize.cpp:336-349, is not supported).  SC_CONTACTS=2
+// selects the two-point contacts of the src/cuda 2p resize driver
+// (src/cuda/main_2point_resize.cpp, resize_box_2p).
 #include <chrono>
 #include <vector>
 
@@ -52,6 +54,7 @@ int main(int argc, char** argv) {
   sc_options opt;
   sc_default_options(&opt);
   opt.precision = cli::precision();
+  if (cli::env_int("SC_CONTACTS", 1) == 2) opt.contact_model = SC_CONTACT_TWO;
   sc_handle* h = nullptr;
   int rc = sc_create(&opt, 1, &n, &L, &pad, x.data(), y.data(), p.data(), R.data(), A.data(), &h);
   if (rc) return cli::fail("create", rc);

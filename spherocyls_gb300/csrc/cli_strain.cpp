@@ -9,7 +9,8 @@
 // initial configuration code (0-9) and the aspect-ratio spread (see
 // cli::random_start); for change 3 the maximum gamma comes last (main.cpp:269-275).
 // SC_PRECISION=mixed selects the mixed form, SC_OUTPUT_FORMAT=sd the src/cuda file
-// layout, SC_SEED the seed of the random configuration.
+// layout, SC_SEED the seed of the random configuration, SC_CONTACTS=2 the two-point
+// contact model of the src/cuda 2p code.
 #include <chrono>
 #include <vector>
 
@@ -65,6 +66,7 @@ int main(int argc, char** argv) {
   sc_options opt;
   sc_default_options(&opt);
   opt.precision = cli::precision();
+  if (cli::env_int("SC_CONTACTS", 1) == 2) opt.contact_model = SC_CONTACT_TWO;
   sc_handle* h = nullptr;
   if (Ly == 0) Ly = L;
   int rc = sc_create_rect(&opt, 1, &n, &L, &Ly, &pad, x.data(), y.data(), p.data(), R.data(),
