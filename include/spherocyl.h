@@ -329,6 +329,13 @@ int sc_run_pure_strain(sc_handle *h, const char *out_dir, double stop_aspect, do
  * final packing fraction (negated if the step limit of 10^6 resizes ran out). */
 int sc_run_find_jam(sc_handle *h, const char *out_dir, double e_jam, double step,
                     double ftol, int max_iter, int *steps, double *phi_jam);
+/* y_compress_energy_2p with output, src/cuda/2point_dynamics.cu:4458-4530, 4608-4631:
+ * sc_run_find_jam's bisection and files with resizes of Ly and the y coordinates
+ * alone (y_resize_step_2p: factors 1 - step and 1/(1 - step)), towards the energy
+ * per unit area e_target, until the step is below 1e-14.  *packing: the final
+ * packing fraction (negated if 10^6 resizes ran out). */
+int sc_run_y_compress(sc_handle *h, const char *out_dir, double e_target, double step,
+                      double ftol, int max_iter, int *steps, double *packing);
 /* compress_qs2p / expand_qs2p with output, src/cuda/2point_dynamics.cu:4296-4391,
  * for a one-system handle: relaxation, then affine resizes by the length factor
  * 1 - |step| (compression, final_packing above the current packing fraction) or

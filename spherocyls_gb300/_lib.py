@@ -136,6 +136,8 @@ SIGNATURES = [
                                        ctypes.c_int, _ip]),
     ("sc_run_find_jam", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_double, ctypes.c_double,
                                        ctypes.c_double, ctypes.c_int, _ip, _dp]),
+    ("sc_run_y_compress", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_double, ctypes.c_double,
+                                         ctypes.c_double, ctypes.c_int, _ip, _dp]),
     ("sc_run_qs_compress", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_double,
                                           ctypes.c_double, ctypes.c_double, ctypes.c_int, _ip]),
     ("sc_forces_noalloc", ctypes.c_int, [ctypes.c_int, ctypes.c_double, ctypes.c_double,

@@ -394,6 +394,17 @@ class BoxBatch:
                                         ctypes.byref(phi)))
         return phi.value, s.value
 
+    def run_y_compress(self, out_dir: str, e_target: float, step: float, ftol: float = 1e-13,
+                       max_iter: int = 200000):
+        """y_compress_energy_2p with its files: find_jam_2p's bisection resizing Ly
+        and y alone.  Returns (packing fraction, resizes made)."""
+        s = ctypes.c_int()
+        phi = ctypes.c_double()
+        self._chk(lib().sc_run_y_compress(self.h, out_dir.encode(), float(e_target), float(step),
+                                          float(ftol), int(max_iter), ctypes.byref(s),
+                                          ctypes.byref(phi)))
+        return phi.value, s.value
+
     def run_qs_compress(self, out_dir: str, final_packing: float, step: float,
                         ftol: float = 1e-13, max_iter: int = 1000000) -> int:
         """compress_qs2p (expand_qs2p below the current packing fraction) with its

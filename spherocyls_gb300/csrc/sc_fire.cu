@@ -211,14 +211,15 @@ __global__ void k_fire_reset(Dev d, FireState f, double dt0) {
   }
 }
 
-// affine rescale of the FP64 positions of the systems with factor != 1
+// affine rescale of the FP64 positions: x by factor[2s], y by factor[2s+1] in system s
 __global__ void k_affine(Dev d, const double* factor) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.ntot) return;
-  double f = factor[d.psys[i]];
-  if (f == 1.0) return;
+  const int s = d.psys[i];
+  const double fx = factor[2 * s], fy = factor[2 * s + 1];
+  if (fx == 1.0 && fy == 1.0) return;
   double2 p = d.xy[i];
-  d.xy[i] = make_double2(p.x * f, p.y * f);
+  d.xy[i] = make_double2(p.x * fx, p.y * fy);
 }
 
 // flip_shear_direction / reflect_yaxis (src/cuda/find_neighbors.cu:552-581):

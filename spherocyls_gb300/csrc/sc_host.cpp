@@ -1229,13 +1229,19 @@ int Handle::cg_minimize(int max_iter, int* iters, double* energy, int* reason) {
   return capped ? SC_E_NOCONV : SC_OK;
 }
 
-// Box and positions of each system scaled by factor[s] (1 leaves it alone).
-int Handle::affine_scale(const std::vector<double>& factor) {
+// Box and positions of each system scaled by factor[s] (1 leaves it alone), in y
+// alone with y_only (resize_y_coords_2p).
+int Handle::affine_scale(const std::vector<double>& factor, bool y_only) {
   cudaSetDevice(device);
   if (!materialize()) return last_status;
+  std::vector<double> fxy(2 * (size_t)nsys);
+  for (int s = 0; s < nsys; s++) {
+    fxy[2 * s] = y_only ? 1.0 : factor[s];
+    fxy[2 * s + 1] = factor[s];
+  }
   double* dfac = nullptr;
-  if (!dalloc(&dfac, nsys, "factors")) return last_status;
-  bool ok = cuda_ok(cudaMemcpyAsync(dfac, factor.data(), nsys * sizeof(double),
+  if (!dalloc(&dfac, 2 * (size_t)nsys, "factors")) return last_status;
+  bool ok = cuda_ok(cudaMemcpyAsync(dfac, fxy.data(), 2 * nsys * sizeof(double),
                                     cudaMemcpyHostToDevice, stream), "factors");
   if (ok) launch_affine(d, dfac, stream);
   ok = ok && cuda_ok(cudaStreamSynchronize(stream), "affine");
@@ -1245,10 +1251,10 @@ int Handle::affine_scale(const std::vector<double>& factor) {
   for (int s = 0; s < nsys; s++) {
     if (factor[s] == 1.0) continue;
     HostSys& h = hs[s];
-    double old = h.Lx;
-    h.Lx *= factor[s];
+    const double old_x = h.Lx, old_y = h.Ly;
+    if (!y_only) h.Lx *= factor[s];
     h.Ly *= factor[s];
-    h.packing *= (old / h.Lx) * (old / h.Lx);
+    h.packing *= y_only ? old_y / h.Ly : (old_x / h.Lx) * (old_x / h.Lx);
     int r = h.rows, c = h.cols;
     h.configure(false);
     if (h.rows != r || h.cols != c) regrid = true;
@@ -1401,11 +1407,12 @@ int Handle::quasistatic(double dphi, double ftol, double e_jam, int max_inc, int
 // half the last step, until the step falls below min_step.  e_jam is an energy per
 // particle, or with per_area the reference's measure (calc_fe_2p's energy per unit
 // area, E/N x N / 2LxLy); on_step sees each resize's stress/energy; cg_relax relaxes
-// with the conjugate gradient (cjpr_relax_2p) instead of FIRE.
+// with the conjugate gradient (cjpr_relax_2p) instead of FIRE; y_only resizes Ly and
+// the y coordinates alone (y_compress_energy_2p with y_resize_step_2p).
 int Handle::find_jam(double e_jam, double step0, double min_step, double ftol, int max_iter,
                      int max_steps, double* phi_jam, int* steps_out,
                      const std::function<int(int, const double*)>& on_step, bool cg_relax,
-                     bool per_area) {
+                     bool per_area, bool y_only) {
   if (!(e_jam > 0) || !(step0 > 0) || !(min_step > 0) || max_steps < 0) {
     fail(SC_E_ARG, "find_jam: need e_jam > 0, step > 0, min_step > 0, max_steps >= 0");
     return SC_E_ARG;
@@ -1456,7 +1463,7 @@ int Handle::find_jam(double e_jam, double step0, double min_step, double ftol, i
         any = true;
       }
     if (!any) break;
-    if ((rc = affine_scale(f))) return rc;
+    if ((rc = affine_scale(f, y_only))) return rc;
     rc = relax();
     if (rc && rc != SC_E_NOCONV) return rc;
     if ((rc = calc(true, se.data()))) return rc;

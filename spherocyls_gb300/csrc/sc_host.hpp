@@ -192,7 +192,7 @@ struct Handle {
   bool run_fire_graph(int iters, double ftol, double dt_max);
   int fire_minimize(double ftol, int max_iter, double dt0, double dt_max, int* iters,
                     double* fmax_out, int* done_out);
-  int affine_scale(const std::vector<double>& factor);
+  int affine_scale(const std::vector<double>& factor, bool y_only = false);
   // Polak-Ribiere conjugate gradient with the reference's line search
   CgState cg{};
   static constexpr int kCgChunk = 10;  // iterations per captured graph
@@ -213,7 +213,7 @@ struct Handle {
   int find_jam(double e_jam, double step0, double min_step, double ftol, int max_iter,
                int max_steps, double* phi_jam, int* steps_out,
                const std::function<int(int, const double*)>& on_step = nullptr,
-               bool cg_relax = false, bool per_area = false);
+               bool cg_relax = false, bool per_area = false, bool y_only = false);
 };
 
 // last error of calls made without a handle (creation, file reading)

@@ -251,6 +251,7 @@ void launch_build_nbrs(const Dev& d, const StepScalars* tab, int row, cudaStream
 void launch_fire_reset(const Dev& d, const FireState& f, double dt0, cudaStream_t st);
 void launch_fire_iteration_tail(const Dev& d, const FireState& f, double ftol, double dt_max,
                                 bool mixed, cudaStream_t st);
+// factor: 2 nsys entries, the x and y factors of each system
 void launch_affine(const Dev& d, const double* factor, cudaStream_t st);
 void launch_reflect(const Dev& d, const double* lx, cudaStream_t st);
 void launch_rotate(const Dev& d, const double* q, cudaStream_t st);

@@ -508,18 +508,21 @@ int sc_run_pure_strain(sc_handle* H, const char* out_dir, double stop_aspect, do
   return SC_OK;
 }
 
-// find_jam_2p with its output (src/cuda/2point_dynamics.cu:4393-4456, 4582-4606): the
-// start's position file, then per resize a stress/energy line "t packing E Pxx Pyy
-// Pxy Pyx" in sd_stress_energy.dat and a position file, and the final state as a
-// binary file.  One system per handle.  As there, e_jam and the lines' energy column
-// are calc_fe_2p's energy per unit area, and each resize relaxes with the conjugate gradient (cjpr_relax_2p, up to
-// max_iter iterations) in the FP64 form; the mixed form relaxes with FIRE to ftol.
-int sc_run_find_jam(sc_handle* H, const char* out_dir, double e_jam, double step,
-                    double ftol, int max_iter, int* steps_out, double* phi_jam) {
-  int rc = check_single(H, "sc_run_find_jam");
+// find_jam_2p with its output (src/cuda/2point_dynamics.cu:4393-4456, 4582-4606), and
+// y_compress_energy_2p (:4458-4530, 4608-4631) with y_only: the start's position
+// file, then per resize a stress/energy line "t packing E Pxx Pyy Pxy Pyx" in
+// sd_stress_energy.dat and a position file, and the final state as a binary file.
+// One system per handle.  As there, e_jam and the lines' energy column are
+// calc_fe_2p's energy per unit area, and each resize relaxes with the conjugate
+// gradient (cjpr_relax_2p, up to max_iter iterations) in the FP64 form; the mixed
+// form relaxes with FIRE to ftol.
+static int run_jam_files(sc_handle* H, const char* what, const char* out_dir, double e_jam,
+                         double step, double min_step, double ftol, int max_iter, bool y_only,
+                         int* steps_out, double* phi_jam) {
+  int rc = check_single(H, what);
   if (rc) return rc;
   sc::Handle& h = H->h;
-  if (!out_dir) return io_fail(&h, SC_E_ARG, "sc_run_find_jam: needs an output directory");
+  if (!out_dir) return io_fail(&h, SC_E_ARG, std::string(what) + ": needs an output directory");
   const std::string dir(out_dir);
   std::ofstream se_out(dir + "/sd_stress_energy.dat");
   if (!se_out) return io_fail(&h, SC_E_IO, "cannot open " + dir + "/sd_stress_energy.dat");
@@ -537,8 +540,8 @@ int sc_run_find_jam(sc_handle* H, const char* out_dir, double e_jam, double step
   };
   int steps = 0;
   double phi = 0;
-  rc = h.find_jam(e_jam, step, 1e-15, ftol, max_iter, 1000000, &phi, &steps, each,
-                  h.prec == sc::PREC_FP64, true);
+  rc = h.find_jam(e_jam, step, min_step, ftol, max_iter, 1000000, &phi, &steps, each,
+                  h.prec == sc::PREC_FP64, true, y_only);
   if (rc) return rc;
   se_out.close();
   char bin[32];
@@ -547,6 +550,19 @@ int sc_run_find_jam(sc_handle* H, const char* out_dir, double e_jam, double step
   if (steps_out) *steps_out = steps;
   if (phi_jam) *phi_jam = phi;
   return SC_OK;
+}
+
+int sc_run_find_jam(sc_handle* H, const char* out_dir, double e_jam, double step,
+                    double ftol, int max_iter, int* steps_out, double* phi_jam) {
+  return run_jam_files(H, "sc_run_find_jam", out_dir, e_jam, step, 1e-15, ftol, max_iter, false,
+                       steps_out, phi_jam);
+}
+
+// y_compress_energy_2p stops below a step of 1e-14 (find_jam_2p: 1e-15)
+int sc_run_y_compress(sc_handle* H, const char* out_dir, double e_target, double step,
+                      double ftol, int max_iter, int* steps_out, double* packing) {
+  return run_jam_files(H, "sc_run_y_compress", out_dir, e_target, step, 1e-14, ftol, max_iter,
+                       true, steps_out, packing);
 }
 
 // compress_qs2p / expand_qs2p (src/cuda/2point_dynamics.cu:4296-4391): relaxation,

@@ -27,20 +27,21 @@ def _lines(path):
     return [(int(r[0]),) + tuple(float(v) for v in r[1:]) for r in rows]
 
 
-def _replay(e0, phi0, rows, e_jam, step0):
+def _replay(d0, phi0, rows, e_jam, step0, power=2):
     """The bisection of find_jam_2p / resize_to_energy_2p on the recorded energies:
-    the packing fraction each resize must give.  The lines carry 9 digits of the
+    the packing fraction each resize must give, from the first direction d0 (+1
+    compress, -1 expand: the side of e_jam where the relaxed start lies).  The lines carry 9 digits of the
     energy, so the replay stops at the first energy within 1e-7 of e_jam, where the
     printed value no longer decides the side; returns (packings, last phase step,
-    whether every line was replayed)."""
-    d = 1 if e0 < e_jam else -1
+    whether every line was replayed).  power: 2 when both lengths change, 1 for y alone."""
+    d = d0
     first = nxt = step0
     k = 0
     phi = phi0
     out = []
     for t, _phi, e, *_ in rows:
         f = 1 - nxt if d > 0 else 1 / (1 - nxt)
-        phi = phi / (f * f)
+        phi = phi / f ** power
         out.append(phi)
         if abs(e / e_jam - 1) < 1e-7:
             return np.array(out), first, False
@@ -77,9 +78,11 @@ def test_run_find_jam_files_and_bisection(library, tmp_path):
     assert abs(rows[-1][2] - e_area) <= 1e-8 * e_area
     assert abs(rows[-1][1] - phi) <= 1e-9 and phi > 0
     assert abs(e_area - e_jam) < 0.05 * e_jam, (e_area, e_jam)
-    # the recorded packings follow the bisection rule from the recorded energies
-    # (phi0's minimised energy decides the first direction: below e_jam here)
-    want, last, whole = _replay(0.0, phi0, rows, e_jam, step)
+    # the recorded packings follow the bisection rule from the recorded energies; the
+    # relaxed start's energy (not recorded) sets the first direction, read off the
+    # first line
+    d0 = 1 if rows[0][1] > phi0 else -1
+    want, last, whole = _replay(d0, phi0, rows, e_jam, step)
     got = np.array([r[1] for r in rows[: len(want)]])
     assert len(want) >= 10
     assert np.allclose(got, want, rtol=0, atol=2e-10), np.abs(got - want).max()
@@ -100,6 +103,35 @@ def test_cli_find_jam_random_start(library, tmp_path):
     assert (tmp_path / f"sd{steps:010d}.bin").exists()
     assert abs(rows[-1][2] - 1e-6) < 0.05e-6
     assert 0.80 < rows[-1][1] < 0.95
+
+
+def test_run_y_compress_bisects_in_y_alone(library, tmp_path):
+    """y_compress_energy_2p: the bisection of the find-jam run with Ly and the y
+    coordinates resized alone (the packing fraction changes by 1/f per resize); Lx
+    and every x coordinate stay as they were."""
+    import spherocyls_gb300 as sc
+
+    L, x, y, p, R, A = sc.generate_packing(128, 0.80, 1.0, seed=93)
+    e_t, step = 1e-6, 1e-3
+    with sc.SpherocylBox(L, x, y, p, A, R, 0.1, contacts=2, precision="fp64") as b:
+        phi0 = b.box()["packing"]
+        phi, steps = b.run_y_compress(str(tmp_path), e_t, step, ftol=1e-12)
+        box = b.box()
+        se = b.calc_se()
+    assert box["Lx"] == L and box["Ly"] < L
+    assert abs(box["packing"] - phi0 * L / box["Ly"]) <= 1e-12
+    rows = _lines(tmp_path / "sd_stress_energy.dat")
+    assert len(rows) == steps > 0 and phi > 0
+    e_area = se[0] * 128 / (2 * box["Lx"] * box["Ly"])
+    assert abs(e_area - e_t) < 0.05 * e_t, (e_area, e_t)
+    d0 = 1 if rows[0][1] > phi0 else -1
+    want, last, whole = _replay(d0, phi0, rows, e_t, step, power=1)
+    got = np.array([r[1] for r in rows[: len(want)]])
+    assert len(want) >= 10
+    assert np.allclose(got, want, rtol=0, atol=2e-10), np.abs(got - want).max()
+    assert last <= 1e-14 or not whole
+    hdr, *_ = sc.read_positions(str(tmp_path / f"sd{steps:010d}.bin"))
+    assert hdr["Lx"] == L and hdr["Ly"] == box["Ly"]
 
 
 def test_run_qs_compress_and_expand(library, tmp_path):
