@@ -12,7 +12,8 @@ behind the same Python surface:
   restatement and to produce the golden fixtures under ``tests/golden/``.
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` may use this package, and only as the checker.  The product library
+``bench.py`` may use this package, and only as the oracle the CUDA results are
+compared with (or, in the benchmark, the timed CPU baseline).  The product library
 (``spherocyls_gb300``) never imports it.
 """
 from __future__ import annotations

@@ -3,7 +3,7 @@
  *
  * A plain-C restatement of the single-threaded CPU path of tmarschall/spherocyls
  * (src/cpp).  The tests, the smoke check and the CPU-baseline leg of the benchmark
- * use it as the checker for the CUDA library.  It is never linked into, or called
+ * use it as the oracle the CUDA library is compared with.  It is never linked into, or called
  * by, the product library.
  *
  * Every routine follows one reference routine and cites it.  Arithmetic is written

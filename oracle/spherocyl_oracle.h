@@ -3,7 +3,7 @@
  *
  * C interface of the CPU restatement of tmarschall/spherocyls' src/cpp path
  * (spherocyl_oracle.c).  Only tests, the smoke check and the CPU-baseline leg of
- * the benchmark use it, as the checker; the product library never links it.
+ * the benchmark use it, as the oracle; the product library never links it.
  */
 #ifndef SPHEROCYL_ORACLE_H
 #define SPHEROCYL_ORACLE_H
