@@ -38,7 +38,8 @@ extern "C" {
 #define SC_E_IO 2       /* file could not be read or written */
 #define SC_E_NAN 3      /* a position or angle became non-finite */
 #define SC_E_OVERFLOW 4 /* neighbour list or cell capacity exceeded */
-#define SC_E_NOCONV 5   /* minimiser stopped at its iteration cap */
+#define SC_E_NOCONV 5   /* minimiser stopped at its iteration cap, or a jamming
+                           bisection's step grew to 1 without crossing its target */
 #define SC_E_TIMEOUT 6  /* a bounded device wait gave up */
 #define SC_E_CUDA 7     /* CUDA runtime error */
 #define SC_E_STATE 8    /* call not valid in the handle's current state */
@@ -201,7 +202,8 @@ int sc_quasistatic_compress(sc_handle *h, double dphi, double ftol, double e_jam
  * FIRE to ftol after each, towards energy per particle e_jam, reversing with
  * half the last step each time the energy crosses e_jam, until the step is below
  * min_step or max_steps resizes were made.  phi_jam[s]: final packing fraction of
- * system s (negated when max_steps ran out first); *steps: resizes made. */
+ * system s (negated when max_steps ran out first); *steps: resizes made.
+ * SC_E_NOCONV if a step grows to 1 before the energy crosses e_jam. */
 int sc_find_jam(sc_handle *h, double e_jam, double step, double min_step, double ftol,
                 int max_iter, int max_steps, double *phi_jam, int *steps);
 

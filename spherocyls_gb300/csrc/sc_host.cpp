@@ -1457,6 +1457,12 @@ int Handle::find_jam(double e_jam, double step0, double min_step, double ftol, i
     bool any = false;
     for (int s = 0; s < nsys; s++)
       if (ph[s].dir != 0) {
+        // the step grows by 1.1 per resize while e_jam is not crossed; at 1 the
+        // length factor would reach zero (the reference has no such check)
+        if (!(ph[s].next < 1.0)) {
+          fail(SC_E_NOCONV, "find_jam: the resize step reached 1 before the energy crossed e_jam");
+          return SC_E_NOCONV;
+        }
         // resize_step_2p (src/cuda/2point_dynamics.cu:1187-1195): lengths x (1 - step)
         // to compress, / (1 - step) to expand
         f[s] = ph[s].dir > 0 ? 1.0 - ph[s].next : 1.0 / (1.0 - ph[s].next);
