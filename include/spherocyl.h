@@ -300,6 +300,12 @@ int sc_read_positions(const char *path, int *n, double *hdr, double *x, double *
  * (GzFileInput, src/cpp/gz_file_input.cpp; needs libz.so.1 at run time), any other
  * as text with either header. */
 int sc_save_positions(sc_handle *h, int sys, const char *path, int format);
+/* The same files from host arrays, without a handle (a configuration made on the
+ * host, src/cuda/main_configmaker.cpp's use): hdr[0..6] = Lx Ly packing gamma gamma_total
+ * rate dt as sc_read_positions gives them, n rows "x y phi R A".  Errors: SC_E_ARG,
+ * SC_E_IO, with sc_last_error(NULL) text. */
+int sc_write_positions(const char *path, int format, int n, const double *hdr, const double *x,
+                       const double *y, const double *phi, const double *R, const double *A);
 
 /* run_strain with output, src/cpp/strain_dynamics.cpp:238-319: t runs from t_start
  * to t_start + round(run_gamma/rate) in units of 1/dt steps; stress/energy lines

@@ -7,8 +7,8 @@ C ABI in ``include/spherocyl.h``); this package binds it with ctypes.
 """
 from ._lib import ScError, lib
 from .box import (BoxBatch, SpherocylBox, generate_config, generate_config_rect, generate_packing,
-                  generate_packing_device, read_positions, trim_memory)
+                  generate_packing_device, read_positions, trim_memory, write_positions)
 
 __all__ = ["BoxBatch", "SpherocylBox", "generate_config", "generate_config_rect",
            "generate_packing", "generate_packing_device", "read_positions", "trim_memory",
-           "ScError", "lib"]
+           "write_positions", "ScError", "lib"]

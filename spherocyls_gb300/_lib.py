@@ -123,6 +123,8 @@ SIGNATURES = [
                                                _dp, _dp, _dp, _dp]),
     ("sc_read_positions", ctypes.c_int, [ctypes.c_char_p, _ip, _dp, _dp, _dp, _dp, _dp, _dp]),
     ("sc_save_positions", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_int]),
+    ("sc_write_positions", ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, _dp, _dp,
+                                          _dp, _dp, _dp, _dp]),
     ("sc_run_strain", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.c_double, ctypes.c_double,
                                      ctypes.c_double, ctypes.c_ulong, ctypes.c_int,
                                      ctypes.POINTER(ctypes.c_ulong)]),

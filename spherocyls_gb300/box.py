@@ -138,6 +138,19 @@ def read_positions(path: str):
     return dict(zip(keys, hdr.tolist())), x, y, p, R, A
 
 
+def write_positions(path: str, hdr: dict, x, y, phi, R, A, fmt: str = "sd"):
+    """Write a position file from host arrays (no GPU): hdr holds Lx, Ly, packing,
+    gamma, gamma_total, rate, dt as read_positions returns them."""
+    keys = ("Lx", "Ly", "packing", "gamma", "gamma_total", "rate", "dt")
+    h = np.array([float(hdr[k]) for k in keys])
+    x, y, phi, R, A = (_f64(v) for v in (x, y, phi, R, A))
+    n = x.shape[0]
+    if any(v.shape[0] != n for v in (y, phi, R, A)):
+        raise ValueError("x, y, phi, R and A need the same length")
+    check(lib().sc_write_positions(path.encode(), FMT[fmt], n, _ptr(h), _ptr(x), _ptr(y),
+                                   _ptr(phi), _ptr(R), _ptr(A)), None)
+
+
 class BoxBatch:
     """One or more independent periodic boxes advanced together on one GPU."""
 

@@ -41,6 +41,7 @@ CLI_UNITS = {
     "spherocyl_find_jam": "cli_find_jam.cpp",
     "spherocyl_qs_compress": "cli_qs_compress.cpp",
     "spherocyl_y_compress": "cli_y_compress.cpp",
+    "spherocyl_configmaker": "cli_configmaker.cpp",
 }
 
 

@@ -252,6 +252,50 @@ static int read_text(std::istream& in, const char* path, int* n, double* hdr, do
   return SC_OK;
 }
 
+// One position file from host arrays; head = Lx Ly packing gamma gamma_total rate dt.
+// On failure *err says why.
+static int write_positions(const char* path, int format, int n, const double head[7],
+                           const double* x, const double* y, const double* p, const double* R,
+                           const double* A, std::string* err) {
+  const double Lx = head[0], Ly = head[1], packing = head[2];
+  if (format == SC_FMT_BIN) {
+    FILE* f = fopen(path, "wb");
+    if (!f) return *err = std::string("cannot open ") + path, SC_E_IO;
+    bool ok = fwrite(&n, sizeof n, 1, f) == 1 && fwrite(head, sizeof(double), 7, f) == 7;
+    for (int k = 0; k < n && ok; k++) {
+      const double v[5] = {x[k], y[k], p[k], R[k], A[k]};
+      ok = fwrite(v, sizeof(double), 5, f) == 5;
+    }
+    ok = (fclose(f) == 0) && ok;
+    return ok ? SC_OK : (*err = std::string("write failed: ") + path, SC_E_IO);
+  }
+  if (format != SC_FMT_SP && format != SC_FMT_SD)
+    return *err = "save_positions: unknown format", SC_E_ARG;
+  if (format == SC_FMT_SD) {
+    FILE* f = fopen(path, "w");
+    if (!f) return *err = std::string("cannot open ") + path, SC_E_IO;
+    fprintf(f, "%d %.17g %.17g %f %.17g %.14g %g %g\n", n, Lx, Ly, packing, head[3], head[4],
+            head[5], head[6]);
+    for (int k = 0; k < n; k++)
+      fprintf(f, "%.17g %.17g %.17g %.2g %.17g\n", x[k], y[k], p[k], R[k], A[k]);
+    bool ok = fclose(f) == 0;
+    return ok ? SC_OK : (*err = std::string("write failed: ") + path, SC_E_IO);
+  }
+  std::ofstream o(path);
+  if (!o) return *err = std::string("cannot open ") + path, SC_E_IO;
+  o.precision(14);
+  // the src/cpp header has one box length; a rectangular box (after a rotation or
+  // pure shear) takes the src/cuda header's two, which the reader tells by its length
+  o << n << " " << Lx << " ";
+  if (Ly != Lx) o << Ly << " ";
+  o << packing << " " << head[3] << " " << head[4] << " " << head[5] << " " << head[6]
+    << std::endl;
+  for (int k = 0; k < n; k++)
+    o << x[k] << " " << y[k] << " " << p[k] << " " << R[k] << " " << A[k] << std::endl;
+  o.close();
+  return o ? SC_OK : (*err = std::string("write failed: ") + path, SC_E_IO);
+}
+
 int sc_save_positions(sc_handle* H, int sys, const char* path, int format) {
   if (!H || !path) return SC_E_ARG;
   sc::Handle& h = H->h;
@@ -261,45 +305,24 @@ int sc_save_positions(sc_handle* H, int sys, const char* path, int format) {
   if (rc) return rc;
   const sc::HostSys& S = h.hs[sys];
   double packing = S.packing * (h.hs[sys].Lx > 0 ? 1.0 : 0.0);
-  if (format == SC_FMT_BIN) {
-    FILE* f = fopen(path, "wb");
-    if (!f) return io_fail(&h, SC_E_IO, std::string("cannot open ") + path);
-    const double head[7] = {S.Lx, S.Ly, packing, S.gamma, S.gamma_total, S.strain_rate, S.step};
-    bool ok = fwrite(&S.n, sizeof S.n, 1, f) == 1 && fwrite(head, sizeof(double), 7, f) == 7;
-    for (int k = 0; k < S.n && ok; k++) {
-      const double v[5] = {x[k], y[k], p[k], h.h_R[S.p0 + k], h.h_A[S.p0 + k]};
-      ok = fwrite(v, sizeof(double), 5, f) == 5;
-    }
-    ok = (fclose(f) == 0) && ok;
-    return ok ? SC_OK : io_fail(&h, SC_E_IO, std::string("write failed: ") + path);
+  const double head[7] = {S.Lx, S.Ly, packing, S.gamma, S.gamma_total, S.strain_rate, S.step};
+  std::string err;
+  rc = write_positions(path, format, S.n, head, x.data(), y.data(), p.data(), h.h_R.data() + S.p0,
+                       h.h_A.data() + S.p0, &err);
+  return rc ? io_fail(&h, rc, err) : SC_OK;
+}
+
+int sc_write_positions(const char* path, int format, int n, const double* hdr, const double* x,
+                       const double* y, const double* phi, const double* R, const double* A) {
+  sc::g_noh_error.clear();
+  if (!path || !hdr || n < 0 || (n > 0 && (!x || !y || !phi || !R || !A))) {
+    sc::g_noh_error = "sc_write_positions: needs a path, a header and n >= 0 rows";
+    return SC_E_ARG;
   }
-  if (format != SC_FMT_SP && format != SC_FMT_SD)
-    return io_fail(&h, SC_E_ARG, "sc_save_positions: unknown format");
-  if (format == SC_FMT_SD) {
-    FILE* f = fopen(path, "w");
-    if (!f) return io_fail(&h, SC_E_IO, std::string("cannot open ") + path);
-    fprintf(f, "%d %.17g %.17g %f %.17g %.14g %g %g\n", S.n, S.Lx, S.Ly, packing, S.gamma,
-            S.gamma_total, S.strain_rate, S.step);
-    for (int k = 0; k < S.n; k++)
-      fprintf(f, "%.17g %.17g %.17g %.2g %.17g\n", x[k], y[k], p[k], h.h_R[S.p0 + k],
-              h.h_A[S.p0 + k]);
-    bool ok = fclose(f) == 0;
-    return ok ? SC_OK : io_fail(&h, SC_E_IO, std::string("write failed: ") + path);
-  }
-  std::ofstream o(path);
-  if (!o) return io_fail(&h, SC_E_IO, std::string("cannot open ") + path);
-  o.precision(14);
-  // the src/cpp header has one box length; a rectangular box (after a rotation or
-  // pure shear) takes the src/cuda header's two, which the reader tells by its length
-  o << S.n << " " << S.Lx << " ";
-  if (S.Ly != S.Lx) o << S.Ly << " ";
-  o << packing << " " << S.gamma << " " << S.gamma_total << " " << S.strain_rate << " " << S.step
-    << std::endl;
-  for (int k = 0; k < S.n; k++)
-    o << x[k] << " " << y[k] << " " << p[k] << " " << h.h_R[S.p0 + k] << " " << h.h_A[S.p0 + k]
-      << std::endl;
-  o.close();
-  return o ? SC_OK : io_fail(&h, SC_E_IO, std::string("write failed: ") + path);
+  std::string err;
+  int rc = write_positions(path, format, n, hdr, x, y, phi, R, A, &err);
+  if (rc) sc::g_noh_error = err;
+  return rc;
 }
 
 int sc_run_strain(sc_handle* H, const char* out_dir, double run_gamma, double pos_save,
