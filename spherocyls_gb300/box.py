@@ -354,7 +354,8 @@ class BoxBatch:
                  ftol: float = 1e-13, max_iter: int = 200000, max_steps: int = 10000):
         """Bisect each system's packing fraction to energy per particle e_jam
         (find_jam_2p); returns (phi[nsys], resizes made), phi negated where
-        max_steps ran out first."""
+        max_steps ran out first.  Raises ScError (SC_E_NOCONV) if a phase's step
+        grows to 1 before the energy crosses e_jam."""
         pj = np.empty(self.nsys)
         n = ctypes.c_int()
         self._chk(lib().sc_find_jam(self.h, float(e_jam), float(step), float(min_step),
