@@ -74,6 +74,8 @@ typedef struct sc_options {
   int contact_model; /* SC_CONTACT_* */
   int stage_inputs;  /* 1: copy the input arrays to the device before building the state,
                       * also where the GPU reads pageable host memory in place (0) */
+  int cg_max_probes; /* energy probes one conjugate-gradient line search may take before
+                      * its system stops with SC_CG_PROBES, 0 = default (256) */
 } sc_options;
 
 const char *sc_version(void);
@@ -160,13 +162,16 @@ int sc_gd_minimize(sc_handle *h, int max_steps, double e_min, int *steps_taken,
  * E(2s); on failure steepest descent, then F/sqrt|F|.  A system stops at zero force
  * (reason SC_CG_ZERO_FORCE), three equal iteration energies (SC_CG_STALLED), no
  * lower energy in any direction (SC_CG_STEP) or max_iter iterations
- * (SC_CG_MAX_ITER).  iters, energy (the calc_se energy at the end) and reason take
- * n_sys entries each and may be NULL.  Returns SC_E_NOCONV when a system reached
- * max_iter. */
+ * (SC_CG_MAX_ITER).  A line search that still asks for another energy probe after
+ * sc_options.cg_max_probes probes (the reference's search has no such cap; its step
+ * limits end it within about 135) stops its system with SC_CG_PROBES.  iters, energy
+ * (the calc_se energy at the end) and reason take n_sys entries each and may be NULL.
+ * Returns SC_E_NOCONV when a system reached max_iter or the probe cap. */
 #define SC_CG_ZERO_FORCE 1
 #define SC_CG_STALLED 2
 #define SC_CG_STEP 3
 #define SC_CG_MAX_ITER 4
+#define SC_CG_PROBES 5
 int sc_cg_minimize(sc_handle *h, int max_iter, int *iters, double *energy, int *reason);
 /* Production minimiser: FIRE on every system of the handle, on the device, until
  * every |F_i| and |tau_i|/sqrt(I_i) is below ftol, or max_iter iterations.  Replaces
@@ -369,10 +374,16 @@ int sc_run_minimize(sc_handle *h, const char *out_dir, int max_steps, double e_m
  * (NULL: the default stream), asynchronously.  The cell lists live in one fixed
  * file-scope device array (about 0.9 MB, resident on every GPU that loads the
  * library until the process exits); no cudaMalloc, cudaFree or other allocation is
- * made.  n above SC_NOALLOC_MAX_PARTICLES is rejected with SC_E_ARG.  The first call
- * on a device looks up the array's address on that device: make it before any
- * stream capture.  Calls share the array, so calls that overlap on the GPU race;
- * serialise them.  sc_noalloc_last_error() describes the last failure. */
+ * made.  n above SC_NOALLOC_MAX_PARTICLES is rejected with SC_E_ARG, and so is a
+ * non-finite gamma.  Any gamma is served: past |gamma| = 1/2 the cells widen to
+ * 2 sqrt(1 + gamma^2)(R_max + A_max) + pad, the width the handle's grid takes for
+ * shear past 1/2 (sc_strain_to_gamma).  A box only a few cells wide (large R + A
+ * against L) sorts each crowded cell on one thread, so such calls are slow for
+ * large n.  The first call on a device looks up the array's address on that device
+ * and keeps it for the process: make that call before any stream capture, and make
+ * no call on a device after cudaDeviceReset on it.  Calls share the array, so calls
+ * that overlap on the GPU race; serialise them.  sc_noalloc_last_error() describes
+ * the last failure. */
 #define SC_NOALLOC_MAX_PARTICLES 65536
 int sc_forces_noalloc(int n, double L, double gamma, double pad, const double *d_x,
                       const double *d_y, const double *d_phi, const double *d_R,

@@ -27,19 +27,31 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libspherocyl_ref.so")
-REF_SRC_DEFAULT = "/root/reference/src/cpp"
+# The reference checkout (its root, holding src/cpp and src/cuda) is named by the
+# SPHEROCYLS_REF environment variable; without it nothing is built from it.
+REF_ENV = "SPHEROCYLS_REF"
+
+
+def ref_root() -> str | None:
+    root = os.environ.get(REF_ENV)
+    return root if root and os.path.isdir(root) else None
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int)
 
 
-def build(with_ref: bool | None = None, ref_src: str = REF_SRC_DEFAULT) -> None:
-    """Compile the oracle (and, when the reference checkout exists, oracle/_ref)."""
+def build(with_ref: bool | None = None) -> None:
+    """Compile the oracle (and, when $SPHEROCYLS_REF names the reference checkout,
+    oracle/_ref from its src/cpp)."""
     subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
+    root = ref_root()
     if with_ref is None:
-        with_ref = os.path.isdir(ref_src)
+        with_ref = root is not None and os.path.isdir(os.path.join(root, "src", "cpp"))
     if with_ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_SRC={ref_src}"], check=True)
+        if root is None:
+            raise RuntimeError(f"{REF_ENV} does not name the reference checkout")
+        subprocess.run(["make", "-s", "-C", HERE, "ref",
+                        f"REF_SRC={os.path.join(root, 'src', 'cpp')}"], check=True)
 
 
 def _ptr(a: np.ndarray):
@@ -130,6 +142,26 @@ def _lib(kind: str) -> _Lib:
                 raise RuntimeError("reference build oracle/_ref is not available on this machine")
             _LIBS[kind] = _Lib(REF_SO, "ref_")
     return _LIBS[kind]
+
+
+def generate_packing(n: int, packing: float, a_over_r: float, r_small: float = 0.5,
+                     r_ratio: float = 1.4, seed: int = 0, min_sep: float = 0.1):
+    """The benchmark workload's seeded crossing-free packing (the library's
+    generate_packing, restated so that the CPU arm needs no product code):
+    returns (L, x, y, phi, R, A)."""
+    L = _lib("orc").lib
+    f = L.orc_generate_packing
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                  ctypes.c_double, ctypes.c_uint64, ctypes.c_double, _dp, _dp, _dp, _dp, _dp, _dp]
+    x, y, p, R, A = (np.empty(n) for _ in range(5))
+    out = ctypes.c_double()
+    rc = f(int(n), float(packing), float(a_over_r), float(r_small), float(r_ratio),
+           ctypes.c_uint64(int(seed)), float(min_sep), _ptr(x), _ptr(y), _ptr(p), _ptr(R), _ptr(A),
+           ctypes.byref(out))
+    if rc != 0:
+        raise RuntimeError(f"oracle packing generation failed ({rc})")
+    return out.value, x, y, p, R, A
 
 
 class _BoxBase:

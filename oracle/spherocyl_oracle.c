@@ -17,6 +17,7 @@
  * traversal order (own cell, then the 8 neighbour cells in table order).
  */
 #include <math.h>
+#include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -1041,4 +1042,142 @@ int orc_run_gd_steps(orc_box *b, int nsteps, double emin, double *e_out) {
     if (orc_gd_step(b)) return -1;
   }
   return s;
+}
+
+/* ---- workload inputs: the seeded crossing-free packing ----
+ *
+ * The benchmark's reference arm runs the oracle on the same input packing as the
+ * CUDA arm without loading the product library, so the generator of the inputs is
+ * restated here: a SplitMix64 stream per seed, species alternating by index
+ * (R_small, R_small * r_ratio, as src/cuda/spherocyl_box.cpp:1313-1314), A = a/R * R,
+ * L from the packing fraction sum(pi R^2 + 4 A R)/L^2, and centres and angles
+ * drawn uniformly with a placement redrawn while its spine comes closer than
+ * min_sep (R_i + R_j) to an earlier spine (the reference's own rule,
+ * check_particle_cross src/cpp/spherocyl_box.cpp:597-645, rejects only touching
+ * spines and lets crossing-prone starts through; see the reference's 0/0 force
+ * direction at src/cpp/strain_dynamics.cpp:58-62).  The draws and the rejection
+ * test are the same floating-point operations as the library's generator, so the
+ * two give the same packing bit for bit (tests/test_oracle_pin.py). */
+
+static uint64_t sm64_next(uint64_t *s) {
+  uint64_t z = (*s += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+static double sm64_uniform(uint64_t *s) {
+  return (double)(sm64_next(s) >> 11) * (1.0 / 9007199254740992.0);
+}
+
+static double gen_cross(double ax, double ay, double bx, double by) { return ax * by - ay * bx; }
+
+/* distance from a point to the segment c + t u, t in [-1, 1] */
+static double gen_point_seg(double px, double py, double cx, double cy, double ux, double uy) {
+  double uu = ux * ux + uy * uy;
+  double t = 0.0;
+  if (uu > 0) {
+    t = ((px - cx) * ux + (py - cy) * uy) / uu;
+    t = t < -1 ? -1 : (t > 1 ? 1 : t);
+  }
+  double dx = px - (cx + t * ux), dy = py - (cy + t * uy);
+  return sqrt(dx * dx + dy * dy);
+}
+
+/* distance between the segments a + s u and b + t v: zero when they cross, else the
+ * least endpoint-to-segment distance */
+static double gen_seg_seg(double ax, double ay, double ux, double uy, double bx, double by,
+                          double vx, double vy) {
+  double p0x = ax - ux, p0y = ay - uy, p1x = ax + ux, p1y = ay + uy;
+  double q0x = bx - vx, q0y = by - vy, q1x = bx + vx, q1y = by + vy;
+  double d1 = gen_cross(q1x - q0x, q1y - q0y, p0x - q0x, p0y - q0y);
+  double d2 = gen_cross(q1x - q0x, q1y - q0y, p1x - q0x, p1y - q0y);
+  double d3 = gen_cross(p1x - p0x, p1y - p0y, q0x - p0x, q0y - p0y);
+  double d4 = gen_cross(p1x - p0x, p1y - p0y, q1x - p0x, q1y - p0y);
+  if (((d1 > 0 && d2 < 0) || (d1 < 0 && d2 > 0)) && ((d3 > 0 && d4 < 0) || (d3 < 0 && d4 > 0)))
+    return 0.0;
+  double m = gen_point_seg(p0x, p0y, bx, by, vx, vy);
+  m = fmin(m, gen_point_seg(p1x, p1y, bx, by, vx, vy));
+  m = fmin(m, gen_point_seg(q0x, q0y, ax, ay, ux, uy));
+  m = fmin(m, gen_point_seg(q1x, q1y, ax, ay, ux, uy));
+  return m;
+}
+
+int orc_generate_packing(int n, double packing, double a_over_r, double r_small, double r_ratio,
+                         uint64_t seed, double min_sep, double *x, double *y, double *phi,
+                         double *R, double *A, double *L_out) {
+  if (n < 2 || !(packing > 0 && packing < 1) || !(a_over_r >= 0) || !(r_small > 0) ||
+      !(r_ratio > 0) || !(min_sep >= 0) || !x || !y || !phi || !R || !A || !L_out)
+    return 1;
+  const double pi = 3.14159265358979323846;
+  double filled = 0.0, rmax = 0.0, amax = 0.0;
+  for (int i = 0; i < n; i++) {
+    R[i] = (i % 2 == 0) ? r_small : r_small * r_ratio;
+    A[i] = a_over_r * R[i];
+    filled += pi * R[i] * R[i] + 4.0 * A[i] * R[i];
+    rmax = fmax(rmax, R[i]);
+    amax = fmax(amax, A[i]);
+  }
+  const double L = sqrt(filled / packing);
+  *L_out = L;
+  /* bins of at least the reach: two spines closer than min_sep (R_i + R_j) have
+   * centres within 2 A_max + 2 min_sep R_max; a bin list is a linked list */
+  const double reach = 2.0 * amax + 2.0 * min_sep * rmax;
+  int ng = (int)(L / fmax(reach, 1e-300));
+  if (ng > 2048) ng = 2048;
+  const int gridded = ng >= 3;
+  if (!gridded) ng = 1;
+  const double gw = L / ng;
+  int *head = (int *)malloc((size_t)ng * ng * sizeof(int));
+  int *next = (int *)malloc((size_t)n * sizeof(int));
+  if (!head || !next) {
+    free(head);
+    free(next);
+    return 2;
+  }
+  for (long c = 0; c < (long)ng * ng; c++) head[c] = -1;
+  uint64_t rng = seed * 0x2545F4914F6CDD1Dull + 0x1234567ull;
+  const long max_tries = 1000000;
+  int rc = 0;
+  for (int i = 0; i < n && rc == 0; i++) {
+    long tries = 0;
+    for (;;) {
+      if (++tries > max_tries) {
+        rc = 3;
+        break;
+      }
+      double xi = L * sm64_uniform(&rng), yi = L * sm64_uniform(&rng);
+      double pi_ = pi * sm64_uniform(&rng);
+      double ux = A[i] * cos(pi_), uy = A[i] * sin(pi_);
+      int gx = gridded ? (int)(xi / gw) : 0, gy = gridded ? (int)(yi / gw) : 0;
+      if (gx > ng - 1) gx = ng - 1;
+      if (gy > ng - 1) gy = ng - 1;
+      int ok = 1, span = gridded ? 1 : 0;
+      for (int a = -span; a <= span && ok; a++)
+        for (int b = -span; b <= span && ok; b++) {
+          int cx = (gx + b + ng) % ng, cy = (gy + a + ng) % ng;
+          for (int j = head[(long)cy * ng + cx]; j >= 0; j = next[j]) {
+            double dx = xi - x[j], dy = yi - y[j];
+            dx -= L * round(dx / L);
+            dy -= L * round(dy / L);
+            double vx = A[j] * cos(phi[j]), vy = A[j] * sin(phi[j]);
+            if (gen_seg_seg(dx, dy, ux, uy, 0.0, 0.0, vx, vy) < min_sep * (R[i] + R[j])) {
+              ok = 0;
+              break;
+            }
+          }
+        }
+      if (!ok) continue;
+      x[i] = xi;
+      y[i] = yi;
+      phi[i] = pi_;
+      long c = (long)gy * ng + gx;
+      next[i] = head[c];
+      head[c] = i;
+      break;
+    }
+  }
+  free(head);
+  free(next);
+  return rc;
 }

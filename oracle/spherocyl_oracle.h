@@ -8,6 +8,8 @@
 #ifndef SPHEROCYL_ORACLE_H
 #define SPHEROCYL_ORACLE_H
 
+#include <stdint.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -52,6 +54,12 @@ void orc_get_scalars(const orc_box *b, double *out);
 void orc_get_se(const orc_box *b, double *out);
 long orc_get_pairs(const orc_box *b, int *pairs, long cap);
 long orc_n_rebuilds(const orc_box *b);
+
+/* The benchmark workload's input packing (seeded, crossing-free; the same packing as
+ * the library's sc_generate_packing).  Returns 0 on success. */
+int orc_generate_packing(int n, double packing, double a_over_r, double r_small, double r_ratio,
+                         uint64_t seed, double min_sep, double *x, double *y, double *phi,
+                         double *R, double *A, double *L_out);
 
 #ifdef __cplusplus
 }

@@ -43,6 +43,7 @@ class ScOptions(ctypes.Structure):
         ("profile", ctypes.c_int),
         ("contact_model", ctypes.c_int),
         ("stage_inputs", ctypes.c_int),
+        ("cg_max_probes", ctypes.c_int),
     ]
 
 

@@ -157,7 +157,8 @@ class BoxBatch:
     def __init__(self, n_per_sys, L, x, y, phi, A, R, pad=0.0, *, precision: str = "fp64",
                  stress: str = "compat", device: int = 0, max_nbrs: int = 0,
                  use_graphs: bool = True, block: int = 0, profile: bool = False,
-                 contacts: int = 1, Ly=None, stage_inputs: bool = False):
+                 contacts: int = 1, Ly=None, stage_inputs: bool = False,
+                 cg_max_probes: int = 0):
         n_per_sys = np.ascontiguousarray(np.atleast_1d(n_per_sys), dtype=np.int32)
         self.nsys = int(n_per_sys.shape[0])
         self.n_per_sys = n_per_sys
@@ -181,6 +182,7 @@ class BoxBatch:
             raise ValueError("contacts must be 1 (one contact per pair) or 2")
         opt.contact_model = 1 if int(contacts) == 2 else 0
         opt.stage_inputs = int(bool(stage_inputs))
+        opt.cg_max_probes = int(cg_max_probes)
         self.precision = precision
         h = ctypes.c_void_p()
         nps = n_per_sys.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
@@ -297,7 +299,8 @@ class BoxBatch:
         """The reference's Polak-Ribiere conjugate gradient (cjpr_relax_2p,
         src/cuda/2point_dynamics.cu:4233-4296) on every system: returns per-system
         (iterations, energy, stop reason) with reason 1 zero force, 2 three equal
-        energies, 3 no lower energy along any direction, 4 max_iter."""
+        energies, 3 no lower energy along any direction, 4 max_iter, 5 a line search
+        that reached the probe cap (the handle's cg_max_probes)."""
         it = np.zeros(self.nsys, dtype=np.int32)
         e = np.zeros(self.nsys)
         why = np.zeros(self.nsys, dtype=np.int32)

@@ -112,6 +112,7 @@ __global__ void k_cg_begin(Dev d, CgState c, int max_iter, unsigned long long se
   q.max_step = 2 / q.norm;
   q.attempt = 0;
   q.redirect = 0;
+  q.probes = 0;
   q.t = q.step;
   q.phase = CG_TOP;
   *c.searching = 1;
@@ -213,7 +214,10 @@ __device__ void cg_find_min(CgSys& q) {
 // probe (line_search_2p :3609-3780 as a flat state machine: TOP probes the step,
 // SECOND twice the step, HALVE and DOUBLE are the reference's recursive calls with
 // (first, second) = (1, 0) and (0, 1), FINAL the parabola's minimum).  `search` is
-// switched off when no system probes again.
+// switched off when no system probes again.  The halvings and doublings are bounded
+// by the step limits (about 45 probes per direction attempt, three attempts), and a
+// search that still asks for another probe after c.max_probes ends its system with
+// reason CG_PROBES, so the WHILE node ends whatever the energies do.
 __global__ void k_cg_search(Dev d, CgState c, unsigned long long search) {
   bool again = false;
   for (int s = threadIdx.x; s < d.nsys; s += blockDim.x) {
@@ -260,6 +264,12 @@ __global__ void k_cg_search(Dev d, CgState c, unsigned long long search) {
           if (E > q.E1) q.tmin = 1;
           q.phase = CG_MOVE;
           break;
+      }
+      q.probes += 1;
+      if (!q.done && q.phase >= CG_TOP && q.phase <= CG_FINAL && q.probes >= c.max_probes) {
+        q.phase = CG_IDLE;
+        q.done = 1;
+        q.reason = CG_PROBES;
       }
       again = again || (!q.done && q.phase >= CG_TOP && q.phase <= CG_FINAL);
     }

@@ -345,7 +345,7 @@ bool Handle::rebuild_all() {
 }
 
 void Handle::launch_pass(int mode, bool se, int row, bool fast) {
-  kernels += 1;
+  kernels += (prec == PREC_MIXED && se) ? 3 : 1;  // mixed: the FP64 stress kernels
   Dev dd = d;
   dd.cond = (mode == PASS_CORR_STRAIN || mode == PASS_CORR_RESIZE) ? step_cond : 0;
   if (prec == PREC_MIXED)
@@ -1065,6 +1065,7 @@ bool Handle::ensure_cg() {
   cg.sys = sys;
   cg.part = part;
   cg.searching = searching;
+  cg.max_probes = opt.cg_max_probes > 0 ? opt.cg_max_probes : kCgMaxProbes;
   d.cg0x = x0;  // the rebuild permutes the previous forces from now on
   d.cg0y = y0;
   d.cg0p = p0;
@@ -1160,7 +1161,13 @@ bool Handle::run_cg_eager(int max_iter) {
   for (int k = 0; k < kCgChunk; k++) {
     if (!cuda_ok(cudaMemsetAsync(cg.searching, 0, sizeof(int), stream), "cg flag")) return false;
     enqueue_cg_head(max_iter, 0, stream);
-    for (;;) {
+    // the device ends every search within max_probes probes; this bound only
+    // guards the host against a device state that never clears the word
+    for (int probe = 0;; probe++) {
+      if (probe > cg.max_probes + 8) {
+        fail(SC_E_NOCONV, "cg: a line search did not end within its probe cap");
+        return false;
+      }
       int searching = 0;
       if (!cuda_ok(cudaMemcpyAsync(h_pinned + 2, cg.searching, sizeof(int),
                                    cudaMemcpyDeviceToHost, stream), "cg flag") ||
@@ -1219,12 +1226,17 @@ int Handle::cg_minimize(int max_iter, int* iters, double* energy, int* reason) {
   }
   pred_valid = false;
   forces_valid = false;
-  bool capped = false;
+  bool capped = false, probes = false;
   for (int s = 0; s < nsys; s++) {
     if (iters) iters[s] = hsys[s].iters;
     if (energy) energy[s] = hsys[s].E0;
     if (reason) reason[s] = hsys[s].reason;
     capped = capped || hsys[s].reason == CG_MAX_ITER;
+    probes = probes || hsys[s].reason == CG_PROBES;
+  }
+  if (probes) {
+    fail(SC_E_NOCONV, "cg: a line search reached its probe cap (reason SC_CG_PROBES)");
+    return SC_E_NOCONV;
   }
   return capped ? SC_E_NOCONV : SC_OK;
 }

@@ -78,7 +78,8 @@ struct FireState {
 enum CgPhase { CG_IDLE = 0, CG_TOP = 1, CG_SECOND = 2, CG_HALVE = 3, CG_DOUBLE = 4,
                CG_FINAL = 5, CG_MOVE = 6 };
 enum CgReason { CG_RUNNING = 0, CG_ZERO_FORCE = 1, CG_STALLED = 2, CG_STEP = 3,
-                CG_MAX_ITER = 4 };
+                CG_MAX_ITER = 4, CG_PROBES = 5 };
+constexpr int kCgMaxProbes = 256;  // default probe cap of one line search
 struct CgSys {
   double E0, E1, E2;     // energies at 0, one step and two steps along D
   double Eh1, Eh2;       // iteration-start energies of the two iterations before
@@ -89,12 +90,14 @@ struct CgSys {
   int phase, attempt;    // CgPhase; 0 PR direction, 1 steepest descent, 2 sqrt-scaled
   int redirect;          // the next probe first sets D (1: F, 2: F/sqrt|F|)
   int done, reason, iters;
+  int probes;            // energy probes of this iteration's line search
 };
 
 struct CgState {
   CgSys* sys;      // [nsys]
   double* part;    // [3 * npchunks] chunk partials of |F|^2, F.F0, |F0|^2
   int* searching;  // any system probing (for the host-driven loop)
+  int max_probes;  // a line search that needs more probes ends the system (CG_PROBES)
 };
 
 // Device pointers handed to every kernel by value.
@@ -262,6 +265,8 @@ void launch_mx_local(const Dev& d, const StepScalars* tab, int row, bool all, cu
 void launch_mx_order(const Dev& d, bool all, cudaStream_t st);
 void launch_mx_build_list(const Dev& d, const StepScalars* tab, int row, bool all,
                           cudaStream_t st);
+// FP64 stress and energy partials of the mixed state (two kernels)
+void launch_mx_se64(const Dev& d, const StepScalars* tab, int row, cudaStream_t st);
 
 constexpr int kWalkBlocks = 152 * 8;  // fixed grid of the worklist kernels
 

@@ -12,7 +12,9 @@
 // The scratch array exists once per GPU that loads the library and stays resident
 // until the process exits.  Its device address is looked up once per device
 // (cudaGetSymbolAddress, with that device current) on the first call made on that
-// device; make that first call before any stream capture.  Every call shares the
+// device and kept for the process; make that first call before any stream capture,
+// and make no call on a device after cudaDeviceReset on it (the reset unloads the
+// module, so the kept address no longer names the array).  Every call shares the
 // array and leaves the previous call's lists in it; the cell counters are cleared
 // at the start of each call.  Calls whose work overlaps on the GPU (two streams,
 // or two host threads on one device) race on the array: serialise them.
@@ -21,6 +23,7 @@
 // uses the reference's operation order.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <mutex>
 #include <string>
 
@@ -62,9 +65,13 @@ __host__ __device__ inline NaView na_view(int* base) {
 }
 
 // configure_cells (src/cpp/spherocyl_box.cpp:223-241) on the device: the largest
-// R and A, the grid, and a cleared counter for every cell used.
-__global__ void k_na_setup(int* scratch, int n, double L, double pad, const double* R,
-                           const double* A) {
+// R and A, the grid, and a cleared counter for every cell used.  The cell width
+// factor is the reference's 2.24 for |gamma| <= 1/2 and 2 sqrt(1 + gamma^2) beyond
+// (the width the handle's grid takes for shear past gamma = 1/2): in sheared
+// coordinates two touching spines are at most 2 (R + A) sqrt(1 + gamma^2) apart in
+// x, so the 3x3 block of cells holds every contact at any gamma.
+__global__ void k_na_setup(int* scratch, int n, double L, double pad, double wfac,
+                           const double* R, const double* A) {
   NaView v = na_view(scratch);
   __shared__ double sr[256], sa[256];
   double r = 0.0, a = 0.0;
@@ -85,7 +92,7 @@ __global__ void k_na_setup(int* scratch, int n, double L, double pad, const doub
   __shared__ int dims[2];
   if (threadIdx.x == 0) {
     double ra = sr[0] + sa[0];
-    double wmin = 2.24 * ra + pad, hmin = 2 * ra + pad;
+    double wmin = wfac * ra + pad, hmin = 2 * ra + pad;
     int rows = (int)(L / hmin), cols = (int)(L / wmin);
     rows = rows > 1 ? rows : 1;
     cols = cols > 1 ? cols : 1;
@@ -265,6 +272,12 @@ extern "C" int sc_forces_noalloc(int n, double L, double gamma, double pad, cons
     g_na_error = "sc_forces_noalloc: L > 0, pad >= 0 and all ten device arrays are required";
     return SC_E_ARG;
   }
+  if (!std::isfinite(gamma) || std::fabs(gamma) > 1e6) {
+    g_na_error = "sc_forces_noalloc: gamma must be finite (|gamma| <= 1e6)";
+    return SC_E_ARG;
+  }
+  // the sheared-grid width factor of the handle's grid (see k_na_setup)
+  const double wfac = std::fabs(gamma) > 0.5 ? 2 * std::sqrt(gamma * gamma + 1) : 2.24;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
     g_na_error = "sc_forces_noalloc: no current CUDA device";
@@ -287,7 +300,7 @@ extern "C" int sc_forces_noalloc(int n, double L, double gamma, double pad, cons
     scratch = g_na_addr[dev];
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  k_na_setup<<<1, 256, 0, st>>>(scratch, n, L, pad, R, A);
+  k_na_setup<<<1, 256, 0, st>>>(scratch, n, L, pad, wfac, R, A);
   int grid = (n + 255) / 256;
   k_na_hash<<<grid, 256, 0, st>>>(scratch, n, L, x, y);
   k_na_scan<<<1, 1024, 0, st>>>(scratch);

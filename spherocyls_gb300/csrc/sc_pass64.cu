@@ -323,6 +323,83 @@ __global__ void __launch_bounds__(128) k_pass64(Dev d, const StepScalars* __rest
   }
 }
 
+// ---- stress and energy of the mixed form, in FP64 ----
+//
+// The mixed form advances with FP32 pair forces, but the stress tensor and the
+// energy it reports are those of the FP64 form at its state: on the steps that
+// record them, the compensated state (FP32 value plus FP32 compensation, about
+// 48 bits) is widened to FP64 relative to each particle's cell centre, the shaft
+// vectors are recomputed in FP64, and every listed pair is evaluated by the FP64
+// pair code (the reference's operation order, lower particle index as "p") with
+// the sums of calc_se (src/cpp/spherocyl_box.cpp:425-522).  The quantities then
+// differ from the FP64 form's only through the states themselves.
+
+// FP64 local positions and shaft vectors of the state (scratch: the FP64 predictor
+// arrays, which the mixed form does not use)
+__global__ void k_mx_se_prep(Dev d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.ntot) return;
+  const float4 r = d.rec[i];
+  const float4 c = d.mc[i];
+  const double phi = (double)c.z + (double)c.w;
+  const double A = d.ra[i].y;
+  double sn, cs;
+  sincos(phi, &sn, &cs);
+  d.xy_t[i] = make_double2((double)r.x + (double)c.x, (double)r.y + (double)c.y);
+  d.nxy_t[i] = make_double2(A * cs, A * sn);
+}
+
+// One thread per slot over the mixed list (entries: slot | cell offset code); each
+// pair once, from its lower particle index.  The state's scalars (the _p fields).
+template <bool TWO>
+__global__ void __launch_bounds__(128) k_mx_se64(Dev d, const StepScalars* __restrict__ tab,
+                                                int row) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.ntot) return;
+  const int s = d.psys[i];
+  const SysGeom& g = d.geom[s];
+  const StepScalars& ts = tab[row * d.nsys + s];
+  const double W = ts.W_p, H = ts.H_p, gamma = ts.gamma_p, Lx = ts.Lx_p, Ly = ts.Ly_p;
+  const bool virial = d.stress_mode == STRESS_VIRIAL;
+  const double two_n = 2.0 * g.n;
+  const double2 pi = d.xy_t[i];
+  const double2 ni = d.nxy_t[i];
+  const double2 rai = d.ra[i];
+  const int idi = d.id[i];
+  double se0 = 0.0, se1 = 0.0, se2 = 0.0, se3 = 0.0, se4 = 0.0;
+  int cnt = d.nbr_n[i];
+  if (cnt > d.maxn) cnt = d.maxn;
+  for (int k = 0; k < cnt; k++) {
+    const unsigned e = (unsigned)d.nbr[(size_t)k * d.ntot + i];
+    const int j = (int)(e & kSlotMask);
+    if (!(idi < d.id[j])) continue;
+    const double2 pj = d.xy_t[j];
+    const double2 nj = d.nxy_t[j];
+    const double2 raj = d.ra[j];
+    // x_i - x_j with the cell centres: the neighbour's cell is (dc, dr) away
+    const double dX = (pi.x - pj.x) + (double)(1 - (int)((e >> 28) & 3u)) * W;
+    const double dY = (pi.y - pj.y) + (double)(1 - (int)(e >> 30)) * H;
+    PairF64 o;
+    const bool hit =
+        TWO ? pair2_fp64<true>(dX, dY, ni.x, ni.y, rai.y, nj.x, nj.y, raj.y, rai.x + raj.x,
+                               gamma, Lx, Ly, two_n, o)
+            : pair_fp64<true>(dX, dY, ni.x, ni.y, rai.y, nj.x, nj.y, raj.y, rai.x + raj.x, gamma,
+                              Lx, Ly, virial, two_n, o);
+    if (hit) {
+      se0 += o.e;
+      se1 += o.pxx;
+      se2 += o.pyy;
+      se3 += o.pxy;
+      se4 += o.pyx;
+    }
+  }
+  d.se_part[i] = se0;
+  d.se_part[(size_t)d.ntot + i] = se1;
+  d.se_part[(size_t)2 * d.ntot + i] = se2;
+  d.se_part[(size_t)3 * d.ntot + i] = se3;
+  d.se_part[(size_t)4 * d.ntot + i] = se4;
+}
+
 template <int MODE, bool SE>
 void launch_one(const Dev& d, const StepScalars* tab, int row, cudaStream_t st) {
   int block = 128;
@@ -362,6 +439,15 @@ void launch_pass_fp64(const Dev& d, int mode, bool se, const StepScalars* tab, i
       break;
     case PASS_ENERGY_T: launch_one<PASS_ENERGY_T, true>(d, tab, row, st); break;
   }
+}
+
+void launch_mx_se64(const Dev& d, const StepScalars* tab, int row, cudaStream_t st) {
+  const int grid = (d.ntot + 127) / 128;
+  k_mx_se_prep<<<grid, 128, 0, st>>>(d);
+  if (d.contact_model == 1)
+    k_mx_se64<true><<<grid, 128, 0, st>>>(d, tab, row);
+  else
+    k_mx_se64<false><<<grid, 128, 0, st>>>(d, tab, row);
 }
 
 void launch_build_nbrs(const Dev& d, const StepScalars* tab, int row, cudaStream_t st) {

@@ -4,9 +4,10 @@
 // last sorted into, as an FP32 value plus an FP32 compensation term (Kahan), and
 // its angle likewise; the absolute FP64 position is (col+1/2)W + x_local + x_comp,
 // materialised only for the cell sort, the Lees-Edwards set-back and for output.
-// Pair geometry and forces are FP32; stress and energy accumulate in FP64.  No
-// FP64 instruction runs in the force passes except the stress/energy sums on the
-// steps that record them.
+// Pair geometry and forces are FP32, and no FP64 instruction runs in the force
+// passes.  On the steps that record stress and energy, those come from an FP64
+// evaluation of the state (k_mx_se64, sc_pass64.cu), so they differ from the FP64
+// form's only through the state itself.
 //
 // Neighbour list: every pair whose spines, in the Lees-Edwards frame of the build,
 // are closer than R_i + R_j + pad (the capsule distance; FP32, bound inflated by
@@ -22,9 +23,7 @@
 // length in the FP32 arithmetic.
 //
 // Force pass: one thread per list position gathers over its particle's list and
-// evaluates each pair from its own side; stress and energy are summed on the
-// lower-index side of each pair, where that evaluation is the reference's (its
-// "p" is the lower index).
+// evaluates each pair from its own side.
 #include "sc_internal.hpp"
 #include "sc_pair.cuh"
 
@@ -53,8 +52,8 @@ __device__ __forceinline__ void kahan_affine(float& s, float& c, float v, float 
   s = t;
 }
 
-template <int MODE, bool SE, bool TWO>
-__global__ void __launch_bounds__(128, TWO ? 6 : (SE ? 10 : 12)) k_pass_mixed(Dev d,
+template <int MODE, bool TWO>
+__global__ void __launch_bounds__(128, TWO ? 6 : 12) k_pass_mixed(Dev d,
                                                        const StepScalars* __restrict__ tab,
                                                        int row) {
   constexpr bool kPred = (MODE == PASS_CORR_STRAIN || MODE == PASS_CORR_RESIZE);
@@ -71,12 +70,10 @@ __global__ void __launch_bounds__(128, TWO ? 6 : (SE ? 10 : 12)) k_pass_mixed(De
   const float gam = kPred ? ts.f_gamma_c : ts.f_gamma_p;
   const bool smallx = g.cols < 3, smally = g.rows < 3;
   const float Lxf = W * g.cols, Lyf = H * g.rows;
-  const bool virial = d.stress_mode == STRESS_VIRIAL;
   constexpr bool two_point = TWO;
 
   const float4 ri = REC[i];
   const float4 pai = d.pa[i];  // (R, A, index bits, 1/I)
-  const int idi = __float_as_int(pai.z);
   const int cnt = d.nbr_pn[pos];
   // the list is column-major: entry k of this slot sits k * ntot words further on;
   // Lst walks it, two entries ahead of the pair being computed
@@ -84,33 +81,27 @@ __global__ void __launch_bounds__(128, TWO ? 6 : (SE ? 10 : 12)) k_pass_mixed(De
   const int stride = d.ntot;
 
   float fx = 0.f, fy = 0.f, tq = 0.f;
-  double e_acc = 0.0, pxx = 0.0, pyy = 0.0, pxy = 0.0, pyx = 0.0;
   // software pipeline: the list entry two ahead and the neighbour data one ahead
   // are in flight while the current pair is computed
   unsigned e1 = cnt > 0 ? __ldg(Lst) : 0u;
   Lst += stride;
   unsigned e2 = cnt > 1 ? __ldg(Lst) : 0u;
-  // the neighbour's record and radius (its A^2 is |shaft|^2 from the record);
-  // its particle index only on the passes that sum stress and energy
+  // the neighbour's record and radius (its A^2 is |shaft|^2 from the record)
   float4 r1 = make_float4(0.f, 0.f, 0.f, 0.f);
   float R1 = 0.f;
-  int id1 = 0;
   if (cnt > 0) {
     r1 = REC[e1 & kSlotMask];
     R1 = d.rf[e1 & kSlotMask];
-    if (SE) id1 = __float_as_int(d.pa[e1 & kSlotMask].z);
   }
   const float ai = pai.y * pai.y;
   for (int k = 0; k < cnt; k++) {
     const unsigned e = e1;
     const float4 rj = r1;
     const float Rj = R1;
-    const int idj = id1;
     e1 = e2;
     if (k + 1 < cnt) {
       r1 = REC[e1 & kSlotMask];
       R1 = d.rf[e1 & kSlotMask];
-      if (SE) id1 = __float_as_int(d.pa[e1 & kSlotMask].z);
     }
     Lst += stride;
     if (k + 2 < cnt) e2 = __ldg(Lst);
@@ -118,53 +109,20 @@ __global__ void __launch_bounds__(128, TWO ? 6 : (SE ? 10 : 12)) k_pass_mixed(De
     float dy = ri.y - rj.y + (float)(1 - (int)(e >> 30)) * H;
     if (smallx) dx += Lxf * (float)((dx < -0.5f * Lxf) - (dx > 0.5f * Lxf));
     if (smally) dy += Lyf * (float)((dy < -0.5f * Lyf) - (dy > 0.5f * Lyf));
-    // Each thread evaluates the pair from its own particle's side (i as "p"):
-    // the forces need no canonical order, the two evaluations of a pair differ
-    // only by FP32 rounding.  Stress and energy, whose compat form is not
-    // symmetric in p and q, are summed on the lower-index side only, where this
-    // evaluation is the reference's.
+    // Each thread evaluates the pair from its own particle's side (i as "p"): the
+    // forces need no canonical order, the two evaluations of a pair differ only by
+    // FP32 rounding.  Stress and energy are not summed here: on the steps that
+    // record them they come from the FP64 evaluation of the state (k_mx_se64).
     PairF32 o;
     const float cj = fmaf(rj.z, rj.z, rj.w * rj.w);
     const bool touch =
         two_point ? pair2_fp32(dx, dy, ri.z, ri.w, ai, rj.z, rj.w, cj, pai.x + Rj, gam, o)
-                  : pair_fp32<SE>(dx, dy, ri.z, ri.w, ai, rj.z, rj.w, cj, pai.x + Rj, gam, virial,
-                                  o);
+                  : pair_fp32<false>(dx, dy, ri.z, ri.w, ai, rj.z, rj.w, cj, pai.x + Rj, gam,
+                                     false, o);
     if (!touch) continue;
     fx += o.fx;
     fy += o.fy;
     tq += o.tp;
-    const bool ip = SE && idi < idj;
-    if (SE && ip && two_point) {
-      e_acc += (double)o.ov;
-      pxx += (double)o.cxa;
-      pyy += (double)o.cya;
-      pxy += (double)o.cxb;
-      pyx += (double)o.cyb;
-    } else if (SE && ip) {
-      {
-        e_acc += (double)(o.ov * o.ov);
-        if (!virial) {
-          pxx += (double)(o.fx * o.cxa) - (double)(o.fx * o.cxb) - (double)(o.fy * o.cxb);
-          pyy += (double)(o.fy * o.cya) - (double)(o.fy * o.cyb);
-          pxy += (double)(o.fy * o.cxa);
-          pyx += (double)(o.fx * o.cya) - (double)(o.fx * o.cyb);
-        } else {
-          pxx += (double)(o.fx * o.cxa) - (double)(o.fx * o.cxb);
-          pyy += (double)(o.fy * o.cya) - (double)(o.fy * o.cyb);
-          pxy += (double)(o.fy * o.cxa) - (double)(o.fy * o.cxb);
-          pyx += (double)(o.fx * o.cya) - (double)(o.fx * o.cyb);
-        }
-      }
-    }
-  }
-  if (SE) {
-    const double Lx = kPred ? ts.Lx_c : ts.Lx_p, Ly = kPred ? ts.Ly_c : ts.Ly_p;
-    const double inv_area = 1.0 / (Lx * Ly);
-    d.se_part[i] = e_acc * 0.5 * g.inv_n;
-    d.se_part[(size_t)d.ntot + i] = pxx * inv_area;
-    d.se_part[(size_t)2 * d.ntot + i] = pyy * inv_area;
-    d.se_part[(size_t)3 * d.ntot + i] = pxy * inv_area;
-    d.se_part[(size_t)4 * d.ntot + i] = pyx * inv_area;
   }
 
   const float dt = ts.f_step;
@@ -281,13 +239,13 @@ __global__ void __launch_bounds__(128, TWO ? 6 : (SE ? 10 : 12)) k_pass_mixed(De
   }
 }
 
-template <int MODE, bool SE>
+template <int MODE>
 void launch_one(const Dev& d, const StepScalars* tab, int row, cudaStream_t st, int block) {
   int grid = (d.ntot + block - 1) / block;
   if (d.contact_model == 1)
-    k_pass_mixed<MODE, SE, true><<<grid, block, 0, st>>>(d, tab, row);
+    k_pass_mixed<MODE, true><<<grid, block, 0, st>>>(d, tab, row);
   else
-    k_pass_mixed<MODE, SE, false><<<grid, block, 0, st>>>(d, tab, row);
+    k_pass_mixed<MODE, false><<<grid, block, 0, st>>>(d, tab, row);
 }
 
 // ---- rebuild support ----
@@ -427,21 +385,14 @@ void launch_pass_mixed(const Dev& d, int mode, bool se, const StepScalars* tab, 
                        cudaStream_t st, int block) {
   if (block <= 0) block = 128;
   switch (mode) {
-    case PASS_FORCE:
-      se ? launch_one<PASS_FORCE, true>(d, tab, row, st, block)
-         : launch_one<PASS_FORCE, false>(d, tab, row, st, block);
-      break;
-    case PASS_CORR_STRAIN: launch_one<PASS_CORR_STRAIN, false>(d, tab, row, st, block); break;
-    case PASS_PRED_STRAIN:
-      se ? launch_one<PASS_PRED_STRAIN, true>(d, tab, row, st, block)
-         : launch_one<PASS_PRED_STRAIN, false>(d, tab, row, st, block);
-      break;
-    case PASS_CORR_RESIZE: launch_one<PASS_CORR_RESIZE, false>(d, tab, row, st, block); break;
-    case PASS_PRED_RESIZE:
-      se ? launch_one<PASS_PRED_RESIZE, true>(d, tab, row, st, block)
-         : launch_one<PASS_PRED_RESIZE, false>(d, tab, row, st, block);
-      break;
+    case PASS_FORCE: launch_one<PASS_FORCE>(d, tab, row, st, block); break;
+    case PASS_CORR_STRAIN: launch_one<PASS_CORR_STRAIN>(d, tab, row, st, block); break;
+    case PASS_PRED_STRAIN: launch_one<PASS_PRED_STRAIN>(d, tab, row, st, block); break;
+    case PASS_CORR_RESIZE: launch_one<PASS_CORR_RESIZE>(d, tab, row, st, block); break;
+    case PASS_PRED_RESIZE: launch_one<PASS_PRED_RESIZE>(d, tab, row, st, block); break;
   }
+  // stress and energy of the state (forces and predictor passes) in FP64
+  if (se) launch_mx_se64(d, tab, row, st);
 }
 
 void launch_mx_materialize(const Dev& d, const StepScalars* tab, int row, bool all,

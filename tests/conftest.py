@@ -35,8 +35,10 @@ def periodic_diff(a, b, period):
 
 @pytest.fixture(scope="session")
 def oracle_built():
+    import __graft_entry__
     import oracle
 
+    __graft_entry__.ref_env()
     oracle.build(with_ref=None)
     return oracle
 

@@ -129,6 +129,9 @@ def case_pairs_geometry(name):
 
 
 def main() -> None:
+    import __graft_entry__
+
+    __graft_entry__.ref_env()  # $SPHEROCYLS_REF: the reference checkout to compile
     oracle.build(with_ref=True)
     if not oracle.ref_available():
         raise SystemExit("the reference build oracle/_ref is needed to make the fixtures")

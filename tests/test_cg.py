@@ -123,3 +123,33 @@ def test_cg_refuses_the_mixed_form(sc):
     with sc.SpherocylBox(L, x, y, p, A, R, 0.2, precision="mixed") as b:
         with pytest.raises(sc.ScError):
             b.cg_minimize(10)
+
+
+@sc_gpu
+@pytest.mark.parametrize("graphs", [True, False])
+def test_cg_probe_cap_stops_the_search_with_a_status(sc, graphs):
+    """A line search that still wants another energy probe after the handle's probe
+    cap (here 2; every search takes at least three probes: the step, twice the
+    step or a halving, and the parabola's minimum) ends its system with reason 5
+    and sc_cg_minimize returns SC_E_NOCONV, through the graph WHILE node and the
+    host-driven loop alike; the handle stays usable."""
+    import ctypes
+
+    from spherocyls_gb300 import _lib
+
+    L, x, y, p, A, R = _packing(sc)
+    b = sc.BoxBatch([256, 256], [L, L], np.r_[x, x], np.r_[y, y], np.r_[p, p], np.r_[A, A],
+                    np.r_[R, R], 0.2, use_graphs=graphs, cg_max_probes=2)
+    it = np.zeros(2, dtype=np.int32)
+    e = np.zeros(2)
+    why = np.zeros(2, dtype=np.int32)
+    ip = ctypes.POINTER(ctypes.c_int)
+    st = _lib.lib().sc_cg_minimize(b.h, 100, it.ctypes.data_as(ip),
+                                   e.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                   why.ctypes.data_as(ip))
+    assert st == _lib.SC_E_NOCONV
+    assert list(why) == [5, 5] and list(it) == [1, 1]
+    assert b"probe cap" in _lib.lib().sc_last_error(b.h)
+    b.calc_forces()  # still usable
+    assert np.all(np.isfinite(np.array(b.forces())))
+    b.close()

@@ -127,3 +127,18 @@ def test_oracle_matches_live_reference_when_available(oracle_built):
         assert np.array_equal(np.array(ob.state()), np.array(rb.state()))
         assert np.array_equal(ob.pairs(), rb.pairs())
     assert ob.scalars() == rb.scalars()
+
+
+@pytest.mark.parametrize("n,phi,aor,seed", [(2, 0.5, 1.0, 0), (600, 0.84, 1.0, 3),
+                                            (5000, 0.86, 0.5, 1), (3000, 0.80, 2.0, 7)])
+def test_oracle_generator_equals_library_generator(library, oracle_built, n, phi, aor, seed):
+    """The CPU reference arm of the benchmark generates its input packing with the
+    oracle's restatement of the library's generator: both give the same packing bit
+    for bit, so the two arms run the same workload."""
+    import spherocyls_gb300 as sc
+
+    a = oracle_built.generate_packing(n, phi, aor, seed=seed)
+    b = sc.generate_packing(n, phi, aor, seed=seed)
+    assert a[0] == b[0]
+    for u, v in zip(a[1:], b[1:]):
+        assert np.array_equal(u, v)
