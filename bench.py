@@ -3,14 +3,23 @@
 Workload (default): N = 1,048,576 bidisperse spherocylinders (R = 0.5 / 0.7
 alternating, A = R), packing fraction 0.84, strain rate 1e-4, dt = 0.02, seeded
 crossing-free synthetic packing (seed 3).  A "step" is one Heun step (two force
-passes) of every particle.  The headline line times the mixed-precision form; the
-plain FP64 form, the force-pass roofline, the CPU baseline (the oracle restatement
-of the reference's CPU path on host cores), an end-to-end run through the C ABI
-with host buffers and the minimisation time to tolerance of batched jamming
-replicas (mixed sweeps then FP64 refinement against FP64 alone) are reported in
-the same JSON line.
+passes) of every particle.  Every arm times the same window of the same run: W
+untimed warm-up steps from the generated packing, then K timed steps.
+
+The headline `value` is the mixed-precision form with its state resident on the
+device; `value_fp64` is the plain FP64 form over the same window; `e2e` is the
+same window through the C ABI from host arrays (handle creation from the state
+after the warm-up, K steps, state and stress read back).  The same JSON line
+carries the force-pass roofline, a steady-state figure (after a longer shear), the
+CPU baseline (the oracle restatement of the reference's CPU path on the host
+cores), the precision A/B of the N = 16384 workload, the 512-system batch and the
+minimisation time to tolerance of batched jamming replicas.
 
     python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference]
+
+`--impl reference` runs only the reference's CPU path (the compiled reference in
+oracle/_ref when it exists, else the oracle restatement) on the same packing,
+generated by the oracle, with no product code loaded.
 """
 from __future__ import annotations
 
@@ -35,23 +44,52 @@ WORKLOADS = {
     # a/R U[0.2, 2.0], strain rate log-uniform in [1e-6, 1e-3], seed 2
     "batch512": (512, None, None, None, 0.02, 2),
 }
+PAD = 0.2  # neighbour padding of the workload (the reference's rebuild timing)
+METRIC = "particle-steps/s (Lees-Edwards shear, Heun step)"
+REF_PI = 3.14159265358979  # the reference's pi (src/cpp/spherocyl_box.cpp:12)
 
 
-def make_batch(seed=2, nsys=512):
-    from spherocyls_gb300 import generate_packing
-
+def make_batch(generate, seed=2, nsys=512):
     rng = np.random.default_rng(seed)
     ns = (np.exp(rng.uniform(np.log(64), np.log(8192), nsys)) / 2).round().astype(int) * 2
     phis = rng.uniform(0.75, 0.90, nsys)
     aors = rng.uniform(0.2, 2.0, nsys)
     rates = np.exp(rng.uniform(np.log(1e-6), np.log(1e-3), nsys))
-    parts = [generate_packing(int(n), float(f), float(a), seed=int(seed * 100000 + k))
+    parts = [generate(int(n), float(f), float(a), seed=int(seed * 100000 + k))
              for k, (n, f, a) in enumerate(zip(ns, phis, aors))]
-    return dict(ns=ns, phis=phis, aors=aors, rates=rates,
+    return dict(ns=ns, phis=phis, aors=aors, rates=rates, n=int(ns.sum()), dt=0.02, seed=seed,
                 L=np.array([pk[0] for pk in parts]),
                 x=np.concatenate([pk[1] for pk in parts]), y=np.concatenate([pk[2] for pk in parts]),
                 p=np.concatenate([pk[3] for pk in parts]), R=np.concatenate([pk[4] for pk in parts]),
                 A=np.concatenate([pk[5] for pk in parts]))
+
+
+def make_workload(name, generate):
+    """The workload's inputs; `generate` is the library's or the oracle's packing
+    generator (the same packing bit for bit, tests/test_oracle_pin.py)."""
+    if name == "batch512":
+        return make_batch(generate)
+    n, phi, a, rate, dt, seed = WORKLOADS[name]
+    L, x, y, p, R, A = generate(n, phi, a, seed=seed)
+    return dict(n=n, phi=phi, a=a, rate=rate, dt=dt, seed=seed, L=L, x=x, y=y, p=p, R=R, A=A)
+
+
+def config_of(name, world):
+    """The workload's definition (identical in both arms)."""
+    if name == "batch512":
+        return {"workload": name, "systems": 512, "N": "log-uniform [64, 8192], even",
+                "packing": "U[0.75, 0.90]", "a_over_r": "U[0.2, 2.0]",
+                "strain_rate": "log-uniform [1e-6, 1e-3]", "dt": 0.02, "seed": 2, "pad": PAD,
+                "parallelism": "replicas" if world > 1 else "single"}
+    n, phi, a, rate, dt, seed = WORKLOADS[name]
+    return {"workload": name, "N": n, "packing": phi, "a_over_r": a, "strain_rate": rate,
+            "dt": dt, "seed": seed, "pad": PAD,
+            "start": "the generated packing; W warm-up steps, then the K timed steps",
+            "l2": "inputs larger than L2: a mixed step moves 152 + 8 n B per particle "
+                  "(about 200 B, 210 MB at N = 2^20) against 129 MB of L2",
+            "parallelism": "replicas" if world > 1 else "single"}
+
+
 # Algorithmic bytes per particle-step (two force passes plus the state update):
 # mixed form 152 + 8 n, plain FP64 form 232 + 8 n, n the mean length of the full
 # neighbour list actually used (4 bytes per entry and pass).  Per force pass: half.
@@ -61,10 +99,7 @@ def bytes_per_pass(precision: str, nbar: float) -> float:
 
 # DRAM bytes (read + write) per particle of one mixed force pass, the mean of the
 # predictor and corrector launches in one ncu capture of the default workload
-# (profiles/k_pass_mixed_n1048576.md: 108.7 and 167.6 MB per launch at N = 2^20,
-# padding 0.4).
-REF_PI = 3.14159265358979  # the reference's pi (src/cpp/spherocyl_box.cpp:12)
-
+# (profiles/k_pass_mixed_n1048576.md, the autotuned padding).
 PASS_DRAM_BYTES_PER_PARTICLE = {"shear_n1048576_phi084": 138.17e6 / (1 << 20)}
 
 
@@ -109,6 +144,8 @@ class ClockSampler:
 
     def __exit__(self, *a):
         if self.proc:
+            # one more sample after the timed work
+            time.sleep(0.25)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -129,17 +166,90 @@ class ClockSampler:
                 "samples": len(rows)}
 
 
-def make_workload(name):
-    from spherocyls_gb300 import generate_packing
+def max_over_ranks(secs: float, world: int, device: str) -> float:
+    """The slowest rank's time (replicas run independently; this all-reduce is the
+    only collective, outside the timed region)."""
+    if world <= 1:
+        return secs
+    import torch
+    import torch.distributed as dist
 
-    if name == "batch512":
-        b = make_batch()
-        b.update(n=int(b["ns"].sum()), phi=None, a=None, rate=None, dt=0.02, seed=2)
-        return b
-    n, phi, a, rate, dt, seed = WORKLOADS[name]
-    L, x, y, p, R, A = generate_packing(n, phi, a, seed=seed)
-    return dict(n=n, phi=phi, a=a, rate=rate, dt=dt, seed=seed, L=L, x=x, y=y, p=p, R=R, A=A)
+    t = torch.tensor([secs], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
+
+# ---------------------------------------------------------------- CPU (oracle) arm
+
+def cpu_run(w, warmup, steps, threads):
+    """The reference's CPU path (the compiled reference when present, else the
+    oracle restatement) on `threads` host cores: each core advances its own copy of
+    the workload's system (the reference is single-threaded) through `warmup`
+    untimed and `steps` timed Heun steps; the timed region spans all copies."""
+    import oracle
+
+    oracle.build(with_ref=False)
+    kind, cls = ("reference", oracle.RefBox) if oracle.ref_available() else ("port",
+                                                                             oracle.OracleBox)
+    boxes = [None] * threads
+    barrier = threading.Barrier(threads + 1)
+    times = [0.0] * threads
+
+    def run(k):
+        b = cls(w["L"], w["x"], w["y"], w["p"], w["A"], w["R"], PAD, strain_rate=w["rate"],
+                step=w["dt"])
+        if warmup:
+            b.run_strain_steps(warmup)
+        boxes[k] = b
+        barrier.wait()
+        t = time.perf_counter()
+        b.run_strain_steps(steps)
+        times[k] = time.perf_counter() - t
+        barrier.wait()
+
+    ts = [threading.Thread(target=run, args=(k,)) for k in range(threads)]
+    for t in ts:
+        t.start()
+    barrier.wait()  # every copy built and warmed up
+    t0 = time.perf_counter()
+    barrier.wait()
+    dt = time.perf_counter() - t0
+    for t in ts:
+        t.join()
+    for b in boxes:
+        b.close()
+    return {"value": threads * w["n"] * steps / dt, "unit": "particle-steps/s", "cores": threads,
+            "kind": kind, "seconds": dt,
+            "sample": f"{threads} concurrent copies (one per host core) of the N={w['n']} "
+                      f"workload, steps {warmup + 1}-{warmup + steps} of the run from the "
+                      f"generated packing, {dt:.1f} s"}
+
+
+def run_reference_arm(args, w, rank, world):
+    """The reference's CPU path on every host core over the same window as the GPU
+    arm (rank 0 only; the other ranks exit without work)."""
+    if rank != 0:
+        return
+    if w.get("phi") is None:
+        print(json.dumps({"impl": "reference", "unavailable":
+                          "the CPU arm runs single-system workloads only"}))
+        return
+    threads = os.cpu_count() or 1
+    steps, warmup = min(args.steps, args.ref_max_steps), min(args.warmup, args.ref_max_warmup)
+    base = cpu_run(w, warmup, steps, threads)
+    line = {"impl": "reference", "metric": METRIC,
+            "value": base["value"], "unit": "particle-steps/s", "n_gpus": args.gpus,
+            "steps": steps, "warmup": warmup, "ms_per_step": 1e3 * base["seconds"] / steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded crossing-free packing, oracle generator)",
+            "config": config_of(args.workload, world),
+            "cpu_baseline": base,
+            "e2e": {"value": base["value"], "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------- GPU arm helpers
 
 _STREAM = None
 
@@ -167,39 +277,112 @@ def time_steps(box, steps, torch):
     return e0.elapsed_time(e1) / 1e3
 
 
-def cpu_baseline(w, sample_n, steps, threads, pad):
-    """The oracle restatement of the reference's CPU path on host cores: `threads`
-    independent replicas of a sample box (same density, shape, rate, step)."""
-    import oracle
-    from spherocyls_gb300 import generate_packing
+def precision_ab(device, steps_per_step=100, total=100000, every=100, prep_steps=300):
+    """The N = 16384 precision workload (packing 0.86, a = R, strain rate 1e-4, dt
+    0.02, seed 1): mixed and FP64 from one sheared state (`prep_steps` FP64 steps
+    after the generated packing).  Per-step errors of the energy and shear stress of
+    the mixed run against the FP64 run over the first `steps_per_step` steps (stress
+    recorded every step), then both runs continue to `total` steps with the stress
+    recorded every `every` steps for the time averages (block standard errors over 10
+    blocks, after the first 10% of the run)."""
+    from spherocyls_gb300 import SpherocylBox, generate_packing
 
-    oracle.build(with_ref=False)
-    kind = "port"
-    cls = oracle.OracleBox
-    if oracle.ref_available():
-        kind, cls = "reference", oracle.RefBox
-    L, x, y, p, R, A = generate_packing(sample_n, w["phi"], w["a"], seed=w["seed"])
-    boxes = [cls(L, x, y, p, A, R, pad, strain_rate=w["rate"], step=w["dt"]) for _ in range(threads)]
-    for b in boxes:
-        b.run_strain_steps(1)
+    n, phi, a, rate, dt, seed = WORKLOADS["shear_n16384_phi086"]
+    L, x, y, p, R, A = generate_packing(n, phi, a, seed=seed)
+    prep = SpherocylBox(L, x, y, p, A, R, PAD, device=device)
+    prep.set_strain_rate(rate)
+    prep.set_step(dt)
+    prep.strain_steps(prep_steps)
+    x, y, p = prep.state()
+    bx = prep.box()
+    prep.close()
+    first, series, secs = {}, {}, {}
+    for precision in ("fp64", "mixed"):
+        b = SpherocylBox(L, x, y, p, A, R, PAD, precision=precision, device=device)
+        b.set_strain_rate(rate)
+        b.set_step(dt)
+        b.set_gamma(bx["gamma"])
+        b.set_total_gamma(bx["gamma_total"])
+        first[precision] = b.strain_steps(steps_per_step, se_every=1)[:, 0, :]
+        t = time.perf_counter()
+        rest = b.strain_steps(total - steps_per_step, se_every=every)
+        secs[precision] = time.perf_counter() - t
+        series[precision] = rest[:, 0, :]
+        b.close()
+    fa, fm = first["fp64"], first["mixed"]
+    rel_e = np.abs(fm[:, 0] - fa[:, 0]) / np.abs(fa[:, 0])
+    rel_pxy = np.abs(fm[:, 3] - fa[:, 3]) / np.abs(fa[:, 3])
+    over = np.nonzero(rel_pxy > 1e-6)[0]
 
-    def run(b):
-        b.run_strain_steps(steps)
+    def avg(v):
+        v = v[len(v) // 10:]
+        blocks = np.array_split(v, 10)
+        means = np.array([bl.mean() for bl in blocks])
+        return float(v.mean()), float(means.std(ddof=1) / np.sqrt(len(means)))
 
-    ts = [threading.Thread(target=run, args=(b,)) for b in boxes]
-    t0 = time.perf_counter()
-    for t in ts:
-        t.start()
-    for t in ts:
-        t.join()
-    dt = time.perf_counter() - t0
-    return {"value": threads * sample_n * steps / dt, "unit": "particle-steps/s",
-            "cores": threads, "kind": kind,
-            "sample": f"{threads} independent box(es) of N={sample_n} (same packing, a/R, rate, dt), "
-                      f"{steps} Heun steps each, {dt:.1f} s"}
+    out = {"workload": "shear_n16384_phi086", "steps": total,
+           "start": f"{prep_steps} FP64 shear steps after the generated packing",
+           "per_step": {"steps": steps_per_step,
+                        "energy_rel_err_max": float(rel_e.max()),
+                        "pxy_rel_err_max": float(rel_pxy.max()),
+                        "pxy_rel_err_max_first10": float(rel_pxy[:10].max()),
+                        "pxy_rel_err_max_first50": float(rel_pxy[:50].max()),
+                        "first_step_pxy_rel_err_over_1e-6": int(over[0]) + 1 if len(over) else None,
+                        "note": "mixed minus FP64 from the same start, each relative to the "
+                                "FP64 run's own value (Pxy relative to |Pxy|)"},
+           "time_average": {}, "seconds": secs}
+    for precision in ("fp64", "mixed"):
+        s = series[precision]
+        e_m, e_se = avg(s[:, 0])
+        p_m, p_se = avg(s[:, 3])
+        out["time_average"][precision] = {"energy": e_m, "energy_stderr": e_se, "pxy": p_m,
+                                          "pxy_stderr": p_se}
+    ta = out["time_average"]
+    out["time_average"]["pxy_diff_over_stderr"] = abs(ta["mixed"]["pxy"] - ta["fp64"]["pxy"]) / \
+        float(np.hypot(ta["mixed"]["pxy_stderr"], ta["fp64"]["pxy_stderr"]))
+    return out
 
 
-METRIC = "particle-steps/s (Lees-Edwards shear, Heun step)"
+def batched_leg(args, device, torch):
+    """The 512-system batch (mixed form): the same warm-up and window as the
+    headline, with its force-pass roofline from per-pass CUDA events."""
+    from spherocyls_gb300 import BoxBatch, generate_packing
+
+    w = make_batch(generate_packing)
+
+    def new(profile=False, pad=PAD, block=0):
+        b = BoxBatch(w["ns"], w["L"], w["x"], w["y"], w["p"], w["A"], w["R"], pad,
+                     precision="mixed", device=device, profile=profile, block=block)
+        for k, r in enumerate(w["rates"]):
+            b.set_strain_rate(float(r), sys=k)
+        b.set_step(w["dt"])
+        return b
+
+    t = new()
+    t.strain_steps(args.warmup)
+    f, blk = t.autotune(50)
+    t.close()
+    b = new(pad=PAD * f, block=blk)
+    b.strain_steps(args.warmup)
+    secs = time_steps(b, args.steps, torch)
+    b.close()
+    pr = new(profile=True, pad=PAD * f, block=blk)
+    pr.strain_steps(args.warmup)
+    pr.pass_times()
+    pr.strain_steps(max(args.steps, 20))
+    pt = pr.pass_times()
+    pairs = sum(len(pr.pairs(s)) for s in range(pr.nsys))
+    pr.close()
+    nbar = 2.0 * pairs / w["n"]
+    pass_ms = 0.5 * (pt["corr_ms"] + pt["pred_ms"])
+    achieved = bytes_per_pass("mixed", nbar) * w["n"] / (pass_ms / 1e3) / 1e9
+    peak, _ = _peaks()
+    return {"workload": "batch512", "particles": w["n"], "value": w["n"] * args.steps / secs,
+            "unit": "particle-steps/s", "ms_per_step": 1e3 * secs / args.steps,
+            "steps": args.steps, "warmup": args.warmup,
+            "tuning": {"pad": PAD * f, "block": blk},
+            "pass_ms": pass_ms, "mean_list_length": nbar,
+            "roofline_frac": achieved / peak, "achieved_gbs": achieved}
 
 
 def minimise_leg(replicas=32, n=4096, max_iter=20000, ftol=1e-14, device=0, e_jam=1e-12,
@@ -210,12 +393,11 @@ def minimise_leg(replicas=32, n=4096, max_iter=20000, ftol=1e-14, device=0, e_ja
     jamming in affine steps of 2e-3 in packing fraction (FIRE to 1e-6 after each,
     jammed once E/N > 1e-12; a replica whose FP64 minimum has E/N <= 1e-16 was not
     jammed and is left out of the energy comparison), and each replica is then
-    compressed by one more
-    1e-4 increment.  From that same state the two timed arms minimise to
-    max|F_i|, |tau_i|/sqrt(I_i) < ftol: (a) mixed FIRE to 1e-6, then FP64 FIRE;
-    (b) FP64 FIRE alone; (c) the reference's conjugate gradient (FP64) on one replica
-    of each aspect ratio, stopped by the reference's rules.  Each FP64 stage stops
-    after max_iter iterations."""
+    compressed by one more 1e-4 increment.  From that same state the two timed arms
+    minimise to max|F_i|, |tau_i|/sqrt(I_i) < ftol: (a) mixed FIRE to 1e-6, then
+    FP64 FIRE; (b) FP64 FIRE alone; (c) the reference's conjugate gradient (FP64) on
+    one replica of each aspect ratio, stopped by the reference's rules.  Each FP64
+    stage stops after max_iter iterations."""
     from spherocyls_gb300 import BoxBatch, generate_packing
 
     aors = [0.25, 0.5, 1.0, 2.0]
@@ -255,9 +437,6 @@ def minimise_leg(replicas=32, n=4096, max_iter=20000, ftol=1e-14, device=0, e_ja
     tc, ic, fc, dc = run(p, ftol, max_iter)
     e_c = p.calc_se()[:, 0]
     p.close()
-    # (c) the reference's conjugate gradient (FP64, on the device) from the same start
-    # on one replica of each aspect ratio (its line search evaluates the energy some
-    # tens of times per iteration), stopped by its own rules; residual as for FIRE
     sub = sorted({(k * replicas) // 4 for k in range(4)})
     sel = np.concatenate([np.arange(k * n, (k + 1) * n) for k in sub])
     q = BoxBatch([n] * len(sub), L1[sub], x1[sel], y1[sel], ps[sel], A[sel], R[sel], 0.1,
@@ -274,7 +453,6 @@ def minimise_leg(replicas=32, n=4096, max_iter=20000, ftol=1e-14, device=0, e_ja
     inertia = Rs ** 4 * C / (6 * Rs * (REF_PI * Rs + 4 * As))
     res = np.maximum(np.hypot(qfx, qfy), np.abs(qtq) / np.sqrt(inertia)).reshape(len(sub), n)
     cres = res.max(axis=1)
-    # jammed replicas (E/N > 1e-16 at the FP64 minimum) that both arms converged
     both = da & db & dc & (e_c > 1e-16) & (e_a > 1e-16)
     return {
         "workload": f"jam_{replicas}x{n}", "replicas": replicas, "N": n, "ftol": ftol,
@@ -287,83 +465,37 @@ def minimise_leg(replicas=32, n=4096, max_iter=20000, ftol=1e-14, device=0, e_ja
                  "max_residual": float(fc.max())},
         "cg_fp64": {"replicas": len(sub), "seconds": tcg, "iters_max": int(cit.max()),
                     "iters_mean": float(cit.mean()),
-                    "stop_reasons": {str(k): int((cwhy == k).sum()) for k in (1, 2, 3, 4)},
-                    "below_ftol": int((cres < ftol).sum()), "max_residual": float(cres.max()),
-                    "note": "the reference's Polak-Ribiere CG and line search, stopped by its "
-                            "rules (1 zero force, 2 three equal energies, 3 no lower energy, "
-                            "4 max_iter)"},
+                    "stop_reasons": {str(k): int((cwhy == k).sum()) for k in (1, 2, 3, 4, 5)},
+                    "below_ftol": int((cres < ftol).sum()), "max_residual": float(cres.max())},
         "speedup": tc / (ta + tb),
         "energy_rel_diff_max": (float(np.max(np.abs(e_a[both] - e_c[both]) / e_c[both]))
                                 if both.any() else None),
-        "note": "iterations capped at max_iter per FP64 stage; 'converged' counts replicas "
-                "below ftol",
     }
 
 
-def max_over_ranks(secs: float, world: int, device: str) -> float:
-    """The slowest rank's time (replicas run independently; this all-reduce is the
-    only collective, outside the timed region)."""
-    if world <= 1:
-        return secs
-    import torch
-    import torch.distributed as dist
-
-    t = torch.tensor([secs], dtype=torch.float64, device=device)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
-
-
-def config_of(args, w, world, tuned=None):
-    tuned = tuned or {"pad": args.pad, "block": 128}
-    return {"workload": args.workload, "N": w["n"], "packing": w["phi"], "a_over_r": w["a"],
-            "strain_rate": w["rate"], "dt": w["dt"], "seed": w["seed"], "pad": args.pad,
-            "mixed_pad": tuned["pad"], "mixed_block": tuned["block"],
-            "l2": "inputs larger than L2: a mixed step moves 152 + 8 n B per particle "
-                  "(about 200 B, 210 MB at N = 2^20) against 129 MB of L2",
-            "parallelism": "replicas" if world > 1 else "single"}
-
-
-def run_reference_arm(args, w, rank, world):
-    """The reference's CPU path (the compiled reference when present, else the
-    oracle restatement of it) on every host core: one independent N = 65536 box of
-    the workload's density, shape, rate and step per core; each timed step is a
-    bounded sample of the workload."""
-    if rank != 0:
-        return
-    threads = os.cpu_count() or 1
-    steps = max(min(args.steps, args.cpu_steps), 3)
-    base = cpu_baseline(w, 65536, steps, threads, args.pad)
-    line = {"impl": "reference", "metric": METRIC,
-            "value": base["value"], "unit": "particle-steps/s", "n_gpus": args.gpus,
-            "steps": steps, "warmup": 1, "ms_per_step": None, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": config_of(args, w, world),
-            "cpu_baseline": base,
-            "e2e": {"value": base["value"], "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 0}}
-    print(json.dumps(line))
-
+# ---------------------------------------------------------------- main
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2000)
-    ap.add_argument("--warmup", type=int, default=300)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="shear_n1048576_phi084", choices=list(WORKLOADS))
-    ap.add_argument("--fp64-steps", type=int, default=20)
-    ap.add_argument("--cpu-steps", type=int, default=60,
-                    help="Heun steps of each N=65536 CPU replica (about 5-10 s of work)")
+    ap.add_argument("--ref-max-steps", type=int, default=20,
+                    help="timed steps of the CPU reference arm at most (a bounded sample)")
+    ap.add_argument("--ref-max-warmup", type=int, default=5)
+    ap.add_argument("--cpu-steps", type=int, default=2,
+                    help="Heun steps of the CPU baseline sample in the GPU arm's line")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--only", choices=["mixed", "fp64"], default=None,
                     help="time one form only (for profiler captures)")
-    ap.add_argument("--pad", type=float, default=0.2, help="neighbour-list padding")
-    ap.add_argument("--e2e-steps", type=int, default=1000,
-                    help="length of the end-to-end run (1000 steps: the large shear run)")
+    ap.add_argument("--steady-steps", type=int, default=300,
+                    help="shear steps before the steady-state window")
     ap.add_argument("--autotune", action=argparse.BooleanOptionalAction, default=True,
                     help="pick the mixed form's padding and block size with sc_autotune")
-    ap.add_argument("--no-minimise", action="store_true",
-                    help="skip the minimisation time-to-tolerance leg")
+    ap.add_argument("--legs", default="precision,batched,minimise",
+                    help="extra legs of the GPU arm (comma separated, or 'none')")
     ap.add_argument("--min-replicas", type=int, default=32)
     ap.add_argument("--min-iters", type=int, default=40000,
                     help="FP64 FIRE iteration cap of the minimisation leg")
@@ -372,16 +504,16 @@ def main():
                          "kernels inside graphs with conditional nodes cannot be profiled)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    legs = set() if args.legs == "none" else set(args.legs.split(","))
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
-    w = make_workload(args.workload)
     if args.impl == "reference":
-        if w.get("phi") is None:
-            print(json.dumps({"impl": "reference", "unavailable":
-                              "the CPU arm samples single-system workloads only"}))
-            return
-        run_reference_arm(args, w, rank, world)
+        # the oracle alone: its own generator, no product code loaded
+        import oracle
+
+        run_reference_arm(args, make_workload(args.workload, oracle.generate_packing), rank,
+                          world)
         return
 
     import torch
@@ -395,30 +527,32 @@ def main():
     import __graft_entry__
 
     __graft_entry__.build()
-    from spherocyls_gb300 import SpherocylBox
+    from spherocyls_gb300 import BoxBatch, SpherocylBox, generate_packing
 
+    w = make_workload(args.workload, generate_packing)
     n = w["n"]
+    tuned = {"pad": PAD, "block": 128}
 
-    tuned = {"pad": args.pad, "block": 128}
-
-    def new_box(precision, profile=False):
+    def new_box(precision, profile=False, state=None):
         # the mixed form runs with the autotuned padding and block size
-        pad = tuned["pad"] if precision == "mixed" else args.pad
+        pad = tuned["pad"] if precision == "mixed" else PAD
         block = tuned["block"] if precision == "mixed" else 0
+        x, y, p = state[:3] if state is not None else (w["x"], w["y"], w["p"])
         if args.workload == "batch512":
-            from spherocyls_gb300 import BoxBatch
-
-            b = BoxBatch(w["ns"], w["L"], w["x"], w["y"], w["p"], w["A"], w["R"], pad,
-                         precision=precision, device=local, profile=profile,
-                         use_graphs=not args.no_graphs, block=block)
+            b = BoxBatch(w["ns"], w["L"], x, y, p, w["A"], w["R"], pad, precision=precision,
+                         device=local, profile=profile, use_graphs=not args.no_graphs,
+                         block=block)
             for k, r in enumerate(w["rates"]):
                 b.set_strain_rate(float(r), sys=k)
         else:
-            b = SpherocylBox(w["L"], w["x"], w["y"], w["p"], w["A"], w["R"], pad,
+            b = SpherocylBox(w["L"], x, y, p, w["A"], w["R"], pad,
                              precision=precision, device=local, profile=profile,
                              use_graphs=not args.no_graphs, block=block)
             b.set_strain_rate(w["rate"])
         b.set_step(w["dt"])
+        if state is not None:
+            b.set_gamma(state[3])
+            b.set_total_gamma(state[4])
         return b
 
     if args.autotune and not args.only:
@@ -428,7 +562,7 @@ def main():
         t.strain_steps(args.warmup)
         f, blk = t.autotune(100)  # long enough to include rebuilds
         t.close()
-        tuned = {"pad": args.pad * f, "block": blk}
+        tuned = {"pad": PAD * f, "block": blk}
 
     if args.only:
         b = new_box(args.only)
@@ -438,7 +572,7 @@ def main():
         c1 = b.counters()
         if rank == 0:
             print(json.dumps({"only": args.only, "workload": args.workload, "steps": args.steps,
-                              "pad": args.pad, "ms_per_step": 1e3 * secs / args.steps,
+                              "ms_per_step": 1e3 * secs / args.steps,
                               "value": n * args.steps / secs,
                               "rebuilds": c1["rebuilds"] - c0["rebuilds"],
                               "mean_list_length": mean_list_length(b)}))
@@ -447,6 +581,9 @@ def main():
     # ---- mixed precision, device-resident: the headline value ----
     box = new_box("mixed")
     box.strain_steps(args.warmup)
+    # the state after the warm-up, on the host: the start of the end-to-end run
+    bx = box.box(0)
+    start = (*box.state(), bx["gamma"], bx["gamma_total"])
     counters0 = box.counters()
     if world > 1:
         torch.distributed.barrier()
@@ -456,15 +593,26 @@ def main():
         torch.distributed.barrier()
     secs = max_over_ranks(secs, world, "cuda")
     value = world * n * args.steps / secs
-    k_before = counters0["kernels"]
     counters = box.counters()
-    launches = counters["kernels"] - k_before
+    launches = counters["kernels"] - counters0["kernels"]
+    rebuild_chains = counters["rebuilds"] - counters0["rebuilds"]
 
-    # ---- force-pass timing with per-pass CUDA events (same workload, same state) ----
+    # ---- the same run continued: a steady-state window after a longer shear ----
+    box.strain_steps(args.steady_steps)
+    c2 = box.counters()
+    steady_k = 200
+    secs_ss = time_steps(box, steady_k, torch)
+    c3 = box.counters()
+    steady = {"value": n * steady_k / secs_ss, "ms_per_step": 1e3 * secs_ss / steady_k,
+              "steps": steady_k, "after_steps": args.warmup + args.steps + args.steady_steps,
+              "rebuild_chains": c3["rebuilds"] - c2["rebuilds"]}
+    box.close()
+
+    # ---- force-pass timing with per-pass CUDA events (same workload, same window) ----
     prof = new_box("mixed", profile=True)
     prof.strain_steps(args.warmup)
     prof.pass_times()
-    prof.strain_steps(min(args.steps, 100))
+    prof.strain_steps(max(args.steps, 20))
     pt = prof.pass_times()
     pass_ms = 0.5 * (pt["corr_ms"] + pt["pred_ms"])
     peak, peak_kind = _peaks()
@@ -480,57 +628,61 @@ def main():
     full_rebuild_ms = 1e3 * (time.perf_counter() - t0) / 10
     prof.close()
 
-    # ---- plain FP64 form on the same workload ----
+    # ---- plain FP64 form, same window ----
     b64 = new_box("fp64")
-    b64.strain_steps(3)
-    secs64 = time_steps(b64, args.fp64_steps, torch)
-    value64 = n * args.fp64_steps / secs64
+    b64.strain_steps(args.warmup)
+    secs64 = time_steps(b64, args.steps, torch)
+    value64 = world * n * args.steps / max_over_ranks(secs64, world, "cuda")
     b64.close()
 
-    # ---- end to end through the C ABI with host buffers ----
-    box.close()
+    # ---- end to end through the C ABI with host buffers, same window ----
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    e2e_box = new_box("mixed")
-    rec_every = 100
-    h2d = 40 * n  # x, y, phi, R, A
-    d2h = 0
-    done = 0
-    while done < args.e2e_steps:
-        k = min(rec_every, args.e2e_steps - done)
-        e2e_box.strain_steps(k, se_every=k)
-        e2e_box.state()
-        d2h += 24 * n + 40
-        done += k
+    e2e_box = new_box("mixed", state=start)  # sc_create copies x, y, phi, R, A in
+    se = e2e_box.strain_steps(args.steps, se_every=args.steps)
+    xs, ys, ps = e2e_box.state()
     torch.cuda.synchronize()
     e2e_secs = time.perf_counter() - t0
     e2e_box.close()
-    e2e = {"value": n * args.e2e_steps / e2e_secs, "unit": "particle-steps/s",
-           "h2d_bytes_per_step": h2d / args.e2e_steps, "d2h_bytes_per_step": d2h / args.e2e_steps,
-           "steps": args.e2e_steps,
-           "note": "a run as a user makes it: sc_create from host arrays, then steps in chunks "
-                   "of 100 with stress/energy and positions read back to host arrays after "
-                   "each chunk"}
+    assert se is not None and np.all(np.isfinite(xs))
+    e2e_secs = max_over_ranks(e2e_secs, world, "cuda")
+    e2e = {"value": world * n * args.steps / e2e_secs, "unit": "particle-steps/s",
+           "h2d_bytes_per_step": 40 * n / args.steps,
+           "d2h_bytes_per_step": (24 * n + 40) / args.steps, "steps": args.steps,
+           "note": "the same window through the C ABI: handle created from host arrays of "
+                   "the state after the warm-up, K steps, stress/energy of the last step "
+                   "and positions read back to host arrays"}
 
-    mini = None
-    if rank == 0 and not args.no_minimise:
-        mini = minimise_leg(args.min_replicas, 4096, args.min_iters, device=local)
+    extra = {}
+    if rank == 0 and "precision" in legs:
+        extra["precision_ab"] = precision_ab(local)
+    if rank == 0 and "batched" in legs and args.workload != "batch512":
+        extra["batched"] = batched_leg(args, local, torch)
+    if rank == 0 and "minimise" in legs:
+        extra["minimise"] = minimise_leg(args.min_replicas, 4096, args.min_iters, device=local)
 
     base = None
     if rank == 0 and not args.no_cpu and w.get("phi") is not None:
-        base = cpu_baseline(w, 65536, args.cpu_steps, os.cpu_count() or 1, args.pad)
+        import oracle
+
+        wo = make_workload(args.workload, oracle.generate_packing)
+        base = cpu_run(wo, 0, args.cpu_steps, os.cpu_count() or 1)
 
     if rank == 0:
         line = {
             "metric": METRIC,
             "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64",
             "data": "synthetic (seeded crossing-free packing)",
-            "config": config_of(args, w, world, tuned),
+            "config": config_of(args.workload, world),
+            "tuning": {"mixed_pad": tuned["pad"], "mixed_block": tuned["block"]},
+            "value_fp64": value64,
             "plain_fp64": {"value": value64, "unit": "particle-steps/s",
-                           "ms_per_step": 1e3 * secs64 / args.fp64_steps,
-                           "steps": args.fp64_steps, "mixed_over_fp64": value / value64},
+                           "ms_per_step": 1e3 * secs64 / args.steps, "steps": args.steps,
+                           "mixed_over_fp64": value / value64},
+            "steady_state": steady,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": (PASS_DRAM_BYTES_PER_PARTICLE[args.workload] * n
@@ -538,15 +690,16 @@ def main():
                                      else None),
                          "traffic_unit": "bytes per launch (ncu capture)",
                          "kernel": "k_pass_mixed (corrector/predictor force passes)",
-                         "pass_ms": pass_ms, "bytes_per_particle_pass": bpp, "mean_list_length": nbar,
+                         "pass_ms": pass_ms, "bytes_per_particle_pass": bpp,
+                         "mean_list_length": nbar,
                          "rebuild_body_ms_mean_eager": pt["rebuild_ms"],
                          "full_rebuild_ms": full_rebuild_ms},
             "cpu_baseline": base,
-            "minimise": mini,
             "e2e": e2e,
             "gpu_launches": launches,
             "clocks": clk.summary(local),
-            "rebuild_chains": counters["rebuilds"],
+            "rebuild_chains": rebuild_chains,
+            **extra,
         }
         print(json.dumps(line))
     if world > 1:

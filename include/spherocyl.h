@@ -76,7 +76,16 @@ typedef struct sc_options {
                       * also where the GPU reads pageable host memory in place (0) */
   int cg_max_probes; /* energy probes one conjugate-gradient line search may take before
                       * its system stops with SC_CG_PROBES, 0 = default (256) */
+  int pass_kind;     /* mixed form's force pass: SC_PASS_AUTO (tiles), SC_PASS_LIST (one
+                      * thread per particle over its full list, each pair twice) or
+                      * SC_PASS_TILE (blocks of cells staged in shared memory, each pair
+                      * inside a tile once) */
+  int tile_target;   /* particles per tile the tile pass aims at, 0 = default (256) */
 } sc_options;
+
+#define SC_PASS_AUTO 0
+#define SC_PASS_LIST 1
+#define SC_PASS_TILE 2
 
 const char *sc_version(void);
 const char *sc_status_string(int status);
@@ -213,11 +222,17 @@ int sc_find_jam(sc_handle *h, double e_jam, double step, double min_step, double
                 int max_iter, int max_steps, double *phi_jam, int *steps);
 
 /* Mixed form: times `steps` shear steps (after as many warm-up steps) of a copy of
- * the handle for padding factors {0.5, 1, 1.5, 2, 3} x the current padding and
- * block sizes {64, 128}, and gives the handle the fastest pair (*pad_factor,
- * *block).  The live state is not advanced.  The FP64 form is left as it is
- * (factor 1). */
+ * the handle for each candidate -- padding factors {0.5, 1, 1.5, 2, 3} x the current
+ * padding, crossed with the per-particle force pass at block sizes {64, 128} and the
+ * tile force pass at {128, 256, 384} particles per tile -- and gives the handle the
+ * fastest (*pad_factor, *block; the pass kind and tile size through
+ * sc_get_options).  The live state is not advanced.  The FP64 form is left as it is
+ * (factor 1).  Replaces the reference's fixed launch-shape table
+ * (src/cuda/spherocyl_box.cpp:193-238). */
 int sc_autotune(sc_handle *h, int steps, double *pad_factor, int *block);
+/* The handle's current options (after sc_autotune: the chosen pass kind, block and
+ * tile size). */
+int sc_get_options(const sc_handle *h, sc_options *out);
 
 /* State readers, original particle order, systems concatenated. */
 int sc_get_state(sc_handle *h, double *x, double *y, double *phi);

@@ -30,6 +30,7 @@ SC_E_NOMEM = 9
 
 PREC = {"fp64": 0, "mixed": 1}
 STRESS = {"compat": 0, "virial": 1}
+PASS = {"auto": 0, "list": 1, "tile": 2}
 
 
 class ScOptions(ctypes.Structure):
@@ -44,6 +45,8 @@ class ScOptions(ctypes.Structure):
         ("contact_model", ctypes.c_int),
         ("stage_inputs", ctypes.c_int),
         ("cg_max_probes", ctypes.c_int),
+        ("pass_kind", ctypes.c_int),
+        ("tile_target", ctypes.c_int),
     ]
 
 
@@ -95,6 +98,7 @@ SIGNATURES = [
     ("sc_find_jam", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                    ctypes.c_double, ctypes.c_int, ctypes.c_int, _dp, _ip]),
     ("sc_autotune", ctypes.c_int, [_vp, ctypes.c_int, _dp, _ip]),
+    ("sc_get_options", ctypes.c_int, [_vp, ctypes.c_void_p]),
     ("sc_flip_shear", ctypes.c_int, [_vp, ctypes.c_int]),
     ("sc_rotate_shear", ctypes.c_int, [_vp, ctypes.c_int]),
     ("sc_create_rect", ctypes.c_int, [ctypes.POINTER(ScOptions), ctypes.c_int, _ip, _dp, _dp,

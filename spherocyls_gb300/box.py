@@ -15,7 +15,7 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from ._lib import PREC, STRESS, ScOptions, check, lib
+from ._lib import PASS, PREC, STRESS, ScOptions, check, lib
 
 _dp = ctypes.POINTER(ctypes.c_double)
 
@@ -158,7 +158,7 @@ class BoxBatch:
                  stress: str = "compat", device: int = 0, max_nbrs: int = 0,
                  use_graphs: bool = True, block: int = 0, profile: bool = False,
                  contacts: int = 1, Ly=None, stage_inputs: bool = False,
-                 cg_max_probes: int = 0):
+                 cg_max_probes: int = 0, pass_kind: str = "auto", tile_target: int = 0):
         n_per_sys = np.ascontiguousarray(np.atleast_1d(n_per_sys), dtype=np.int32)
         self.nsys = int(n_per_sys.shape[0])
         self.n_per_sys = n_per_sys
@@ -183,6 +183,10 @@ class BoxBatch:
         opt.contact_model = 1 if int(contacts) == 2 else 0
         opt.stage_inputs = int(bool(stage_inputs))
         opt.cg_max_probes = int(cg_max_probes)
+        if pass_kind not in PASS:
+            raise ValueError("pass_kind must be 'auto', 'list' or 'tile'")
+        opt.pass_kind = PASS[pass_kind]
+        opt.tile_target = int(tile_target)
         self.precision = precision
         h = ctypes.c_void_p()
         nps = n_per_sys.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
@@ -346,12 +350,22 @@ class BoxBatch:
         return pj, n.value
 
     def autotune(self, steps: int = 50):
-        """Pick the neighbour-list padding and force-pass block size of the mixed
-        form by timing copies of this batch; returns (pad_factor, block)."""
+        """Pick the neighbour-list padding, the force pass (per particle or by tiles)
+        and its block or tile size of the mixed form by timing copies of this batch;
+        returns (pad_factor, block) -- the pass and tile size are in options()."""
         f = ctypes.c_double()
         b = ctypes.c_int()
         self._chk(lib().sc_autotune(self.h, int(steps), ctypes.byref(f), ctypes.byref(b)))
         return f.value, b.value
+
+    def options(self) -> dict:
+        """The handle's current options (pass kind, block, tile size, ...)."""
+        o = ScOptions()
+        self._chk(lib().sc_get_options(self.h, ctypes.byref(o)))
+        kinds = {v: k for k, v in PASS.items()}
+        return {"precision": o.precision, "block": o.block, "contact_model": o.contact_model,
+                "pass_kind": kinds.get(o.pass_kind, o.pass_kind), "tile_target": o.tile_target,
+                "cg_max_probes": o.cg_max_probes}
 
     def find_jam(self, e_jam: float, step: float = 1e-3, min_step: float = 1e-12,
                  ftol: float = 1e-13, max_iter: int = 200000, max_steps: int = 10000):

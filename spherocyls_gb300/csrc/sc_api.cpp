@@ -96,6 +96,11 @@ int sc_create_rect(const sc_options* opt_in, int n_sys, const int* n_per_sys, co
     g_create_error = "sc_create: unknown contact model";
     return SC_E_ARG;
   }
+  if (opt.pass_kind < SC_PASS_AUTO || opt.pass_kind > SC_PASS_TILE || opt.tile_target < 0 ||
+      opt.tile_target > 65536 || opt.cg_max_probes < 0) {
+    g_create_error = "sc_create: pass_kind, tile_target or cg_max_probes out of range";
+    return SC_E_ARG;
+  }
   long long ntot_ll = 0;
   for (int s = 0; s < n_sys; s++) {
     if (n_per_sys[s] < 2 || !(L[s] > 0) || !std::isfinite(L[s]) || !(Ly[s] > 0) ||
@@ -195,6 +200,9 @@ int sc_create_rect(const sc_options* opt_in, int n_sys, const int* n_per_sys, co
   d.stress_mode = opt.stress_mode == SC_STRESS_VIRIAL ? sc::STRESS_VIRIAL : sc::STRESS_COMPAT;
   d.contact_model = opt.contact_model == SC_CONTACT_TWO ? 1 : 0;
   d.maxn = opt.max_nbrs > 0 ? opt.max_nbrs : 64;
+  // the tile pass keeps slots below 2^27 in its entries (kTileInt)
+  d.pass_kind = (opt.precision == SC_PREC_MIXED && opt.pass_kind != SC_PASS_LIST &&
+                 N < (size_t)sc::kTileInt) ? 1 : 0;
   std::vector<int> pchunk_sys, pchunk_p0, pchunk_np;
   for (int s = 0; s < n_sys; s++) {
     const sc::HostSys& S = h.hs[s];
@@ -223,6 +231,11 @@ int sc_create_rect(const sc_options* opt_in, int n_sys, const int* n_per_sys, co
          h.dalloc(&d.cellp, N, "cellp") && h.dalloc(&d.gbuild, n_sys, "gbuild") &&
          h.dalloc(&d.ord, N, "ord") && h.dalloc(&d.nbr_p, N * d.maxn, "nbr_p") &&
          h.dalloc(&d.nbr_pn, N, "nbr_pn");
+  if (d.pass_kind == 1)
+    ok = ok && h.dalloc(&d.t_own, N * sc::kTileEPP, "tile owners") &&
+         h.dalloc(&d.t_pe, N * sc::kTileEPP, "tile partners") &&
+         h.dalloc(&d.t_rd, N * sc::kTileEPP, "tile reads") && h.dalloc(&d.t_meta, N, "tile meta") &&
+         h.dalloc(&d.t_pb, N * sc::kTileEPP, "tile pair results");
   ok = ok && h.dalloc(&d.nbr, N * d.maxn, "nbr");
   ok = ok && h.dalloc(&d.nbr_n, N, "nbr_n");
   ok = ok && h.dalloc(&d.cell_tmp, N, "cell_tmp") && h.dalloc(&d.rank, N, "rank") &&
@@ -408,44 +421,54 @@ int sc_autotune(sc_handle* H, int steps, double* pad_factor, int* block) {
     Ly[s] = h.hs[s].Ly;
     pad0[s] = h.hs[s].pad;
   }
-  const double factors[] = {0.5, 1.0, 1.5, 2.0, 3.0};
-  const int blocks[] = {64, 128};
-  double best_ms = 1e300, best_f = 1.0;
-  int best_b = h.block;
+  // candidates: padding factor x (per-particle pass at two block sizes, or the
+  // tile pass at three tile sizes)
+  struct Cand {
+    double f;
+    int kind, block, target;
+  };
+  std::vector<Cand> cands;
+  for (double f : {0.5, 1.0, 1.5, 2.0, 3.0}) {
+    for (int b : {64, 128}) cands.push_back({f, SC_PASS_LIST, b, 0});
+    if (h.ntot < (int)sc::kTileInt)
+      for (int t : {128, 256, 384}) cands.push_back({f, SC_PASS_TILE, h.block, t});
+  }
+  Cand best{1.0, h.d.pass_kind == 1 ? SC_PASS_TILE : SC_PASS_LIST, h.block, h.opt.tile_target};
+  double best_ms = 1e300;
   cudaEvent_t e0, e1;
   if (!h.cuda_ok(cudaEventCreate(&e0), "event") || !h.cuda_ok(cudaEventCreate(&e1), "event"))
     return h.last_status;
-  for (double f : factors)
-    for (int b : blocks) {
-      sc_options o = h.opt;
-      o.block = b;
-      o.profile = 0;
-      for (int s = 0; s < ns; s++) pads[s] = f * pad0[s];
-      sc_handle* T = nullptr;
-      if (sc_create_rect(&o, ns, nps.data(), L.data(), Ly.data(), pads.data(), x.data(),
-                         y.data(), p.data(), h.h_R.data(), h.h_A.data(), &T) != SC_OK)
-        continue;  // e.g. out of memory for the copy: skip the candidate
-      bool ok = true;
-      for (int s = 0; s < ns && ok; s++) {
-        const sc::HostSys& S = h.hs[s];
-        ok = sc_set_strain_rate(T, s, S.strain_rate) == SC_OK &&
-             sc_set_step(T, s, S.step) == SC_OK && sc_set_gamma(T, s, S.gamma) == SC_OK &&
-             sc_set_total_gamma(T, s, S.gamma_total) == SC_OK;
-      }
-      float ms = 0.f;
-      ok = ok && sc_strain_steps(T, steps, 0, nullptr) == SC_OK &&
-           cudaEventRecord(e0, T->h.stream) == cudaSuccess &&
-           sc_strain_steps(T, steps, 0, nullptr) == SC_OK &&
-           cudaEventRecord(e1, T->h.stream) == cudaSuccess &&
-           cudaEventSynchronize(e1) == cudaSuccess &&
-           cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess;
-      sc_destroy(T);
-      if (ok && ms < best_ms) {
-        best_ms = ms;
-        best_f = f;
-        best_b = b;
-      }
+  for (const Cand& c : cands) {
+    sc_options o = h.opt;
+    o.block = c.block;
+    o.pass_kind = c.kind;
+    o.tile_target = c.target;
+    o.profile = 0;
+    for (int s = 0; s < ns; s++) pads[s] = c.f * pad0[s];
+    sc_handle* T = nullptr;
+    if (sc_create_rect(&o, ns, nps.data(), L.data(), Ly.data(), pads.data(), x.data(), y.data(),
+                       p.data(), h.h_R.data(), h.h_A.data(), &T) != SC_OK)
+      continue;  // e.g. out of memory for the copy: skip the candidate
+    bool ok = true;
+    for (int s = 0; s < ns && ok; s++) {
+      const sc::HostSys& S = h.hs[s];
+      ok = sc_set_strain_rate(T, s, S.strain_rate) == SC_OK &&
+           sc_set_step(T, s, S.step) == SC_OK && sc_set_gamma(T, s, S.gamma) == SC_OK &&
+           sc_set_total_gamma(T, s, S.gamma_total) == SC_OK;
     }
+    float ms = 0.f;
+    ok = ok && sc_strain_steps(T, steps, 0, nullptr) == SC_OK &&
+         cudaEventRecord(e0, T->h.stream) == cudaSuccess &&
+         sc_strain_steps(T, steps, 0, nullptr) == SC_OK &&
+         cudaEventRecord(e1, T->h.stream) == cudaSuccess &&
+         cudaEventSynchronize(e1) == cudaSuccess &&
+         cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess;
+    sc_destroy(T);
+    if (ok && ms < best_ms) {
+      best_ms = ms;
+      best = c;
+    }
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaGetLastError();
@@ -453,20 +476,41 @@ int sc_autotune(sc_handle* H, int steps, double* pad_factor, int* block) {
     h.fail(SC_E_CUDA, "sc_autotune: no candidate ran");
     return SC_E_CUDA;
   }
-  if (best_f != 1.0) {
+  const int kind = best.kind == SC_PASS_TILE ? 1 : 0;
+  const bool relayout = best.f != 1.0 || kind != h.d.pass_kind ||
+                        (kind == 1 && best.target != h.opt.tile_target);
+  if (relayout) {
     if (!h.materialize()) return h.last_status;
+    if (kind == 1 && !h.d.t_own) {
+      const size_t N = h.ntot;
+      if (!h.dalloc(&h.d.t_own, N * sc::kTileEPP, "tile owners") ||
+          !h.dalloc(&h.d.t_pe, N * sc::kTileEPP, "tile partners") ||
+          !h.dalloc(&h.d.t_rd, N * sc::kTileEPP, "tile reads") ||
+          !h.dalloc(&h.d.t_meta, N, "tile meta") ||
+          !h.dalloc(&h.d.t_pb, N * sc::kTileEPP, "tile pair results"))
+        return h.last_status;
+    }
+    h.d.pass_kind = kind;
+    h.opt.pass_kind = best.kind;
+    h.opt.tile_target = best.target;
     for (int s = 0; s < ns; s++) {
-      h.hs[s].pad = best_f * pad0[s];
+      h.hs[s].pad = best.f * pad0[s];
       h.hs[s].configure(false);
     }
     if (!h.layout_cells() || !h.rebuild_all() || !h.check_status("sc_autotune"))
       return h.last_status;
   }
-  h.block = best_b;
-  h.opt.block = best_b;
+  h.block = best.block;
+  h.opt.block = best.block;
   h.invalidate_graph();
-  if (pad_factor) *pad_factor = best_f;
-  if (block) *block = best_b;
+  if (pad_factor) *pad_factor = best.f;
+  if (block) *block = best.block;
+  return SC_OK;
+}
+
+int sc_get_options(const sc_handle* H, sc_options* out) {
+  if (!H || !out) return SC_E_ARG;
+  *out = H->h.opt;
   return SC_OK;
 }
 

@@ -3,7 +3,8 @@
 //
 // The rebuild follows the reference's find_cells / find_neighbors
 // (tmarschall/spherocyls src/cpp/spherocyl_box.cpp:270-355): positions are wrapped
-// into the box, each particle is hashed to cell col + row*cols, and the cell lists
+// into the box, each particle is hashed to its cell (col + row*cols in the
+// reference; here numbered tile by tile, see cell_local), and the cell lists
 // hold particles in increasing particle index.  On the GPU the lists are a
 // counting sort of the particle arrays themselves into cell order:
 //
@@ -163,7 +164,7 @@ __global__ void k_rb_hash(Dev d, const StepScalars* __restrict__ tab, int row, i
     if (rw >= g.rows) rw = g.rows - 1;
     if (col < 0) col = 0;
     if (rw < 0) rw = 0;
-    int c = g.c0 + col + rw * g.cols;
+    int c = g.c0 + cell_local(g, col, rw);
     d.cell_tmp[i] = c;
     d.rank[i] = atomicAdd(&d.cell_count[c], 1);
   });
@@ -569,7 +570,10 @@ void launch_rebuild(const Dev& d, bool mixed, const StepScalars* tab, int row, c
   if (mixed) {
     launch_mx_local(d, tab, row, false, st);
     launch_mx_build_list(d, tab, row, false, st);
-    launch_mx_order(d, false, st);
+    if (d.pass_kind == 1)
+      launch_tile_lists(d, false, st);
+    else
+      launch_mx_order(d, false, st);
   } else {
     launch_build_nbrs(d, tab, row, st);
   }

@@ -170,10 +170,28 @@ bool Handle::layout_cells() {
   // cells, scan chunks and particle chunks for all systems
   int c = 0, ch = 0;
   std::vector<int> chunk_sys, chunk_c0, chunk_nc, cell_sys;
+  std::vector<int4> tiles;
+  // tiles of about tile_target particles for the tile pass (one tile per system
+  // otherwise): square blocks of cells at the system's mean occupancy
+  const double target = opt.tile_target > 0 ? opt.tile_target : 256.0;
   for (int s = 0; s < nsys; s++) {
     HostSys& h = hs[s];
     h.c0 = c;
     int nc = h.rows * h.cols;
+    h.ntx = h.nty = 1;
+    if (d.pass_kind == 1) {
+      const double occ = (double)h.n / nc;
+      const int side = std::max(1, (int)std::lround(std::sqrt(target / occ)));
+      h.ntx = (h.cols + side - 1) / side;
+      h.nty = (h.rows + side - 1) / side;
+    }
+    for (int ky = 0; ky < h.nty; ky++) {
+      const int y0 = tile_lo(ky, h.rows, h.nty), hy = tile_lo(ky + 1, h.rows, h.nty) - y0;
+      for (int kx = 0; kx < h.ntx; kx++) {
+        const int x0 = tile_lo(kx, h.cols, h.ntx), wx = tile_lo(kx + 1, h.cols, h.ntx) - x0;
+        tiles.push_back(make_int4(s, c + y0 * h.cols + hy * x0, hy * wx, 0));
+      }
+    }
     h.chunk0 = ch;
     h.nchunks = (nc + kScanChunk - 1) / kScanChunk;
     for (int k = 0; k < h.nchunks; k++) {
@@ -219,6 +237,18 @@ bool Handle::layout_cells() {
     d.chunk_nc = g;
     chunk_cap = cap;
   }
+  const int ntiles = (int)tiles.size();
+  if (ntiles > tile_cap) {
+    dfree((void*)d.tiles);
+    dfree(d.tinfo);
+    int cap = ntiles + ntiles / 4 + 16;
+    int4 *a = nullptr, *b = nullptr;
+    if (!dalloc(&a, cap, "tiles") || !dalloc(&b, cap, "tile info")) return false;
+    d.tiles = a;
+    d.tinfo = b;
+    tile_cap = cap;
+  }
+  d.ntiles = ntiles;
   d.ncells = ncells;
   d.nchunks = nchunks;
   invalidate_graph();  // captured kernels hold the old layout
@@ -232,6 +262,8 @@ bool Handle::layout_cells() {
     o.c0 = h.c0;
     o.cols = h.cols;
     o.rows = h.rows;
+    o.ntx = h.ntx;
+    o.nty = h.nty;
     o.chunk0 = h.chunk0;
     o.nchunks = h.nchunks;
     o.pad = h.pad;
@@ -248,7 +280,10 @@ bool Handle::layout_cells() {
             cuda_ok(cudaMemcpyAsync((void*)d.chunk_c0, chunk_c0.data(), nchunks * sizeof(int),
                                     cudaMemcpyHostToDevice, stream), "upload chunks") &&
             cuda_ok(cudaMemcpyAsync((void*)d.chunk_nc, chunk_nc.data(), nchunks * sizeof(int),
-                                    cudaMemcpyHostToDevice, stream), "upload chunks");
+                                    cudaMemcpyHostToDevice, stream), "upload chunks") &&
+            cuda_ok(cudaMemcpyAsync((void*)d.tiles, tiles.data(), ntiles * sizeof(int4),
+                                    cudaMemcpyHostToDevice, stream), "upload tiles") &&
+            cuda_ok(cudaMemsetAsync(d.tinfo, 0, ntiles * sizeof(int4), stream), "tile info");
   if (!ok) return false;
   // host copies must outlive the async copies
   return cuda_ok(cudaStreamSynchronize(stream), "layout sync");

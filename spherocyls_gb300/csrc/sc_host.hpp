@@ -24,6 +24,7 @@ struct HostSys {
   double Rmax = 0, Amax = 0;
   double packing = 0;
   int rows = 1, cols = 1;
+  int ntx = 1, nty = 1;  // tiles across and down (the tile pass's cell numbering)
   int c0 = 0, chunk0 = 0, nchunks = 0;
   // cell width over R_max + A_max (configure_cells, src/cpp/spherocyl_box.cpp:225:
   // 2.24, enough for |gamma| <= 1/2; 2 sqrt(1 + gamma^2) for a run to larger gamma,
@@ -67,7 +68,7 @@ struct Handle {
   bool own_stream = false;
   Dev d{};
   std::vector<void*> allocs;
-  int cell_cap = 0, chunk_cap = 0;
+  int cell_cap = 0, chunk_cap = 0, tile_cap = 0;
   StepScalars* d_tab = nullptr;
   int tab_cap = 0;
   std::vector<StepScalars> h_tab;

@@ -20,17 +20,57 @@ namespace sc {
 enum Precision { PREC_FP64 = 0, PREC_MIXED = 1 };
 enum StressMode { STRESS_COMPAT = 0, STRESS_VIRIAL = 1 };
 
+#ifdef __CUDACC__
+#define SC_HDI __host__ __device__ __forceinline__
+#else
+#define SC_HDI inline
+#endif
+
 // Per-system constants of the current cell grid; changed only by the host.
 struct SysGeom {
   int n, p0;           // particle count and first slot
   int c0, cols, rows;  // first global cell and grid dimensions
   int chunk0, nchunks; // cell-scan chunks owned by the system
+  int ntx, nty;        // tiles across and down (cell numbering, see cell_local)
   int pad_;
   double pad;          // neighbour padding (configure_cells auto-value applied)
   double inv_n;        // 1/n, energy normalisation
   float smax;          // largest R_i + A_i + R_j + A_j of the system
   float fpad;          // pad in FP32
 };
+
+// Cell numbering of a system.  The grid is cut into ntx x nty tiles of nearly
+// equal size (tile k along a dimension of n cells covers [k n / nt, (k+1) n / nt));
+// cells are numbered tile by tile (tiles row-major), row-major inside a tile.  The
+// particles of a tile then occupy one contiguous range of slots, which the tile
+// force pass stages in shared memory.  With one tile (ntx = nty = 1, the FP64
+// form) this is the reference's col + row * cols.
+SC_HDI int tile_lo(int k, int n, int nt) { return (int)(((long long)k * n) / nt); }
+SC_HDI int tile_of(int c, int n, int nt) {
+  int k = (int)(((long long)c * nt) / n);
+  if (k > nt - 1) k = nt - 1;
+  while (k + 1 < nt && tile_lo(k + 1, n, nt) <= c) k++;
+  while (k > 0 && tile_lo(k, n, nt) > c) k--;
+  return k;
+}
+// local cell index (add c0 for the global one) of column col, row row
+SC_HDI int cell_local(const SysGeom& g, int col, int row) {
+  const int kx = tile_of(col, g.cols, g.ntx), ky = tile_of(row, g.rows, g.nty);
+  const int x0 = tile_lo(kx, g.cols, g.ntx), x1 = tile_lo(kx + 1, g.cols, g.ntx);
+  const int y0 = tile_lo(ky, g.rows, g.nty), y1 = tile_lo(ky + 1, g.rows, g.nty);
+  return y0 * g.cols + (y1 - y0) * x0 + (row - y0) * (x1 - x0) + (col - x0);
+}
+// column and row of local cell lc
+SC_HDI void cell_colrow(const SysGeom& g, int lc, int* col, int* row) {
+  const int ky = tile_of(lc / g.cols, g.rows, g.nty);
+  const int y0 = tile_lo(ky, g.rows, g.nty), hy = tile_lo(ky + 1, g.rows, g.nty) - y0;
+  const int off = lc - y0 * g.cols;
+  const int kx = tile_of(off / hy, g.cols, g.ntx);
+  const int x0 = tile_lo(kx, g.cols, g.ntx), wx = tile_lo(kx + 1, g.cols, g.ntx) - x0;
+  const int o2 = off - hy * x0;
+  *row = y0 + o2 / wx;
+  *col = x0 + o2 % wx;
+}
 
 // Per-(step, system) scalars, computed on the host with the reference's own
 // floating-point operations so that gamma and the box lengths are bit-identical
@@ -152,6 +192,20 @@ struct Dev {
   int* ord;     // [ntot] position -> slot
   int* nbr_p;   // column-major [k * ntot + position]
   int* nbr_pn;  // [ntot] list length at each position (capped at maxn)
+  // mixed form, tile force pass (pass_kind 1): each tile's pairs once.  The tile's
+  // compute entries (owner-major) and read entries live in the slot range of its
+  // particles times kTileEPP; a pair inside the tile is computed by its lower slot
+  // and read back by the other partner from the pair results.
+  int pass_kind;            // 0: one thread per particle over its full list, 1: tiles
+  int ntiles;
+  const int4* tiles;        // [ntiles] (system, first global cell, cells, 0)
+  int4* tinfo;              // [ntiles] (first slot, particles, compute entries, read entries)
+  unsigned short* t_own;    // [ntot * kTileEPP] owner (index in the tile) of each entry
+  unsigned* t_pe;           // [ntot * kTileEPP] partner: kTileInt | index in the tile, or
+                            // the slot; the cell offset code in the top 4 bits
+  unsigned* t_rd;           // [ntot * kTileEPP] read entries: the compute entry of the pair
+  int2* t_meta;             // [ntot] (compute offset | count << 24, read offset | count << 24)
+  float4* t_pb;             // [ntot * kTileEPP] pair results of tiles too large for shared memory
   // rebuild scratch
   int* cell_tmp;
   int* rank;
@@ -205,6 +259,16 @@ constexpr int kOrderWindow = 128;  // slots per window of the force-pass orderin
 // mixed-form list entries: slot in the low 28 bits, cell offset (dc+1, dr+1) above
 constexpr int kSlotBits = 28;
 constexpr unsigned kSlotMask = (1u << kSlotBits) - 1u;
+// tile force pass: entry capacity per particle of a tile (compute and read lists
+// each), particles and pair results held in shared memory, threads per tile; a
+// tile's partner index below kTileInt (bit 27) is a slot, so slots stay below 2^27
+constexpr int kTileEPP = 16;
+constexpr int kTileCap = 512;
+constexpr int kTilePairCap = 2048;
+constexpr int kTileThreads = 256;
+constexpr unsigned kTileInt = 1u << 27;
+constexpr unsigned kTilePayload = kTileInt - 1u;
+constexpr unsigned kTileNoEntry = 0xffffffffu;  // a read entry whose pair nobody computes
 
 // pass modes for the force kernels
 enum PassMode {
@@ -265,6 +329,8 @@ void launch_mx_local(const Dev& d, const StepScalars* tab, int row, bool all, cu
 void launch_mx_order(const Dev& d, bool all, cudaStream_t st);
 void launch_mx_build_list(const Dev& d, const StepScalars* tab, int row, bool all,
                           cudaStream_t st);
+// tile lists from the mixed lists (after launch_mx_build_list)
+void launch_tile_lists(const Dev& d, bool all, cudaStream_t st);
 // FP64 stress and energy partials of the mixed state (two kernels)
 void launch_mx_se64(const Dev& d, const StepScalars* tab, int row, cudaStream_t st);
 

@@ -43,7 +43,8 @@ __global__ void __launch_bounds__(128) k_build_nbrs(Dev d, const StepScalars* __
     double2 rai = d.ra[i];
     int idi = d.id[i];
     int c = d.cell[i] - g.c0;
-    int col = c % g.cols, rw = c / g.cols;
+    int col, rw;
+    cell_colrow(g, c, &col, &rw);
     // 3x3 block of cells; a dimension with fewer than three cells is scanned once
     // per distinct cell (the reference would list such cells twice).
     int ncx = g.cols < 3 ? g.cols : 3, ncy = g.rows < 3 ? g.rows : 3;
@@ -52,7 +53,7 @@ __global__ void __launch_bounds__(128) k_build_nbrs(Dev d, const StepScalars* __
       int r2 = ncy == 3 ? wrap_index(rw + a - 1, g.rows) : a;
       for (int b = 0; b < ncx; b++) {
         int c2 = ncx == 3 ? wrap_index(col + b - 1, g.cols) : b;
-        int cc = g.c0 + r2 * g.cols + c2;
+        int cc = g.c0 + cell_local(g, c2, r2);
         int st = d.cell_start[cc], nn = d.cell_count[cc];
         for (int j = st; j < st + nn; j++) {
           if (j == i) continue;

@@ -52,79 +52,15 @@ __device__ __forceinline__ void kahan_affine(float& s, float& c, float v, float 
   s = t;
 }
 
-template <int MODE, bool TWO>
-__global__ void __launch_bounds__(128, TWO ? 6 : 12) k_pass_mixed(Dev d,
-                                                       const StepScalars* __restrict__ tab,
-                                                       int row) {
-  constexpr bool kPred = (MODE == PASS_CORR_STRAIN || MODE == PASS_CORR_RESIZE);
-  if (kPred) mark_pending_rebuilds(d, tab, row);
-  const int pos = blockIdx.x * blockDim.x + threadIdx.x;
-  if (pos >= d.ntot) return;
-  const int i = d.ord[pos];  // the slot this thread works on (lists ordered by length)
-  const int s = d.psys[i];
-  const SysGeom& g = d.geom[s];
-  const StepScalars& ts = tab[row * d.nsys + s];
-  const float4* __restrict__ REC = kPred ? d.rec_t : d.rec;
-  const float W = kPred ? ts.f_Wc : ts.f_Wp;
-  const float H = kPred ? ts.f_Hc : ts.f_Hp;
-  const float gam = kPred ? ts.f_gamma_c : ts.f_gamma_p;
-  const bool smallx = g.cols < 3, smally = g.rows < 3;
-  const float Lxf = W * g.cols, Lyf = H * g.rows;
-  constexpr bool two_point = TWO;
-
-  const float4 ri = REC[i];
-  const float4 pai = d.pa[i];  // (R, A, index bits, 1/I)
-  const int cnt = d.nbr_pn[pos];
-  // the list is column-major: entry k of this slot sits k * ntot words further on;
-  // Lst walks it, two entries ahead of the pair being computed
-  const unsigned* __restrict__ Lst = reinterpret_cast<const unsigned*>(d.nbr_p) + pos;
-  const int stride = d.ntot;
-
-  float fx = 0.f, fy = 0.f, tq = 0.f;
-  // software pipeline: the list entry two ahead and the neighbour data one ahead
-  // are in flight while the current pair is computed
-  unsigned e1 = cnt > 0 ? __ldg(Lst) : 0u;
-  Lst += stride;
-  unsigned e2 = cnt > 1 ? __ldg(Lst) : 0u;
-  // the neighbour's record and radius (its A^2 is |shaft|^2 from the record)
-  float4 r1 = make_float4(0.f, 0.f, 0.f, 0.f);
-  float R1 = 0.f;
-  if (cnt > 0) {
-    r1 = REC[e1 & kSlotMask];
-    R1 = d.rf[e1 & kSlotMask];
-  }
-  const float ai = pai.y * pai.y;
-  for (int k = 0; k < cnt; k++) {
-    const unsigned e = e1;
-    const float4 rj = r1;
-    const float Rj = R1;
-    e1 = e2;
-    if (k + 1 < cnt) {
-      r1 = REC[e1 & kSlotMask];
-      R1 = d.rf[e1 & kSlotMask];
-    }
-    Lst += stride;
-    if (k + 2 < cnt) e2 = __ldg(Lst);
-    float dx = ri.x - rj.x + (float)(1 - (int)((e >> 28) & 3u)) * W;
-    float dy = ri.y - rj.y + (float)(1 - (int)(e >> 30)) * H;
-    if (smallx) dx += Lxf * (float)((dx < -0.5f * Lxf) - (dx > 0.5f * Lxf));
-    if (smally) dy += Lyf * (float)((dy < -0.5f * Lyf) - (dy > 0.5f * Lyf));
-    // Each thread evaluates the pair from its own particle's side (i as "p"): the
-    // forces need no canonical order, the two evaluations of a pair differ only by
-    // FP32 rounding.  Stress and energy are not summed here: on the steps that
-    // record them they come from the FP64 evaluation of the state (k_mx_se64).
-    PairF32 o;
-    const float cj = fmaf(rj.z, rj.z, rj.w * rj.w);
-    const bool touch =
-        two_point ? pair2_fp32(dx, dy, ri.z, ri.w, ai, rj.z, rj.w, cj, pai.x + Rj, gam, o)
-                  : pair_fp32<false>(dx, dy, ri.z, ri.w, ai, rj.z, rj.w, cj, pai.x + Rj, gam,
-                                     false, o);
-    if (!touch) continue;
-    fx += o.fx;
-    fy += o.fy;
-    tq += o.tp;
-  }
-
+// The Heun step of one particle after its forces (fx, fy, tq) at the pass's
+// positions are known: the predictor (MODE 2, 4) or corrector (MODE 1, 3) with the
+// compensated FP32 state, the rebuild test, or (MODE 0) the forces alone.  ri is
+// the particle's record at the pass's positions, gam the pass's gamma.
+template <int MODE>
+__device__ __forceinline__ void mixed_epilogue(const Dev& d, const StepScalars& ts,
+                                               const SysGeom& g, int s, int i, float4 ri,
+                                               float4 pai, float gam, float fx, float fy,
+                                               float tq) {
   const float dt = ts.f_step;
   const float A = pai.y, invI = pai.w;
   if (MODE == PASS_FORCE) {
@@ -239,6 +175,82 @@ __global__ void __launch_bounds__(128, TWO ? 6 : 12) k_pass_mixed(Dev d,
   }
 }
 
+template <int MODE, bool TWO>
+__global__ void __launch_bounds__(128, TWO ? 6 : 12) k_pass_mixed(Dev d,
+                                                       const StepScalars* __restrict__ tab,
+                                                       int row) {
+  constexpr bool kPred = (MODE == PASS_CORR_STRAIN || MODE == PASS_CORR_RESIZE);
+  if (kPred) mark_pending_rebuilds(d, tab, row);
+  const int pos = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pos >= d.ntot) return;
+  const int i = d.ord[pos];  // the slot this thread works on (lists ordered by length)
+  const int s = d.psys[i];
+  const SysGeom& g = d.geom[s];
+  const StepScalars& ts = tab[row * d.nsys + s];
+  const float4* __restrict__ REC = kPred ? d.rec_t : d.rec;
+  const float W = kPred ? ts.f_Wc : ts.f_Wp;
+  const float H = kPred ? ts.f_Hc : ts.f_Hp;
+  const float gam = kPred ? ts.f_gamma_c : ts.f_gamma_p;
+  const bool smallx = g.cols < 3, smally = g.rows < 3;
+  const float Lxf = W * g.cols, Lyf = H * g.rows;
+  constexpr bool two_point = TWO;
+
+  const float4 ri = REC[i];
+  const float4 pai = d.pa[i];  // (R, A, index bits, 1/I)
+  const int cnt = d.nbr_pn[pos];
+  // the list is column-major: entry k of this slot sits k * ntot words further on;
+  // Lst walks it, two entries ahead of the pair being computed
+  const unsigned* __restrict__ Lst = reinterpret_cast<const unsigned*>(d.nbr_p) + pos;
+  const int stride = d.ntot;
+
+  float fx = 0.f, fy = 0.f, tq = 0.f;
+  // software pipeline: the list entry two ahead and the neighbour data one ahead
+  // are in flight while the current pair is computed
+  unsigned e1 = cnt > 0 ? __ldg(Lst) : 0u;
+  Lst += stride;
+  unsigned e2 = cnt > 1 ? __ldg(Lst) : 0u;
+  // the neighbour's record and radius (its A^2 is |shaft|^2 from the record)
+  float4 r1 = make_float4(0.f, 0.f, 0.f, 0.f);
+  float R1 = 0.f;
+  if (cnt > 0) {
+    r1 = REC[e1 & kSlotMask];
+    R1 = d.rf[e1 & kSlotMask];
+  }
+  const float ai = pai.y * pai.y;
+  for (int k = 0; k < cnt; k++) {
+    const unsigned e = e1;
+    const float4 rj = r1;
+    const float Rj = R1;
+    e1 = e2;
+    if (k + 1 < cnt) {
+      r1 = REC[e1 & kSlotMask];
+      R1 = d.rf[e1 & kSlotMask];
+    }
+    Lst += stride;
+    if (k + 2 < cnt) e2 = __ldg(Lst);
+    float dx = ri.x - rj.x + (float)(1 - (int)((e >> 28) & 3u)) * W;
+    float dy = ri.y - rj.y + (float)(1 - (int)(e >> 30)) * H;
+    if (smallx) dx += Lxf * (float)((dx < -0.5f * Lxf) - (dx > 0.5f * Lxf));
+    if (smally) dy += Lyf * (float)((dy < -0.5f * Lyf) - (dy > 0.5f * Lyf));
+    // Each thread evaluates the pair from its own particle's side (i as "p"): the
+    // forces need no canonical order, the two evaluations of a pair differ only by
+    // FP32 rounding.  Stress and energy are not summed here: on the steps that
+    // record them they come from the FP64 evaluation of the state (k_mx_se64).
+    PairF32 o;
+    const float cj = fmaf(rj.z, rj.z, rj.w * rj.w);
+    const bool touch =
+        two_point ? pair2_fp32(dx, dy, ri.z, ri.w, ai, rj.z, rj.w, cj, pai.x + Rj, gam, o)
+                  : pair_fp32<false>(dx, dy, ri.z, ri.w, ai, rj.z, rj.w, cj, pai.x + Rj, gam,
+                                     false, o);
+    if (!touch) continue;
+    fx += o.fx;
+    fy += o.fy;
+    tq += o.tp;
+  }
+
+  mixed_epilogue<MODE>(d, ts, g, s, i, ri, pai, gam, fx, fy, tq);
+}
+
 template <int MODE>
 void launch_one(const Dev& d, const StepScalars* tab, int row, cudaStream_t st, int block) {
   int grid = (d.ntot + block - 1) / block;
@@ -246,6 +258,220 @@ void launch_one(const Dev& d, const StepScalars* tab, int row, cudaStream_t st, 
     k_pass_mixed<MODE, true><<<grid, block, 0, st>>>(d, tab, row);
   else
     k_pass_mixed<MODE, false><<<grid, block, 0, st>>>(d, tab, row);
+}
+
+// ---- tile force pass ----
+//
+// One block per tile of cells (a contiguous range of slots).  The tile's records
+// and radii are staged in shared memory.  Its compute entries, ordered by owner,
+// hold every pair of an owner with a partner outside the tile and every pair with
+// a partner of higher slot inside it, so a pair inside the tile is evaluated once:
+// the threads take the entries in turn (one pair per thread, whatever the list
+// lengths) and leave each pair's forces and both torques in shared memory; then
+// each owner sums its own entries in list order and, with the opposite sign, the
+// entries of the pairs whose lower partner computed them (its read entries, in
+// list order).  The sums are deterministic.  A tile with more particles or pair
+// entries than shared memory holds uses global memory for the excess.
+template <int MODE, bool TWO>
+__global__ void __launch_bounds__(kTileThreads, TWO ? 2 : 4) k_tile_pass(
+    Dev d, const StepScalars* __restrict__ tab, int row) {
+  constexpr bool kCorr = (MODE == PASS_CORR_STRAIN || MODE == PASS_CORR_RESIZE);
+  if (kCorr) mark_pending_rebuilds(d, tab, row);
+  __shared__ float4 s_rec[kTileCap];
+  __shared__ float s_R[kTileCap];
+  __shared__ float4 s_pb[kTilePairCap];
+  const int4 ti = d.tinfo[blockIdx.x];
+  const int p0 = ti.x, nown = ti.y, ne = ti.z;
+  if (nown <= 0) return;
+  const int s = d.psys[p0];
+  const SysGeom& g = d.geom[s];
+  const StepScalars& ts = tab[row * d.nsys + s];
+  const float4* __restrict__ REC = kCorr ? d.rec_t : d.rec;
+  const float W = kCorr ? ts.f_Wc : ts.f_Wp;
+  const float H = kCorr ? ts.f_Hc : ts.f_Hp;
+  const float gam = kCorr ? ts.f_gamma_c : ts.f_gamma_p;
+  const bool smallx = g.cols < 3, smally = g.rows < 3;
+  const float Lxf = W * g.cols, Lyf = H * g.rows;
+  const int nst = nown < kTileCap ? nown : kTileCap;
+  for (int l = threadIdx.x; l < nst; l += blockDim.x) {
+    s_rec[l] = REC[p0 + l];
+    s_R[l] = d.rf[p0 + l];
+  }
+  float4* pb = ne <= kTilePairCap ? s_pb : d.t_pb + (size_t)p0 * kTileEPP;
+  const size_t ebase = (size_t)p0 * kTileEPP;
+  __syncthreads();
+  for (int e = threadIdx.x; e < ne; e += blockDim.x) {
+    const int o = d.t_own[ebase + e];
+    const unsigned pe = d.t_pe[ebase + e];
+    const float4 ri = o < kTileCap ? s_rec[o] : REC[p0 + o];
+    const float Ri = o < kTileCap ? s_R[o] : d.rf[p0 + o];
+    const unsigned pl = pe & kTilePayload;
+    float4 rj;
+    float Rj;
+    if (pe & kTileInt) {
+      rj = pl < (unsigned)kTileCap ? s_rec[pl] : REC[p0 + pl];
+      Rj = pl < (unsigned)kTileCap ? s_R[pl] : d.rf[p0 + pl];
+    } else {
+      rj = REC[pl];
+      Rj = d.rf[pl];
+    }
+    float dx = ri.x - rj.x + (float)(1 - (int)((pe >> 28) & 3u)) * W;
+    float dy = ri.y - rj.y + (float)(1 - (int)(pe >> 30)) * H;
+    if (smallx) dx += Lxf * (float)((dx < -0.5f * Lxf) - (dx > 0.5f * Lxf));
+    if (smally) dy += Lyf * (float)((dy < -0.5f * Lyf) - (dy > 0.5f * Lyf));
+    PairF32 res;
+    const float ai = fmaf(ri.z, ri.z, ri.w * ri.w);
+    const float cj = fmaf(rj.z, rj.z, rj.w * rj.w);
+    const bool touch =
+        TWO ? pair2_fp32(dx, dy, ri.z, ri.w, ai, rj.z, rj.w, cj, Ri + Rj, gam, res)
+            : pair_fp32<false>(dx, dy, ri.z, ri.w, ai, rj.z, rj.w, cj, Ri + Rj, gam, false,
+                               res);
+    pb[e] = touch ? make_float4(res.fx, res.fy, res.tp, res.tq) : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  __syncthreads();
+  for (int l = threadIdx.x; l < nown; l += blockDim.x) {
+    const int i = p0 + l;
+    const int2 m = d.t_meta[i];
+    const int c0 = m.x & 0xffffff, nc = (int)((unsigned)m.x >> 24);
+    const int r0 = m.y & 0xffffff, nr = (int)((unsigned)m.y >> 24);
+    float fx = 0.f, fy = 0.f, tq = 0.f;
+    for (int k = 0; k < nc; k++) {
+      const float4 v = pb[c0 + k];
+      fx += v.x;
+      fy += v.y;
+      tq += v.z;
+    }
+    for (int k = 0; k < nr; k++) {
+      const unsigned e = d.t_rd[ebase + r0 + k];
+      if (e == kTileNoEntry) continue;
+      const float4 v = pb[e];
+      fx -= v.x;
+      fy -= v.y;
+      tq += v.w;
+    }
+    const float4 ri = l < kTileCap ? s_rec[l] : REC[i];
+    mixed_epilogue<MODE>(d, ts, g, s, i, ri, d.pa[i], gam, fx, fy, tq);
+  }
+}
+
+template <int MODE>
+void launch_tile(const Dev& d, const StepScalars* tab, int row, cudaStream_t st) {
+  if (d.contact_model == 1)
+    k_tile_pass<MODE, true><<<d.ntiles, kTileThreads, 0, st>>>(d, tab, row);
+  else
+    k_tile_pass<MODE, false><<<d.ntiles, kTileThreads, 0, st>>>(d, tab, row);
+}
+
+// block-wide exclusive scan of one int per thread; *total the block's sum
+__device__ __forceinline__ int tile_excl_scan(int v, int* sh, int* total) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sh[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    int t = lane < nw ? sh[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    sh[lane] = t;
+  }
+  __syncthreads();
+  const int excl = x - v + (w > 0 ? sh[w - 1] : 0);
+  *total = sh[nw - 1];
+  __syncthreads();
+  return excl;
+}
+
+// The tile lists of the rebuilt systems from their mixed lists (one block per
+// tile): each particle's entries split into compute entries (partner outside the
+// tile, or inside it at a higher slot) and read entries (inside, at a lower slot);
+// offsets by block scans; then every read entry finds the compute entry of its pair
+// among the partner's.  A pair listed by one side only (the capsule test's rounding
+// at the padding's edge, far from contact) is computed by nobody.
+__global__ void __launch_bounds__(kTileThreads) k_tile_lists(Dev d, int all) {
+  if (!all && *d.any == 0) return;
+  const int4 tl = d.tiles[blockIdx.x];
+  if (!all && d.flags[tl.x] == 0) return;
+  __shared__ int sh[32];
+  const int cl = tl.y + tl.z - 1;
+  const int p0 = d.cell_start[tl.y];
+  const int p1 = d.cell_start[cl] + d.cell_count[cl];
+  const int nown = p1 - p0;
+  const size_t ebase = (size_t)p0 * kTileEPP;
+  const int ecap = nown * kTileEPP;
+  const int ntot = d.ntot;
+  int cc = 0, cr = 0;  // running offsets (the same in every thread)
+  bool over = false;
+  for (int base = 0; base < nown; base += blockDim.x) {
+    const int l = base + threadIdx.x;
+    int nc = 0, nr = 0;
+    if (l < nown) {
+      const int i = p0 + l;
+      const int cnt = min(d.nbr_n[i], d.maxn);
+      for (int k = 0; k < cnt; k++) {
+        const int j = (int)((unsigned)d.nbr[(size_t)k * ntot + i] & kSlotMask);
+        if (j >= p0 && j < p1 && j - p0 < l)
+          nr++;
+        else
+          nc++;
+      }
+      over = over || nc > 255 || nr > 255;
+    }
+    int tc, tr;
+    const int ec = tile_excl_scan(nc, sh, &tc);
+    const int er = tile_excl_scan(nr, sh, &tr);
+    if (l < nown) d.t_meta[p0 + l] = make_int2((cc + ec) | (nc << 24), (cr + er) | (nr << 24));
+    cc += tc;
+    cr += tr;
+  }
+  over = __syncthreads_or(over) != 0;
+  if (cc > ecap || cr > ecap || over) {
+    if (threadIdx.x == 0) atomicOr(d.status, ST_NBR_OVERFLOW);
+    cc = min(cc, ecap);
+    cr = min(cr, ecap);
+  }
+  if (threadIdx.x == 0) d.tinfo[blockIdx.x] = make_int4(p0, nown, cc, cr);
+  for (int l = threadIdx.x; l < nown; l += blockDim.x) {
+    const int i = p0 + l;
+    const int cnt = min(d.nbr_n[i], d.maxn);
+    int q = d.t_meta[i].x & 0xffffff;
+    for (int k = 0; k < cnt; k++) {
+      const unsigned e = (unsigned)d.nbr[(size_t)k * ntot + i];
+      const int j = (int)(e & kSlotMask);
+      const bool in = j >= p0 && j < p1;
+      if (in && j - p0 < l) continue;
+      if (q < ecap) {
+        d.t_own[ebase + q] = (unsigned short)l;
+        d.t_pe[ebase + q] = (e & ~kSlotMask) | (in ? (kTileInt | (unsigned)(j - p0)) : (unsigned)j);
+      }
+      q++;
+    }
+  }
+  __syncthreads();  // every compute entry of the tile is written
+  for (int l = threadIdx.x; l < nown; l += blockDim.x) {
+    const int i = p0 + l;
+    const int cnt = min(d.nbr_n[i], d.maxn);
+    int r = d.t_meta[i].y & 0xffffff;
+    for (int k = 0; k < cnt; k++) {
+      const int j = (int)((unsigned)d.nbr[(size_t)k * ntot + i] & kSlotMask);
+      if (!(j >= p0 && j < p1 && j - p0 < l)) continue;
+      const int2 m = d.t_meta[j];
+      const int q0 = m.x & 0xffffff, qn = (int)((unsigned)m.x >> 24);
+      unsigned found = kTileNoEntry;
+      for (int q = q0; q < q0 + qn && q < ecap; q++)
+        if ((d.t_pe[ebase + q] & (kTileInt | kTilePayload)) == (kTileInt | (unsigned)l)) {
+          found = (unsigned)q;
+          break;
+        }
+      if (r < ecap) d.t_rd[ebase + r] = found;
+      r++;
+    }
+  }
 }
 
 // ---- rebuild support ----
@@ -274,7 +500,8 @@ __global__ void k_mx_local(Dev d, const StepScalars* __restrict__ tab, int row, 
     const SysGeom& g = d.geom[s];
     const StepScalars& ts = tab[row * d.nsys + s];
     int lc = d.cell[i] - g.c0;
-    int col = lc % g.cols, rw = lc / g.cols;
+    int col, rw;
+    cell_colrow(g, lc, &col, &rw);
     d.cellp[i] = col | (rw << 16);
     double2 p = d.xy[i];
     double lx = p.x - (col + 0.5) * ts.W_p;
@@ -317,7 +544,7 @@ __global__ void __launch_bounds__(128, 12) k_mx_build_list(Dev d, const StepScal
       for (int b = 0; b < ncx; b++) {
         int dc = smallx ? b - col : b - 1;
         int c2 = smallx ? b : wrap_index(col + dc, g.cols);
-        int cc = g.c0 + r2 * g.cols + c2;
+        int cc = g.c0 + cell_local(g, c2, r2);
         int st = d.cell_start[cc], en = st + d.cell_count[cc];
         unsigned code = ((unsigned)(dc + 1) << 28) | ((unsigned)(dr + 1) << 30);
         for (int j = st; j < en; j++) {
@@ -384,15 +611,29 @@ void launch_mx_order(const Dev& d, bool all, cudaStream_t st) {
 void launch_pass_mixed(const Dev& d, int mode, bool se, const StepScalars* tab, int row,
                        cudaStream_t st, int block) {
   if (block <= 0) block = 128;
-  switch (mode) {
-    case PASS_FORCE: launch_one<PASS_FORCE>(d, tab, row, st, block); break;
-    case PASS_CORR_STRAIN: launch_one<PASS_CORR_STRAIN>(d, tab, row, st, block); break;
-    case PASS_PRED_STRAIN: launch_one<PASS_PRED_STRAIN>(d, tab, row, st, block); break;
-    case PASS_CORR_RESIZE: launch_one<PASS_CORR_RESIZE>(d, tab, row, st, block); break;
-    case PASS_PRED_RESIZE: launch_one<PASS_PRED_RESIZE>(d, tab, row, st, block); break;
+  if (d.pass_kind == 1) {
+    switch (mode) {
+      case PASS_FORCE: launch_tile<PASS_FORCE>(d, tab, row, st); break;
+      case PASS_CORR_STRAIN: launch_tile<PASS_CORR_STRAIN>(d, tab, row, st); break;
+      case PASS_PRED_STRAIN: launch_tile<PASS_PRED_STRAIN>(d, tab, row, st); break;
+      case PASS_CORR_RESIZE: launch_tile<PASS_CORR_RESIZE>(d, tab, row, st); break;
+      case PASS_PRED_RESIZE: launch_tile<PASS_PRED_RESIZE>(d, tab, row, st); break;
+    }
+  } else {
+    switch (mode) {
+      case PASS_FORCE: launch_one<PASS_FORCE>(d, tab, row, st, block); break;
+      case PASS_CORR_STRAIN: launch_one<PASS_CORR_STRAIN>(d, tab, row, st, block); break;
+      case PASS_PRED_STRAIN: launch_one<PASS_PRED_STRAIN>(d, tab, row, st, block); break;
+      case PASS_CORR_RESIZE: launch_one<PASS_CORR_RESIZE>(d, tab, row, st, block); break;
+      case PASS_PRED_RESIZE: launch_one<PASS_PRED_RESIZE>(d, tab, row, st, block); break;
+    }
   }
   // stress and energy of the state (forces and predictor passes) in FP64
   if (se) launch_mx_se64(d, tab, row, st);
+}
+
+void launch_tile_lists(const Dev& d, bool all, cudaStream_t st) {
+  k_tile_lists<<<d.ntiles, kTileThreads, 0, st>>>(d, all ? 1 : 0);
 }
 
 void launch_mx_materialize(const Dev& d, const StepScalars* tab, int row, bool all,
