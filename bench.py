@@ -350,9 +350,9 @@ def batched_leg(args, device, torch):
 
     w = make_batch(generate_packing)
 
-    def new(profile=False, pad=PAD, block=0):
+    def new(profile=False, pad=PAD, block=0, **kw):
         b = BoxBatch(w["ns"], w["L"], w["x"], w["y"], w["p"], w["A"], w["R"], pad,
-                     precision="mixed", device=device, profile=profile, block=block)
+                     precision="mixed", device=device, profile=profile, block=block, **kw)
         for k, r in enumerate(w["rates"]):
             b.set_strain_rate(float(r), sys=k)
         b.set_step(w["dt"])
@@ -361,12 +361,14 @@ def batched_leg(args, device, torch):
     t = new()
     t.strain_steps(args.warmup)
     f, blk = t.autotune(50)
+    o = t.options()
     t.close()
-    b = new(pad=PAD * f, block=blk)
+    kw = dict(pass_kind=o["pass_kind"], tile_target=o["tile_target"])
+    b = new(pad=PAD * f, block=blk, **kw)
     b.strain_steps(args.warmup)
     secs = time_steps(b, args.steps, torch)
     b.close()
-    pr = new(profile=True, pad=PAD * f, block=blk)
+    pr = new(profile=True, pad=PAD * f, block=blk, **kw)
     pr.strain_steps(args.warmup)
     pr.pass_times()
     pr.strain_steps(max(args.steps, 20))
@@ -380,13 +382,13 @@ def batched_leg(args, device, torch):
     return {"workload": "batch512", "particles": w["n"], "value": w["n"] * args.steps / secs,
             "unit": "particle-steps/s", "ms_per_step": 1e3 * secs / args.steps,
             "steps": args.steps, "warmup": args.warmup,
-            "tuning": {"pad": PAD * f, "block": blk},
+            "tuning": {"pad": PAD * f, "block": blk, **kw},
             "pass_ms": pass_ms, "mean_list_length": nbar,
             "roofline_frac": achieved / peak, "achieved_gbs": achieved}
 
 
-def minimise_leg(replicas=32, n=4096, max_iter=20000, ftol=1e-14, device=0, e_jam=1e-12,
-                 dt_max=0.2):
+def minimise_leg(replicas=128, n=4096, max_iter=150000, ftol=1e-14, device=0, e_jam=1e-12,
+                 dt_max=0.2, cg_iter=2000):
     """Minimisation time to tolerance on the jamming workload's shape: replicas of
     N = 4096 with a/R in {0.25, 0.5, 1, 2} (a quarter each), seeds 100 + k, from
     packing 0.70.  Untimed preparation: the mixed form compresses every replica to
@@ -396,8 +398,9 @@ def minimise_leg(replicas=32, n=4096, max_iter=20000, ftol=1e-14, device=0, e_ja
     compressed by one more 1e-4 increment.  From that same state the two timed arms
     minimise to max|F_i|, |tau_i|/sqrt(I_i) < ftol: (a) mixed FIRE to 1e-6, then
     FP64 FIRE; (b) FP64 FIRE alone; (c) the reference's conjugate gradient (FP64) on
-    one replica of each aspect ratio, stopped by the reference's rules.  Each FP64
-    stage stops after max_iter iterations."""
+    one replica of each aspect ratio, stopped by the reference's rules or after
+    cg_iter iterations.  Each FP64 FIRE stage stops after max_iter iterations; a
+    replica that has converged takes no further force passes."""
     from spherocyls_gb300 import BoxBatch, generate_packing
 
     aors = [0.25, 0.5, 1.0, 2.0]
@@ -442,7 +445,7 @@ def minimise_leg(replicas=32, n=4096, max_iter=20000, ftol=1e-14, device=0, e_ja
     q = BoxBatch([n] * len(sub), L1[sub], x1[sel], y1[sel], ps[sel], A[sel], R[sel], 0.1,
                  precision="fp64", **kw)
     t = time.perf_counter()
-    cit, ce, cwhy = q.cg_minimize(max_iter)
+    cit, ce, cwhy = q.cg_minimize(cg_iter)
     tcg = time.perf_counter() - t
     q.calc_forces()
     qfx, qfy, qtq = q.forces()
@@ -496,9 +499,14 @@ def main():
                     help="pick the mixed form's padding and block size with sc_autotune")
     ap.add_argument("--legs", default="precision,batched,minimise",
                     help="extra legs of the GPU arm (comma separated, or 'none')")
-    ap.add_argument("--min-replicas", type=int, default=32)
-    ap.add_argument("--min-iters", type=int, default=40000,
+    ap.add_argument("--min-replicas", type=int, default=128)
+    ap.add_argument("--min-iters", type=int, default=150000,
                     help="FP64 FIRE iteration cap of the minimisation leg")
+    ap.add_argument("--pass-kind", choices=["auto", "list", "tile"], default="auto",
+                    help="the mixed form's force pass before autotuning (profiler captures)")
+    ap.add_argument("--tile-target", type=int, default=0)
+    ap.add_argument("--pad-factor", type=float, default=1.0,
+                    help="padding factor of the mixed form when not autotuned")
     ap.add_argument("--no-graphs", action="store_true",
                     help="launch eagerly instead of through CUDA graphs (profiler captures: "
                          "kernels inside graphs with conditional nodes cannot be profiled)")
@@ -531,23 +539,26 @@ def main():
 
     w = make_workload(args.workload, generate_packing)
     n = w["n"]
-    tuned = {"pad": PAD, "block": 128}
+    tuned = {"pad": PAD * args.pad_factor, "block": 128, "pass_kind": args.pass_kind,
+             "tile_target": args.tile_target}
 
     def new_box(precision, profile=False, state=None):
         # the mixed form runs with the autotuned padding and block size
         pad = tuned["pad"] if precision == "mixed" else PAD
         block = tuned["block"] if precision == "mixed" else 0
+        kw = dict(pass_kind=tuned["pass_kind"], tile_target=tuned["tile_target"]) \
+            if precision == "mixed" else {}
         x, y, p = state[:3] if state is not None else (w["x"], w["y"], w["p"])
         if args.workload == "batch512":
             b = BoxBatch(w["ns"], w["L"], x, y, p, w["A"], w["R"], pad, precision=precision,
                          device=local, profile=profile, use_graphs=not args.no_graphs,
-                         block=block)
+                         block=block, **kw)
             for k, r in enumerate(w["rates"]):
                 b.set_strain_rate(float(r), sys=k)
         else:
             b = SpherocylBox(w["L"], x, y, p, w["A"], w["R"], pad,
                              precision=precision, device=local, profile=profile,
-                             use_graphs=not args.no_graphs, block=block)
+                             use_graphs=not args.no_graphs, block=block, **kw)
             b.set_strain_rate(w["rate"])
         b.set_step(w["dt"])
         if state is not None:
@@ -561,8 +572,10 @@ def main():
         t = new_box("mixed")
         t.strain_steps(args.warmup)
         f, blk = t.autotune(100)  # long enough to include rebuilds
+        o = t.options()
         t.close()
-        tuned = {"pad": PAD * f, "block": blk}
+        tuned = {"pad": PAD * f, "block": blk, "pass_kind": o["pass_kind"],
+                 "tile_target": o["tile_target"]}
 
     if args.only:
         b = new_box(args.only)
@@ -677,7 +690,8 @@ def main():
             "dtype": "f32+f64",
             "data": "synthetic (seeded crossing-free packing)",
             "config": config_of(args.workload, world),
-            "tuning": {"mixed_pad": tuned["pad"], "mixed_block": tuned["block"]},
+            "tuning": {"mixed_pad": tuned["pad"], "mixed_block": tuned["block"],
+                       "pass_kind": tuned["pass_kind"], "tile_target": tuned["tile_target"]},
             "value_fp64": value64,
             "plain_fp64": {"value": value64, "unit": "particle-steps/s",
                            "ms_per_step": 1e3 * secs64 / args.steps, "steps": args.steps,
@@ -689,7 +703,8 @@ def main():
                                      if args.workload in PASS_DRAM_BYTES_PER_PARTICLE
                                      else None),
                          "traffic_unit": "bytes per launch (ncu capture)",
-                         "kernel": "k_pass_mixed (corrector/predictor force passes)",
+                         "kernel": ("k_tile_pass" if tuned["pass_kind"] == "tile" else
+                                    "k_pass_mixed") + " (corrector/predictor force passes)",
                          "pass_ms": pass_ms, "bytes_per_particle_pass": bpp,
                          "mean_list_length": nbar,
                          "rebuild_body_ms_mean_eager": pt["rebuild_ms"],

@@ -76,10 +76,10 @@ typedef struct sc_options {
                       * also where the GPU reads pageable host memory in place (0) */
   int cg_max_probes; /* energy probes one conjugate-gradient line search may take before
                       * its system stops with SC_CG_PROBES, 0 = default (256) */
-  int pass_kind;     /* mixed form's force pass: SC_PASS_AUTO (tiles), SC_PASS_LIST (one
-                      * thread per particle over its full list, each pair twice) or
-                      * SC_PASS_TILE (blocks of cells staged in shared memory, each pair
-                      * inside a tile once) */
+  int pass_kind;     /* mixed form's force pass: SC_PASS_LIST (one thread per particle
+                      * over its full list, each pair twice), SC_PASS_TILE (blocks of
+                      * cells staged in shared memory, each pair inside a tile once) or
+                      * SC_PASS_AUTO (the list pass until sc_autotune times both) */
   int tile_target;   /* particles per tile the tile pass aims at, 0 = default (256) */
 } sc_options;
 

@@ -52,6 +52,9 @@ def build(with_ref: bool | None = None) -> None:
             raise RuntimeError(f"{REF_ENV} does not name the reference checkout")
         subprocess.run(["make", "-s", "-C", HERE, "ref",
                         f"REF_SRC={os.path.join(root, 'src', 'cpp')}"], check=True)
+        cuda = os.path.join(root, "src", "cuda")
+        if os.path.isdir(cuda):
+            subprocess.run(["make", "-s", "-C", HERE, "ref_cuda", f"REF_CUDA={cuda}"], check=True)
 
 
 def _ptr(a: np.ndarray):

