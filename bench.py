@@ -363,7 +363,8 @@ def batched_leg(args, device, torch):
     f, blk = t.autotune(50)
     o = t.options()
     t.close()
-    kw = dict(pass_kind=o["pass_kind"], tile_target=o["tile_target"])
+    kw = dict(pass_kind=o["pass_kind"], tile_target=o["tile_target"],
+              persist_steps=o["persist_steps"])
     b = new(pad=PAD * f, block=blk, **kw)
     b.strain_steps(args.warmup)
     secs = time_steps(b, args.steps, torch)
@@ -456,7 +457,8 @@ def minimise_leg(replicas=128, n=4096, max_iter=150000, ftol=1e-14, device=0, e_
     inertia = Rs ** 4 * C / (6 * Rs * (REF_PI * Rs + 4 * As))
     res = np.maximum(np.hypot(qfx, qfy), np.abs(qtq) / np.sqrt(inertia)).reshape(len(sub), n)
     cres = res.max(axis=1)
-    both = da & db & dc & (e_c > 1e-16) & (e_a > 1e-16)
+    jammed = (e_c > 1e-16) & (e_a > 1e-16)
+    both = da & db & dc & jammed
     return {
         "workload": f"jam_{replicas}x{n}", "replicas": replicas, "N": n, "ftol": ftol,
         "prep": {"seconds": t_prep, "increments": n_inc,
@@ -470,6 +472,9 @@ def minimise_leg(replicas=128, n=4096, max_iter=150000, ftol=1e-14, device=0, e_
                     "iters_mean": float(cit.mean()),
                     "stop_reasons": {str(k): int((cwhy == k).sum()) for k in (1, 2, 3, 4, 5)},
                     "below_ftol": int((cres < ftol).sum()), "max_residual": float(cres.max())},
+        "jammed_converged_both": int(both.sum()),
+        "energy_per_particle_range": [float(min(e_a.min(), e_c.min())),
+                                      float(max(e_a.max(), e_c.max()))],
         "speedup": tc / (ta + tb),
         "energy_rel_diff_max": (float(np.max(np.abs(e_a[both] - e_c[both]) / e_c[both]))
                                 if both.any() else None),
@@ -505,6 +510,8 @@ def main():
     ap.add_argument("--pass-kind", choices=["auto", "list", "tile"], default="auto",
                     help="the mixed form's force pass before autotuning (profiler captures)")
     ap.add_argument("--tile-target", type=int, default=0)
+    ap.add_argument("--persist", action="store_true",
+                    help="persistent step kernel for the mixed form when not autotuned")
     ap.add_argument("--pad-factor", type=float, default=1.0,
                     help="padding factor of the mixed form when not autotuned")
     ap.add_argument("--no-graphs", action="store_true",
@@ -540,14 +547,14 @@ def main():
     w = make_workload(args.workload, generate_packing)
     n = w["n"]
     tuned = {"pad": PAD * args.pad_factor, "block": 128, "pass_kind": args.pass_kind,
-             "tile_target": args.tile_target}
+             "tile_target": args.tile_target, "persist_steps": args.persist}
 
     def new_box(precision, profile=False, state=None):
         # the mixed form runs with the autotuned padding and block size
         pad = tuned["pad"] if precision == "mixed" else PAD
         block = tuned["block"] if precision == "mixed" else 0
-        kw = dict(pass_kind=tuned["pass_kind"], tile_target=tuned["tile_target"]) \
-            if precision == "mixed" else {}
+        kw = dict(pass_kind=tuned["pass_kind"], tile_target=tuned["tile_target"],
+                  persist_steps=tuned["persist_steps"]) if precision == "mixed" else {}
         x, y, p = state[:3] if state is not None else (w["x"], w["y"], w["p"])
         if args.workload == "batch512":
             b = BoxBatch(w["ns"], w["L"], x, y, p, w["A"], w["R"], pad, precision=precision,
@@ -575,7 +582,7 @@ def main():
         o = t.options()
         t.close()
         tuned = {"pad": PAD * f, "block": blk, "pass_kind": o["pass_kind"],
-                 "tile_target": o["tile_target"]}
+                 "tile_target": o["tile_target"], "persist_steps": o["persist_steps"]}
 
     if args.only:
         b = new_box(args.only)
@@ -691,7 +698,8 @@ def main():
             "data": "synthetic (seeded crossing-free packing)",
             "config": config_of(args.workload, world),
             "tuning": {"mixed_pad": tuned["pad"], "mixed_block": tuned["block"],
-                       "pass_kind": tuned["pass_kind"], "tile_target": tuned["tile_target"]},
+                       "pass_kind": tuned["pass_kind"], "tile_target": tuned["tile_target"],
+                       "persist_steps": tuned["persist_steps"]},
             "value_fp64": value64,
             "plain_fp64": {"value": value64, "unit": "particle-steps/s",
                            "ms_per_step": 1e3 * secs64 / args.steps, "steps": args.steps,

@@ -81,6 +81,10 @@ typedef struct sc_options {
                       * cells staged in shared memory, each pair inside a tile once) or
                       * SC_PASS_AUTO (the list pass until sc_autotune times both) */
   int tile_target;   /* particles per tile the tile pass aims at, 0 = default (256) */
+  int persist_steps; /* mixed form, per-particle pass, simple shear: 1 advances runs of
+                      * steps in one persistent cooperative launch (corrector and
+                      * predictor passes separated by bounded grid barriers) until a
+                      * step needs a rebuild; 0 launches each pass (CUDA graphs) */
 } sc_options;
 
 #define SC_PASS_AUTO 0
@@ -223,10 +227,10 @@ int sc_find_jam(sc_handle *h, double e_jam, double step, double min_step, double
 
 /* Mixed form: times `steps` shear steps (after as many warm-up steps) of a copy of
  * the handle for each candidate -- padding factors {0.5, 1, 1.5, 2, 3} x the current
- * padding, crossed with the per-particle force pass at block sizes {64, 128} and the
- * tile force pass at {128, 256, 384} particles per tile -- and gives the handle the
- * fastest (*pad_factor, *block; the pass kind and tile size through
- * sc_get_options).  The live state is not advanced.  The FP64 form is left as it is
+ * padding, crossed with the per-particle force pass at block sizes {64, 128}, the
+ * same pass in the persistent step kernel, and the tile force pass at {128, 256, 384}
+ * particles per tile -- and gives the handle the fastest (*pad_factor, *block; the
+ * pass kind, tile size and persistence through sc_get_options).  The live state is not advanced.  The FP64 form is left as it is
  * (factor 1).  Replaces the reference's fixed launch-shape table
  * (src/cuda/spherocyl_box.cpp:193-238). */
 int sc_autotune(sc_handle *h, int steps, double *pad_factor, int *block);

@@ -47,6 +47,7 @@ class ScOptions(ctypes.Structure):
         ("cg_max_probes", ctypes.c_int),
         ("pass_kind", ctypes.c_int),
         ("tile_target", ctypes.c_int),
+        ("persist_steps", ctypes.c_int),
     ]
 
 

@@ -158,7 +158,8 @@ class BoxBatch:
                  stress: str = "compat", device: int = 0, max_nbrs: int = 0,
                  use_graphs: bool = True, block: int = 0, profile: bool = False,
                  contacts: int = 1, Ly=None, stage_inputs: bool = False,
-                 cg_max_probes: int = 0, pass_kind: str = "auto", tile_target: int = 0):
+                 cg_max_probes: int = 0, pass_kind: str = "auto", tile_target: int = 0,
+                 persist_steps: bool = False):
         n_per_sys = np.ascontiguousarray(np.atleast_1d(n_per_sys), dtype=np.int32)
         self.nsys = int(n_per_sys.shape[0])
         self.n_per_sys = n_per_sys
@@ -187,6 +188,7 @@ class BoxBatch:
             raise ValueError("pass_kind must be 'auto', 'list' or 'tile'")
         opt.pass_kind = PASS[pass_kind]
         opt.tile_target = int(tile_target)
+        opt.persist_steps = int(bool(persist_steps))
         self.precision = precision
         h = ctypes.c_void_p()
         nps = n_per_sys.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
@@ -365,7 +367,7 @@ class BoxBatch:
         kinds = {v: k for k, v in PASS.items()}
         return {"precision": o.precision, "block": o.block, "contact_model": o.contact_model,
                 "pass_kind": kinds.get(o.pass_kind, o.pass_kind), "tile_target": o.tile_target,
-                "cg_max_probes": o.cg_max_probes}
+                "cg_max_probes": o.cg_max_probes, "persist_steps": bool(o.persist_steps)}
 
     def find_jam(self, e_jam: float, step: float = 1e-3, min_step: float = 1e-12,
                  ftol: float = 1e-13, max_iter: int = 200000, max_steps: int = 10000):

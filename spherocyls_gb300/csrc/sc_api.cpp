@@ -97,8 +97,9 @@ int sc_create_rect(const sc_options* opt_in, int n_sys, const int* n_per_sys, co
     return SC_E_ARG;
   }
   if (opt.pass_kind < SC_PASS_AUTO || opt.pass_kind > SC_PASS_TILE || opt.tile_target < 0 ||
-      opt.tile_target > 65536 || opt.cg_max_probes < 0) {
-    g_create_error = "sc_create: pass_kind, tile_target or cg_max_probes out of range";
+      opt.tile_target > 65536 || opt.cg_max_probes < 0 || opt.persist_steps < 0 ||
+      opt.persist_steps > 1) {
+    g_create_error = "sc_create: pass_kind, tile_target, cg_max_probes or persist_steps out of range";
     return SC_E_ARG;
   }
   long long ntot_ll = 0;
@@ -231,6 +232,10 @@ int sc_create_rect(const sc_options* opt_in, int n_sys, const int* n_per_sys, co
          h.dalloc(&d.cellp, N, "cellp") && h.dalloc(&d.gbuild, n_sys, "gbuild") &&
          h.dalloc(&d.ord, N, "ord") && h.dalloc(&d.nbr_p, N * d.maxn, "nbr_p") &&
          h.dalloc(&d.nbr_pn, N, "nbr_pn");
+  if (opt.precision == SC_PREC_MIXED) {
+    ok = ok && h.dalloc(&d.gbar, 2, "grid barrier") && h.dalloc(&h.d_persist, 1, "persist out");
+    if (ok) ok = h.cuda_ok(cudaMemsetAsync(d.gbar, 0, 2 * sizeof(unsigned), h.stream), "barrier");
+  }
   if (d.pass_kind == 1)
     ok = ok && h.dalloc(&d.t_own, N * sc::kTileEPP, "tile owners") &&
          h.dalloc(&d.t_pe, N * sc::kTileEPP, "tile partners") &&
@@ -425,15 +430,17 @@ int sc_autotune(sc_handle* H, int steps, double* pad_factor, int* block) {
   // tile pass at three tile sizes)
   struct Cand {
     double f;
-    int kind, block, target;
+    int kind, block, target, persist;
   };
   std::vector<Cand> cands;
   for (double f : {0.5, 1.0, 1.5, 2.0, 3.0}) {
-    for (int b : {64, 128}) cands.push_back({f, SC_PASS_LIST, b, 0});
+    for (int b : {64, 128}) cands.push_back({f, SC_PASS_LIST, b, 0, 0});
+    cands.push_back({f, SC_PASS_LIST, 128, 0, 1});
     if (h.ntot < (int)sc::kTileInt)
-      for (int t : {128, 256, 384}) cands.push_back({f, SC_PASS_TILE, h.block, t});
+      for (int t : {128, 256, 384}) cands.push_back({f, SC_PASS_TILE, h.block, t, 0});
   }
-  Cand best{1.0, h.d.pass_kind == 1 ? SC_PASS_TILE : SC_PASS_LIST, h.block, h.opt.tile_target};
+  Cand best{1.0, h.d.pass_kind == 1 ? SC_PASS_TILE : SC_PASS_LIST, h.block, h.opt.tile_target,
+            h.opt.persist_steps};
   double best_ms = 1e300;
   cudaEvent_t e0, e1;
   if (!h.cuda_ok(cudaEventCreate(&e0), "event") || !h.cuda_ok(cudaEventCreate(&e1), "event"))
@@ -443,6 +450,7 @@ int sc_autotune(sc_handle* H, int steps, double* pad_factor, int* block) {
     o.block = c.block;
     o.pass_kind = c.kind;
     o.tile_target = c.target;
+    o.persist_steps = c.persist;
     o.profile = 0;
     for (int s = 0; s < ns; s++) pads[s] = c.f * pad0[s];
     sc_handle* T = nullptr;
@@ -502,6 +510,7 @@ int sc_autotune(sc_handle* H, int steps, double* pad_factor, int* block) {
   }
   h.block = best.block;
   h.opt.block = best.block;
+  h.opt.persist_steps = best.persist;
   h.invalidate_graph();
   if (pad_factor) *pad_factor = best.f;
   if (block) *block = best.block;

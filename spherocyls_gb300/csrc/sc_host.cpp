@@ -332,6 +332,10 @@ bool Handle::check_status(const char* where) {
     fail(SC_E_OVERFLOW, "%s: cell sort lost particles", where);
     return false;
   }
+  if (st & ST_BARRIER_TIMEOUT) {
+    fail(SC_E_TIMEOUT, "%s: a grid barrier of the persistent step kernel timed out", where);
+    return false;
+  }
   return true;
 }
 
@@ -853,8 +857,12 @@ int Handle::run_steps(int kind, int shrink, int nsteps, int se_every, double* se
       pred_kind = pkind;
     }
     bool aligned = se_every == 0 || done % se_every == 0;
-    bool use_graph = opt.use_graphs && !opt.profile && nk >= 16 && aligned;
-    if (use_graph) {
+    const bool use_persist = opt.persist_steps && prec == PREC_MIXED && d.pass_kind == 0 &&
+                             kind == KIND_STRAIN && !opt.profile && d_persist;
+    bool use_graph = !use_persist && opt.use_graphs && !opt.profile && nk >= 16 && aligned;
+    if (use_persist) {
+      if (!run_persist(nk, done, se_every)) return last_status;
+    } else if (use_graph) {
       if (!run_graph(resize, nk, se_every)) return last_status;
     } else {
       int r = 0;
@@ -894,6 +902,51 @@ int Handle::run_steps(int kind, int shrink, int nsteps, int se_every, double* se
   if (se_out && nrec_total > 0)
     std::memcpy(se_out, se_host.data(), se_host.size() * sizeof(double));
   return SC_OK;
+}
+
+// Steps 1..nk of the uploaded table with the persistent step kernel: runs of steps
+// without a stress record go to one cooperative launch, which returns at the first
+// step whose corrector asks for a rebuild; that step's rebuild and predictor are
+// launched here, and the next run starts after it.  Recording steps take the
+// regular launches.  One host synchronisation per launch (to read where it ended).
+bool Handle::run_persist(int nk, int done, int se_every) {
+  int r = 0;
+  for (int k = 1; k <= nk;) {
+    int kp = nk;  // last step of the run without a record
+    if (se_every > 0) {
+      const int next = ((done + k + se_every - 1) / se_every) * se_every - done;
+      kp = std::min(nk, next - 1);
+    }
+    if (kp >= k) {
+      if (!launch_persist_steps(d, d_tab, k, kp - k + 1, d_persist, stream)) {
+        cudaGetLastError();
+        fail(SC_E_CUDA, "persistent step kernel: cooperative launch failed");
+        return false;
+      }
+      kernels += 1;
+      if (!cuda_ok(cudaMemcpyAsync(h_pinned + 3, d_persist, sizeof(int), cudaMemcpyDeviceToHost,
+                                   stream), "persist result") ||
+          !cuda_ok(cudaStreamSynchronize(stream), "persist result"))
+        return false;
+      const int v = h_pinned[3];
+      const int m = v >> 1;
+      if (m < 0 || m > kp - k + 1 || (m == kp - k + 1 && (v & 1))) {
+        fail(SC_E_STATE, "persistent step kernel returned %d", v);
+        return false;
+      }
+      k += m;
+      if (v & 1) {  // step k's corrector ran; its rebuild and predictor follow
+        kernels += enqueue_rebuild_body(false, k, false, stream);
+        enqueue_pred(false, k, false, false);
+        k++;
+      }
+      continue;
+    }
+    enqueue_step(false, k, true, false);  // a recording step
+    enqueue_se_record(r++);
+    k++;
+  }
+  return true;
 }
 
 int Handle::calc(bool se, double* se_out) {
@@ -1020,7 +1073,9 @@ bool Handle::run_fire_graph(int iters, double ftol, double dt_max) {
     const bool mixed = prec == PREC_MIXED;
     cudaError_t e = cudaSuccess;
     for (int k = 0; k < iters && e == cudaSuccess; k++) {
+      pass_skip = fire.done;  // converged systems: no force pass
       launch_pass(PASS_FORCE, false, 0, true);
+      pass_skip = nullptr;
       launch_fire_iteration_tail(d, fire, ftol, dt_max, mixed, stream);
       e = capture_rebuild_node(0, [&](cudaStream_t st) {
         if (mixed) launch_mx_materialize(d, d_tab, 0, false, st);

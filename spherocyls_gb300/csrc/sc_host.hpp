@@ -70,6 +70,7 @@ struct Handle {
   std::vector<void*> allocs;
   int cell_cap = 0, chunk_cap = 0, tile_cap = 0;
   const int* pass_skip = nullptr;  // Dev::skip of the force passes being enqueued
+  int* d_persist = nullptr;        // result word of the persistent step kernel
   StepScalars* d_tab = nullptr;
   int tab_cap = 0;
   std::vector<StepScalars> h_tab;
@@ -180,6 +181,7 @@ struct Handle {
   void enqueue_se_record(int rec);
   void invalidate_graph();
   bool run_graph(bool resize, int nsteps, int se_every);
+  bool run_persist(int nk, int done, int se_every);
 
   int run_steps(int kind, int shrink, int nsteps, int se_every, double* se_out);
   int calc(bool se, double* se_out);

@@ -197,6 +197,7 @@ struct Dev {
   // compute entries (owner-major) and read entries live in the slot range of its
   // particles times kTileEPP; a pair inside the tile is computed by its lower slot
   // and read back by the other partner from the pair results.
+  unsigned* gbar;           // [2] grid barrier of the persistent step kernel (count, generation)
   const int* skip;          // [nsys] or null: force passes leave systems with skip[s] != 0
                             // alone (converged minimiser systems)
   int pass_kind;            // 0: one thread per particle over its full list, 1: tiles
@@ -252,7 +253,10 @@ struct Dev {
 };
 
 // sticky device status bits
-enum { ST_NBR_OVERFLOW = 1, ST_NAN = 2, ST_CELL_OVERFLOW = 4 };
+enum { ST_NBR_OVERFLOW = 1, ST_NAN = 2, ST_CELL_OVERFLOW = 4, ST_BARRIER_TIMEOUT = 8 };
+// spins (of about 64 ns each) a block waits at a grid barrier of the persistent
+// step kernel before it gives up, records ST_BARRIER_TIMEOUT and goes on
+constexpr unsigned kBarrierSpins = 1u << 24;
 
 constexpr int kScanChunk = 1024;  // cells per scan chunk
 constexpr int kSeChunk = 1024;    // particles per reduction chunk
@@ -331,6 +335,13 @@ void launch_mx_materialize(const Dev& d, const StepScalars* tab, int row, bool a
 void launch_mx_local(const Dev& d, const StepScalars* tab, int row, bool all, cudaStream_t st);
 void launch_mx_order(const Dev& d, bool all, cudaStream_t st);
 void launch_mx_build_list(const Dev& d, const StepScalars* tab, int row, bool all,
+                          cudaStream_t st);
+// Persistent mixed shear steps (per-particle pass): rows row0 .. row0 + nsteps - 1 of
+// the table in one cooperative launch, corrector and predictor passes separated by
+// grid barriers, until a step's corrector asks for a rebuild (or a set-back).
+// *out = 2 m + stopped: m steps completed, stopped = the corrector of step m + 1 ran
+// and its rebuild is pending.  Returns false when the cooperative launch failed.
+bool launch_persist_steps(const Dev& d, const StepScalars* tab, int row0, int nsteps, int* out,
                           cudaStream_t st);
 // tile lists from the mixed lists (after launch_mx_build_list)
 void launch_tile_lists(const Dev& d, bool all, cudaStream_t st);

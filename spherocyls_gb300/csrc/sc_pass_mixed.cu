@@ -175,14 +175,13 @@ __device__ __forceinline__ void mixed_epilogue(const Dev& d, const StepScalars& 
   }
 }
 
+// The force pass of one list position (the per-particle pass): the particle's
+// pairs from its own side over its full list, then the Heun epilogue.
 template <int MODE, bool TWO>
-__global__ void __launch_bounds__(128, TWO ? 6 : 12) k_pass_mixed(Dev d,
-                                                       const StepScalars* __restrict__ tab,
-                                                       int row) {
+__device__ __forceinline__ void pass_mixed_position(const Dev& d,
+                                                    const StepScalars* __restrict__ tab,
+                                                    int row, int pos) {
   constexpr bool kPred = (MODE == PASS_CORR_STRAIN || MODE == PASS_CORR_RESIZE);
-  if (kPred) mark_pending_rebuilds(d, tab, row);
-  const int pos = blockIdx.x * blockDim.x + threadIdx.x;
-  if (pos >= d.ntot) return;
   const int i = d.ord[pos];  // the slot this thread works on (lists ordered by length)
   const int s = d.psys[i];
   if (d.skip && d.skip[s]) return;  // a converged minimiser system
@@ -250,6 +249,83 @@ __global__ void __launch_bounds__(128, TWO ? 6 : 12) k_pass_mixed(Dev d,
   }
 
   mixed_epilogue<MODE>(d, ts, g, s, i, ri, pai, gam, fx, fy, tq);
+}
+
+template <int MODE, bool TWO>
+__global__ void __launch_bounds__(128, TWO ? 6 : 12) k_pass_mixed(Dev d,
+                                                       const StepScalars* __restrict__ tab,
+                                                       int row) {
+  constexpr bool kPred = (MODE == PASS_CORR_STRAIN || MODE == PASS_CORR_RESIZE);
+  if (kPred) mark_pending_rebuilds(d, tab, row);
+  const int pos = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pos >= d.ntot) return;
+  pass_mixed_position<MODE, TWO>(d, tab, row, pos);
+}
+
+// ---- persistent shear steps ----
+//
+// For small and medium systems a step's two passes are short next to their launch
+// and the gaps between launches.  One cooperative launch (every block resident, so a
+// grid barrier cannot wait for a block that never runs) advances several steps:
+// the corrector pass over all positions, a grid barrier, the predictor pass, a grid
+// barrier.  A step whose corrector requests a rebuild (or whose row sets gamma back)
+// ends the launch after that corrector; the host runs the rebuild and the predictor
+// and relaunches.  Every wait is bounded (kBarrierSpins): a barrier that times out
+// records ST_BARRIER_TIMEOUT, which the host reports as an error.
+
+// generation barrier over all blocks of the grid (thread 0 of each block arrives)
+__device__ __forceinline__ void grid_barrier(unsigned* bar, int* status) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned* vgen = bar + 1;
+    const unsigned gen = *vgen;
+    __threadfence();
+    if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      unsigned it = 0;
+      while (*vgen == gen) {
+        if (++it > kBarrierSpins) {
+          atomicOr(status, ST_BARRIER_TIMEOUT);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+}
+
+template <bool TWO>
+__global__ void __launch_bounds__(128, TWO ? 6 : 12) k_persist_steps(
+    Dev d, const StepScalars* __restrict__ tab, int row0, int nsteps, int* out) {
+  const int stride = gridDim.x * blockDim.x;
+  const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+  int k = 0, stopped = 0;
+  for (; k < nsteps; k++) {
+    const int row = row0 + k;
+    // systems that set gamma back at this step rebuild after its corrector
+    if (blockIdx.x == 0)
+      for (int s = threadIdx.x; s < d.nsys; s += blockDim.x)
+        if (tab[row * d.nsys + s].setback) {
+          atomicOr(&d.flags[s], 2);
+          atomicExch(d.any, 1);
+        }
+    for (int pos = t0; pos < d.ntot; pos += stride)
+      pass_mixed_position<PASS_CORR_STRAIN, TWO>(d, tab, row, pos);
+    grid_barrier(d.gbar, d.status);
+    if (*(volatile int*)d.any != 0) {  // the same value in every block after the barrier
+      stopped = 1;
+      break;
+    }
+    for (int pos = t0; pos < d.ntot; pos += stride)
+      pass_mixed_position<PASS_PRED_STRAIN, TWO>(d, tab, row, pos);
+    grid_barrier(d.gbar, d.status);
+  }
+  if (t0 == 0) *out = 2 * k + stopped;
 }
 
 template <int MODE>
@@ -633,6 +709,26 @@ void launch_pass_mixed(const Dev& d, int mode, bool se, const StepScalars* tab, 
   }
   // stress and energy of the state (forces and predictor passes) in FP64
   if (se) launch_mx_se64(d, tab, row, st);
+}
+
+bool launch_persist_steps(const Dev& d, const StepScalars* tab, int row0, int nsteps, int* out,
+                          cudaStream_t st) {
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return false;
+  const void* fn = d.contact_model == 1 ? (const void*)k_persist_steps<true>
+                                        : (const void*)k_persist_steps<false>;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 128, 0) != cudaSuccess ||
+      per_sm < 1)
+    return false;
+  int grid = sms * per_sm;
+  const int need = (d.ntot + 127) / 128;
+  if (need < grid) grid = need;
+  Dev dd = d;
+  dd.cond = 0;  // no graph node to switch: the launch ends at a pending rebuild
+  void* args[] = {&dd, (void*)&tab, &row0, &nsteps, &out};
+  return cudaLaunchCooperativeKernel(fn, grid, 128, args, 0, st) == cudaSuccess;
 }
 
 void launch_tile_lists(const Dev& d, bool all, cudaStream_t st) {
