@@ -389,14 +389,15 @@ def batched_leg(args, device, torch):
 
 
 def minimise_leg(replicas=128, n=4096, max_iter=150000, ftol=1e-14, device=0, e_jam=1e-12,
-                 dt_max=0.2, cg_iter=2000):
+                 dt_max=0.2, cg_iter=2000, over=2e-3):
     """Minimisation time to tolerance on the jamming workload's shape: replicas of
     N = 4096 with a/R in {0.25, 0.5, 1, 2} (a quarter each), seeds 100 + k, from
     packing 0.70.  Untimed preparation: the mixed form compresses every replica to
     jamming in affine steps of 2e-3 in packing fraction (FIRE to 1e-6 after each,
-    jammed once E/N > 1e-12; a replica whose FP64 minimum has E/N <= 1e-16 was not
-    jammed and is left out of the energy comparison), and each replica is then
-    compressed by one more 1e-4 increment.  From that same state the two timed arms
+    jammed once E/N > 1e-12 at that tolerance), and each replica is then compressed
+    by `over` in packing fraction past that point, so that its FP64 minimum is jammed
+    (E/N > 1e-16; a replica that is not is left out of the energy comparison).  From
+    that same state the two timed arms
     minimise to max|F_i|, |tau_i|/sqrt(I_i) < ftol: (a) mixed FIRE to 1e-6, then
     FP64 FIRE; (b) FP64 FIRE alone; (c) the reference's conjugate gradient (FP64) on
     one replica of each aspect ratio, stopped by the reference's rules or after
@@ -420,7 +421,7 @@ def minimise_leg(replicas=128, n=4096, max_iter=150000, ftol=1e-14, device=0, e_
     Lj = np.array([prep.box(s)["Lx"] for s in range(replicas)])
     xs, ys, ps = prep.state()
     prep.close()
-    f = np.sqrt(phi_j / (phi_j + 1e-4))
+    f = np.sqrt(phi_j / (phi_j + over))
     fp = np.repeat(f, n)
     L1, x1, y1 = Lj * f, xs * fp, ys * fp
 
@@ -461,7 +462,7 @@ def minimise_leg(replicas=128, n=4096, max_iter=150000, ftol=1e-14, device=0, e_
     both = da & db & dc & jammed
     return {
         "workload": f"jam_{replicas}x{n}", "replicas": replicas, "N": n, "ftol": ftol,
-        "prep": {"seconds": t_prep, "increments": n_inc,
+        "prep": {"seconds": t_prep, "increments": n_inc, "over_compression": over,
                  "phi_jam_range": [float(phi_j.min()), float(phi_j.max())]},
         "mixed_then_fp64": {"seconds": ta + tb, "mixed_seconds": ta, "mixed_iters": ia,
                             "fp64_iters": ib, "converged": int((da & db).sum()),

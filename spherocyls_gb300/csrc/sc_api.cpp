@@ -511,6 +511,8 @@ int sc_autotune(sc_handle* H, int steps, double* pad_factor, int* block) {
   h.block = best.block;
   h.opt.block = best.block;
   h.opt.persist_steps = best.persist;
+  h.opt.pass_kind = best.kind;
+  if (kind == 1) h.opt.tile_target = best.target;
   h.invalidate_graph();
   if (pad_factor) *pad_factor = best.f;
   if (block) *block = best.block;

@@ -195,19 +195,24 @@ __global__ void k_rb_chunksum(Dev d) {
   if (threadIdx.x == 0) d.chunk_sum[ch] = v;
 }
 
-// One thread per system: exclusive scan of its chunk sums (a system owns at most a
-// few hundred chunks).
-__global__ void k_rb_sysscan(Dev d) {
+// One block per system: exclusive scan of its chunk sums (a large system owns a few
+// hundred chunks).
+__global__ void __launch_bounds__(256) k_rb_sysscan(Dev d) {
   if (*d.any == 0) return;
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= d.nsys || d.flags[s] == 0) return;
+  const int s = blockIdx.x;
+  if (d.flags[s] == 0) return;
+  __shared__ int sh[32];
   const SysGeom& g = d.geom[s];
-  int off = 0;
-  for (int k = 0; k < g.nchunks; k++) {
-    d.chunk_off[g.chunk0 + k] = off;
-    off += d.chunk_sum[g.chunk0 + k];
+  int off = 0;  // running total (the same in every thread)
+  for (int k0 = 0; k0 < g.nchunks; k0 += blockDim.x) {
+    const int k = k0 + threadIdx.x;
+    const int v = k < g.nchunks ? d.chunk_sum[g.chunk0 + k] : 0;
+    int tot;
+    const int ex = block_excl_scan(v, sh, &tot);
+    if (k < g.nchunks) d.chunk_off[g.chunk0 + k] = off + ex;
+    off += tot;
   }
-  if (off != g.n) atomicOr(d.status, ST_CELL_OVERFLOW);
+  if (threadIdx.x == 0 && off != g.n) atomicOr(d.status, ST_CELL_OVERFLOW);
 }
 
 // One 1024-thread block per chunk: exclusive scan of cell counts.
@@ -561,7 +566,7 @@ void launch_rebuild(const Dev& d, bool mixed, const StepScalars* tab, int row, c
   k_rb_zero<<<kWalkBlocks, B, 0, st>>>(d);
   k_rb_hash<<<kWalkBlocks, B, 0, st>>>(d, tab, row, mixed ? 1 : 0);
   k_rb_chunksum<<<d.nchunks, 256, 0, st>>>(d);
-  k_rb_sysscan<<<nblk(d.nsys, 128), 128, 0, st>>>(d);
+  k_rb_sysscan<<<d.nsys, 256, 0, st>>>(d);
   k_rb_cellscan<<<d.nchunks, 1024, 0, st>>>(d);
   k_rb_scatter<<<kWalkBlocks, B, 0, st>>>(d);
   k_rb_cellsort<<<2 * kWalkBlocks, 128, 0, st>>>(d);
