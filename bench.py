@@ -388,16 +388,17 @@ def batched_leg(args, device, torch):
             "roofline_frac": achieved / peak, "achieved_gbs": achieved}
 
 
-def minimise_leg(replicas=128, n=4096, max_iter=150000, ftol=1e-14, device=0, e_jam=1e-12,
-                 dt_max=0.2, cg_iter=2000, over=2e-3):
+def minimise_leg(replicas=128, n=4096, max_iter=150000, ftol=1e-14, device=0, e_jam=1e-8,
+                 dt_max=0.2, cg_iter=2000, over=1e-4, graphs=True):
     """Minimisation time to tolerance on the jamming workload's shape: replicas of
     N = 4096 with a/R in {0.25, 0.5, 1, 2} (a quarter each), seeds 100 + k, from
-    packing 0.70.  Untimed preparation: the mixed form compresses every replica to
-    jamming in affine steps of 2e-3 in packing fraction (FIRE to 1e-6 after each,
-    jammed once E/N > 1e-12 at that tolerance), and each replica is then compressed
-    by `over` in packing fraction past that point, so that its FP64 minimum is jammed
-    (E/N > 1e-16; a replica that is not is left out of the energy comparison).  From
-    that same state the two timed arms
+    packing 0.70.  Untimed preparation: the mixed form compresses every replica in
+    affine steps of 2e-3 in packing fraction (FIRE to 1e-6 after each) until E/N >
+    e_jam: 1e-8, well above what the residual forces of that tolerance leave (about
+    1e-12), so the replica is jammed; each replica is then compressed by one more
+    increment `over` (the 1e-4 increment of the jamming protocol) and its FP64
+    minimum must have E/N > 1e-16 (a replica that does not is left out of the energy
+    comparison).  From that same state the two timed arms
     minimise to max|F_i|, |tau_i|/sqrt(I_i) < ftol: (a) mixed FIRE to 1e-6, then
     FP64 FIRE; (b) FP64 FIRE alone; (c) the reference's conjugate gradient (FP64) on
     one replica of each aspect ratio, stopped by the reference's rules or after
@@ -411,7 +412,7 @@ def minimise_leg(replicas=128, n=4096, max_iter=150000, ftol=1e-14, device=0, e_
     cat = lambda i: np.concatenate([pk[i] for pk in packs])  # noqa: E731
     L0 = np.array([pk[0] for pk in packs])
     R, A = cat(4), cat(5)
-    kw = dict(contacts=2, device=device)
+    kw = dict(contacts=2, device=device, use_graphs=graphs)
     prep = BoxBatch([n] * replicas, L0, cat(1), cat(2), cat(3), A, R, 0.1, precision="mixed",
                     **kw)
     t0 = time.perf_counter()
@@ -497,8 +498,11 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=2,
                     help="Heun steps of the CPU baseline sample in the GPU arm's line")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--only", choices=["mixed", "fp64"], default=None,
-                    help="time one form only (for profiler captures)")
+    ap.add_argument("--only", choices=["mixed", "fp64", "minimise"], default=None,
+                    help="time one form only, or run the minimisation leg alone "
+                         "(for profiler captures)")
+    ap.add_argument("--forced-rebuilds", type=int, default=0,
+                    help="with --only mixed|fp64: full rebuilds after the timed steps")
     ap.add_argument("--steady-steps", type=int, default=300,
                     help="shear steps before the steady-state window")
     ap.add_argument("--autotune", action=argparse.BooleanOptionalAction, default=True,
@@ -579,18 +583,32 @@ def main():
         # block size (it times copies; the copies' steps are not timed here)
         t = new_box("mixed")
         t.strain_steps(args.warmup)
-        f, blk = t.autotune(100)  # long enough to include rebuilds
+        # timed on a window as long as the measured one (candidates run as many
+        # steps again first); the copies' steps are not timed here
+        f, blk = t.autotune(max(args.steps, 20))
         o = t.options()
         t.close()
         tuned = {"pad": PAD * f, "block": blk, "pass_kind": o["pass_kind"],
                  "tile_target": o["tile_target"], "persist_steps": o["persist_steps"]}
 
+    if args.only == "minimise":
+        # the minimisation leg alone (profiler captures: --no-graphs launches eagerly)
+        print(json.dumps(minimise_leg(args.min_replicas, 4096, args.min_iters, device=local,
+                                      graphs=not args.no_graphs)))
+        return
     if args.only:
         b = new_box(args.only)
         b.strain_steps(args.warmup)
         c0 = b.counters()
         secs = time_steps(b, args.steps, torch)
         c1 = b.counters()
+        # forced full rebuilds of the sorted state in an NVTX range (profiler captures
+        # of the rebuild chain select it with --nvtx-include forced_rebuild/)
+        torch.cuda.nvtx.range_push("forced_rebuild")
+        for _ in range(args.forced_rebuilds):
+            b.find_neighbors()
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
         if rank == 0:
             print(json.dumps({"only": args.only, "workload": args.workload, "steps": args.steps,
                               "ms_per_step": 1e3 * secs / args.steps,

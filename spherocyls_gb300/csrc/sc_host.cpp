@@ -636,35 +636,40 @@ bool Handle::run_graph(bool resize, int nsteps, int se_every) {
 
 // The chunk (rows 1..nsteps of the table, records of steps that are multiples of
 // se_every) as nsteps / kGraphSteps launches of sub-chunk graphs.
-bool Handle::run_subgraphs(bool resize, int nsteps, int se_every) {
+// The sub-chunk graph of kGraphSteps steps of this kind with the records of `mask`,
+// captured on first use against the step and record windows.
+Handle::SubGraph* Handle::subgraph(bool resize, unsigned mask) {
   const int G = kGraphSteps;
   if (!d_win && (!dalloc(&d_win, (size_t)(G + 1) * nsys, "step window") ||
                  !dalloc(&d_win_se, (size_t)G * nsys * 5, "record window")))
-    return false;
+    return nullptr;
+  for (auto& c : sub_graphs)
+    if (c.resize == resize && c.se_mask == mask && c.prec == prec) return &c;
+  // capture against the windows: swap them in for the table and record buffer
+  std::vector<char> se(G + 1, 0);
+  for (int k = 1; k <= G; k++) se[k] = (mask >> (k - 1)) & 1u;
+  StepScalars* tab_keep = d_tab;
+  double* rec_keep = d_se_hist;
+  d_tab = d_win;
+  d_se_hist = d_win_se;
+  SubGraph c{resize, mask, prec, nullptr, 0};
+  bool ok = instantiate_steps(resize, G, se, &c.exec, &c.kernels);
+  d_tab = tab_keep;
+  d_se_hist = rec_keep;
+  if (!ok) return nullptr;
+  sub_graphs.push_back(c);
+  return &sub_graphs.back();
+}
+
+bool Handle::run_subgraphs(bool resize, int nsteps, int se_every) {
+  const int G = kGraphSteps;
   int rec = 0;
   for (int j = 0; j < nsteps / G; j++) {
     unsigned mask = 0;
     for (int k = 1; k <= G; k++)
       if (se_every > 0 && (j * G + k) % se_every == 0) mask |= 1u << (k - 1);
-    SubGraph* sg = nullptr;
-    for (auto& c : sub_graphs)
-      if (c.resize == resize && c.se_mask == mask && c.prec == prec) sg = &c;
-    if (!sg) {
-      // capture against the windows: swap them in for the table and record buffer
-      std::vector<char> se(G + 1, 0);
-      for (int k = 1; k <= G; k++) se[k] = (mask >> (k - 1)) & 1u;
-      StepScalars* tab_keep = d_tab;
-      double* rec_keep = d_se_hist;
-      d_tab = d_win;
-      d_se_hist = d_win_se;
-      SubGraph c{resize, mask, prec, nullptr, 0};
-      bool ok = instantiate_steps(resize, G, se, &c.exec, &c.kernels);
-      d_tab = tab_keep;
-      d_se_hist = rec_keep;
-      if (!ok) return false;
-      sub_graphs.push_back(c);
-      sg = &sub_graphs.back();
-    }
+    SubGraph* sg = subgraph(resize, mask);
+    if (!sg) return false;
     const int nrec = __builtin_popcount(mask);
     if (!cuda_ok(cudaMemcpyAsync(d_win, d_tab + (size_t)j * G * nsys,
                                  (size_t)(G + 1) * nsys * sizeof(StepScalars),
@@ -784,6 +789,13 @@ int Handle::run_steps(int kind, int shrink, int nsteps, int se_every, double* se
       }
   }
   cudaSetDevice(device);
+  // The first step call of a kind captures the plain sub-chunk graph of that kind,
+  // whatever its length, so that later calls (a long run after a short warm-up) do
+  // not pay the capture.
+  if (opt.use_graphs && !opt.profile && use_conditional &&
+      !(opt.persist_steps && prec == PREC_MIXED && d.pass_kind == 0 && kind == KIND_STRAIN) &&
+      !subgraph(kind != KIND_STRAIN, 0u))
+    cudaGetLastError();  // capture failed: the chunks fall back to eager launches
   int nrec_total = (se_every > 0) ? nsteps / se_every : 0;
   std::vector<double> se_host((size_t)nrec_total * nsys * 5);
   int done = 0, rec_done = 0;

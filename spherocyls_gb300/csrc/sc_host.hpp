@@ -181,6 +181,7 @@ struct Handle {
   void enqueue_se_record(int rec);
   void invalidate_graph();
   bool run_graph(bool resize, int nsteps, int se_every);
+  SubGraph* subgraph(bool resize, unsigned mask);
   bool run_persist(int nk, int done, int se_every);
 
   int run_steps(int kind, int shrink, int nsteps, int se_every, double* se_out);
