@@ -98,9 +98,10 @@ def bytes_per_pass(precision: str, nbar: float) -> float:
 
 
 # DRAM bytes (read + write) per particle of one mixed force pass, the mean of the
-# predictor and corrector launches in one ncu capture of the default workload
-# (profiles/k_pass_mixed_n1048576.md, the autotuned padding).
-PASS_DRAM_BYTES_PER_PARTICLE = {"shear_n1048576_phi084": 138.17e6 / (1 << 20)}
+# predictor (113.6 MB) and corrector (172.4 MB) launches in one ncu capture of the
+# default workload at the padding the autotuner picks for it, 0.6
+# (profiles/k_pass_mixed_n1048576.md).
+PASS_DRAM_BYTES_PER_PARTICLE = {"shear_n1048576_phi084": 143.0e6 / (1 << 20)}
 
 
 def _peaks():

@@ -289,16 +289,33 @@ bool Handle::layout_cells() {
   return cuda_ok(cudaStreamSynchronize(stream), "layout sync");
 }
 
+// The step table holds at least a full chunk from its first allocation, so that a
+// run of short calls (a warm-up) followed by long ones does not re-allocate it.  Its
+// address is captured by the whole-chunk, FIRE and CG graphs, which are dropped when
+// it moves; the sub-chunk graphs read their rows from the step window instead and
+// stay valid.
 bool Handle::ensure_table(int rows) {
   if (rows * nsys <= tab_cap) return true;
   dfree(d_tab);
-  int cap = std::max(rows * nsys, 2 * tab_cap);
+  int cap = std::max(std::max(rows, kChunk + 1) * nsys, 2 * tab_cap);
   StepScalars* t = nullptr;
   if (!dalloc(&t, cap, "step table")) return false;
   d_tab = t;
   tab_cap = cap;
-  invalidate_graph();
+  invalidate_table_graphs();
   return true;
+}
+
+void Handle::invalidate_table_graphs() {
+  if (graph_exec) cudaGraphExecDestroy(graph_exec);
+  graph_exec = nullptr;
+  graph_key = GraphKey{};
+  if (cg_exec) cudaGraphExecDestroy(cg_exec);
+  cg_exec = nullptr;
+  cg_key_iter = -1;
+  if (fire_exec) cudaGraphExecDestroy(fire_exec);
+  fire_exec = nullptr;
+  fire_key_iters = 0;
 }
 
 bool Handle::upload_table(const std::vector<StepScalars>& rows) {
@@ -603,9 +620,13 @@ bool Handle::instantiate_steps(bool resize, int nsteps, const std::vector<char>&
     body_kernels = 0;
     if (!cuda_ok(cudaStreamEndCapture(stream, &g), "end capture")) return false;
   }
+  *exec = nullptr;
   cudaError_t e = cudaGraphInstantiate(exec, g, 0);
   cudaGraphDestroy(g);
+  // upload now, so that the first launch does not carry the upload
+  if (e == cudaSuccess) e = cudaGraphUpload(*exec, stream);
   if (!cuda_ok(e, "graph instantiate")) {
+    if (*exec) cudaGraphExecDestroy(*exec);
     *exec = nullptr;
     return false;
   }
@@ -698,7 +719,7 @@ bool Handle::ensure_se_hist(int nrec) {
   if (!dalloc(&p, cap, "se history")) return false;
   d_se_hist = p;
   se_hist_cap = cap;
-  invalidate_graph();
+  invalidate_table_graphs();  // the sub-chunk graphs record into their own window
   return true;
 }
 

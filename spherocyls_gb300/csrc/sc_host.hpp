@@ -182,6 +182,7 @@ struct Handle {
   void invalidate_graph();
   bool run_graph(bool resize, int nsteps, int se_every);
   SubGraph* subgraph(bool resize, unsigned mask);
+  void invalidate_table_graphs();
   bool run_persist(int nk, int done, int se_every);
 
   int run_steps(int kind, int shrink, int nsteps, int se_every, double* se_out);
