@@ -389,17 +389,17 @@ def batched_leg(args, device, torch):
             "roofline_frac": achieved / peak, "achieved_gbs": achieved}
 
 
-def minimise_leg(replicas=128, n=4096, max_iter=150000, ftol=1e-14, device=0, e_jam=1e-8,
-                 dt_max=0.2, cg_iter=2000, over=1e-4, graphs=True):
+def minimise_leg(replicas=128, n=4096, max_iter=40000, ftol=1e-14, device=0, e_jam=1e-12,
+                 dt_max=0.2, cg_iter=2000, over=4e-3, graphs=True, mixed_iter=50000):
     """Minimisation time to tolerance on the jamming workload's shape: replicas of
     N = 4096 with a/R in {0.25, 0.5, 1, 2} (a quarter each), seeds 100 + k, from
     packing 0.70.  Untimed preparation: the mixed form compresses every replica in
     affine steps of 2e-3 in packing fraction (FIRE to 1e-6 after each) until E/N >
-    e_jam: 1e-8, well above what the residual forces of that tolerance leave (about
-    1e-12), so the replica is jammed; each replica is then compressed by one more
-    increment `over` (the 1e-4 increment of the jamming protocol) and its FP64
-    minimum must have E/N > 1e-16 (a replica that does not is left out of the energy
-    comparison).  From that same state the two timed arms
+    e_jam = 1e-12 at that tolerance (close to, and mostly below, the jamming point:
+    the residual forces of that tolerance leave about that energy); each replica is
+    then compressed by `over` past that point.  A replica whose FP64 minimum has
+    E/N <= 1e-16 is below jamming at that packing; the energy comparison covers the
+    jammed ones (E/N > 1e-16) that both arms brought below ftol.  From that same state the two timed arms
     minimise to max|F_i|, |tau_i|/sqrt(I_i) < ftol: (a) mixed FIRE to 1e-6, then
     FP64 FIRE; (b) FP64 FIRE alone; (c) the reference's conjugate gradient (FP64) on
     one replica of each aspect ratio, stopped by the reference's rules or after
@@ -433,7 +433,7 @@ def minimise_leg(replicas=128, n=4096, max_iter=150000, ftol=1e-14, device=0, e_
         return time.perf_counter() - t, it, fmax, done
 
     m = BoxBatch([n] * replicas, L1, x1, y1, ps, A, R, 0.1, precision="mixed", **kw)
-    ta, ia, _, da = run(m, 1e-6, 200000)
+    ta, ia, _, da = run(m, 1e-6, mixed_iter)
     xm, ym, pm = m.state()
     m.close()
     r = BoxBatch([n] * replicas, L1, xm, ym, pm, A, R, 0.1, precision="fp64", **kw)
@@ -481,6 +481,9 @@ def minimise_leg(replicas=128, n=4096, max_iter=150000, ftol=1e-14, device=0, e_
         "speedup": tc / (ta + tb),
         "energy_rel_diff_max": (float(np.max(np.abs(e_a[both] - e_c[both]) / e_c[both]))
                                 if both.any() else None),
+        "energy_per_particle_abs_diff_max_unjammed": (
+            float(np.max(np.abs(e_a - e_c)[da & db & dc & ~jammed]))
+            if (da & db & dc & ~jammed).any() else None),
     }
 
 
@@ -511,8 +514,10 @@ def main():
     ap.add_argument("--legs", default="precision,batched,minimise",
                     help="extra legs of the GPU arm (comma separated, or 'none')")
     ap.add_argument("--min-replicas", type=int, default=128)
-    ap.add_argument("--min-iters", type=int, default=150000,
+    ap.add_argument("--min-iters", type=int, default=40000,
                     help="FP64 FIRE iteration cap of the minimisation leg")
+    ap.add_argument("--min-over", type=float, default=4e-3,
+                    help="compression past the detected jamming point (minimisation leg)")
     ap.add_argument("--pass-kind", choices=["auto", "list", "tile"], default="auto",
                     help="the mixed form's force pass before autotuning (profiler captures)")
     ap.add_argument("--tile-target", type=int, default=0)
@@ -595,7 +600,7 @@ def main():
     if args.only == "minimise":
         # the minimisation leg alone (profiler captures: --no-graphs launches eagerly)
         print(json.dumps(minimise_leg(args.min_replicas, 4096, args.min_iters, device=local,
-                                      graphs=not args.no_graphs)))
+                                      graphs=not args.no_graphs, over=args.min_over)))
         return
     if args.only:
         b = new_box(args.only)
@@ -699,7 +704,8 @@ def main():
     if rank == 0 and "batched" in legs and args.workload != "batch512":
         extra["batched"] = batched_leg(args, local, torch)
     if rank == 0 and "minimise" in legs:
-        extra["minimise"] = minimise_leg(args.min_replicas, 4096, args.min_iters, device=local)
+        extra["minimise"] = minimise_leg(args.min_replicas, 4096, args.min_iters, device=local,
+                                         over=args.min_over)
 
     base = None
     if rank == 0 and not args.no_cpu and w.get("phi") is not None:

@@ -157,8 +157,19 @@ __global__ void k_rb_hash(Dev d, const StepScalars* __restrict__ tab, int row, i
     d.xy[i] = p;
     d.ph[i] = phi;
     d.nxy_t[i] = mv;  // displacement counter to carry into the new slot
-    int col = (int)(p.x / ts.W_p);
-    int rw = (int)(p.y / ts.H_p);
+    // the FP64 form divides as the reference does (find_cells); the mixed form,
+    // whose records are relative to whatever cell it is given, takes the FP32
+    // quotient (two FP64 divisions per particle dominate this kernel on GB300; a
+    // particle a rounding error outside its cell is still well inside the 3x3 block
+    // its list search covers, whose cells are 0.24 (R + A) wider than the reach)
+    int col, rw;
+    if (mixed) {
+      col = (int)__fdividef((float)p.x, ts.f_Wp);
+      rw = (int)__fdividef((float)p.y, ts.f_Hp);
+    } else {
+      col = (int)(p.x / ts.W_p);
+      rw = (int)(p.y / ts.H_p);
+    }
     // a coordinate at (or, after a resize, just past) the box edge stays on the grid
     if (col >= g.cols) col = g.cols - 1;
     if (rw >= g.rows) rw = g.rows - 1;

@@ -45,9 +45,11 @@ struct SysGeom {
 // particles of a tile then occupy one contiguous range of slots, which the tile
 // force pass stages in shared memory.  With one tile (ntx = nty = 1, the FP64
 // form) this is the reference's col + row * cols.
-SC_HDI int tile_lo(int k, int n, int nt) { return (int)(((long long)k * n) / nt); }
+// (n < 65536 cells a side, so the products fit 32 unsigned bits)
+SC_HDI int tile_lo(int k, int n, int nt) { return (int)(((unsigned)k * (unsigned)n) / (unsigned)nt); }
 SC_HDI int tile_of(int c, int n, int nt) {
-  int k = (int)(((long long)c * nt) / n);
+  if (nt == 1) return 0;
+  int k = (int)(((unsigned)c * (unsigned)nt) / (unsigned)n);
   if (k > nt - 1) k = nt - 1;
   while (k + 1 < nt && tile_lo(k + 1, n, nt) <= c) k++;
   while (k > 0 && tile_lo(k, n, nt) > c) k--;
@@ -55,6 +57,7 @@ SC_HDI int tile_of(int c, int n, int nt) {
 }
 // local cell index (add c0 for the global one) of column col, row row
 SC_HDI int cell_local(const SysGeom& g, int col, int row) {
+  if (g.ntx == 1 && g.nty == 1) return row * g.cols + col;
   const int kx = tile_of(col, g.cols, g.ntx), ky = tile_of(row, g.rows, g.nty);
   const int x0 = tile_lo(kx, g.cols, g.ntx), x1 = tile_lo(kx + 1, g.cols, g.ntx);
   const int y0 = tile_lo(ky, g.rows, g.nty), y1 = tile_lo(ky + 1, g.rows, g.nty);
@@ -62,6 +65,11 @@ SC_HDI int cell_local(const SysGeom& g, int col, int row) {
 }
 // column and row of local cell lc
 SC_HDI void cell_colrow(const SysGeom& g, int lc, int* col, int* row) {
+  if (g.ntx == 1 && g.nty == 1) {
+    *row = lc / g.cols;
+    *col = lc - *row * g.cols;
+    return;
+  }
   const int ky = tile_of(lc / g.cols, g.rows, g.nty);
   const int y0 = tile_lo(ky, g.rows, g.nty), hy = tile_lo(ky + 1, g.rows, g.nty) - y0;
   const int off = lc - y0 * g.cols;

@@ -595,13 +595,21 @@ __global__ void k_mx_local(Dev d, const StepScalars* __restrict__ tab, int row, 
     d.rec[i] = make_float4(xl, yl, A * cs, A * sn);
     d.mc[i] = make_float4((float)(lx - xl), (float)(ly - yl), pf, (float)(phi - pf));
     d.mm[i] = make_float4(0.f, 0.f, pf + (float)(phi - pf), 0.f);
-    d.pa[i] = make_float4((float)ra.x, A, __int_as_float(d.id[i]), (float)(1.0 / irc.x));
+    // 1/I in FP32 (an FP64 division per particle costs more than the whole record)
+    d.pa[i] = make_float4((float)ra.x, A, __int_as_float(d.id[i]), __frcp_rn((float)irc.x));
     d.rcf[i] = (float)irc.y;
     d.rf[i] = (float)ra.x;
   });
 }
 
-// The padded neighbour list in FP32 (see the file comment).
+// The padded neighbour list in FP32 (see the file comment).  Two stages per
+// particle: the centre-distance test over the candidates of the 3x3 cells, whose
+// survivors (about a third) are queued in scan order, and the capsule test over the
+// queue.  Threads of a warp then run the expensive test about as often as their own
+// survivors need, not once per candidate of the slowest lane; the list order (cell
+// by cell, slots ascending) is the scan order either way.
+constexpr int kMxQueue = 24;
+
 __global__ void __launch_bounds__(128, 12) k_mx_build_list(Dev d, const StepScalars* __restrict__ tab,
                                                       int row, int all) {
   if (!all && *d.any == 0) return;
@@ -613,10 +621,30 @@ __global__ void __launch_bounds__(128, 12) k_mx_build_list(Dev d, const StepScal
     const int cp = d.cellp[i];
     const int col = cp & 0xffff, rw = cp >> 16;
     const float4 ri = d.rec[i];
-    const float4 pai = d.pa[i];
+    const float2 rai = reinterpret_cast<const float2*>(d.pa)[2 * (size_t)i];  // (R, A)
     const int ncx = g.cols < 3 ? g.cols : 3, ncy = g.rows < 3 ? g.rows : 3;
     const bool smallx = ncx < 3, smally = ncy < 3;
-    int cnt = 0;
+    unsigned queue[kMxQueue];  // survivors of the centre test: slot | cell offset code
+    int nq = 0, cnt = 0;
+    // capsule test of the queued candidates, accepted ones appended in queue order
+    auto flush = [&]() {
+      for (int q = 0; q < nq; q++) {
+        const unsigned e = queue[q];
+        const int j = (int)(e & kSlotMask);
+        const float4 rj = d.rec[j];
+        const float Rj = d.rf[j];
+        float dx = ri.x - rj.x + (float)(1 - (int)((e >> 28) & 3u)) * W;
+        float dy = ri.y - rj.y + (float)(1 - (int)(e >> 30)) * H;
+        if (smallx) dx += Lxf * (float)((dx < -0.5f * Lxf) - (dx > 0.5f * Lxf));
+        if (smally) dy += Lyf * (float)((dy < -0.5f * Lyf) - (dy > 0.5f * Lyf));
+        if (capsules_within(fmaf(gam, dy, dx), dy, ri.z, ri.w, rj.z, rj.w,
+                            (rai.x + Rj + pad) * 1.00002f + 1e-5f)) {
+          if (cnt < d.maxn) d.nbr[(size_t)cnt * d.ntot + i] = (int)e;
+          cnt++;
+        }
+      }
+      nq = 0;
+    };
     for (int a = 0; a < ncy; a++) {
       int dr = smally ? a - rw : a - 1;
       int r2 = smally ? a : wrap_index(rw + dr, g.rows);
@@ -626,25 +654,25 @@ __global__ void __launch_bounds__(128, 12) k_mx_build_list(Dev d, const StepScal
         int cc = g.c0 + cell_local(g, c2, r2);
         int st = d.cell_start[cc], en = st + d.cell_count[cc];
         unsigned code = ((unsigned)(dc + 1) << 28) | ((unsigned)(dr + 1) << 30);
+        const float ox = (float)dc * W, oy = (float)dr * H;
         for (int j = st; j < en; j++) {
           if (j == i) continue;
-          float4 rj = d.rec[j];
-          float4 paj = d.pa[j];
-          float dx = ri.x - rj.x - (float)dc * W;
-          float dy = ri.y - rj.y - (float)dr * H;
+          const float4 rj = d.rec[j];
+          const float2 raj = reinterpret_cast<const float2*>(d.pa)[2 * (size_t)j];
+          float dx = ri.x - rj.x - ox;
+          float dy = ri.y - rj.y - oy;
           if (smallx) dx += Lxf * (float)((dx < -0.5f * Lxf) - (dx > 0.5f * Lxf));
           if (smally) dy += Lyf * (float)((dy < -0.5f * Lyf) - (dy > 0.5f * Lyf));
-          float lim = (pai.x + pai.y + paj.x + paj.y + pad) * 1.00002f + 1e-6f;
-          float dxl = fmaf(gam, dy, dx);
-          if (dxl * dxl + dy * dy < lim * lim &&
-              capsules_within(dxl, dy, ri.z, ri.w, rj.z, rj.w,
-                              (pai.x + paj.x + pad) * 1.00002f + 1e-5f)) {
-            if (cnt < d.maxn) d.nbr[(size_t)cnt * d.ntot + i] = (int)((unsigned)j | code);
-            cnt++;
+          const float lim = (rai.x + rai.y + raj.x + raj.y + pad) * 1.00002f + 1e-6f;
+          const float dxl = fmaf(gam, dy, dx);
+          if (dxl * dxl + dy * dy < lim * lim) {
+            queue[nq++] = (unsigned)j | code;
+            if (nq == kMxQueue) flush();
           }
         }
       }
     }
+    flush();
     d.nbr_n[i] = cnt;
     if (cnt > d.maxn) atomicOr(d.status, ST_NBR_OVERFLOW);
     if (i == g.p0) d.gbuild[s] = gam;
