@@ -390,7 +390,8 @@ def batched_leg(args, device, torch):
 
 
 def minimise_leg(replicas=128, n=4096, max_iter=40000, ftol=1e-14, device=0, e_jam=1e-12,
-                 dt_max=0.2, cg_iter=2000, over=4e-3, graphs=True, mixed_iter=50000):
+                 dt_max=0.2, cg_iter=2000, over=4e-3, graphs=True, mixed_iter=50000,
+                 contacts=2):
     """Minimisation time to tolerance on the jamming workload's shape: replicas of
     N = 4096 with a/R in {0.25, 0.5, 1, 2} (a quarter each), seeds 100 + k, from
     packing 0.70.  Untimed preparation: the mixed form compresses every replica in
@@ -413,7 +414,7 @@ def minimise_leg(replicas=128, n=4096, max_iter=40000, ftol=1e-14, device=0, e_j
     cat = lambda i: np.concatenate([pk[i] for pk in packs])  # noqa: E731
     L0 = np.array([pk[0] for pk in packs])
     R, A = cat(4), cat(5)
-    kw = dict(contacts=2, device=device, use_graphs=graphs)
+    kw = dict(contacts=contacts, device=device, use_graphs=graphs)
     prep = BoxBatch([n] * replicas, L0, cat(1), cat(2), cat(3), A, R, 0.1, precision="mixed",
                     **kw)
     t0 = time.perf_counter()
@@ -464,6 +465,7 @@ def minimise_leg(replicas=128, n=4096, max_iter=40000, ftol=1e-14, device=0, e_j
     both = da & db & dc & jammed
     return {
         "workload": f"jam_{replicas}x{n}", "replicas": replicas, "N": n, "ftol": ftol,
+        "contacts": contacts,
         "prep": {"seconds": t_prep, "increments": n_inc, "over_compression": over,
                  "phi_jam_range": [float(phi_j.min()), float(phi_j.max())]},
         "mixed_then_fp64": {"seconds": ta + tb, "mixed_seconds": ta, "mixed_iters": ia,
@@ -516,6 +518,8 @@ def main():
     ap.add_argument("--min-replicas", type=int, default=128)
     ap.add_argument("--min-iters", type=int, default=40000,
                     help="FP64 FIRE iteration cap of the minimisation leg")
+    ap.add_argument("--min-contacts", type=int, default=2, choices=[1, 2],
+                    help="contact points per pair in the minimisation leg")
     ap.add_argument("--min-over", type=float, default=4e-3,
                     help="compression past the detected jamming point (minimisation leg)")
     ap.add_argument("--pass-kind", choices=["auto", "list", "tile"], default="auto",
@@ -600,7 +604,8 @@ def main():
     if args.only == "minimise":
         # the minimisation leg alone (profiler captures: --no-graphs launches eagerly)
         print(json.dumps(minimise_leg(args.min_replicas, 4096, args.min_iters, device=local,
-                                      graphs=not args.no_graphs, over=args.min_over)))
+                                      graphs=not args.no_graphs, over=args.min_over,
+                                      contacts=args.min_contacts)))
         return
     if args.only:
         b = new_box(args.only)

@@ -88,14 +88,12 @@ __device__ __forceinline__ void flag_moved(const Dev& d, int s, int id, double2 
   }
 }
 
+// The FP64 pass of one slot: its pairs over its full list, then the Heun epilogue.
 template <int MODE, bool SE, bool TWO, bool FAST = false>
-__global__ void __launch_bounds__(128) k_pass64(Dev d, const StepScalars* __restrict__ tab,
-                                               int row) {
+__device__ __forceinline__ void pass64_slot(const Dev& d, const StepScalars* __restrict__ tab,
+                                            int row, int i) {
   constexpr bool kPred =
       (MODE == PASS_CORR_STRAIN || MODE == PASS_CORR_RESIZE || MODE == PASS_ENERGY_T);
-  if (MODE == PASS_CORR_STRAIN || MODE == PASS_CORR_RESIZE) mark_pending_rebuilds(d, tab, row);
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= d.ntot) return;
   int s = d.psys[i];
   if (d.skip && d.skip[s]) return;  // a converged minimiser system
   const SysGeom& g = d.geom[s];
@@ -323,6 +321,15 @@ __global__ void __launch_bounds__(128) k_pass64(Dev d, const StepScalars* __rest
     if (!(isfinite(p.x) && isfinite(p.y) && isfinite(phi))) atomicOr(d.status, ST_NAN);
     flag_moved(d, s, idi, m, g.pad);
   }
+}
+
+template <int MODE, bool SE, bool TWO, bool FAST = false>
+__global__ void __launch_bounds__(128) k_pass64(Dev d, const StepScalars* __restrict__ tab,
+                                               int row) {
+  if (MODE == PASS_CORR_STRAIN || MODE == PASS_CORR_RESIZE) mark_pending_rebuilds(d, tab, row);
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.ntot) return;
+  pass64_slot<MODE, SE, TWO, FAST>(d, tab, row, i);
 }
 
 // ---- stress and energy of the mixed form, in FP64 ----
