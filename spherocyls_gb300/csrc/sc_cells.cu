@@ -476,11 +476,12 @@ __global__ void k_se_chunk(Dev d) {
 __global__ void k_se_sys(Dev d) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= d.nsys) return;
-  // particle chunks of a system are contiguous and ordered; find them by scan
+  // particle chunks of a system are contiguous and ordered
+  const SysGeom& g = d.geom[s];
+  const int ch0 = g.pch0, ch1 = g.pch0 + pchunk_count(g);
   for (int comp = 0; comp < 5; comp++) {
     double v = 0.0;
-    for (int ch = 0; ch < d.npchunks; ch++)
-      if (d.pchunk_sys[ch] == s) v += d.se_chunk[(size_t)comp * d.npchunks + ch];
+    for (int ch = ch0; ch < ch1; ch++) v += d.se_chunk[(size_t)comp * d.npchunks + ch];
     d.se_sys[(size_t)comp * d.nsys + s] = v;
   }
 }

@@ -76,12 +76,12 @@ __global__ void k_cg_begin(Dev d, CgState c, int max_iter, unsigned long long se
   CgSys& q = c.sys[s];
   if (q.done) return;
   double F2 = 0, FF0 = 0, F02 = 0;
-  for (int ch = 0; ch < d.npchunks; ch++)
-    if (d.pchunk_sys[ch] == s) {
-      F2 += c.part[3 * ch + 0];
-      FF0 += c.part[3 * ch + 1];
-      F02 += c.part[3 * ch + 2];
-    }
+  const int ch0 = d.geom[s].pch0, ch1 = ch0 + pchunk_count(d.geom[s]);
+  for (int ch = ch0; ch < ch1; ch++) {
+    F2 += c.part[3 * ch + 0];
+    FF0 += c.part[3 * ch + 1];
+    F02 += c.part[3 * ch + 2];
+  }
   q.Eh2 = q.Eh1;
   q.Eh1 = q.E0;
   q.E0 = d.se_sys[s];  // se_sys is [5][nsys]: the energies come first

@@ -71,13 +71,13 @@ __device__ __forceinline__ void fire_sys(const Dev& d, const FireState& f, int s
   FireSys& q = f.sys[s];
   if (q.done) return;
   double P = 0, vv = 0, ff = 0, fm = 0;
-  for (int ch = 0; ch < d.npchunks; ch++)
-    if (d.pchunk_sys[ch] == s) {
-      P += f.part[4 * ch + 0];
-      vv += f.part[4 * ch + 1];
-      ff += f.part[4 * ch + 2];
-      fm = fmax(fm, f.part[4 * ch + 3]);
-    }
+  const int ch0 = d.geom[s].pch0, ch1 = ch0 + pchunk_count(d.geom[s]);
+  for (int ch = ch0; ch < ch1; ch++) {
+    P += f.part[4 * ch + 0];
+    vv += f.part[4 * ch + 1];
+    ff += f.part[4 * ch + 2];
+    fm = fmax(fm, f.part[4 * ch + 3]);
+  }
   q.fmax = sqrt(fm);
   q.iters += 1;
   if (q.fmax < ftol) {

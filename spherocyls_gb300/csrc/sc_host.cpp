@@ -253,6 +253,7 @@ bool Handle::layout_cells() {
   d.nchunks = nchunks;
   invalidate_graph();  // captured kernels hold the old layout
   std::vector<SysGeom> g(nsys);
+  int pch = 0;
   for (int s = 0; s < nsys; s++) {
     const HostSys& h = hs[s];
     SysGeom& o = g[s];
@@ -266,6 +267,8 @@ bool Handle::layout_cells() {
     o.nty = h.nty;
     o.chunk0 = h.chunk0;
     o.nchunks = h.nchunks;
+    o.pch0 = pch;
+    pch += (h.n + kSeChunk - 1) / kSeChunk;
     o.pad = h.pad;
     o.inv_n = 1.0 / h.n;
     o.smax = (float)(2.0 * (h.Rmax + h.Amax));
@@ -1135,6 +1138,40 @@ bool Handle::run_fire_graph(int iters, double ftol, double dt_max) {
   return cuda_ok(cudaGraphLaunch(fire_exec, stream), "fire graph launch");
 }
 
+// `iters` FIRE iterations with the persistent kernel of the mixed form.  A launch
+// returns after the iteration that asks for a rebuild, which is launched here before
+// the next one (as the graph's conditional node does), or once every system has
+// converged.  One host synchronisation per launch, to read where it ended.
+bool Handle::run_persist_fire(int iters, double ftol, double dt_max) {
+  for (int k = 0; k < iters;) {
+    if (!launch_persist_fire(d, fire, d_tab, ftol, dt_max, iters - k, d_persist, stream)) {
+      cudaGetLastError();
+      fail(SC_E_CUDA, "persistent FIRE kernel: cooperative launch failed");
+      return false;
+    }
+    kernels += 1;
+    if (!cuda_ok(cudaMemcpyAsync(h_pinned + 3, d_persist, sizeof(int), cudaMemcpyDeviceToHost,
+                                 stream), "persist result") ||
+        !cuda_ok(cudaStreamSynchronize(stream), "persist result"))
+      return false;
+    const int v = h_pinned[3];
+    const int m = v >> 2, why = v & 3;
+    if (m < 1 || m > iters - k || why == 3) {
+      if (!check_status("persistent FIRE")) return false;
+      fail(SC_E_STATE, "persistent FIRE kernel returned %d", v);
+      return false;
+    }
+    k += m;
+    if (why == 2) break;  // every system has converged
+    if (why == 1) {
+      launch_mx_materialize(d, d_tab, 0, false, stream);
+      launch_rebuild(d, true, d_tab, 0, stream);
+      kernels += 14;
+    }
+  }
+  return true;
+}
+
 // FIRE on every system until max |F| < ftol (or max_iter iterations); the host
 // looks at the per-system state only between chunks of iterations.
 int Handle::fire_minimize(double ftol, int max_iter, double dt0, double dt_max, int* iters,
@@ -1151,12 +1188,16 @@ int Handle::fire_minimize(double ftol, int max_iter, double dt0, double dt_max, 
   launch_fire_reset(d, fire, dt0, stream);
   std::vector<FireSys> hsys(nsys);
   const bool mixed = prec == PREC_MIXED;
+  const bool persist = opt.persist_steps && mixed && d.pass_kind == 0 && d_persist;
   int it = 0;
   bool all_done = false;
   while (it < max_iter && !all_done) {
     int chunk = std::min(kFireChunk, max_iter - it);
-    if (!(opt.use_graphs && chunk == kFireChunk && run_fire_graph(chunk, ftol, dt_max)))
+    if (persist) {
+      if (!run_persist_fire(chunk, ftol, dt_max)) return last_status;
+    } else if (!(opt.use_graphs && chunk == kFireChunk && run_fire_graph(chunk, ftol, dt_max))) {
       for (int k = 0; k < chunk; k++) enqueue_fire_iteration(ftol, dt_max);
+    }
     it += chunk;
     if (!cuda_ok(cudaGetLastError(), "fire launch") ||
         !cuda_ok(cudaMemcpyAsync(hsys.data(), fire.sys, nsys * sizeof(FireSys),

@@ -184,6 +184,7 @@ struct Handle {
   SubGraph* subgraph(bool resize, unsigned mask);
   void invalidate_table_graphs();
   bool run_persist(int nk, int done, int se_every);
+  bool run_persist_fire(int iters, double ftol, double dt_max);
 
   int run_steps(int kind, int shrink, int nsteps, int se_every, double* se_out);
   int calc(bool se, double* se_out);

@@ -32,7 +32,7 @@ struct SysGeom {
   int c0, cols, rows;  // first global cell and grid dimensions
   int chunk0, nchunks; // cell-scan chunks owned by the system
   int ntx, nty;        // tiles across and down (cell numbering, see cell_local)
-  int pad_;
+  int pch0;            // first particle-reduction chunk (kSeChunk particles each)
   double pad;          // neighbour padding (configure_cells auto-value applied)
   double inv_n;        // 1/n, energy normalisation
   float smax;          // largest R_i + A_i + R_j + A_j of the system
@@ -268,6 +268,8 @@ constexpr unsigned kBarrierSpins = 1u << 24;
 
 constexpr int kScanChunk = 1024;  // cells per scan chunk
 constexpr int kSeChunk = 1024;    // particles per reduction chunk
+// a system's particle-reduction chunks: [pch0, pch0 + pchunk_count), in slot order
+SC_HDI int pchunk_count(const SysGeom& g) { return (g.n + kSeChunk - 1) / kSeChunk; }
 constexpr int kMaxCellSort = 48;  // cells above this occupancy use the in-place slow sort
 constexpr int kNoTrigger = 0x7f7f7f7f;  // istar value when no particle triggered
 constexpr int kOrderWindow = 128;  // slots per window of the force-pass ordering
@@ -351,6 +353,12 @@ void launch_mx_build_list(const Dev& d, const StepScalars* tab, int row, bool al
 // and its rebuild is pending.  Returns false when the cooperative launch failed.
 bool launch_persist_steps(const Dev& d, const StepScalars* tab, int row0, int nsteps, int* out,
                           cudaStream_t st);
+// Mixed form: up to `iters` FIRE iterations (force pass, reductions, updates) in one
+// cooperative launch of 256-thread blocks, ending early at a pending rebuild or when
+// every system has converged.  *out = 4 k + (0 all ran, 1 rebuild pending, 2 all
+// converged).  Returns false when the cooperative launch failed.
+bool launch_persist_fire(const Dev& d, const FireState& f, const StepScalars* tab, double ftol,
+                         double dt_max, int iters, int* out, cudaStream_t st);
 // tile lists from the mixed lists (after launch_mx_build_list)
 void launch_tile_lists(const Dev& d, bool all, cudaStream_t st);
 // FP64 stress and energy partials of the mixed state (two kernels)

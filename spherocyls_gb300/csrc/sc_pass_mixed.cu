@@ -24,6 +24,7 @@
 //
 // Force pass: one thread per list position gathers over its particle's list and
 // evaluates each pair from its own side.
+#include "sc_fire.cuh"
 #include "sc_internal.hpp"
 #include "sc_pair.cuh"
 
@@ -176,8 +177,11 @@ __device__ __forceinline__ void mixed_epilogue(const Dev& d, const StepScalars& 
 }
 
 // The force pass of one list position (the per-particle pass): the particle's
-// pairs from its own side over its full list, then the Heun epilogue.
-template <int MODE, bool TWO>
+// pairs from its own side over its full list, then the Heun epilogue.  COH: the
+// records were written by other blocks of the same (persistent) launch, so they are
+// loaded through L2 (ld.global.cg) and never through the read-only path, which holds
+// only data that stays unchanged for a whole launch.
+template <int MODE, bool TWO, bool COH = false>
 __device__ __forceinline__ void pass_mixed_position(const Dev& d,
                                                     const StepScalars* __restrict__ tab,
                                                     int row, int pos) {
@@ -195,7 +199,8 @@ __device__ __forceinline__ void pass_mixed_position(const Dev& d,
   const float Lxf = W * g.cols, Lyf = H * g.rows;
   constexpr bool two_point = TWO;
 
-  const float4 ri = REC[i];
+#define SC_REC(k) (COH ? __ldcg(REC + (k)) : REC[(k)])
+  const float4 ri = SC_REC(i);
   const float4 pai = d.pa[i];  // (R, A, index bits, 1/I)
   const int cnt = d.nbr_pn[pos];
   // the list is column-major: entry k of this slot sits k * ntot words further on;
@@ -213,7 +218,7 @@ __device__ __forceinline__ void pass_mixed_position(const Dev& d,
   float4 r1 = make_float4(0.f, 0.f, 0.f, 0.f);
   float R1 = 0.f;
   if (cnt > 0) {
-    r1 = REC[e1 & kSlotMask];
+    r1 = SC_REC(e1 & kSlotMask);
     R1 = d.rf[e1 & kSlotMask];
   }
   const float ai = pai.y * pai.y;
@@ -223,7 +228,7 @@ __device__ __forceinline__ void pass_mixed_position(const Dev& d,
     const float Rj = R1;
     e1 = e2;
     if (k + 1 < cnt) {
-      r1 = REC[e1 & kSlotMask];
+      r1 = SC_REC(e1 & kSlotMask);
       R1 = d.rf[e1 & kSlotMask];
     }
     Lst += stride;
@@ -248,6 +253,7 @@ __device__ __forceinline__ void pass_mixed_position(const Dev& d,
     tq += o.tp;
   }
 
+#undef SC_REC
   mixed_epilogue<MODE>(d, ts, g, s, i, ri, pai, gam, fx, fy, tq);
 }
 
@@ -315,17 +321,63 @@ __global__ void __launch_bounds__(128, TWO ? 6 : 12) k_persist_steps(
           atomicExch(d.any, 1);
         }
     for (int pos = t0; pos < d.ntot; pos += stride)
-      pass_mixed_position<PASS_CORR_STRAIN, TWO>(d, tab, row, pos);
+      pass_mixed_position<PASS_CORR_STRAIN, TWO, true>(d, tab, row, pos);
     grid_barrier(d.gbar, d.status);
     if (*(volatile int*)d.any != 0) {  // the same value in every block after the barrier
       stopped = 1;
       break;
     }
     for (int pos = t0; pos < d.ntot; pos += stride)
-      pass_mixed_position<PASS_PRED_STRAIN, TWO>(d, tab, row, pos);
+      pass_mixed_position<PASS_PRED_STRAIN, TWO, true>(d, tab, row, pos);
     grid_barrier(d.gbar, d.status);
   }
   if (t0 == 0) *out = 2 * k + stopped;
+}
+
+// ---- persistent FIRE ----
+//
+// FIRE iterations of the mixed form in one cooperative launch: the force pass over
+// all positions, the chunk partials, the per-system FIRE update and the particle
+// update, each followed by a grid barrier.  The blocks have the 256 threads of the
+// launch-per-kernel reductions (k_fire_chunk), so each chunk sums in the same order
+// and the iterates equal those of the graph and eager paths bit for bit.  The launch
+// ends after `iters` iterations, after the iteration whose update asks for a
+// rebuild (the host runs it), or at the iteration in which the last system
+// converges: *out = 4 * iterations + (0 all ran, 1 rebuild pending, 2 all converged).
+template <bool TWO>
+__global__ void __launch_bounds__(256, TWO ? 3 : 4) k_persist_fire(
+    Dev d, FireState f, const StepScalars* __restrict__ tab, double ftol, double dt_max,
+    int iters, int* out) {
+  const int stride = gridDim.x * blockDim.x;
+  const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+  int k = 0, why = 0;
+  while (k < iters) {
+    for (int pos = t0; pos < d.ntot; pos += stride)
+      pass_mixed_position<PASS_FORCE, TWO, true>(d, tab, 0, pos);
+    grid_barrier(d.gbar, d.status);
+    for (int ch = blockIdx.x; ch < d.npchunks; ch += gridDim.x) {
+      fire::fire_chunk(d, f, ch);
+      __syncthreads();  // the next chunk reuses the block's shared partials
+    }
+    grid_barrier(d.gbar, d.status);
+    for (int s = t0; s < d.nsys; s += stride) fire::fire_sys(d, f, s, ftol, dt_max);
+    grid_barrier(d.gbar, d.status);
+    k++;
+    // every block sees the same flags: they change only in the phase before the barrier
+    int pending = 0;
+    for (int s = threadIdx.x; s < d.nsys; s += blockDim.x) pending |= (__ldcg(f.done + s) == 0);
+    if (!__syncthreads_or(pending)) {
+      why = 2;
+      break;
+    }
+    for (int i = t0; i < d.ntot; i += stride) fire::fire_update(d, f, i, 1);
+    grid_barrier(d.gbar, d.status);
+    if (*(volatile int*)d.any != 0) {
+      why = 1;
+      break;
+    }
+  }
+  if (t0 == 0) *out = 4 * k + why;
 }
 
 template <int MODE>
@@ -757,6 +809,28 @@ bool launch_persist_steps(const Dev& d, const StepScalars* tab, int row0, int ns
   dd.cond = 0;  // no graph node to switch: the launch ends at a pending rebuild
   void* args[] = {&dd, (void*)&tab, &row0, &nsteps, &out};
   return cudaLaunchCooperativeKernel(fn, grid, 128, args, 0, st) == cudaSuccess;
+}
+
+bool launch_persist_fire(const Dev& d, const FireState& f, const StepScalars* tab, double ftol,
+                         double dt_max, int iters, int* out, cudaStream_t st) {
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return false;
+  const void* fn = d.contact_model == 1 ? (const void*)k_persist_fire<true>
+                                        : (const void*)k_persist_fire<false>;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, 0) != cudaSuccess ||
+      per_sm < 1)
+    return false;
+  int grid = sms * per_sm;
+  const int need = (d.ntot + 255) / 256;
+  if (need < grid) grid = need;
+  Dev dd = d;
+  dd.cond = 0;
+  dd.skip = f.done;  // converged systems: no force pass
+  FireState ff = f;
+  void* args[] = {&dd, &ff, (void*)&tab, &ftol, &dt_max, &iters, &out};
+  return cudaLaunchCooperativeKernel(fn, grid, 256, args, 0, st) == cudaSuccess;
 }
 
 void launch_tile_lists(const Dev& d, bool all, cudaStream_t st) {

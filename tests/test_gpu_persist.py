@@ -57,3 +57,30 @@ def test_persistent_steps_in_a_batch(sc):
     got = _run(sc, packs, rates, 300, 7, persist_steps=True)
     assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1])
     assert got[2] == ref[2]
+
+
+def _fire(sc, packs, ftol, iters, **kw):
+    b = sc.BoxBatch([len(pk[1]) for pk in packs], [pk[0] * 0.97 for pk in packs],
+                    np.concatenate([pk[1] * 0.97 for pk in packs]),
+                    np.concatenate([pk[2] * 0.97 for pk in packs]),
+                    np.concatenate([pk[3] for pk in packs]), np.concatenate([pk[5] for pk in packs]),
+                    np.concatenate([pk[4] for pk in packs]), 0.1, precision="mixed", **kw)
+    it, fm, dn = b.fire_minimize(ftol, iters)
+    out = (np.array(b.state()), it, fm, dn, b.counters()["rebuilds"])
+    b.close()
+    return out
+
+
+@pytest.mark.parametrize("contacts", [1, 2])
+def test_persistent_fire_equals_graph_and_eager(sc, contacts):
+    """FIRE from affinely compressed packings (3% in length: overlaps to relax, list
+    rebuilds on the way); one system converges early and stops taking force passes."""
+    packs = [sc.generate_packing(n, phi, a, seed=s)
+             for n, phi, a, s in ((3000, 0.80, 1.0, 95), (500, 0.6, 0.5, 96), (1200, 0.84, 2.0, 97))]
+    ref = _fire(sc, packs, 1e-6, 3000, contacts=contacts)
+    assert ref[4] > 0 and ref[3].any()
+    for kw in (dict(persist_steps=True), dict(use_graphs=False)):
+        got = _fire(sc, packs, 1e-6, 3000, contacts=contacts, **kw)
+        assert np.array_equal(got[0], ref[0]), kw
+        assert got[1] == ref[1] and np.array_equal(got[2], ref[2]), kw
+        assert np.array_equal(got[3], ref[3]) and got[4] == ref[4], kw
