@@ -390,22 +390,24 @@ def batched_leg(args, device, torch):
 
 
 def minimise_leg(replicas=128, n=4096, max_iter=40000, ftol=1e-14, device=0, e_jam=1e-12,
-                 dt_max=0.2, cg_iter=2000, over=4e-3, graphs=True, mixed_iter=50000,
+                 dt_max=0.2, cg_iter=2000, over=1e-2, graphs=True, mixed_iter=20000,
                  contacts=2):
     """Minimisation time to tolerance on the jamming workload's shape: replicas of
     N = 4096 with a/R in {0.25, 0.5, 1, 2} (a quarter each), seeds 100 + k, from
-    packing 0.70.  Untimed preparation: the mixed form compresses every replica in
-    affine steps of 2e-3 in packing fraction (FIRE to 1e-6 after each) until E/N >
-    e_jam = 1e-12 at that tolerance (close to, and mostly below, the jamming point:
-    the residual forces of that tolerance leave about that energy); each replica is
-    then compressed by `over` past that point.  A replica whose FP64 minimum has
-    E/N <= 1e-16 is below jamming at that packing; the energy comparison covers the
-    jammed ones (E/N > 1e-16) that both arms brought below ftol.  From that same state the two timed arms
-    minimise to max|F_i|, |tau_i|/sqrt(I_i) < ftol: (a) mixed FIRE to 1e-6, then
-    FP64 FIRE; (b) FP64 FIRE alone; (c) the reference's conjugate gradient (FP64) on
-    one replica of each aspect ratio, stopped by the reference's rules or after
-    cg_iter iterations.  Each FP64 FIRE stage stops after max_iter iterations; a
-    replica that has converged takes no further force passes."""
+    packing 0.70, two-point contacts (the reference's jamming code).  Untimed
+    preparation: the mixed form compresses every replica in affine steps of 2e-3 in
+    packing fraction (FIRE to 1e-6 after each) until E/N > e_jam = 1e-12 at that
+    tolerance.  Incomplete minimisation leaves that much energy below the jamming
+    point, so each replica is then compressed by `over` more.  From that same state the
+    two timed arms minimise to max|F_i|, |tau_i|/sqrt(I_i) < ftol: (a) mixed FIRE to
+    1e-6 (the FP32 pair geometry resolves overlaps to about 1e-7), then FP64 FIRE;
+    (b) FP64 FIRE alone; and (c) the reference's conjugate gradient (FP64) on one
+    replica of each aspect ratio, stopped by the reference's rules or after cg_iter
+    iterations.  Each FIRE stage stops after its iteration cap; a replica that has
+    converged takes no further force passes.  A replica is jammed when its final
+    E/N > 1e-16.  The two-point rule's energy jumps where a second contact ends, so
+    FIRE stalls above ftol on some jammed replicas; the report gives the residuals
+    reached, and compares the energies of the replicas jammed in both arms."""
     from spherocyls_gb300 import BoxBatch, generate_packing
 
     aors = [0.25, 0.5, 1.0, 2.0]
@@ -431,18 +433,30 @@ def minimise_leg(replicas=128, n=4096, max_iter=40000, ftol=1e-14, device=0, e_j
     def run(b, tol, cap):
         t = time.perf_counter()
         it, fmax, done = b.fire_minimize(tol, cap, dt_max=dt_max)
-        return time.perf_counter() - t, it, fmax, done
+        return time.perf_counter() - t, it, fmax, done, b.fire_iterations()
 
+    def iteration_ms(precision, iters):
+        # one FIRE iteration of the whole batch, every replica active (from the
+        # same start, on a copy)
+        b = BoxBatch([n] * replicas, L1, x1, y1, ps, A, R, 0.1, precision=precision, **kw)
+        b.fire_minimize(1e-300, 20, dt_max=dt_max)  # graph capture
+        t = time.perf_counter()
+        b.fire_minimize(1e-300, iters, dt_max=dt_max)
+        dt = time.perf_counter() - t
+        b.close()
+        return 1e3 * dt / iters
+
+    c_mixed, c_fp64 = iteration_ms("mixed", 500), iteration_ms("fp64", 100)
     m = BoxBatch([n] * replicas, L1, x1, y1, ps, A, R, 0.1, precision="mixed", **kw)
-    ta, ia, _, da = run(m, 1e-6, mixed_iter)
+    ta, ia, fa, da, pa = run(m, 1e-6, mixed_iter)
     xm, ym, pm = m.state()
     m.close()
     r = BoxBatch([n] * replicas, L1, xm, ym, pm, A, R, 0.1, precision="fp64", **kw)
-    tb, ib, fb, db = run(r, ftol, max_iter)
+    tb, ib, fb, db, pb = run(r, ftol, max_iter)
     e_a = r.calc_se()[:, 0]
     r.close()
     p = BoxBatch([n] * replicas, L1, x1, y1, ps, A, R, 0.1, precision="fp64", **kw)
-    tc, ic, fc, dc = run(p, ftol, max_iter)
+    tc, ic, fc, dc, pc = run(p, ftol, max_iter)
     e_c = p.calc_se()[:, 0]
     p.close()
     sub = sorted({(k * replicas) // 4 for k in range(4)})
@@ -461,31 +475,60 @@ def minimise_leg(replicas=128, n=4096, max_iter=40000, ftol=1e-14, device=0, e_j
     inertia = Rs ** 4 * C / (6 * Rs * (REF_PI * Rs + 4 * As))
     res = np.maximum(np.hypot(qfx, qfy), np.abs(qtq) / np.sqrt(inertia)).reshape(len(sub), n)
     cres = res.max(axis=1)
-    jammed = (e_c > 1e-16) & (e_a > 1e-16)
-    both = da & db & dc & jammed
+    jam_a, jam_c = e_a > 1e-16, e_c > 1e-16
+    jam = jam_a & jam_c
+    conv = da & db & dc
+    rel = np.abs(e_a - e_c) / np.maximum(e_c, 1e-300)
+    levels = (1e-14, 1e-12, 1e-10, 1e-8, 1e-6)
+
+    def below(fm):
+        return {f"{v:g}": int((fm < v).sum()) for v in levels}
+
+    def med(v):
+        return float(np.median(v)) if len(v) else None
+
     return {
         "workload": f"jam_{replicas}x{n}", "replicas": replicas, "N": n, "ftol": ftol,
         "contacts": contacts,
         "prep": {"seconds": t_prep, "increments": n_inc, "over_compression": over,
                  "phi_jam_range": [float(phi_j.min()), float(phi_j.max())]},
         "mixed_then_fp64": {"seconds": ta + tb, "mixed_seconds": ta, "mixed_iters": ia,
-                            "fp64_iters": ib, "converged": int((da & db).sum()),
-                            "max_residual": float(fb.max())},
+                            "fp64_iters": ib, "mixed_reached_1e-6": int(da.sum()),
+                            "converged": int((da & db).sum()), "max_residual": float(fb.max()),
+                            "residual_below": below(fb), "jammed": int(jam_a.sum())},
         "fp64": {"seconds": tc, "iters": ic, "converged": int(dc.sum()),
-                 "max_residual": float(fc.max())},
+                 "max_residual": float(fc.max()), "residual_below": below(fc),
+                 "jammed": int(jam_c.sum())},
+        "iterations_median_converged_both": {
+            "mixed": med(pa[conv]), "fp64_after_mixed": med(pb[conv]),
+            "fp64_alone": med(pc[conv])},
+        "iteration_ms": {"mixed": c_mixed, "fp64": c_fp64,
+                         "note": "one FIRE iteration of the 128-replica batch, all active"},
+        "time_to_tolerance_speedup_converged_both": (
+            {"median": float(np.median(pc[conv] * c_fp64 / (pa[conv] * c_mixed + pb[conv] * c_fp64))),
+             "aggregate": float(np.sum(pc[conv]) * c_fp64 /
+                                np.sum(pa[conv] * c_mixed + pb[conv] * c_fp64)),
+             "replicas": int(conv.sum()),
+             "note": "per replica, its iterations in each stage times the batch's cost per "
+                     "iteration (modelled: the batch's wall time is set by its slowest replica)"}
+            if conv.any() else None),
         "cg_fp64": {"replicas": len(sub), "seconds": tcg, "iters_max": int(cit.max()),
                     "iters_mean": float(cit.mean()),
                     "stop_reasons": {str(k): int((cwhy == k).sum()) for k in (1, 2, 3, 4, 5)},
                     "below_ftol": int((cres < ftol).sum()), "max_residual": float(cres.max())},
-        "jammed_converged_both": int(both.sum()),
+        "jammed_both": int(jam.sum()),
+        "jammed_energy_rel_diff": {
+            "max": float(rel[jam].max()) if jam.any() else None,
+            "median": med(rel[jam]),
+            "within_1e-10": int((rel[jam] <= 1e-10).sum())},
+        "jammed_converged_both": int((conv & jam).sum()),
+        "energy_rel_diff_max": (float(rel[conv & jam].max()) if (conv & jam).any() else None),
         "energy_per_particle_range": [float(min(e_a.min(), e_c.min())),
                                       float(max(e_a.max(), e_c.max()))],
-        "speedup": tc / (ta + tb),
-        "energy_rel_diff_max": (float(np.max(np.abs(e_a[both] - e_c[both]) / e_c[both]))
-                                if both.any() else None),
         "energy_per_particle_abs_diff_max_unjammed": (
-            float(np.max(np.abs(e_a - e_c)[da & db & dc & ~jammed]))
-            if (da & db & dc & ~jammed).any() else None),
+            float(np.max(np.abs(e_a - e_c)[conv & ~jam_a & ~jam_c]))
+            if (conv & ~jam_a & ~jam_c).any() else None),
+        "speedup": tc / (ta + tb),
     }
 
 
@@ -520,7 +563,7 @@ def main():
                     help="FP64 FIRE iteration cap of the minimisation leg")
     ap.add_argument("--min-contacts", type=int, default=2, choices=[1, 2],
                     help="contact points per pair in the minimisation leg")
-    ap.add_argument("--min-over", type=float, default=4e-3,
+    ap.add_argument("--min-over", type=float, default=1e-2,
                     help="compression past the detected jamming point (minimisation leg)")
     ap.add_argument("--pass-kind", choices=["auto", "list", "tile"], default="auto",
                     help="the mixed form's force pass before autotuning (profiler captures)")
@@ -710,7 +753,7 @@ def main():
         extra["batched"] = batched_leg(args, local, torch)
     if rank == 0 and "minimise" in legs:
         extra["minimise"] = minimise_leg(args.min_replicas, 4096, args.min_iters, device=local,
-                                         over=args.min_over)
+                                         over=args.min_over, contacts=args.min_contacts)
 
     base = None
     if rank == 0 and not args.no_cpu and w.get("phi") is not None:

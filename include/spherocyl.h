@@ -195,6 +195,10 @@ int sc_cg_minimize(sc_handle *h, int max_iter, int *iters, double *energy, int *
  * Returns SC_E_NOCONV when some system did not reach ftol. */
 int sc_fire_minimize(sc_handle *h, double ftol, int max_iter, double dt0, double dt_max,
                      int *iters, double *fmax, int *done);
+/* Iterations each system took in the handle's last sc_fire_minimize (up to and
+ * including the one that brought it below ftol): iters[s], s < the system count.
+ * All zero before the first call. */
+int sc_fire_iterations(const sc_handle *h, int *iters);
 /* Affine rescale of box and positions by factor (the src/cuda resize_coords,
  * src/cuda/strain_dynamics.cu:1111-1122, as one step); sys = -1 for all. */
 int sc_affine_scale(sc_handle *h, int sys, double factor);

@@ -92,6 +92,7 @@ SIGNATURES = [
     ("sc_cg_minimize", ctypes.c_int, [_vp, ctypes.c_int, _ip, _dp, _ip]),
     ("sc_fire_minimize", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_int, ctypes.c_double,
                                         ctypes.c_double, _ip, _dp, _ip]),
+    ("sc_fire_iterations", ctypes.c_int, [_vp, _ip]),
     ("sc_affine_scale", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double]),
     ("sc_quasistatic_compress", ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_double,
                                                ctypes.c_double, ctypes.c_int, ctypes.c_int, _dp,

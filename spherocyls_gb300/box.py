@@ -330,6 +330,12 @@ class BoxBatch:
             self._chk(st)
         return it.value, fm, dn.astype(bool)
 
+    def fire_iterations(self) -> np.ndarray:
+        """Per-system iterations of the last fire_minimize."""
+        it = np.zeros(self.nsys, dtype=np.int32)
+        self._chk(lib().sc_fire_iterations(self.h, it.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+        return it
+
     def rotate_shear(self, sys: int = -1):
         """Turn to the frame in which the sheared cell is upright (rotate_by_gamma)."""
         self._chk(lib().sc_rotate_shear(self.h, int(sys)))

@@ -660,6 +660,13 @@ int sc_fire_minimize(sc_handle* H, double ftol, int max_iter, double dt0, double
   return H->h.fire_minimize(ftol, max_iter, dt0, dt_max, iters, fmax, done);
 }
 
+int sc_fire_iterations(const sc_handle* H, int* iters) {
+  if (!H || !iters) return SC_E_ARG;
+  const sc::Handle& h = H->h;
+  for (int s = 0; s < h.nsys; s++) iters[s] = s < (int)h.fire_iters.size() ? h.fire_iters[s] : 0;
+  return SC_OK;
+}
+
 int sc_strain_to_gamma(sc_handle* H, double gamma_max, long* steps) {
   if (!H) return SC_E_ARG;
   return H->h.strain_to_gamma(gamma_max, steps);

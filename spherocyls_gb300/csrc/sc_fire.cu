@@ -23,16 +23,18 @@ namespace sc {
 namespace {
 
 // one block per chunk
-__global__ void k_fire_chunk(Dev d, FireState f) { fire::fire_chunk(d, f, blockIdx.x); }
+template <bool MIXED>
+__global__ void k_fire_chunk(Dev d, FireState f) { fire::fire_chunk<MIXED>(d, f, blockIdx.x); }
 
 __global__ void k_fire_sys(Dev d, FireState f, double ftol, double dt_max) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s < d.nsys) fire::fire_sys(d, f, s, ftol, dt_max);
 }
 
-__global__ void k_fire_update(Dev d, FireState f, int mixed) {
+template <bool MIXED>
+__global__ void k_fire_update(Dev d, FireState f) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < d.ntot) fire::fire_update(d, f, i, mixed);
+  if (i < d.ntot) fire::fire_update<MIXED>(d, f, i);
 }
 
 __global__ void k_fire_reset(Dev d, FireState f, double dt0) {
@@ -125,9 +127,15 @@ void launch_fire_reset(const Dev& d, const FireState& f, double dt0, cudaStream_
 
 void launch_fire_iteration_tail(const Dev& d, const FireState& f, double ftol, double dt_max,
                                 bool mixed, cudaStream_t st) {
-  k_fire_chunk<<<d.npchunks, 256, 0, st>>>(d, f);
+  if (mixed)
+    k_fire_chunk<true><<<d.npchunks, 256, 0, st>>>(d, f);
+  else
+    k_fire_chunk<false><<<d.npchunks, 256, 0, st>>>(d, f);
   k_fire_sys<<<nblk(d.nsys, 128), 128, 0, st>>>(d, f, ftol, dt_max);
-  k_fire_update<<<nblk(d.ntot, 256), 256, 0, st>>>(d, f, mixed ? 1 : 0);
+  if (mixed)
+    k_fire_update<true><<<nblk(d.ntot, 256), 256, 0, st>>>(d, f);
+  else
+    k_fire_update<false><<<nblk(d.ntot, 256), 256, 0, st>>>(d, f);
 }
 
 void launch_rotate(const Dev& d, const double* q, cudaStream_t st) {

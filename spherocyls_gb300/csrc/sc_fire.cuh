@@ -19,21 +19,38 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
   s = t;
 }
 
-// per-particle reduction terms of one chunk -> chunk partials (fixed order)
+// per-particle reduction terms of one chunk -> chunk partials (fixed order).  The
+// mixed form's forces and velocities are FP32 values (held in the FP64 arrays): its
+// per-particle products are FP32 and only the sums are FP64, which keeps the FP64
+// pipe (a small fraction of the FP32 rate on this GPU) out of the per-particle work.
+template <bool MIXED>
 __device__ __forceinline__ void fire_chunk(const Dev& d, const FireState& f, int ch) {
   if (f.sys[d.pchunk_sys[ch]].done) return;  // converged: its partials are not read
   int p0 = d.pchunk_p0[ch], np = d.pchunk_np[ch];
   double P = 0, vv = 0, ff = 0, fm = 0;
   for (int k = threadIdx.x; k < np; k += blockDim.x) {
     int i = p0 + k;
-    double I = d.irc[i].x;
-    double fx = d.fx[i], fy = d.fy[i], tq = d.tau[i];
-    double vx = f.vx[i], vy = f.vy[i], vp = f.vp[i];
-    P += fx * vx + fy * vy + tq * vp;
-    vv += vx * vx + vy * vy + I * vp * vp;
-    ff += fx * fx + fy * fy + tq * tq / I;
-    double m = fmax(fx * fx + fy * fy, tq * tq / I);
-    fm = fmax(fm, m);
+    if (MIXED) {
+      const float fx = (float)d.fx[i], fy = (float)d.fy[i], tq = (float)d.tau[i];
+      const float vx = (float)f.vx[i], vy = (float)f.vy[i], vp = (float)f.vp[i];
+      const float invI = d.pa[i].w;  // FP32 1/I of the mixed records
+      const float t2 = tq * tq * invI;
+      const float f2 = fmaf(fx, fx, fy * fy);
+      P += (double)fmaf(fx, vx, fmaf(fy, vy, tq * vp));
+      vv += (double)fmaf(vx, vx, fmaf(vy, vy, __fdividef(vp * vp, invI)));
+      ff += (double)(f2 + t2);
+      fm = fmax(fm, (double)fmaxf(f2, t2));
+    } else {
+      double I = d.irc[i].x;
+      double fx = d.fx[i], fy = d.fy[i], tq = d.tau[i];
+      double vx = f.vx[i], vy = f.vy[i], vp = f.vp[i];
+      const double t2 = tq * tq / I;  // one FP64 division per particle
+      P += fx * vx + fy * vy + tq * vp;
+      vv += vx * vx + vy * vy + I * vp * vp;
+      ff += fx * fx + fy * fy + t2;
+      double m = fmax(fx * fx + fy * fy, t2);
+      fm = fmax(fm, m);
+    }
   }
   __shared__ double sh[4][32];
   int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -107,56 +124,78 @@ __device__ __forceinline__ void fire_sys(const Dev& d, const FireState& f, int s
   }
 }
 
-// v <- (1-a) v + a |v| F/|F| (or 0 after an uphill step); v += dt F/m; x += dt v
-__device__ __forceinline__ void fire_update(const Dev& d, const FireState& f, int i, int mixed) {
+// v <- (1-a) v + a |v| F/|F| (or 0 after an uphill step); v += dt F/m; x += dt v.
+// The mixed form's velocity update is FP32 (its forces are FP32), stored in the
+// FP64 arrays; the FP64 form's is FP64.
+template <bool MIXED>
+__device__ __forceinline__ void fire_update(const Dev& d, const FireState& f, int i) {
   int s = d.psys[i];
   const FireSys q = f.sys[s];
   if (q.done) return;
   const SysGeom& g = d.geom[s];
-  double I = d.irc[i].x;
-  double fx = d.fx[i], fy = d.fy[i], tq = d.tau[i];
-  double vx = f.vx[i], vy = f.vy[i], vp = f.vp[i];
-  if (q.zero_v) {
-    vx = vy = vp = 0.0;
-  } else {
-    vx = q.c1 * vx + q.c2 * fx;
-    vy = q.c1 * vy + q.c2 * fy;
-    vp = q.c1 * vp + q.c2 * tq / I;
-  }
-  vx += q.dt * fx;
-  vy += q.dt * fy;
-  vp += q.dt * tq / I;
-  f.vx[i] = vx;
-  f.vy[i] = vy;
-  f.vp[i] = vp;
-  double ddx = q.dt * vx, ddy = q.dt * vy, ddp = q.dt * vp;
-  if (mixed) {
+  if (MIXED) {
+    const float4 pa = d.pa[i];  // (R, A, index bits, 1/I)
+    const float A = pa.y;
+    const float fx = (float)d.fx[i], fy = (float)d.fy[i], ap = (float)d.tau[i] * pa.w;
+    float vx = (float)f.vx[i], vy = (float)f.vy[i], vp = (float)f.vp[i];
+    const float c1 = (float)q.c1, c2 = (float)q.c2, dt = (float)q.dt;
+    if (q.zero_v) {
+      vx = vy = vp = 0.f;
+    } else {
+      vx = fmaf(c1, vx, c2 * fx);
+      vy = fmaf(c1, vy, c2 * fy);
+      vp = fmaf(c1, vp, c2 * ap);
+    }
+    vx = fmaf(dt, fx, vx);
+    vy = fmaf(dt, fy, vy);
+    vp = fmaf(dt, ap, vp);
+    f.vx[i] = vx;
+    f.vy[i] = vy;
+    f.vp[i] = vp;
+    const float ddx = dt * vx, ddy = dt * vy, ddp = dt * vp;
     float4 r = d.rec[i];
     float4 c = d.mc[i];
-    kahan_add(r.x, c.x, (float)ddx);
-    kahan_add(r.y, c.y, (float)ddy);
-    kahan_add(c.z, c.w, (float)ddp);
+    kahan_add(r.x, c.x, ddx);
+    kahan_add(r.y, c.y, ddy);
+    kahan_add(c.z, c.w, ddp);
     float sn, cs;
     sincosf(c.z + c.w, &sn, &cs);
-    float A = d.pa[i].y;
     r.z = A * cs;
     r.w = A * sn;
     d.rec[i] = r;
     d.mc[i] = c;
     float4 m = d.mm[i];
-    m.x += (float)ddx;
-    m.y += (float)ddy;
+    m.x += ddx;
+    m.y += ddy;
     d.mm[i] = m;
     // the mixed list criterion (fixed gamma): spine movement since the build
     // (centre plus A times the rotation) and the next step's allowance within half
     // the padding
-    float dd = (float)sqrt(ddx * ddx + ddy * ddy) + A * (float)fabs(ddp);
+    float dd = sqrtf(fmaf(ddx, ddx, ddy * ddy)) + A * fabsf(ddp);
     float moved = sqrtf(m.x * m.x + m.y * m.y) + A * fabsf((c.z + c.w) - m.z);
     if (!(moved + dd < 0.5f * g.fpad)) {
       if (d.flags[s] == 0) atomicOr(&d.flags[s], 1);
       if (*d.any == 0) atomicExch(d.any, 1);
     }
   } else {
+    double I = d.irc[i].x;
+    double fx = d.fx[i], fy = d.fy[i], tq = d.tau[i];
+    double vx = f.vx[i], vy = f.vy[i], vp = f.vp[i];
+    const double ap = tq / I;  // angular acceleration (one FP64 division)
+    if (q.zero_v) {
+      vx = vy = vp = 0.0;
+    } else {
+      vx = q.c1 * vx + q.c2 * fx;
+      vy = q.c1 * vy + q.c2 * fy;
+      vp = q.c1 * vp + q.c2 * ap;
+    }
+    vx += q.dt * fx;
+    vy += q.dt * fy;
+    vp += q.dt * ap;
+    f.vx[i] = vx;
+    f.vy[i] = vy;
+    f.vp[i] = vp;
+    double ddx = q.dt * vx, ddy = q.dt * vy, ddp = q.dt * vp;
     double2 p = d.xy[i];
     p.x += ddx;
     p.y += ddy;

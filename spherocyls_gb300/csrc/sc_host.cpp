@@ -1211,7 +1211,9 @@ int Handle::fire_minimize(double ftol, int max_iter, double dt0, double dt_max, 
   forces_valid = false;
   if (mixed) fp64_valid = false;
   int max_it = 0;
+  fire_iters.assign(nsys, 0);
   for (int s = 0; s < nsys; s++) {
+    fire_iters[s] = hsys[s].iters;
     if (fmax_out) fmax_out[s] = hsys[s].fmax;
     if (done_out) done_out[s] = hsys[s].done;
     max_it = std::max(max_it, hsys[s].iters);

@@ -185,6 +185,7 @@ struct Handle {
   void invalidate_table_graphs();
   bool run_persist(int nk, int done, int se_every);
   bool run_persist_fire(int iters, double ftol, double dt_max);
+  std::vector<int> fire_iters;  // per-system iterations of the last FIRE run
 
   int run_steps(int kind, int shrink, int nsteps, int se_every, double* se_out);
   int calc(bool se, double* se_out);

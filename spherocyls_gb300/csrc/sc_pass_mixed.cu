@@ -356,7 +356,7 @@ __global__ void __launch_bounds__(256, TWO ? 3 : 4) k_persist_fire(
       pass_mixed_position<PASS_FORCE, TWO, true>(d, tab, 0, pos);
     grid_barrier(d.gbar, d.status);
     for (int ch = blockIdx.x; ch < d.npchunks; ch += gridDim.x) {
-      fire::fire_chunk(d, f, ch);
+      fire::fire_chunk<true>(d, f, ch);
       __syncthreads();  // the next chunk reuses the block's shared partials
     }
     grid_barrier(d.gbar, d.status);
@@ -370,7 +370,7 @@ __global__ void __launch_bounds__(256, TWO ? 3 : 4) k_persist_fire(
       why = 2;
       break;
     }
-    for (int i = t0; i < d.ntot; i += stride) fire::fire_update(d, f, i, 1);
+    for (int i = t0; i < d.ntot; i += stride) fire::fire_update<true>(d, f, i);
     grid_barrier(d.gbar, d.status);
     if (*(volatile int*)d.any != 0) {
       why = 1;

@@ -66,7 +66,9 @@ def _fire(sc, packs, ftol, iters, **kw):
                     np.concatenate([pk[3] for pk in packs]), np.concatenate([pk[5] for pk in packs]),
                     np.concatenate([pk[4] for pk in packs]), 0.1, precision="mixed", **kw)
     it, fm, dn = b.fire_minimize(ftol, iters)
-    out = (np.array(b.state()), it, fm, dn, b.counters()["rebuilds"])
+    per = b.fire_iterations()
+    assert per.max() == it and np.all(per <= iters)
+    out = (np.array(b.state()), it, fm, dn, b.counters()["rebuilds"], per)
     b.close()
     return out
 
@@ -84,3 +86,4 @@ def test_persistent_fire_equals_graph_and_eager(sc, contacts):
         assert np.array_equal(got[0], ref[0]), kw
         assert got[1] == ref[1] and np.array_equal(got[2], ref[2]), kw
         assert np.array_equal(got[3], ref[3]) and got[4] == ref[4], kw
+        assert np.array_equal(got[5], ref[5]), kw

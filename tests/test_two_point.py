@@ -197,3 +197,48 @@ def test_find_jam_bisects_to_target_energy(library):
     assert np.all(phi > 0.8) and np.all(phi < 0.95), phi
     e = batch.calc_se()[:, 0]
     assert np.all(np.abs(e - e_jam) < 0.05 * e_jam), e
+
+
+def _pair(oracle_built, x, y, phi, two):
+    R = np.array([0.5, 0.5])
+    b = oracle_built.OracleBox(20.0, np.asarray(x, float), np.asarray(y, float),
+                               np.asarray(phi, float), R.copy(), R, 0.1, two_point=two)
+    b.calc_se()
+    e = b.se()[0] * 2
+    b.calc_forces()
+    f = np.array(b.forces())
+    b.close()
+    return e, f
+
+
+def test_one_point_torque_flips_at_parallel_alignment(oracle_built):
+    """The one-point rule (src/cpp calc_force_pair) puts the contact at one end of the
+    overlapping stretch of two side-by-side spines, and which end flips as the tilt
+    passes through zero: the torques jump, so a minimum at parallel alignment is a
+    cusp with no zero of the generalised force.  The two-point rule is smooth there."""
+    out = {}
+    for two in (False, True):
+        out[two] = [_pair(oracle_built, [5.0, 5.4], [5.0, 5.95], [t, 0.0], two)[1][2]
+                    for t in (-1e-9, 1e-9)]
+    (tm, tp) = out[False]
+    assert abs(tm[0] - tp[0]) > 0.02  # torque on the tilted spine: +0.005 -> -0.025
+    (tm, tp) = out[True]
+    assert np.max(np.abs(tm - tp)) < 1e-8
+
+
+def test_two_point_energy_jumps_where_the_second_contact_ends(oracle_built):
+    """The two-point rule (euler_est_2p, src/cuda/2point_dynamics.cu:385-546) drops its
+    second contact when the two contact points meet (s1 == s2 or t1 == t2).  Sliding
+    two overlapping parallel spines apart along their axis, that happens while the
+    second contact still overlaps: the pair energy falls by one contact's share in a
+    single step of 5e-4.  Minimisers cannot bring a residual force to zero across such
+    a step, which is why FIRE and the reference's CG stall on some jammed states."""
+    dxs = np.linspace(0.9, 1.1, 401)
+    e = np.array([_pair(oracle_built, [5.0, 5.0 + dx], [5.0, 5.95], [0.0, 0.0], True)[0]
+                  for dx in dxs])
+    de = np.abs(np.diff(e))
+    k = int(np.argmax(de))
+    assert abs(dxs[k] - 1.0) < 1e-3  # the spine ends (a = 0.5 each) line up at dx = 2a
+    assert de[k] > 0.4 * e[k]  # half of the pair energy (one of two equal contacts)
+    rest = np.delete(de, k)
+    assert np.max(rest) < 5e-3 * de[k]  # the smooth part changes by 2e-6 per step
