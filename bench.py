@@ -663,6 +663,11 @@ def main():
             b.find_neighbors()
         torch.cuda.synchronize()
         torch.cuda.nvtx.range_pop()
+        # one stress and energy evaluation (profiler captures of the reductions)
+        torch.cuda.nvtx.range_push("stress_energy")
+        b.calc_se()
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
         if rank == 0:
             print(json.dumps({"only": args.only, "workload": args.workload, "steps": args.steps,
                               "ms_per_step": 1e3 * secs / args.steps,
