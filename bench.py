@@ -607,21 +607,22 @@ def main():
     tuned = {"pad": PAD * args.pad_factor, "block": 128, "pass_kind": args.pass_kind,
              "tile_target": args.tile_target, "persist_steps": args.persist}
 
-    def new_box(precision, profile=False, state=None):
+    def new_box(precision, profile=False, state=None, shapes=None):
         # the mixed form runs with the autotuned padding and block size
         pad = tuned["pad"] if precision == "mixed" else PAD
         block = tuned["block"] if precision == "mixed" else 0
         kw = dict(pass_kind=tuned["pass_kind"], tile_target=tuned["tile_target"],
                   persist_steps=tuned["persist_steps"]) if precision == "mixed" else {}
         x, y, p = state[:3] if state is not None else (w["x"], w["y"], w["p"])
+        A, R = shapes if shapes is not None else (w["A"], w["R"])
         if args.workload == "batch512":
-            b = BoxBatch(w["ns"], w["L"], x, y, p, w["A"], w["R"], pad, precision=precision,
+            b = BoxBatch(w["ns"], w["L"], x, y, p, A, R, pad, precision=precision,
                          device=local, profile=profile, use_graphs=not args.no_graphs,
                          block=block, **kw)
             for k, r in enumerate(w["rates"]):
                 b.set_strain_rate(float(r), sys=k)
         else:
-            b = SpherocylBox(w["L"], x, y, p, w["A"], w["R"], pad,
+            b = SpherocylBox(w["L"], x, y, p, A, R, pad,
                              precision=precision, device=local, profile=profile,
                              use_graphs=not args.no_graphs, block=block, **kw)
             b.set_strain_rate(w["rate"])
@@ -734,11 +735,22 @@ def main():
     b64.close()
 
     # ---- end to end through the C ABI with host buffers, same window ----
+    # inputs and outputs in pinned host memory (filled before the timed region)
+    def pinned(a=None, size=None):
+        t = torch.empty(len(a) if a is not None else size, dtype=torch.float64, pin_memory=True)
+        v = t.numpy()
+        if a is not None:
+            v[:] = a
+        return v
+
+    h_in = [pinned(a) for a in (start[0], start[1], start[2], w["A"], w["R"])]
+    h_out = [pinned(size=len(start[0])) for _ in range(3)]
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    e2e_box = new_box("mixed", state=start)  # sc_create copies x, y, phi, R, A in
+    # sc_create copies x, y, phi, A, R in
+    e2e_box = new_box("mixed", state=(*h_in[:3], start[3], start[4]), shapes=h_in[3:])
     se = e2e_box.strain_steps(args.steps, se_every=args.steps)
-    xs, ys, ps = e2e_box.state()
+    xs, ys, ps = e2e_box.state(out=h_out)
     torch.cuda.synchronize()
     e2e_secs = time.perf_counter() - t0
     e2e_box.close()
@@ -747,9 +759,9 @@ def main():
     e2e = {"value": world * n * args.steps / e2e_secs, "unit": "particle-steps/s",
            "h2d_bytes_per_step": 40 * n / args.steps,
            "d2h_bytes_per_step": (24 * n + 40) / args.steps, "steps": args.steps,
-           "note": "the same window through the C ABI: handle created from host arrays of "
-                   "the state after the warm-up, K steps, stress/energy of the last step "
-                   "and positions read back to host arrays"}
+           "note": "the same window through the C ABI: handle created from pinned host "
+                   "arrays of the state after the warm-up, K steps, stress/energy of the "
+                   "last step and positions read back to pinned host arrays"}
 
     extra = {}
     if rank == 0 and "precision" in legs:

@@ -455,8 +455,17 @@ class BoxBatch:
         return s.value
 
     # --- state ------------------------------------------------------------
-    def state(self):
-        x, y, p = (np.empty(self.ntot) for _ in range(3))
+    def state(self, out=None):
+        """(x, y, phi) in input order; `out`: three caller arrays of ntot float64 (for
+        example in pinned host memory) to read into instead of new ones."""
+        if out is None:
+            x, y, p = (np.empty(self.ntot) for _ in range(3))
+        else:
+            x, y, p = out
+            for a in (x, y, p):
+                if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and
+                        a.flags.c_contiguous and a.size == self.ntot):
+                    raise ValueError("state(out=...): three contiguous float64 arrays of ntot")
         self._chk(lib().sc_get_state(self.h, _ptr(x), _ptr(y), _ptr(p)))
         return x, y, p
 

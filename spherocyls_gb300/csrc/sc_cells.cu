@@ -473,16 +473,26 @@ __global__ void k_se_chunk(Dev d) {
   }
 }
 
-__global__ void k_se_sys(Dev d) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= d.nsys) return;
-  // particle chunks of a system are contiguous and ordered
+// One block per system: each thread sums its strided share of the system's chunk
+// partials in order, then a fixed tree over the block (deterministic).
+__global__ void __launch_bounds__(256) k_se_sys(Dev d) {
+  const int s = blockIdx.x;
   const SysGeom& g = d.geom[s];
   const int ch0 = g.pch0, ch1 = g.pch0 + pchunk_count(g);
+  __shared__ double sh[5][8];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int comp = 0; comp < 5; comp++) {
     double v = 0.0;
-    for (int ch = ch0; ch < ch1; ch++) v += d.se_chunk[(size_t)comp * d.npchunks + ch];
-    d.se_sys[(size_t)comp * d.nsys + s] = v;
+    for (int ch = ch0 + threadIdx.x; ch < ch1; ch += blockDim.x)
+      v += d.se_chunk[(size_t)comp * d.npchunks + ch];
+    for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[comp][w] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 5) {
+    double v = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); k++) v += sh[threadIdx.x][k];
+    d.se_sys[(size_t)threadIdx.x * d.nsys + s] = v;
   }
 }
 
@@ -664,7 +674,7 @@ void launch_se_store(const Dev& d, double* dst, cudaStream_t st) {
 
 void launch_se_reduce(const Dev& d, cudaStream_t st) {
   k_se_chunk<<<d.npchunks, 256, 0, st>>>(d);
-  k_se_sys<<<nblk(d.nsys, 128), 128, 0, st>>>(d);
+  k_se_sys<<<d.nsys, 256, 0, st>>>(d);
 }
 
 }  // namespace sc

@@ -61,11 +61,14 @@ __device__ __forceinline__ Recip64 recip64(double a, double c, double delta, dou
 
 // dX, dY: raw coordinate differences P - Q (no minimum image yet).
 // Returns true when the spherocylinders overlap.
+// FAST with SE (the mixed form's FP64 stress): inv_LL = 1/(Lx Ly) and inv_two_n =
+// 1/(2n) from the caller replace the per-term divisions.
 template <bool SE, bool FAST = false>
 __device__ __forceinline__ bool pair_fp64(double dX, double dY, double nxA, double nyA, double aP,
                                           double nxB, double nyB, double aQ, double sig,
                                           double gamma, double Lx, double Ly, bool virial,
-                                          double two_n, PairF64& o) {
+                                          double two_n, PairF64& o, double inv_LL = 0.0,
+                                          double inv_two_n = 0.0) {
   dX += Lx * (double)((dX < -0.5 * Lx) - (dX > 0.5 * Lx));
   dY += Ly * (double)((dY < -0.5 * Ly) - (dY > 0.5 * Ly));
   dX += gamma * dY;
@@ -108,7 +111,24 @@ __device__ __forceinline__ bool pair_fp64(double dX, double dY, double nxA, doub
   o.fy = Fy;
   o.tp = s * nxA * Fy - s * nyA * Fx;
   o.tq = t * nyB * Fx - t * nxB * Fy;
-  if (SE) {
+  if (SE && FAST) {
+    const double CxA = s * nxA - 0.5 * dDx, CyA = s * nyA - 0.5 * dDy;
+    const double CxB = t * nxB + 0.5 * dDx;
+    const double CyB = (virial ? t * nyB : t * nxB) + 0.5 * dDy;
+    const double gx = Fx * inv_LL, gy = Fy * inv_LL;
+    o.e = dvij * sig * (1.0 - dij * iv.sig) * inv_two_n;
+    if (!virial) {  // the reference's slips, as below
+      o.pxx = gx * (CxA - CxB) - gy * CxB;
+      o.pyy = gy * (CyA - CyB);
+      o.pxy = gy * CxA;
+      o.pyx = gx * (CyA - CyB);
+    } else {
+      o.pxx = gx * (CxA - CxB);
+      o.pyy = gy * (CyA - CyB);
+      o.pxy = gy * (CxA - CxB);
+      o.pyx = gx * (CyA - CyB);
+    }
+  } else if (SE) {
     double LL = Lx * Ly;
     double CxA = s * nxA - 0.5 * dDx;
     double CyA = s * nyA - 0.5 * dDy;
@@ -340,7 +360,8 @@ template <bool SE, bool FAST = false>
 __device__ __forceinline__ bool contact_fp64(double dX, double dY, double s, double t, double nxA,
                                              double nyA, double nxB, double nyB, double sig,
                                              double LL, double two_n, PairF64& o,
-                                             double inv_sig = 0.0) {
+                                             double inv_sig = 0.0, double inv_LL = 0.0,
+                                             double inv_two_n = 0.0) {
   double dDx = dX + s * nxA - t * nxB;
   double dDy = dY + s * nyA - t * nyB;
   double dsq = dDx * dDx + dDy * dDy;
@@ -362,7 +383,16 @@ __device__ __forceinline__ bool contact_fp64(double dX, double dY, double s, dou
   o.fy += Fy;
   o.tp += s * nxA * Fy - s * nyA * Fx;
   o.tq += t * nyB * Fx - t * nxB * Fy;
-  if (SE) {
+  if (SE && FAST) {
+    const double CxA = s * nxA - 0.5 * dDx, CyA = s * nyA - 0.5 * dDy;
+    const double CxB = t * nxB + 0.5 * dDx, CyB = t * nyB + 0.5 * dDy;
+    const double gx = Fx * inv_LL, gy = Fy * inv_LL;
+    o.e += dvij * sig * (1.0 - dij * inv_sig) * inv_two_n;
+    o.pxx += gx * (CxA - CxB);
+    o.pyy += gy * (CyA - CyB);
+    o.pxy += gy * (CxA - CxB);
+    o.pyx += gx * (CyA - CyB);
+  } else if (SE) {
     double CxA = s * nxA - 0.5 * dDx, CyA = s * nyA - 0.5 * dDy;
     double CxB = t * nxB + 0.5 * dDx, CyB = t * nyB + 0.5 * dDy;
     o.e += dvij * sig * (1.0 - dij / sig) / two_n;
@@ -380,7 +410,8 @@ template <bool SE, bool FAST = false>
 __device__ __forceinline__ bool pair2_fp64(double dX, double dY, double nxA, double nyA,
                                            double aP, double nxB, double nyB, double aQ,
                                            double sig, double gamma, double Lx, double Ly,
-                                           double two_n, PairF64& o) {
+                                           double two_n, PairF64& o, double inv_LL = 0.0,
+                                           double inv_two_n = 0.0) {
   dX += Lx * (double)((dX < -0.5 * Lx) - (dX > 0.5 * Lx));
   dY += Ly * (double)((dY < -0.5 * Ly) - (dY > 0.5 * Ly));
   dX += gamma * dY;
@@ -398,10 +429,10 @@ __device__ __forceinline__ bool pair2_fp64(double dX, double dY, double nxA, dou
   o.e = o.pxx = o.pyy = o.pxy = o.pyx = 0.0;
   const double LL = Lx * Ly;
   bool hit = contact_fp64<SE, FAST>(dX, dY, k.s1, k.t1, nxA, nyA, nxB, nyB, sig, LL, two_n, o,
-                                    iv.sig);
+                                    iv.sig, inv_LL, inv_two_n);
   if (k.has2)
     hit |= contact_fp64<SE, FAST>(dX, dY, k.s2, k.t2, nxA, nyA, nxB, nyB, sig, LL, two_n, o,
-                                  iv.sig);
+                                  iv.sig, inv_LL, inv_two_n);
   return hit;
 }
 

@@ -360,6 +360,10 @@ __global__ void k_mx_se_prep(Dev d) {
 
 // One thread per slot over the mixed list (entries: slot | cell offset code); each
 // pair once, from its lower particle index.  The state's scalars (the _p fields).
+// An FP32 screen (a conservative bound, see may_touch_fp32) skips the entries that
+// cannot touch; the FP64 contact code uses shared reciprocals (FAST: this stress is
+// the mixed form's, checked against the FP64 form to 1e-9, not the reference's
+// rounding), with one division per particle for 1/(Lx Ly).
 template <bool TWO>
 __global__ void __launch_bounds__(128) k_mx_se64(Dev d, const StepScalars* __restrict__ tab,
                                                 int row) {
@@ -371,9 +375,11 @@ __global__ void __launch_bounds__(128) k_mx_se64(Dev d, const StepScalars* __res
   const double W = ts.W_p, H = ts.H_p, gamma = ts.gamma_p, Lx = ts.Lx_p, Ly = ts.Ly_p;
   const bool virial = d.stress_mode == STRESS_VIRIAL;
   const double two_n = 2.0 * g.n;
+  const double inv_two_n = 0.5 * g.inv_n, inv_LL = 1.0 / (Lx * Ly);
   const double2 pi = d.xy_t[i];
   const double2 ni = d.nxy_t[i];
   const double2 rai = d.ra[i];
+  const float fnx = (float)ni.x, fny = (float)ni.y, fai = (float)rai.y;
   const int idi = d.id[i];
   double se0 = 0.0, se1 = 0.0, se2 = 0.0, se3 = 0.0, se4 = 0.0;
   int cnt = d.nbr_n[i];
@@ -388,12 +394,21 @@ __global__ void __launch_bounds__(128) k_mx_se64(Dev d, const StepScalars* __res
     // x_i - x_j with the cell centres: the neighbour's cell is (dc, dr) away
     const double dX = (pi.x - pj.x) + (double)(1 - (int)((e >> 28) & 3u)) * W;
     const double dY = (pi.y - pj.y) + (double)(1 - (int)(e >> 30)) * H;
+    {
+      // the screen sees the displacement the FP64 code will use (minimum image, shear)
+      double sx = dX + Lx * (double)((dX < -0.5 * Lx) - (dX > 0.5 * Lx));
+      const double sy = dY + Ly * (double)((dY < -0.5 * Ly) - (dY > 0.5 * Ly));
+      sx += gamma * sy;
+      if (!may_touch_fp32((float)sx, (float)sy, fnx, fny, fai, (float)nj.x, (float)nj.y,
+                          (float)raj.y, (float)(rai.x + raj.x)))
+        continue;
+    }
     PairF64 o;
     const bool hit =
-        TWO ? pair2_fp64<true>(dX, dY, ni.x, ni.y, rai.y, nj.x, nj.y, raj.y, rai.x + raj.x,
-                               gamma, Lx, Ly, two_n, o)
-            : pair_fp64<true>(dX, dY, ni.x, ni.y, rai.y, nj.x, nj.y, raj.y, rai.x + raj.x, gamma,
-                              Lx, Ly, virial, two_n, o);
+        TWO ? pair2_fp64<true, true>(dX, dY, ni.x, ni.y, rai.y, nj.x, nj.y, raj.y,
+                                     rai.x + raj.x, gamma, Lx, Ly, two_n, o, inv_LL, inv_two_n)
+            : pair_fp64<true, true>(dX, dY, ni.x, ni.y, rai.y, nj.x, nj.y, raj.y, rai.x + raj.x,
+                                    gamma, Lx, Ly, virial, two_n, o, inv_LL, inv_two_n);
     if (hit) {
       se0 += o.e;
       se1 += o.pxx;
