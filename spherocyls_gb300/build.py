@@ -109,7 +109,7 @@ def build(force: bool = False, jobs: int | None = None, verbose: bool = False) -
         list(ex.map(_run, jobs_list))
     if force or jobs_list or not os.path.exists(LIBNAME):
         tmp = LIBNAME + ".tmp"
-        _run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-cudart=static", "-ldl"])
+        _run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-cudart=static", "-ldl", "-lpthread"])
         os.replace(tmp, LIBNAME)
     # command-line drivers (link against the shared library)
     for exe, src_name in CLI_UNITS.items():

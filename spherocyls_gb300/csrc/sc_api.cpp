@@ -7,6 +7,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/spherocyl.h"
@@ -118,27 +119,58 @@ int sc_create_rect(const sc_options* opt_in, int n_sys, const int* n_per_sys, co
     return SC_E_ARG;
   }
   const int ntot = (int)ntot_ll;
-  // One pass over the caller's arrays: the input checks, and per system the largest
-  // R and A and the filled area (set_particle, src/cpp/spherocyl_box.cpp:216-219;
-  // calculate_packing_fraction :357-366, summed in particle order).
+  // The input checks and per system the largest R and A (set_particle,
+  // src/cpp/spherocyl_box.cpp:216-219) on worker threads over slices of the caller's
+  // arrays, while this thread sums each system's filled area in particle order
+  // (calculate_packing_fraction :357-366; a dependent chain of additions).
   std::vector<double> rmax(n_sys, 0.0), amax(n_sys, 0.0), filled(n_sys, 0.0);
   {
-    bool finite = true, shapes = true;
-    int i = 0;
-    for (int s = 0; s < n_sys; s++) {
-      double rm = 0.0, am = 0.0, f = 0.0;
-      for (int k = 0; k < n_per_sys[s]; k++, i++) {
+    std::vector<int> p0s(n_sys + 1, 0);
+    for (int s = 0; s < n_sys; s++) p0s[s + 1] = p0s[s] + n_per_sys[s];
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int nthreads = ntot < (1 << 16) ? 1 : (int)std::min(8u, std::max(1u, hw));
+    struct Part {
+      int fin = 1, shp = 1;  // all finite; every R > 0 and A >= 0
+      std::vector<double> rm, am;
+    };
+    std::vector<Part> parts(nthreads);
+    auto scan = [&](int w) {
+      Part& P = parts[w];
+      P.rm.assign(n_sys, 0.0);
+      P.am.assign(n_sys, 0.0);
+      const int a0 = (int)((long long)ntot * w / nthreads);
+      const int a1 = (int)((long long)ntot * (w + 1) / nthreads);
+      int s = (int)(std::upper_bound(p0s.begin(), p0s.end(), a0) - p0s.begin()) - 1;
+      int fin = 1, shp = 1;
+      for (int i = a0; i < a1; i++) {
+        while (i >= p0s[s + 1]) s++;
         const double r = R[i], a = A[i];
-        finite = finite && std::isfinite(x[i]) && std::isfinite(y[i]) &&
-                 std::isfinite(phi[i]) && std::isfinite(r) && std::isfinite(a);
-        shapes = shapes && r > 0 && a >= 0;
-        if (a > am) am = a;
-        if (r > rm) rm = r;
-        f += (kRefPi * r + 4.0 * a) * r;
+        fin &= (int)std::isfinite(x[i]) & (int)std::isfinite(y[i]) &
+               (int)std::isfinite(phi[i]) & (int)std::isfinite(r) & (int)std::isfinite(a);
+        shp &= (int)(r > 0) & (int)(a >= 0);
+        if (a > P.am[s]) P.am[s] = a;
+        if (r > P.rm[s]) P.rm[s] = r;
       }
-      rmax[s] = rm;
-      amax[s] = am;
+      P.fin = fin;
+      P.shp = shp;
+    };
+    std::vector<std::thread> workers;
+    for (int w = 1; w < nthreads; w++) workers.emplace_back(scan, w);
+    scan(0);
+    for (int s = 0, i = 0; s < n_sys; s++) {
+      double f = 0.0;
+      for (int k = 0; k < n_per_sys[s]; k++, i++) f += (kRefPi * R[i] + 4.0 * A[i]) * R[i];
       filled[s] = f;
+    }
+    for (auto& t : workers) t.join();
+    bool finite = true, shapes = true;
+    for (const Part& P : parts) {
+      finite = finite && P.fin;
+      shapes = shapes && P.shp;
+      for (int s = 0; s < n_sys; s++) {
+        rmax[s] = std::max(rmax[s], P.rm[s]);
+        amax[s] = std::max(amax[s], P.am[s]);
+      }
     }
     if (!finite) {
       g_create_error = "sc_create: non-finite input";
@@ -159,8 +191,6 @@ int sc_create_rect(const sc_options* opt_in, int n_sys, const int* n_per_sys, co
   h.block = opt.block > 0 ? opt.block : 128;
   h.nsys = n_sys;
   h.ntot = ntot;
-  h.h_R.assign(R, R + ntot);
-  h.h_A.assign(A, A + ntot);
   auto bail = [&](int code) {
     g_create_error = h.err.empty() ? std::string("sc_create failed") : h.err;
     delete H;
@@ -413,6 +443,7 @@ int sc_autotune(sc_handle* H, int steps, double* pad_factor, int* block) {
   sc::Handle& h = H->h;
   cudaSetDevice(h.device);
   if (pad_factor) *pad_factor = 1.0;
+  if (!h.ensure_host_shapes()) return h.last_status;
   if (block) *block = h.block;
   if (h.prec != sc::PREC_MIXED) return SC_OK;
   const int n = h.ntot, ns = h.nsys;

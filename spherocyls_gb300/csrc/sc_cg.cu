@@ -65,22 +65,43 @@ __global__ void k_cg_dots(Dev d, CgState c) {
   }
 }
 
-// Start of an iteration, one thread per system (cjpr_relax_step_2p :3886-3946 and the
-// restart of cjpr_relax_2p :4270-4274): the energy history and its stop tests, the
-// Polak-Ribiere beta = max(0, (F.F - F.F0)/F0.F0), and the first line-search step
+// Start of an iteration, one block per system (cjpr_relax_step_2p :3886-3946 and the
+// restart of cjpr_relax_2p :4270-4274): the system's chunk partials summed in a fixed
+// tree over the block, then, in one thread, the energy history and its stop tests,
+// the Polak-Ribiere beta = max(0, (F.F - F.F0)/F0.F0), and the first line-search step
 // 2e-6/|F|_rms within [1e-18, 2]/|F|_rms.  `search` is the WHILE node of this
 // iteration's line search (switched on when any system starts one).
-__global__ void k_cg_begin(Dev d, CgState c, int max_iter, unsigned long long search) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= d.nsys) return;
+constexpr int kCgBlock = 256;
+__global__ void __launch_bounds__(kCgBlock) k_cg_begin(Dev d, CgState c, int max_iter,
+                                                       unsigned long long search) {
+  const int s = blockIdx.x;
   CgSys& q = c.sys[s];
-  if (q.done) return;
+  if (q.done) return;  // block-uniform
   double F2 = 0, FF0 = 0, F02 = 0;
   const int ch0 = d.geom[s].pch0, ch1 = ch0 + pchunk_count(d.geom[s]);
-  for (int ch = ch0; ch < ch1; ch++) {
+  for (int ch = ch0 + (int)threadIdx.x; ch < ch1; ch += kCgBlock) {
     F2 += c.part[3 * ch + 0];
     FF0 += c.part[3 * ch + 1];
     F02 += c.part[3 * ch + 2];
+  }
+  __shared__ double sh[3][kCgBlock / 32];
+  for (int o = 16; o; o >>= 1) {
+    F2 += __shfl_down_sync(0xffffffffu, F2, o);
+    FF0 += __shfl_down_sync(0xffffffffu, FF0, o);
+    F02 += __shfl_down_sync(0xffffffffu, F02, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    sh[0][threadIdx.x >> 5] = F2;
+    sh[1][threadIdx.x >> 5] = FF0;
+    sh[2][threadIdx.x >> 5] = F02;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  F2 = FF0 = F02 = 0.0;
+  for (int k = 0; k < kCgBlock / 32; k++) {
+    F2 += sh[0][k];
+    FF0 += sh[1][k];
+    F02 += sh[2][k];
   }
   q.Eh2 = q.Eh1;
   q.Eh1 = q.E0;
@@ -348,7 +369,7 @@ void launch_cg_reset(const Dev& d, const CgState& c, cudaStream_t st) {
 void launch_cg_begin(const Dev& d, const CgState& c, int max_iter, unsigned long long search,
                      cudaStream_t st) {
   k_cg_dots<<<d.npchunks, 256, 0, st>>>(d, c);
-  k_cg_begin<<<nblk(d.nsys, 128), 128, 0, st>>>(d, c, max_iter, search);
+  k_cg_begin<<<d.nsys, kCgBlock, 0, st>>>(d, c, max_iter, search);
   k_cg_dir<<<nblk(d.ntot, 256), 256, 0, st>>>(d, c);
 }
 

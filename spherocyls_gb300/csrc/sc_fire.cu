@@ -26,9 +26,10 @@ namespace {
 template <bool MIXED>
 __global__ void k_fire_chunk(Dev d, FireState f) { fire::fire_chunk<MIXED>(d, f, blockIdx.x); }
 
-__global__ void k_fire_sys(Dev d, FireState f, double ftol, double dt_max) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s < d.nsys) fire::fire_sys(d, f, s, ftol, dt_max);
+// one block of fire::kFireBlock threads per system
+__global__ void __launch_bounds__(fire::kFireBlock) k_fire_sys(Dev d, FireState f, double ftol,
+                                                               double dt_max) {
+  fire::fire_sys(d, f, blockIdx.x, ftol, dt_max);
 }
 
 template <bool MIXED>
@@ -131,7 +132,7 @@ void launch_fire_iteration_tail(const Dev& d, const FireState& f, double ftol, d
     k_fire_chunk<true><<<d.npchunks, 256, 0, st>>>(d, f);
   else
     k_fire_chunk<false><<<d.npchunks, 256, 0, st>>>(d, f);
-  k_fire_sys<<<nblk(d.nsys, 128), 128, 0, st>>>(d, f, ftol, dt_max);
+  k_fire_sys<<<d.nsys, fire::kFireBlock, 0, st>>>(d, f, ftol, dt_max);
   if (mixed)
     k_fire_update<true><<<nblk(d.ntot, 256), 256, 0, st>>>(d, f);
   else

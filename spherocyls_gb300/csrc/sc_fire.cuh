@@ -82,24 +82,15 @@ __device__ __forceinline__ void fire_chunk(const Dev& d, const FireState& f, int
   }
 }
 
-// FIRE scalar update of each system (Bitzek et al. 2006, parameters of that paper)
-__device__ __forceinline__ void fire_sys(const Dev& d, const FireState& f, int s, double ftol,
-                                         double dt_max) {
-  FireSys& q = f.sys[s];
-  if (q.done) return;
-  double P = 0, vv = 0, ff = 0, fm = 0;
-  const int ch0 = d.geom[s].pch0, ch1 = ch0 + pchunk_count(d.geom[s]);
-  for (int ch = ch0; ch < ch1; ch++) {
-    P += f.part[4 * ch + 0];
-    vv += f.part[4 * ch + 1];
-    ff += f.part[4 * ch + 2];
-    fm = fmax(fm, f.part[4 * ch + 3]);
-  }
+// The FIRE scalar update of one system from its sums F.v, |v|^2, |F|^2, max|F|^2.
+__device__ __forceinline__ void fire_sys_scalars(FireSys& q, int* done_flag, double P, double vv,
+                                                 double ff, double fm, double ftol,
+                                                 double dt_max) {
   q.fmax = sqrt(fm);
   q.iters += 1;
   if (q.fmax < ftol) {
     q.done = 1;
-    f.done[s] = 1;  // its force passes stop from the next iteration
+    *done_flag = 1;  // its force passes stop from the next iteration
     q.c1 = 1.0;
     q.c2 = 0.0;
     q.dt = 0.0;
@@ -122,6 +113,50 @@ __device__ __forceinline__ void fire_sys(const Dev& d, const FireState& f, int s
     q.alpha = a_start;
     q.zero_v = 1;
   }
+}
+
+// FIRE scalar update of system s (Bitzek et al. 2006, parameters of that paper) by
+// one block of kFireBlock threads: the system's chunk partials are summed in a fixed
+// tree over the block (a large system has hundreds of chunks), then one thread
+// updates the scalars.
+constexpr int kFireBlock = 256;
+__device__ __forceinline__ void fire_sys(const Dev& d, const FireState& f, int s, double ftol,
+                                         double dt_max) {
+  __shared__ double sh[4][kFireBlock / 32];
+  if (f.sys[s].done) return;  // block-uniform
+  double P = 0, vv = 0, ff = 0, fm = 0;
+  const int ch0 = d.geom[s].pch0, ch1 = ch0 + pchunk_count(d.geom[s]);
+  for (int ch = ch0 + (int)threadIdx.x; ch < ch1; ch += kFireBlock) {
+    P += f.part[4 * ch + 0];
+    vv += f.part[4 * ch + 1];
+    ff += f.part[4 * ch + 2];
+    fm = fmax(fm, f.part[4 * ch + 3]);
+  }
+  for (int o = 16; o; o >>= 1) {
+    P += __shfl_down_sync(0xffffffffu, P, o);
+    vv += __shfl_down_sync(0xffffffffu, vv, o);
+    ff += __shfl_down_sync(0xffffffffu, ff, o);
+    fm = fmax(fm, __shfl_down_sync(0xffffffffu, fm, o));
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) {
+    sh[0][w] = P;
+    sh[1][w] = vv;
+    sh[2][w] = ff;
+    sh[3][w] = fm;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    P = vv = ff = fm = 0.0;
+    for (int k = 0; k < kFireBlock / 32; k++) {
+      P += sh[0][k];
+      vv += sh[1][k];
+      ff += sh[2][k];
+      fm = fmax(fm, sh[3][k]);
+    }
+    fire_sys_scalars(f.sys[s], f.done + s, P, vv, ff, fm, ftol, dt_max);
+  }
+  __syncthreads();  // sh is reused by the block's next system
 }
 
 // v <- (1-a) v + a |v| F/|F| (or 0 after an uphill step); v += dt F/m; x += dt v.

@@ -390,6 +390,33 @@ bool Handle::read_unsorted(bool forces, double* a, double* b, double* c) {
   return cuda_ok(cudaStreamSynchronize(stream), "read output");
 }
 
+// R and A in input order, read back from the device the first time a caller needs
+// them on the host (file output, copies for tuning); the handle does not keep host
+// copies from its creation.  Slots stay inside their system's range, and id is the
+// index within the system.
+bool Handle::ensure_host_shapes() {
+  if ((int)h_R.size() == ntot) return true;
+  std::vector<double2> ra(ntot);
+  std::vector<int> id(ntot);
+  if (!cuda_ok(cudaMemcpyAsync(ra.data(), d.ra, (size_t)ntot * sizeof(double2),
+                               cudaMemcpyDeviceToHost, stream), "read shapes") ||
+      !cuda_ok(cudaMemcpyAsync(id.data(), d.id, (size_t)ntot * sizeof(int),
+                               cudaMemcpyDeviceToHost, stream), "read shapes") ||
+      !cuda_ok(cudaStreamSynchronize(stream), "read shapes"))
+    return false;
+  h_R.assign(ntot, 0.0);
+  h_A.assign(ntot, 0.0);
+  for (int s = 0; s < nsys; s++) {
+    const HostSys& S = hs[s];
+    for (int i = S.p0; i < S.p0 + S.n; i++) {
+      const int k = S.p0 + id[i];
+      h_R[k] = ra[i].x;
+      h_A[k] = ra[i].y;
+    }
+  }
+  return true;
+}
+
 // full rebuild of every system at the current state (constructor / setters)
 bool Handle::rebuild_all() {
   if (!materialize()) return false;

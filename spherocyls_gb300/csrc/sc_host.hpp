@@ -63,7 +63,7 @@ struct Handle {
   int block = 128;
   int nsys = 0, ntot = 0;
   std::vector<HostSys> hs;
-  std::vector<double> h_R, h_A;  // particle radii and half shafts, input order
+  std::vector<double> h_R, h_A;  // particle radii and half shafts, input order (on demand)
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   Dev d{};
@@ -185,6 +185,7 @@ struct Handle {
   void invalidate_table_graphs();
   bool run_persist(int nk, int done, int se_every);
   bool run_persist_fire(int iters, double ftol, double dt_max);
+  bool ensure_host_shapes();  // fills h_R, h_A from the device on first use
   std::vector<int> fire_iters;  // per-system iterations of the last FIRE run
 
   int run_steps(int kind, int shrink, int nsteps, int se_every, double* se_out);

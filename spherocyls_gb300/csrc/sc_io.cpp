@@ -303,6 +303,7 @@ int sc_save_positions(sc_handle* H, int sys, const char* path, int format) {
   std::vector<double> x, y, p;
   int rc = system_state(H, sys, x, y, p);
   if (rc) return rc;
+  if (!h.ensure_host_shapes()) return h.last_status;
   const sc::HostSys& S = h.hs[sys];
   double packing = S.packing * (h.hs[sys].Lx > 0 ? 1.0 : 0.0);
   const double head[7] = {S.Lx, S.Ly, packing, S.gamma, S.gamma_total, S.strain_rate, S.step};

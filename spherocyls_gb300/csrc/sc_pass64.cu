@@ -358,70 +358,170 @@ __global__ void k_mx_se_prep(Dev d) {
   d.nxy_t[i] = make_double2(A * cs, A * sn);
 }
 
-// One thread per slot over the mixed list (entries: slot | cell offset code); each
-// pair once, from its lower particle index.  The state's scalars (the _p fields).
-// An FP32 screen (a conservative bound, see may_touch_fp32) skips the entries that
-// cannot touch; the FP64 contact code uses shared reciprocals (FAST: this stress is
-// the mixed form's, checked against the FP64 form to 1e-9, not the reference's
-// rounding), with one division per particle for 1/(Lx Ly).
+// The mixed form's FP64 stress and energy of the state, one block per 128 slots.
+// Each pair is taken once, from its lower particle index, over the mixed list
+// (entries: slot | cell offset code), with the state's scalars (the _p fields).
+// Phase 1: each thread marks, in windows of 64 list entries, the entries it owns
+// that pass an FP32 screen (a conservative bound on the segment distance, see
+// may_touch_fp32).  Phase 2: the block evaluates the marked pairs 128 at a time,
+// one per thread whatever the lane owning it, in FP64 with shared reciprocals
+// (FAST: this stress is the mixed form's, checked against the FP64 form to 1e-9, not
+// the reference's rounding).  Phase 3: each owner adds the results of its own pairs
+// in list order.  The sums are those of a per-slot loop over the list, and
+// deterministic; the FP64 work runs on full warps instead of the lanes that happen
+// to own a touching pair.
+constexpr int kSeBlock = 128;
+
+// position of set bit r (0-based, counted from bit 0) of m; m has more than r bits set
+__device__ __forceinline__ int nth_set_bit64(unsigned long long m, int r) {
+  for (int q = 0; q < r; q++) m &= m - 1ull;
+  return __ffsll((long long)m) - 1;
+}
+
 template <bool TWO>
-__global__ void __launch_bounds__(128) k_mx_se64(Dev d, const StepScalars* __restrict__ tab,
-                                                int row) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= d.ntot) return;
-  const int s = d.psys[i];
-  const SysGeom& g = d.geom[s];
-  const StepScalars& ts = tab[row * d.nsys + s];
-  const double W = ts.W_p, H = ts.H_p, gamma = ts.gamma_p, Lx = ts.Lx_p, Ly = ts.Ly_p;
+__global__ void __launch_bounds__(kSeBlock) k_mx_se64(Dev d, const StepScalars* __restrict__ tab,
+                                                     int row) {
+  // the owners' particle data and system scalars, for whichever thread evaluates
+  // their pairs
+  __shared__ double o_px[kSeBlock], o_py[kSeBlock], o_nx[kSeBlock], o_ny[kSeBlock];
+  __shared__ double o_R[kSeBlock], o_A[kSeBlock];
+  __shared__ double o_W[kSeBlock], o_H[kSeBlock], o_gam[kSeBlock], o_Lx[kSeBlock],
+      o_Ly[kSeBlock], o_iLL[kSeBlock], o_2n[kSeBlock], o_i2n[kSeBlock];
+  __shared__ unsigned long long mask[kSeBlock];
+  __shared__ int off[kSeBlock + 1];
+  __shared__ int sh_scan[kSeBlock / 32];
+  __shared__ double res[5][kSeBlock];
+  const int t = threadIdx.x;
+  const int i = blockIdx.x * kSeBlock + t;
+  const bool valid = i < d.ntot;
   const bool virial = d.stress_mode == STRESS_VIRIAL;
-  const double two_n = 2.0 * g.n;
-  const double inv_two_n = 0.5 * g.inv_n, inv_LL = 1.0 / (Lx * Ly);
-  const double2 pi = d.xy_t[i];
-  const double2 ni = d.nxy_t[i];
-  const double2 rai = d.ra[i];
-  const float fnx = (float)ni.x, fny = (float)ni.y, fai = (float)rai.y;
-  const int idi = d.id[i];
-  double se0 = 0.0, se1 = 0.0, se2 = 0.0, se3 = 0.0, se4 = 0.0;
-  int cnt = d.nbr_n[i];
-  if (cnt > d.maxn) cnt = d.maxn;
-  for (int k = 0; k < cnt; k++) {
-    const unsigned e = (unsigned)d.nbr[(size_t)k * d.ntot + i];
-    const int j = (int)(e & kSlotMask);
-    if (!(idi < d.id[j])) continue;
-    const double2 pj = d.xy_t[j];
-    const double2 nj = d.nxy_t[j];
-    const double2 raj = d.ra[j];
-    // x_i - x_j with the cell centres: the neighbour's cell is (dc, dr) away
-    const double dX = (pi.x - pj.x) + (double)(1 - (int)((e >> 28) & 3u)) * W;
-    const double dY = (pi.y - pj.y) + (double)(1 - (int)(e >> 30)) * H;
-    {
-      // the screen sees the displacement the FP64 code will use (minimum image, shear)
-      double sx = dX + Lx * (double)((dX < -0.5 * Lx) - (dX > 0.5 * Lx));
-      const double sy = dY + Ly * (double)((dY < -0.5 * Ly) - (dY > 0.5 * Ly));
+  int cnt = 0, idi = 0;
+  float fnx = 0.f, fny = 0.f, fai = 0.f;
+  double px = 0, py = 0, Lx = 1, Ly = 1, gamma = 0, W = 0, H = 0, Ri = 0;
+  if (valid) {
+    const int s = d.psys[i];
+    const SysGeom& g = d.geom[s];
+    const StepScalars& ts = tab[row * d.nsys + s];
+    W = ts.W_p;
+    H = ts.H_p;
+    gamma = ts.gamma_p;
+    Lx = ts.Lx_p;
+    Ly = ts.Ly_p;
+    const double2 pi = d.xy_t[i], ni = d.nxy_t[i], rai = d.ra[i];
+    px = pi.x;
+    py = pi.y;
+    Ri = rai.x;
+    o_px[t] = pi.x;
+    o_py[t] = pi.y;
+    o_nx[t] = ni.x;
+    o_ny[t] = ni.y;
+    o_R[t] = rai.x;
+    o_A[t] = rai.y;
+    o_W[t] = W;
+    o_H[t] = H;
+    o_gam[t] = gamma;
+    o_Lx[t] = Lx;
+    o_Ly[t] = Ly;
+    o_iLL[t] = 1.0 / (Lx * Ly);
+    o_2n[t] = 2.0 * g.n;
+    o_i2n[t] = 0.5 * g.inv_n;
+    fnx = (float)ni.x;
+    fny = (float)ni.y;
+    fai = (float)rai.y;
+    idi = d.id[i];
+    cnt = min(d.nbr_n[i], d.maxn);
+  }
+  double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  // the block's longest list sets the number of 64-entry windows
+  int kmax = cnt;
+  for (int o = 16; o; o >>= 1) kmax = max(kmax, __shfl_xor_sync(0xffffffffu, kmax, o));
+  if ((t & 31) == 0) sh_scan[t >> 5] = kmax;
+  __syncthreads();
+  kmax = 0;
+  for (int w = 0; w < kSeBlock / 32; w++) kmax = max(kmax, sh_scan[w]);
+  for (int k0 = 0; k0 < kmax; k0 += 64) {
+    // phase 1: this window's owned entries that may touch
+    unsigned long long m = 0ull;
+    const int kend = min(cnt, k0 + 64);
+    for (int k = k0; k < kend; k++) {
+      const unsigned e = (unsigned)d.nbr[(size_t)k * d.ntot + i];
+      const int j = (int)(e & kSlotMask);
+      if (!(idi < d.id[j])) continue;
+      const double2 pj = d.xy_t[j];
+      const double2 nj = d.nxy_t[j];
+      const double Aj = d.ra[j].y, Rj = d.ra[j].x;
+      double sx = (px - pj.x) + (double)(1 - (int)((e >> 28) & 3u)) * W;
+      double sy = (py - pj.y) + (double)(1 - (int)(e >> 30)) * H;
+      sx += Lx * (double)((sx < -0.5 * Lx) - (sx > 0.5 * Lx));
+      sy += Ly * (double)((sy < -0.5 * Ly) - (sy > 0.5 * Ly));
       sx += gamma * sy;
-      if (!may_touch_fp32((float)sx, (float)sy, fnx, fny, fai, (float)nj.x, (float)nj.y,
-                          (float)raj.y, (float)(rai.x + raj.x)))
-        continue;
+      if (may_touch_fp32((float)sx, (float)sy, fnx, fny, fai, (float)nj.x, (float)nj.y,
+                         (float)Aj, (float)(Ri + Rj)))
+        m |= 1ull << (k - k0);
     }
-    PairF64 o;
-    const bool hit =
-        TWO ? pair2_fp64<true, true>(dX, dY, ni.x, ni.y, rai.y, nj.x, nj.y, raj.y,
-                                     rai.x + raj.x, gamma, Lx, Ly, two_n, o, inv_LL, inv_two_n)
-            : pair_fp64<true, true>(dX, dY, ni.x, ni.y, rai.y, nj.x, nj.y, raj.y, rai.x + raj.x,
-                                    gamma, Lx, Ly, virial, two_n, o, inv_LL, inv_two_n);
-    if (hit) {
-      se0 += o.e;
-      se1 += o.pxx;
-      se2 += o.pyy;
-      se3 += o.pxy;
-      se4 += o.pyx;
+    mask[t] = m;
+    const int c = __popcll(m);
+    // exclusive scan of the counts over the block
+    int v = c;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, v, o);
+      if ((t & 31) >= o) v += u;
+    }
+    __syncthreads();  // sh_scan is free again
+    if ((t & 31) == 31) sh_scan[t >> 5] = v;
+    __syncthreads();
+    int base_w = 0;
+    for (int w = 0; w < (t >> 5); w++) base_w += sh_scan[w];
+    off[t] = base_w + v - c;
+    int total = 0;
+    for (int w = 0; w < kSeBlock / 32; w++) total += sh_scan[w];
+    if (t == 0) off[kSeBlock] = total;
+    __syncthreads();
+    // phases 2 and 3, 128 pairs at a time
+    for (int b0 = 0; b0 < total; b0 += kSeBlock) {
+      const int p = b0 + t;
+      if (p < total) {
+        // the owner: the last thread whose offset is at most p
+        int lo = 0, hi = kSeBlock - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (off[mid] <= p) lo = mid; else hi = mid - 1;
+        }
+        const int o = lo;
+        const int k = k0 + nth_set_bit64(mask[o], p - off[o]);
+        const int io = blockIdx.x * kSeBlock + o;
+        const unsigned e = (unsigned)d.nbr[(size_t)k * d.ntot + io];
+        const int j = (int)(e & kSlotMask);
+        const double2 pj = d.xy_t[j];
+        const double2 nj = d.nxy_t[j];
+        const double2 raj = d.ra[j];
+        const double dX = (o_px[o] - pj.x) + (double)(1 - (int)((e >> 28) & 3u)) * o_W[o];
+        const double dY = (o_py[o] - pj.y) + (double)(1 - (int)(e >> 30)) * o_H[o];
+        PairF64 r;
+        const bool hit =
+            TWO ? pair2_fp64<true, true>(dX, dY, o_nx[o], o_ny[o], o_A[o], nj.x, nj.y, raj.y,
+                                         o_R[o] + raj.x, o_gam[o], o_Lx[o], o_Ly[o], o_2n[o], r,
+                                         o_iLL[o], o_i2n[o])
+                : pair_fp64<true, true>(dX, dY, o_nx[o], o_ny[o], o_A[o], nj.x, nj.y, raj.y,
+                                        o_R[o] + raj.x, o_gam[o], o_Lx[o], o_Ly[o], virial,
+                                        o_2n[o], r, o_iLL[o], o_i2n[o]);
+        res[0][t] = hit ? r.e : 0.0;
+        res[1][t] = hit ? r.pxx : 0.0;
+        res[2][t] = hit ? r.pyy : 0.0;
+        res[3][t] = hit ? r.pxy : 0.0;
+        res[4][t] = hit ? r.pyx : 0.0;
+      }
+      __syncthreads();
+      // each owner adds its pairs of this batch, in list order (a pair that does
+      // not touch adds zeros, as the per-slot loop skipped it)
+      const int q0 = max(off[t], b0), q1 = min(off[t] + c, b0 + kSeBlock);
+      for (int q = q0; q < q1; q++)
+        for (int comp = 0; comp < 5; comp++) acc[comp] += res[comp][q - b0];
+      __syncthreads();
     }
   }
-  d.se_part[i] = se0;
-  d.se_part[(size_t)d.ntot + i] = se1;
-  d.se_part[(size_t)2 * d.ntot + i] = se2;
-  d.se_part[(size_t)3 * d.ntot + i] = se3;
-  d.se_part[(size_t)4 * d.ntot + i] = se4;
+  if (valid)
+    for (int comp = 0; comp < 5; comp++) d.se_part[(size_t)comp * d.ntot + i] = acc[comp];
 }
 
 template <int MODE, bool SE>
@@ -466,12 +566,12 @@ void launch_pass_fp64(const Dev& d, int mode, bool se, const StepScalars* tab, i
 }
 
 void launch_mx_se64(const Dev& d, const StepScalars* tab, int row, cudaStream_t st) {
-  const int grid = (d.ntot + 127) / 128;
-  k_mx_se_prep<<<grid, 128, 0, st>>>(d);
+  const int grid = (d.ntot + kSeBlock - 1) / kSeBlock;
+  k_mx_se_prep<<<grid, kSeBlock, 0, st>>>(d);
   if (d.contact_model == 1)
-    k_mx_se64<true><<<grid, 128, 0, st>>>(d, tab, row);
+    k_mx_se64<true><<<grid, kSeBlock, 0, st>>>(d, tab, row);
   else
-    k_mx_se64<false><<<grid, 128, 0, st>>>(d, tab, row);
+    k_mx_se64<false><<<grid, kSeBlock, 0, st>>>(d, tab, row);
 }
 
 void launch_build_nbrs(const Dev& d, const StepScalars* tab, int row, cudaStream_t st) {

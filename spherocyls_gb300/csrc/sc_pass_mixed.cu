@@ -344,6 +344,8 @@ __global__ void __launch_bounds__(128, TWO ? 6 : 12) k_persist_steps(
 // ends after `iters` iterations, after the iteration whose update asks for a
 // rebuild (the host runs it), or at the iteration in which the last system
 // converges: *out = 4 * iterations + (0 all ran, 1 rebuild pending, 2 all converged).
+static_assert(fire::kFireBlock == 256, "the persistent FIRE blocks are the reduction blocks");
+
 template <bool TWO>
 __global__ void __launch_bounds__(256, TWO ? 3 : 4) k_persist_fire(
     Dev d, FireState f, const StepScalars* __restrict__ tab, double ftol, double dt_max,
@@ -360,7 +362,8 @@ __global__ void __launch_bounds__(256, TWO ? 3 : 4) k_persist_fire(
       __syncthreads();  // the next chunk reuses the block's shared partials
     }
     grid_barrier(d.gbar, d.status);
-    for (int s = t0; s < d.nsys; s += stride) fire::fire_sys(d, f, s, ftol, dt_max);
+    // one block per system, as k_fire_sys (the block has kFireBlock threads)
+    for (int s = blockIdx.x; s < d.nsys; s += gridDim.x) fire::fire_sys(d, f, s, ftol, dt_max);
     grid_barrier(d.gbar, d.status);
     k++;
     // every block sees the same flags: they change only in the phase before the barrier
