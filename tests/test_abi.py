@@ -52,6 +52,41 @@ def test_create_rejects_bad_arguments_without_gpu(library):
     assert library.sc_status_string(_lib.SC_E_OVERFLOW) == b"capacity exceeded"
 
 
+def test_create_checks_every_particle_of_large_inputs_without_gpu(library):
+    """Above 65536 particles the input checks run on several host threads over
+    slices of the arrays: a bad value anywhere, in any system, is still reported
+    (non-finite before a bad shape, as for small inputs)."""
+    import ctypes
+
+    from spherocyls_gb300 import _lib
+
+    sizes = [70000, 50001, 30000]
+    ntot = sum(sizes)
+    n = (ctypes.c_int * 3)(*sizes)
+    L = (ctypes.c_double * 3)(800.0, 700.0, 600.0)
+    dp = ctypes.POINTER(ctypes.c_double)
+
+    def create(arrays):
+        h = ctypes.c_void_p()
+        ptrs = [a.ctypes.data_as(dp) for a in arrays]
+        return library.sc_create(None, 3, n, L, None, *ptrs, ctypes.byref(h))
+
+    base = [np.full(ntot, 1.0), np.full(ntot, 2.0), np.zeros(ntot), np.full(ntot, 0.5),
+            np.full(ntot, 0.5)]  # x, y, phi, R, A
+    for k, idx, val, want in ((0, ntot - 1, np.nan, _lib.SC_E_NAN),
+                              (2, 70000 + 123, np.inf, _lib.SC_E_NAN),
+                              (3, 70000 + 50000, -0.5, _lib.SC_E_ARG),
+                              (4, 5, -1e-9, _lib.SC_E_ARG),
+                              (3, 0, 0.0, _lib.SC_E_ARG)):
+        arrays = [a.copy() for a in base]
+        arrays[k][idx] = val
+        assert create(arrays) == want, (k, idx, val)
+    arrays = [a.copy() for a in base]
+    arrays[3][100] = -1.0
+    arrays[0][140000] = np.nan
+    assert create(arrays) == _lib.SC_E_NAN  # the non-finite input is reported first
+
+
 def test_generator_reproducible_and_crossing_free(library):
     from spherocyls_gb300 import generate_packing
 

@@ -252,15 +252,17 @@ def test_mixed_precision_shear_tracks_fp64(sc):
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_batched_systems_match_single_runs(sc, precision):
-    """Several systems of different size in one handle advance exactly as alone."""
+    """Several systems of different size in one handle advance exactly as alone, and
+    record the same stress and energy (the third system's slots start inside a block
+    of the stress kernels)."""
     specs = [(256, 0.85, 1.0, 1e-3, 21), (400, 0.80, 0.5, 5e-4, 22), (300, 0.88, 2.0, 2e-3, 23)]
     packs = [sc.generate_packing(n, phi, a, seed=s) for n, phi, a, _, s in specs]
-    singles = []
+    singles, single_se = [], []
     for (n, phi, a, rate, s), (L, x, y, p, R, A) in zip(specs, packs):
         box = sc.SpherocylBox(L, x, y, p, A, R, 0.1, precision=precision)
         box.set_strain_rate(rate)
         box.set_step(0.02)
-        box.strain_steps(150)
+        single_se.append(box.strain_steps(150, se_every=50))
         singles.append(np.concatenate(box.state()))
     batch = sc.BoxBatch([sp[0] for sp in specs], [pk[0] for pk in packs],
                         np.concatenate([pk[1] for pk in packs]),
@@ -271,13 +273,14 @@ def test_batched_systems_match_single_runs(sc, precision):
     for i, sp in enumerate(specs):
         batch.set_strain_rate(sp[3], sys=i)
     batch.set_step(0.02)
-    batch.strain_steps(150)
+    se = batch.strain_steps(150, se_every=50)
     x, y, p = batch.state()
     off = 0
     for i, sp in enumerate(specs):
         n = sp[0]
         got = np.concatenate([x[off:off + n], y[off:off + n], p[off:off + n]])
         assert np.array_equal(got, singles[i]), i
+        assert np.array_equal(se[:, i, :], single_se[i][:, 0, :]), i
         off += n
 
 
