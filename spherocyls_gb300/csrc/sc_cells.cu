@@ -75,16 +75,15 @@ __device__ __forceinline__ int block_excl_scan(int v, int* sh, int* total) {
 
 // The rebuild worklist (one block): the flagged systems in increasing order with
 // the exclusive prefix sums of their slot and cell counts.
-__global__ void __launch_bounds__(1024) k_rb_worklist(Dev d) {
+// The systems to rebuild: those flagged, and those whose table row (tab, row; tab may
+// be null) sets gamma back, which the set-back kernel flags after this list is made.
+__global__ void __launch_bounds__(1024) k_rb_worklist(Dev d, const StepScalars* __restrict__ tab,
+                                                       int row) {
   __shared__ int sh[32];
-  if (*d.any == 0) {
-    if (threadIdx.x == 0) d.nwork[0] = d.nwork[1] = d.nwork[2] = 0;
-    return;
-  }
   int ba = 0, bb = 0, bc = 0;  // running totals (identical in every thread)
   for (int s0 = 0; s0 < d.nsys; s0 += blockDim.x) {
     const int s = s0 + threadIdx.x;
-    const bool f = s < d.nsys && d.flags[s] != 0;
+    const bool f = s < d.nsys && (d.flags[s] != 0 || (tab && tab[row * d.nsys + s].setback));
     int ta, tb, tc;
     const int ea = block_excl_scan(f ? 1 : 0, sh, &ta);
     const int eb = block_excl_scan(f ? d.geom[s].n : 0, sh, &tb);
@@ -177,7 +176,17 @@ __global__ void k_rb_hash(Dev d, const StepScalars* __restrict__ tab, int row, i
     if (rw < 0) rw = 0;
     int c = g.c0 + cell_local(g, col, rw);
     d.cell_tmp[i] = c;
-    d.rank[i] = atomicAdd(&d.cell_count[c], 1);
+    // one atomic per cell among the converged lanes: the slots arrive in cell order,
+    // so neighbouring lanes mostly share a cell (the order inside a cell is settled
+    // by k_rb_cellsort)
+    const unsigned act = __activemask();
+    const unsigned peers = __match_any_sync(act, c);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&d.cell_count[c], __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    d.rank[i] = base + __popc(peers & ((1u << lane) - 1u));
   });
 }
 
@@ -377,10 +386,8 @@ __global__ void k_force_all(Dev d) {
 
 // set_back_gamma, spherocyl_box.cpp:524-545 (positions; gamma itself is advanced
 // on the host), for the systems whose table row says so.
-__global__ void k_setback(Dev d, const StepScalars* __restrict__ tab, int row) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= d.ntot) return;
-  int s = d.psys[i];
+__device__ __forceinline__ void setback_slot(const Dev& d, const StepScalars* __restrict__ tab,
+                                             int row, int i, int s) {
   const StepScalars& ts = tab[row * d.nsys + s];
   if (!ts.setback) return;
   double Lx = ts.Lx_p, Ly = ts.Ly_p;
@@ -399,6 +406,10 @@ __global__ void k_setback(Dev d, const StepScalars* __restrict__ tab, int row) {
     atomicOr(&d.flags[s], 2);
     atomicExch(d.any, 1);
   }
+}
+
+__global__ void k_setback(Dev d, const StepScalars* __restrict__ tab, int row) {
+  for_listed_slots(d, [&](int i, int s) { setback_slot(d, tab, row, i, s); });
 }
 
 // Recompute the shaft vectors of the FP64 form from the state, e.g. after the
@@ -581,10 +592,15 @@ inline int nblk(int n, int b) { return (n + b - 1) / b; }
 
 }  // namespace
 
-void launch_rebuild(const Dev& d, bool mixed, const StepScalars* tab, int row, cudaStream_t st) {
+void launch_rb_worklist(const Dev& d, const StepScalars* tab, int row, cudaStream_t st) {
+  k_rb_worklist<<<1, 1024, 0, st>>>(d, tab, row);
+}
+
+void launch_rebuild(const Dev& d, bool mixed, const StepScalars* tab, int row, cudaStream_t st,
+                    bool listed) {
   const int B = 256;
   // the slot and cell kernels walk the worklist with a fixed grid
-  k_rb_worklist<<<1, 1024, 0, st>>>(d);
+  if (!listed) k_rb_worklist<<<1, 1024, 0, st>>>(d, tab, row);
   k_rb_zero<<<kWalkBlocks, B, 0, st>>>(d);
   k_rb_hash<<<kWalkBlocks, B, 0, st>>>(d, tab, row, mixed ? 1 : 0);
   k_rb_chunksum<<<d.nchunks, 256, 0, st>>>(d);
@@ -637,7 +653,7 @@ void launch_pre_rebuild(const Dev& d, const StepScalars* tab, int row,
 }
 
 void launch_setback(const Dev& d, const StepScalars* tab, int row, cudaStream_t st) {
-  k_setback<<<nblk(d.ntot, 256), 256, 0, st>>>(d, tab, row);
+  k_setback<<<kWalkBlocks, 256, 0, st>>>(d, tab, row);
 }
 
 void launch_refresh_geometry(const Dev& d, bool mixed, const StepScalars* tab, int row,

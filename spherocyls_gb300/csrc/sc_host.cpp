@@ -486,6 +486,9 @@ int Handle::enqueue_rebuild_body(bool resize, int k, bool prof, cudaStream_t st)
   int n = 0;
   cudaStream_t keep = stream;
   stream = st;
+  // the systems to rebuild (flagged, or setting gamma back at this row) first, so
+  // that the kernels before the cell sort touch their slots only
+  launch_rb_worklist(d, d_tab, k, st);
   if (prec == PREC_MIXED) {
     // FP64 positions of the systems about to be sorted or set back
     launch_mx_materialize(d, d_tab, k, false, st);
@@ -495,7 +498,7 @@ int Handle::enqueue_rebuild_body(bool resize, int k, bool prof, cudaStream_t st)
     launch_setback(d, d_tab, k, st);
     n++;
   }
-  timed(2, prof, [&] { launch_rebuild(d, prec == PREC_MIXED, d_tab, k, st); });
+  timed(2, prof, [&] { launch_rebuild(d, prec == PREC_MIXED, d_tab, k, st, true); });
   n += prec == PREC_MIXED ? 13 : 11;
   stream = keep;
   return n;
@@ -1112,8 +1115,9 @@ void Handle::enqueue_fire_iteration(double ftol, double dt_max) {
   launch_fire_iteration_tail(d, fire, ftol, dt_max, mixed, stream);
   // the mixed form moves only its FP32 local state: the flagged systems'
   // FP64 copies are refreshed before the cell sort reads them
+  launch_rb_worklist(d, d_tab, 0, stream);
   if (mixed) launch_mx_materialize(d, d_tab, 0, false, stream);
-  launch_rebuild(d, mixed, d_tab, 0, stream);
+  launch_rebuild(d, mixed, d_tab, 0, stream, true);
   kernels += 4 + (mixed ? 14 : 12);
 }
 
@@ -1141,8 +1145,9 @@ bool Handle::run_fire_graph(int iters, double ftol, double dt_max) {
       pass_skip = nullptr;
       launch_fire_iteration_tail(d, fire, ftol, dt_max, mixed, stream);
       e = capture_rebuild_node(0, [&](cudaStream_t st) {
+        launch_rb_worklist(d, d_tab, 0, st);
         if (mixed) launch_mx_materialize(d, d_tab, 0, false, st);
-        launch_rebuild(d, mixed, d_tab, 0, st);
+        launch_rebuild(d, mixed, d_tab, 0, st, true);
         return mixed ? 14 : 12;
       });
     }
@@ -1191,8 +1196,9 @@ bool Handle::run_persist_fire(int iters, double ftol, double dt_max) {
     k += m;
     if (why == 2) break;  // every system has converged
     if (why == 1) {
+      launch_rb_worklist(d, d_tab, 0, stream);
       launch_mx_materialize(d, d_tab, 0, false, stream);
-      launch_rebuild(d, true, d_tab, 0, stream);
+      launch_rebuild(d, true, d_tab, 0, stream, true);
       kernels += 14;
     }
   }

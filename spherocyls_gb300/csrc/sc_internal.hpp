@@ -306,8 +306,13 @@ void launch_pass_fp64(const Dev& d, int mode, bool se, const StepScalars* tab, i
                       cudaStream_t st, bool fast = false);
 void launch_pass_mixed(const Dev& d, int mode, bool se, const StepScalars* tab, int row,
                        cudaStream_t st, int block);
+// set-back of the listed systems whose row says so (after launch_rb_worklist)
 void launch_setback(const Dev& d, const StepScalars* tab, int row, cudaStream_t st);
-void launch_rebuild(const Dev& d, bool mixed, const StepScalars* tab, int row, cudaStream_t st);
+// the rebuild worklist: flagged systems and those whose row (tab, row) sets gamma back
+void launch_rb_worklist(const Dev& d, const StepScalars* tab, int row, cudaStream_t st);
+// the rebuild chain of the listed systems; `listed`: launch_rb_worklist already ran
+void launch_rebuild(const Dev& d, bool mixed, const StepScalars* tab, int row, cudaStream_t st,
+                    bool listed = false);
 void launch_force_rebuild_all(const Dev& d, cudaStream_t st);
 void launch_clear_flags(const Dev& d, cudaStream_t st);
 void launch_pre_rebuild(const Dev& d, const StepScalars* tab, int row,
@@ -340,6 +345,7 @@ void launch_affine(const Dev& d, const double* factor, cudaStream_t st);
 void launch_reflect(const Dev& d, const double* lx, cudaStream_t st);
 void launch_rotate(const Dev& d, const double* q, cudaStream_t st);
 // mixed form
+// all: every slot; else the slots of the listed systems (after launch_rb_worklist)
 void launch_mx_materialize(const Dev& d, const StepScalars* tab, int row, bool all,
                            cudaStream_t st);
 void launch_mx_local(const Dev& d, const StepScalars* tab, int row, bool all, cudaStream_t st);

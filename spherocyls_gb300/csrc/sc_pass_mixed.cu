@@ -612,12 +612,8 @@ __global__ void __launch_bounds__(kTileThreads) k_tile_lists(Dev d, int all) {
 
 // FP64 absolute state from the compensated local state (flagged systems, systems
 // that set back gamma at this step, or all).
-__global__ void k_mx_materialize(Dev d, const StepScalars* __restrict__ tab, int row, int all) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= d.ntot) return;
-  int s = d.psys[i];
-  const StepScalars& ts = tab[row * d.nsys + s];
-  if (!all && d.flags[s] == 0 && !ts.setback) return;
+// FP64 state of slot i from its compensated record and its cell centre
+__device__ __forceinline__ void materialize_slot(const Dev& d, const StepScalars& ts, int i) {
   int cp = d.cellp[i];
   float4 r = d.rec[i];
   float4 c = d.mc[i];
@@ -625,6 +621,16 @@ __global__ void k_mx_materialize(Dev d, const StepScalars* __restrict__ tab, int
   double y = ((cp >> 16) + 0.5) * ts.H_p + ((double)r.y + (double)c.y);
   d.xy[i] = make_double2(x, y);
   d.ph[i] = (double)c.z + (double)c.w;
+}
+
+// every slot (all) or, after launch_rb_worklist, the slots of the listed systems
+__global__ void k_mx_materialize(Dev d, const StepScalars* __restrict__ tab, int row, int all) {
+  if (all) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < d.ntot) materialize_slot(d, tab[row * d.nsys + d.psys[i]], i);
+    return;
+  }
+  for_listed_slots(d, [&](int i, int s) { materialize_slot(d, tab[row * d.nsys + s], i); });
 }
 
 // Compensated local state from the FP64 state after a cell sort.
@@ -842,7 +848,10 @@ void launch_tile_lists(const Dev& d, bool all, cudaStream_t st) {
 
 void launch_mx_materialize(const Dev& d, const StepScalars* tab, int row, bool all,
                            cudaStream_t st) {
-  k_mx_materialize<<<nblk(d.ntot, 256), 256, 0, st>>>(d, tab, row, all ? 1 : 0);
+  if (all)
+    k_mx_materialize<<<nblk(d.ntot, 256), 256, 0, st>>>(d, tab, row, 1);
+  else
+    k_mx_materialize<<<kWalkBlocks, 256, 0, st>>>(d, tab, row, 0);
 }
 
 void launch_mx_local(const Dev& d, const StepScalars* tab, int row, bool all, cudaStream_t st) {
