@@ -155,8 +155,16 @@ int sc_create_rect(const sc_options* opt_in, int n_sys, const int* n_per_sys, co
       P.shp = shp;
     };
     std::vector<std::thread> workers;
-    for (int w = 1; w < nthreads; w++) workers.emplace_back(scan, w);
-    scan(0);
+    std::vector<char> on_worker(nthreads, 0);
+    for (int w = 1; w < nthreads; w++) {
+      try {
+        workers.emplace_back(scan, w);
+        on_worker[w] = 1;
+      } catch (...) {  // no thread to be had: this slice is scanned here
+      }
+    }
+    for (int w = 0; w < nthreads; w++)
+      if (!on_worker[w]) scan(w);
     for (int s = 0, i = 0; s < n_sys; s++) {
       double f = 0.0;
       for (int k = 0; k < n_per_sys[s]; k++, i++) f += (kRefPi * R[i] + 4.0 * A[i]) * R[i];
