@@ -8,8 +8,8 @@ untimed warm-up steps from the generated packing, then K timed steps.
 
 The headline `value` is the mixed-precision form with its state resident on the
 device; `value_fp64` is the plain FP64 form over the same window; `e2e` is the
-same window through the C ABI from host arrays (handle creation from the state
-after the warm-up, K steps, state and stress read back).  The same JSON line
+same window through the C ABI from pinned host arrays (handle creation from the
+state after the warm-up, K steps, state and stress read back into pinned arrays).  The same JSON line
 carries the force-pass roofline, a steady-state figure (after a longer shear), the
 CPU baseline (the oracle restatement of the reference's CPU path on the host
 cores), the precision A/B of the N = 16384 workload, the 512-system batch and the
