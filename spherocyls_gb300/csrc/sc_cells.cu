@@ -612,11 +612,12 @@ void launch_rebuild(const Dev& d, bool mixed, const StepScalars* tab, int row, c
   k_rb_commit<<<kWalkBlocks, B, 0, st>>>(d, tab, row, mixed ? 1 : 0);
   if (mixed) {
     launch_mx_local(d, tab, row, false, st);
-    launch_mx_build_list(d, tab, row, false, st);
-    if (d.pass_kind == 1)
+    if (d.pass_kind == 1) {
+      launch_mx_build_list(d, tab, row, false, st);
       launch_tile_lists(d, false, st);
-    else
-      launch_mx_order(d, false, st);
+    } else {
+      launch_mx_build_order(d, tab, row, false, st);
+    }
   } else {
     launch_build_nbrs(d, tab, row, st);
   }

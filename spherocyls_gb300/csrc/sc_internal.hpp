@@ -350,6 +350,9 @@ void launch_mx_materialize(const Dev& d, const StepScalars* tab, int row, bool a
                            cudaStream_t st);
 void launch_mx_local(const Dev& d, const StepScalars* tab, int row, bool all, cudaStream_t st);
 void launch_mx_order(const Dev& d, bool all, cudaStream_t st);
+// the list build and the ordering in one kernel (the per-particle pass)
+void launch_mx_build_order(const Dev& d, const StepScalars* tab, int row, bool all,
+                           cudaStream_t st);
 void launch_mx_build_list(const Dev& d, const StepScalars* tab, int row, bool all,
                           cudaStream_t st);
 // Persistent mixed shear steps (per-particle pass): rows row0 .. row0 + nsteps - 1 of

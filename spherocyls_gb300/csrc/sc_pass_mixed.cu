@@ -671,85 +671,83 @@ __global__ void k_mx_local(Dev d, const StepScalars* __restrict__ tab, int row, 
 // by cell, slots ascending) is the scan order either way.
 constexpr int kMxQueue = 24;
 
-__global__ void __launch_bounds__(128, 12) k_mx_build_list(Dev d, const StepScalars* __restrict__ tab,
-                                                      int row, int all) {
-  if (!all && *d.any == 0) return;
-  for_slots(d, all != 0, [&](int i, int s) {
-    const SysGeom& g = d.geom[s];
-    const StepScalars& ts = tab[row * d.nsys + s];
-    const float W = ts.f_Wp, H = ts.f_Hp, gam = ts.f_gamma_p, pad = (float)g.pad;
-    const float Lxf = W * g.cols, Lyf = H * g.rows;
-    const int cp = d.cellp[i];
-    const int col = cp & 0xffff, rw = cp >> 16;
-    const float4 ri = d.rec[i];
-    const float2 rai = reinterpret_cast<const float2*>(d.pa)[2 * (size_t)i];  // (R, A)
-    const int ncx = g.cols < 3 ? g.cols : 3, ncy = g.rows < 3 ? g.rows : 3;
-    const bool smallx = ncx < 3, smally = ncy < 3;
-    unsigned queue[kMxQueue];  // survivors of the centre test: slot | cell offset code
-    int nq = 0, cnt = 0;
-    // capsule test of the queued candidates, accepted ones appended in queue order
-    auto flush = [&]() {
-      for (int q = 0; q < nq; q++) {
-        const unsigned e = queue[q];
-        const int j = (int)(e & kSlotMask);
+// The list of slot i (system s): see the file comment and kMxQueue.
+__device__ __forceinline__ void build_list_slot(const Dev& d, const StepScalars* __restrict__ tab,
+                                                int row, int i, int s) {
+  const SysGeom& g = d.geom[s];
+  const StepScalars& ts = tab[row * d.nsys + s];
+  const float W = ts.f_Wp, H = ts.f_Hp, gam = ts.f_gamma_p, pad = (float)g.pad;
+  const float Lxf = W * g.cols, Lyf = H * g.rows;
+  const int cp = d.cellp[i];
+  const int col = cp & 0xffff, rw = cp >> 16;
+  const float4 ri = d.rec[i];
+  const float2 rai = reinterpret_cast<const float2*>(d.pa)[2 * (size_t)i];  // (R, A)
+  const int ncx = g.cols < 3 ? g.cols : 3, ncy = g.rows < 3 ? g.rows : 3;
+  const bool smallx = ncx < 3, smally = ncy < 3;
+  unsigned queue[kMxQueue];  // survivors of the centre test: slot | cell offset code
+  int nq = 0, cnt = 0;
+  // capsule test of the queued candidates, accepted ones appended in queue order
+  auto flush = [&]() {
+    for (int q = 0; q < nq; q++) {
+      const unsigned e = queue[q];
+      const int j = (int)(e & kSlotMask);
+      const float4 rj = d.rec[j];
+      const float Rj = d.rf[j];
+      float dx = ri.x - rj.x + (float)(1 - (int)((e >> 28) & 3u)) * W;
+      float dy = ri.y - rj.y + (float)(1 - (int)(e >> 30)) * H;
+      if (smallx) dx += Lxf * (float)((dx < -0.5f * Lxf) - (dx > 0.5f * Lxf));
+      if (smally) dy += Lyf * (float)((dy < -0.5f * Lyf) - (dy > 0.5f * Lyf));
+      if (capsules_within(fmaf(gam, dy, dx), dy, ri.z, ri.w, rj.z, rj.w,
+                          (rai.x + Rj + pad) * 1.00002f + 1e-5f)) {
+        if (cnt < d.maxn) d.nbr[(size_t)cnt * d.ntot + i] = (int)e;
+        cnt++;
+      }
+    }
+    nq = 0;
+  };
+  for (int a = 0; a < ncy; a++) {
+    int dr = smally ? a - rw : a - 1;
+    int r2 = smally ? a : wrap_index(rw + dr, g.rows);
+    for (int b = 0; b < ncx; b++) {
+      int dc = smallx ? b - col : b - 1;
+      int c2 = smallx ? b : wrap_index(col + dc, g.cols);
+      int cc = g.c0 + cell_local(g, c2, r2);
+      int st = d.cell_start[cc], en = st + d.cell_count[cc];
+      unsigned code = ((unsigned)(dc + 1) << 28) | ((unsigned)(dr + 1) << 30);
+      const float ox = (float)dc * W, oy = (float)dr * H;
+      for (int j = st; j < en; j++) {
+        if (j == i) continue;
         const float4 rj = d.rec[j];
-        const float Rj = d.rf[j];
-        float dx = ri.x - rj.x + (float)(1 - (int)((e >> 28) & 3u)) * W;
-        float dy = ri.y - rj.y + (float)(1 - (int)(e >> 30)) * H;
+        const float2 raj = reinterpret_cast<const float2*>(d.pa)[2 * (size_t)j];
+        float dx = ri.x - rj.x - ox;
+        float dy = ri.y - rj.y - oy;
         if (smallx) dx += Lxf * (float)((dx < -0.5f * Lxf) - (dx > 0.5f * Lxf));
         if (smally) dy += Lyf * (float)((dy < -0.5f * Lyf) - (dy > 0.5f * Lyf));
-        if (capsules_within(fmaf(gam, dy, dx), dy, ri.z, ri.w, rj.z, rj.w,
-                            (rai.x + Rj + pad) * 1.00002f + 1e-5f)) {
-          if (cnt < d.maxn) d.nbr[(size_t)cnt * d.ntot + i] = (int)e;
-          cnt++;
-        }
-      }
-      nq = 0;
-    };
-    for (int a = 0; a < ncy; a++) {
-      int dr = smally ? a - rw : a - 1;
-      int r2 = smally ? a : wrap_index(rw + dr, g.rows);
-      for (int b = 0; b < ncx; b++) {
-        int dc = smallx ? b - col : b - 1;
-        int c2 = smallx ? b : wrap_index(col + dc, g.cols);
-        int cc = g.c0 + cell_local(g, c2, r2);
-        int st = d.cell_start[cc], en = st + d.cell_count[cc];
-        unsigned code = ((unsigned)(dc + 1) << 28) | ((unsigned)(dr + 1) << 30);
-        const float ox = (float)dc * W, oy = (float)dr * H;
-        for (int j = st; j < en; j++) {
-          if (j == i) continue;
-          const float4 rj = d.rec[j];
-          const float2 raj = reinterpret_cast<const float2*>(d.pa)[2 * (size_t)j];
-          float dx = ri.x - rj.x - ox;
-          float dy = ri.y - rj.y - oy;
-          if (smallx) dx += Lxf * (float)((dx < -0.5f * Lxf) - (dx > 0.5f * Lxf));
-          if (smally) dy += Lyf * (float)((dy < -0.5f * Lyf) - (dy > 0.5f * Lyf));
-          const float lim = (rai.x + rai.y + raj.x + raj.y + pad) * 1.00002f + 1e-6f;
-          const float dxl = fmaf(gam, dy, dx);
-          if (dxl * dxl + dy * dy < lim * lim) {
-            queue[nq++] = (unsigned)j | code;
-            if (nq == kMxQueue) flush();
-          }
+        const float lim = (rai.x + rai.y + raj.x + raj.y + pad) * 1.00002f + 1e-6f;
+        const float dxl = fmaf(gam, dy, dx);
+        if (dxl * dxl + dy * dy < lim * lim) {
+          queue[nq++] = (unsigned)j | code;
+          if (nq == kMxQueue) flush();
         }
       }
     }
-    flush();
-    d.nbr_n[i] = cnt;
-    if (cnt > d.maxn) atomicOr(d.status, ST_NBR_OVERFLOW);
-    if (i == g.p0) d.gbuild[s] = gam;
-  });
+  }
+  flush();
+  d.nbr_n[i] = cnt;
+  if (cnt > d.maxn) atomicOr(d.status, ST_NBR_OVERFLOW);
+  if (i == g.p0) d.gbuild[s] = gam;
+}
+
+__global__ void __launch_bounds__(128, 12) k_mx_build_list(Dev d, const StepScalars* __restrict__ tab,
+                                                      int row, int all) {
+  if (!all && *d.any == 0) return;
+  for_slots(d, all != 0, [&](int i, int s) { build_list_slot(d, tab, row, i, s); });
 }
 
 // Force-pass ordering: within each window of kOrderWindow slots, a stable sort
 // of the slots by list length; the lists are copied to their positions.  A window
 // is redone when any of its slots belongs to a system that was rebuilt.
-__global__ void __launch_bounds__(kOrderWindow) k_mx_order(Dev d, int all) {
-  if (!all && *d.any == 0) return;
-  const int base = blockIdx.x * kOrderWindow;
-  const int i = base + threadIdx.x;
-  const bool valid = i < d.ntot;
-  const bool mine = valid && (all || d.flags[d.psys[i]] != 0);
-  if (!__syncthreads_or(mine)) return;
+__device__ __forceinline__ void order_window(const Dev& d, int base, int i, bool valid) {
   __shared__ int len[kOrderWindow];
   int c = 0x7fffffff;  // slots past the end sort last
   if (valid) c = min(d.nbr_n[i], d.maxn);
@@ -768,12 +766,47 @@ __global__ void __launch_bounds__(kOrderWindow) k_mx_order(Dev d, int all) {
   for (int k = 0; k < c; k++) d.nbr_p[k * n + pos] = d.nbr[k * n + i];
 }
 
+__global__ void __launch_bounds__(kOrderWindow) k_mx_order(Dev d, int all) {
+  if (!all && *d.any == 0) return;
+  const int base = blockIdx.x * kOrderWindow;
+  const int i = base + threadIdx.x;
+  const bool valid = i < d.ntot;
+  const bool mine = valid && (all || d.flags[d.psys[i]] != 0);
+  if (!__syncthreads_or(mine)) return;
+  order_window(d, base, i, valid);
+}
+
+// The list build and the force-pass ordering fused (the per-particle pass), one
+// block per window of kOrderWindow slots: the window's slots of rebuilt systems
+// build their lists, then the window is ordered and its lists copied to their
+// positions while they are still in cache.  Same lists and order as
+// k_mx_build_list followed by k_mx_order.
+__global__ void __launch_bounds__(kOrderWindow, 12) k_mx_build_order(
+    Dev d, const StepScalars* __restrict__ tab, int row, int all) {
+  if (!all && *d.any == 0) return;
+  const int base = blockIdx.x * kOrderWindow;
+  const int i = base + threadIdx.x;
+  const bool valid = i < d.ntot;
+  const int s = valid ? d.psys[i] : 0;
+  const bool mine = valid && (all || d.flags[s] != 0);
+  if (!__syncthreads_or(mine)) return;
+  if (mine) build_list_slot(d, tab, row, i, s);
+  __syncthreads();  // the window's lengths and lists are complete
+  order_window(d, base, i, valid);
+}
+
 inline int nblk(int n, int b) { return (n + b - 1) / b; }
 
 }  // namespace
 
 void launch_mx_order(const Dev& d, bool all, cudaStream_t st) {
   k_mx_order<<<nblk(d.ntot, kOrderWindow), kOrderWindow, 0, st>>>(d, all ? 1 : 0);
+}
+
+void launch_mx_build_order(const Dev& d, const StepScalars* tab, int row, bool all,
+                           cudaStream_t st) {
+  k_mx_build_order<<<nblk(d.ntot, kOrderWindow), kOrderWindow, 0, st>>>(d, tab, row,
+                                                                         all ? 1 : 0);
 }
 
 void launch_pass_mixed(const Dev& d, int mode, bool se, const StepScalars* tab, int row,
